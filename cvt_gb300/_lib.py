@@ -1,0 +1,89 @@
+"""ctypes binding of libcvtpm.so (include/cvtpm.h).
+
+The library is the only compute path: if it is missing or cannot be loaded,
+import fails with an error that says how to build it.  There is no CPU
+fallback.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+from .params import CvtpmParams
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "libcvtpm.so")
+
+# every symbol include/cvtpm.h declares
+EXPORTS = (
+    "cvtpm_version", "cvtpm_status_string", "cvtpm_params_default", "cvtpm_create", "cvtpm_destroy",
+    "cvtpm_set_params", "cvtpm_get_params", "cvtpm_last_error", "cvtpm_synchronize", "cvtpm_depthmap",
+    "cvtpm_depthmap_host", "cvtpm_cost_eval", "cvtpm_cost_adjoint", "cvtpm_depthmap_batched",
+)
+
+
+class CvtpmTrace(ctypes.Structure):
+    _fields_ = [("winners", ctypes.c_void_p), ("valid", ctypes.c_void_p), ("states", ctypes.c_void_p)]
+
+
+class CvtpmPair(ctypes.Structure):
+    _fields_ = [("left", ctypes.c_void_p), ("right", ctypes.c_void_p), ("width", ctypes.c_int),
+                ("height", ctypes.c_int), ("pitch", ctypes.c_size_t), ("depthmax", ctypes.c_float),
+                ("dmap", ctypes.c_void_p), ("dmap_pitch", ctypes.c_size_t)]
+
+
+class CvtpmError(RuntimeError):
+    def __init__(self, status: int, message: str):
+        super().__init__(f"cvtpm status {status}: {message}")
+        self.status = status
+
+
+_lib = None
+
+
+def lib() -> ctypes.CDLL:
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise ImportError(f"{LIB_PATH} is missing: build it with `python -c 'import __graft_entry__ as g; g.build()'`")
+    L = ctypes.CDLL(LIB_PATH)
+    vp, i, f, sz = ctypes.c_void_p, ctypes.c_int, ctypes.c_float, ctypes.c_size_t
+    P = ctypes.POINTER(CvtpmParams)
+    L.cvtpm_version.restype = ctypes.c_char_p
+    L.cvtpm_status_string.argtypes = [i]
+    L.cvtpm_status_string.restype = ctypes.c_char_p
+    L.cvtpm_params_default.argtypes = [P, i]
+    L.cvtpm_create.argtypes = [ctypes.POINTER(vp), i]
+    L.cvtpm_destroy.argtypes = [vp]
+    L.cvtpm_set_params.argtypes = [vp, P]
+    L.cvtpm_get_params.argtypes = [vp, P]
+    L.cvtpm_last_error.argtypes = [vp]
+    L.cvtpm_last_error.restype = ctypes.c_char_p
+    L.cvtpm_synchronize.argtypes = [vp, vp]
+    L.cvtpm_depthmap.argtypes = [vp, vp, sz, vp, vp, i, i, sz, i, f, i, i, f, vp, sz, ctypes.POINTER(CvtpmTrace), vp]
+    L.cvtpm_depthmap_host.argtypes = [vp, vp, sz, vp, vp, i, i, sz, i, f, i, i, f, vp, sz, vp]
+    L.cvtpm_cost_eval.argtypes = [vp, vp, vp, i, i, sz, vp, i, vp, vp]
+    L.cvtpm_cost_adjoint.argtypes = [vp, vp, vp, i, i, sz, vp, i, vp, vp, vp, vp, vp, vp]
+    L.cvtpm_depthmap_batched.argtypes = [vp, ctypes.POINTER(CvtpmPair), i, vp]
+    for name in EXPORTS:
+        if name not in ("cvtpm_version", "cvtpm_status_string", "cvtpm_last_error"):
+            getattr(L, name).restype = ctypes.c_int
+    _lib = L
+    return L
+
+
+def version() -> str:
+    return lib().cvtpm_version().decode()
+
+
+def status_string(s: int) -> str:
+    return lib().cvtpm_status_string(int(s)).decode()
+
+
+def c_default_params(preset: int) -> CvtpmParams:
+    p = CvtpmParams()
+    rc = lib().cvtpm_params_default(ctypes.byref(p), int(preset))
+    if rc:
+        raise CvtpmError(rc, "cvtpm_params_default")
+    return p

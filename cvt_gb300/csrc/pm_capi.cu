@@ -1,0 +1,462 @@
+/*
+ * pm_capi.cu — the C ABI of include/cvtpm.h: context, scratch memory and the
+ * host schedule of PMHuberStereo::depthMap (cvt/vision/PMHuberStereo.cpp:64-291)
+ * over the kernels of pm_kernels.cu.
+ *
+ * Differences from the reference host code, none of which changes a result:
+ *  - scratch lives in the context and is reused across calls (the reference
+ *    allocates 14 images and 2 buffers per call, PMHuberStereo.cpp:78-122);
+ *  - launches are stream-ordered with no host synchronisation (the reference
+ *    blocks after every launch with runWait);
+ *  - the debug block that writes PNGs and waits on getchar()
+ *    (PMHuberStereo.cpp:153-185) is not reproduced;
+ *  - the view-candidate buffers hold source positions instead of copies of
+ *    the candidate planes (k_view_list).
+ */
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "cvtpm.h"
+#include "pm_kernels.cuh"
+
+#define CVTPM_VERSION "cvt-gb300 0.1.0 (sm_103a)"
+#define PM_MAX_WIDTH 12288
+
+struct cvtpm_ctx {
+    int device = 0;
+    cvtpm_params prm;
+    std::string err;
+    /* scratch, carved from one allocation */
+    void* pool = nullptr;
+    size_t pool_bytes = 0;
+    int capW = 0, capH = 0;
+    float4 *col[2], *grad[2], *recA[2], *recB[2], *recC[2];
+    float2* recD[2];
+    float* wgt[2];
+    float4* S[2][2];
+    float4* smooth[2];
+    float4 *tmp, *tmp2, *pdT;
+    float4* pdP[2];
+    short4* list[2];
+    uint8_t* win[2];
+    uint8_t* valid;
+    /* staging for the *_host entry points */
+    void* stage = nullptr;
+    size_t stage_bytes = 0;
+};
+
+namespace {
+
+std::mutex g_table_mu;
+struct TableKey { int device; float cw; int prof; bool ok; };
+std::vector<TableKey> g_tables;
+
+cvtpm_status fail(cvtpm_ctx* c, cvtpm_status s, const std::string& m) {
+    if (c) c->err = m;
+    return s;
+}
+cvtpm_status cuda_fail(cvtpm_ctx* c, cudaError_t e, const char* where) {
+    return fail(c, CVTPM_ERR_CUDA, std::string(where) + ": " + cudaGetErrorString(e));
+}
+#define CK(call, where) do { cudaError_t e_ = (call); if (e_ != cudaSuccess) return cuda_fail(ctx, e_, where); } while (0)
+
+size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
+
+void mwc_pow2_table(unsigned long long* t) {
+    const unsigned __int128 M = 18446383549859758079ull;
+    unsigned long long v = 4294883355ull;                 /* A */
+    for (int k = 0; k < 64; ++k) {
+        t[k] = v;
+        v = (unsigned long long)(((unsigned __int128)v * v) % M);
+    }
+}
+
+cvtpm_status ensure_tables(cvtpm_ctx* ctx, const cvtpm_params& p, cudaStream_t st) {
+    std::lock_guard<std::mutex> lk(g_table_mu);
+    for (auto& t : g_tables)
+        if (t.device == ctx->device && t.ok && t.cw == p.color_weight && t.prof == p.weight_profile) return CVTPM_OK;
+    static unsigned long long pow2[64];
+    static float prof[PM_PROF_N * PM_PROF_N];
+    mwc_pow2_table(pow2);
+    for (int dy = -PM_PMAX; dy <= PM_PMAX; ++dy)
+        for (int dx = -PM_PMAX; dx <= PM_PMAX; ++dx)
+            prof[(dy + PM_PMAX) * PM_PROF_N + (dx + PM_PMAX)] = pm_profile(dx, dy, p.color_weight, p.weight_profile);
+    CK(pm_upload_tables(pow2, prof, st), "upload tables");
+    CK(cudaStreamSynchronize(st), "upload tables");
+    bool found = false;
+    for (auto& t : g_tables)
+        if (t.device == ctx->device) { t.cw = p.color_weight; t.prof = p.weight_profile; t.ok = true; found = true; }
+    if (!found) g_tables.push_back({ctx->device, p.color_weight, p.weight_profile, true});
+    return CVTPM_OK;
+}
+
+cvtpm_status ensure_buffers(cvtpm_ctx* ctx, int W, int H) {
+    if (ctx->pool && W * (size_t)H <= (size_t)ctx->capW * ctx->capH && W <= ctx->capW) {
+        /* reuse: the carve below depends only on n = W*H, recompute it */
+    }
+    const size_t n = (size_t)W * H;
+    size_t off = 0;
+    std::vector<std::pair<void**, size_t>> parts;
+    auto add = [&](void** p, size_t bytes) { parts.push_back({p, bytes}); off = align_up(off, 256) + bytes; };
+    for (int v = 0; v < 2; ++v) {
+        add((void**)&ctx->col[v], n * 16);
+        add((void**)&ctx->grad[v], n * 16);
+        add((void**)&ctx->recA[v], n * 16);
+        add((void**)&ctx->recB[v], n * 16);
+        add((void**)&ctx->recC[v], n * 16);
+        add((void**)&ctx->recD[v], n * 8);
+        add((void**)&ctx->wgt[v], n * 4);
+        add((void**)&ctx->S[v][0], n * 16);
+        add((void**)&ctx->S[v][1], n * 16);
+        add((void**)&ctx->smooth[v], n * 16);
+        add((void**)&ctx->list[v], n * 8);
+        add((void**)&ctx->win[v], n);
+        add((void**)&ctx->pdP[v], n * 32);
+    }
+    add((void**)&ctx->tmp, n * 16);
+    add((void**)&ctx->tmp2, n * 16);
+    add((void**)&ctx->pdT, n * 16);
+    add((void**)&ctx->valid, n);
+    const size_t need = align_up(off, 256);
+    if (need > ctx->pool_bytes) {
+        if (ctx->pool) { cudaFree(ctx->pool); ctx->pool = nullptr; ctx->pool_bytes = 0; }
+        cudaError_t e = cudaMalloc(&ctx->pool, need);
+        if (e != cudaSuccess) { ctx->pool = nullptr; return fail(ctx, CVTPM_ERR_ALLOC, std::string("scratch allocation: ") + cudaGetErrorString(e)); }
+        ctx->pool_bytes = need;
+    }
+    size_t o = 0;
+    for (auto& pr : parts) { o = align_up(o, 256); *pr.first = (char*)ctx->pool + o; o += pr.second; }
+    ctx->capW = W; ctx->capH = H;
+    return CVTPM_OK;
+}
+
+cvtpm_status check_params(cvtpm_ctx* ctx, const cvtpm_params& p) {
+    if (p.patchsize < 1 || p.patchsize > PM_PMAX) return fail(ctx, CVTPM_ERR_SIZE, "patchsize must be in 1..31");
+    if (!(p.depthmax > 0.0f)) return fail(ctx, CVTPM_ERR_INVALID_ARGUMENT, "depthmax must be > 0");
+    if (p.iterations < 1) return fail(ctx, CVTPM_ERR_INVALID_ARGUMENT, "iterations must be >= 1");
+    if (p.pd_iterations < 0) return fail(ctx, CVTPM_ERR_INVALID_ARGUMENT, "pd_iterations must be >= 0");
+    if (p.rng != CVTPM_RNG_MWC64X && p.rng != CVTPM_RNG_PHILOX) return fail(ctx, CVTPM_ERR_INVALID_ARGUMENT, "bad rng");
+    if (p.arith != CVTPM_ARITH_EXACT && p.arith != CVTPM_ARITH_FAST) return fail(ctx, CVTPM_ERR_INVALID_ARGUMENT, "bad arith");
+    if (p.schedule != CVTPM_SCHEDULE_JACOBI) return fail(ctx, CVTPM_ERR_NOT_SUPPORTED, "only the Jacobi schedule is built");
+    if (p.weight_profile != CVTPM_PROFILE_SMOOTHSTEP && p.weight_profile != CVTPM_PROFILE_CONSTANT)
+        return fail(ctx, CVTPM_ERR_INVALID_ARGUMENT, "bad weight_profile");
+    return CVTPM_OK;
+}
+
+cvtpm_status check_image(cvtpm_ctx* ctx, const void* p, int W, int H, size_t pitch, const char* what) {
+    if (!p) return fail(ctx, CVTPM_ERR_INVALID_ARGUMENT, std::string(what) + " is NULL");
+    if (W < 1 || H < 1 || W > PM_MAX_WIDTH || H > 65535) return fail(ctx, CVTPM_ERR_SIZE, "image size out of range");
+    if (pitch % 16 != 0 || pitch < (size_t)W * 16) return fail(ctx, CVTPM_ERR_INVALID_ARGUMENT, std::string(what) + " pitch must be a multiple of 16 and >= 16*width");
+    if (((uintptr_t)p & 15) != 0) return fail(ctx, CVTPM_ERR_INVALID_ARGUMENT, std::string(what) + " must be 16-byte aligned");
+    return CVTPM_OK;
+}
+
+PmPassArgs base_args(cvtpm_ctx* ctx, const cvtpm_params& p, int W, int H, int v1) {
+    PmPassArgs a;
+    memset(&a, 0, sizeof(a));
+    a.k.W = W; a.k.H = H; a.k.P = p.patchsize;
+    a.k.Wf = (float)W; a.k.Hf = (float)H;
+    a.k.alpha = p.color_alpha; a.k.oma = 1.0f - p.color_alpha;
+    a.k.cmax = p.color_maxdiff; a.k.gmax = p.grad_maxdiff;
+    const int v2 = 1 - v1;
+    a.v1 = {ctx->col[v1], ctx->grad[v1], ctx->recA[v1], ctx->recB[v1], ctx->recC[v1], ctx->recD[v1]};
+    a.v2 = {ctx->col[v2], ctx->grad[v2], ctx->recA[v2], ctx->recB[v2], ctx->recC[v2], ctx->recD[v2]};
+    a.lr = v1 == 0 ? 1 : 0;
+    a.rng = p.rng;
+    a.key0 = (uint32_t)p.seed; a.key1 = (uint32_t)(p.seed >> 32);
+    a.depthmax = p.depthmax;
+    return a;
+}
+
+cvtpm_status prep_views(cvtpm_ctx* ctx, const cvtpm_params& p, const float* img0, const float* img1, int W, int H,
+                        size_t pitch, cudaStream_t st) {
+    const float* im[2] = {img0, img1};
+    for (int v = 0; v < 2; ++v) {
+        CK(pm_launch_prep((const float4*)im[v], pitch / 16, W, H, ctx->col[v], ctx->grad[v], ctx->wgt[v], st), "prep");
+        if (p.arith == CVTPM_ARITH_FAST)
+            CK(pm_launch_records(ctx->col[v], ctx->grad[v], W, H, ctx->recA[v], ctx->recB[v], ctx->recC[v], ctx->recD[v], st), "records");
+    }
+    return CVTPM_OK;
+}
+
+/* PDROF::apply, cvt/gfx/PDROF.h:50-96: u warm-starts from `output`, p from 0. */
+cvtpm_status pd_apply(cvtpm_ctx* ctx, float4* output, const float4* input, const float* wgt, float lambda, int iters,
+                      int W, int H, cudaStream_t st) {
+    const size_t n = (size_t)W * H;
+    CK(cudaMemcpyAsync(ctx->pdT, input, n * 16, cudaMemcpyDeviceToDevice, st), "pd copy");
+    CK(cudaMemsetAsync(ctx->pdP[0], 0, n * 32, st), "pd clear");
+    CK(cudaMemsetAsync(ctx->pdP[1], 0, n * 32, st), "pd clear");
+    float4* img[2] = {ctx->pdT, output};
+    float4* pp[2] = {ctx->pdP[0], ctx->pdP[1]};
+    int swap = 0;
+    for (int i = 0; i < iters; ++i) {
+        swap = i & 1;
+        CK(pm_launch_pd_step(img[swap], pp[swap], img[1 - swap], pp[1 - swap], input, wgt, lambda, W, H, st), "pd step");
+    }
+    if (!swap) CK(pm_launch_pd_step(img[1], pp[1], img[0], pp[0], input, wgt, lambda, W, H, st), "pd step");
+    return CVTPM_OK;
+}
+
+float smoothstep01(float x) {                                      /* cvt/math/Math.h:88-92 */
+    float t = (x < 0.0f) ? 0.0f : (x > 1.0f) ? 1.0f : x;
+    return t * t * (3.0f - 2.0f * t);
+}
+
+cvtpm_status run_depthmap(cvtpm_ctx* ctx, const cvtpm_params& p, float* dmap, size_t dpitch, const float* left,
+                          const float* right, int W, int H, size_t pitch, float* nmap, size_t npitch,
+                          const cvtpm_trace* trace, cudaStream_t st) {
+    cvtpm_status s;
+    if ((s = check_params(ctx, p)) != CVTPM_OK) return s;
+    if ((s = check_image(ctx, left, W, H, pitch, "left")) != CVTPM_OK) return s;
+    if ((s = check_image(ctx, right, W, H, pitch, "right")) != CVTPM_OK) return s;
+    if (!dmap) return fail(ctx, CVTPM_ERR_INVALID_ARGUMENT, "dmap is NULL");
+    if (dpitch % 4 != 0 || dpitch < (size_t)W * 4) return fail(ctx, CVTPM_ERR_INVALID_ARGUMENT, "dmap pitch");
+    if (nmap && (npitch % 16 != 0 || npitch < (size_t)W * 16)) return fail(ctx, CVTPM_ERR_INVALID_ARGUMENT, "normalmap pitch");
+    CK(cudaSetDevice(ctx->device), "cudaSetDevice");
+    if ((s = ensure_buffers(ctx, W, H)) != CVTPM_OK) return s;
+    if ((s = ensure_tables(ctx, p, st)) != CVTPM_OK) return s;
+    if ((s = prep_views(ctx, p, left, right, W, H, pitch, st)) != CVTPM_OK) return s;
+
+    const size_t n = (size_t)W * H;
+    const bool exact = p.arith == CVTPM_ARITH_EXACT;
+    const float dmax = p.depthmax;
+    const float dscale = p.dscale <= 0.0f ? 1.0f / dmax : p.dscale;
+    const int N = p.iterations;
+    PmPassArgs aL = base_args(ctx, p, W, H, 0), aR = base_args(ctx, p, W, H, 1);
+
+    aL.out = ctx->S[0][0];                                         /* :124-143 */
+    CK(pm_launch_init(aL, exact, st), "init");
+    aR.out = ctx->S[1][0];
+    CK(pm_launch_init(aR, exact, st), "init");
+    CK(cudaMemsetAsync(ctx->smooth[0], 0, n * 16, st), "clear");   /* :108-113 */
+    CK(cudaMemsetAsync(ctx->smooth[1], 0, n * 16, st), "clear");
+    CK(cudaMemsetAsync(ctx->list[1], 0xFF, n * 8, st), "clear");   /* :145-149 */
+
+    float theta = 0.0f;
+    for (int iter = 0; iter < N; ++iter) {                         /* :151-266 */
+        const int sw = iter & 1;
+        aL.iter = aR.iter = iter;
+        aL.theta = aR.theta = theta;
+        aL.old = ctx->S[0][sw]; aL.out = ctx->S[0][1 - sw]; aL.smooth = ctx->smooth[0];
+        aL.viewin = ctx->list[1]; aL.viewsrc = ctx->S[1][sw]; aL.winners = ctx->win[0];
+        CK(pm_launch_propagate(aL, exact, st), "propagate left");
+        CK(pm_launch_view_list(ctx->S[0][1 - sw], W, H, ctx->list[0], st), "view list");
+        aR.old = ctx->S[1][sw]; aR.out = ctx->S[1][1 - sw]; aR.smooth = ctx->smooth[1];
+        aR.viewin = ctx->list[0]; aR.viewsrc = ctx->S[0][1 - sw]; aR.winners = ctx->win[1];
+        CK(pm_launch_propagate(aR, exact, st), "propagate right");
+        CK(pm_launch_view_list(ctx->S[1][1 - sw], W, H, ctx->list[1], st), "view list");
+        const float lambda = theta * p.thetascale + 5.0f;
+        for (int v = 0; v < 2; ++v) {                              /* :228-261 */
+            CK(pm_launch_consistency(ctx->S[v][1 - sw], ctx->S[1 - v][1 - sw], W, H, p.maxdispdiff, p.maxanglediff,
+                                     v == 0 ? 1 : 0, ctx->tmp, nullptr, st), "consistency");
+            CK(pm_launch_fill_state(ctx->tmp, W, H, dmax, v == 0 ? 1 : 0, ctx->tmp2, st), "fill");
+            if ((s = pd_apply(ctx, ctx->smooth[v], ctx->tmp2, ctx->wgt[v], lambda, p.pd_iterations, W, H, st)) != CVTPM_OK)
+                return s;
+        }
+        if (iter >= 5) theta = smoothstep01(((float)iter - 5.0f) / ((float)N - 5.0f)) * 1.0f;
+    }
+    const int fin = 1 - ((N - 1) & 1);                              /* :268-290 */
+    CK(pm_launch_consistency(ctx->S[0][fin], ctx->S[1][fin], W, H, p.maxdispdiff, p.maxanglediff, 1, ctx->tmp,
+                             ctx->valid, st), "consistency");
+    CK(pm_launch_fill_output(ctx->tmp, W, H, dscale, dmap, dpitch / 4, (float4*)nmap, npitch / 16, st), "fill output");
+    if (trace) {
+        if (trace->winners) {
+            CK(cudaMemcpyAsync(trace->winners, ctx->win[0], n, cudaMemcpyDeviceToDevice, st), "trace");
+            CK(cudaMemcpyAsync(trace->winners + n, ctx->win[1], n, cudaMemcpyDeviceToDevice, st), "trace");
+        }
+        if (trace->valid) CK(cudaMemcpyAsync(trace->valid, ctx->valid, n, cudaMemcpyDeviceToDevice, st), "trace");
+        if (trace->states) {
+            CK(cudaMemcpyAsync(trace->states, ctx->S[0][fin], n * 16, cudaMemcpyDeviceToDevice, st), "trace");
+            CK(cudaMemcpyAsync(trace->states + 4 * n, ctx->S[1][fin], n * 16, cudaMemcpyDeviceToDevice, st), "trace");
+        }
+    }
+    return CVTPM_OK;
+}
+
+}  // namespace
+
+/* ====================================================== public API === */
+extern "C" {
+
+const char* cvtpm_version(void) { return CVTPM_VERSION; }
+
+const char* cvtpm_status_string(cvtpm_status s) {
+    switch (s) {
+        case CVTPM_OK: return "ok";
+        case CVTPM_ERR_INVALID_ARGUMENT: return "invalid argument";
+        case CVTPM_ERR_SIZE: return "size out of range";
+        case CVTPM_ERR_INCONSISTENT: return "left/right images inconsistent";
+        case CVTPM_ERR_CUDA: return "CUDA error";
+        case CVTPM_ERR_ALLOC: return "device allocation failed";
+        case CVTPM_ERR_TIMEOUT: return "device wait timed out";
+        case CVTPM_ERR_NOT_SUPPORTED: return "not supported";
+    }
+    return "unknown status";
+}
+
+cvtpm_status cvtpm_params_default(cvtpm_params* p, int preset) {
+    if (!p) return CVTPM_ERR_INVALID_ARGUMENT;
+    memset(p, 0, sizeof(*p));
+    p->patchsize = 17;
+    p->depthmax = 64.0f;
+    p->iterations = 3;
+    p->viewsamples = 4;
+    p->dscale = -1.0f;
+    p->maxdispdiff = 0.5f;
+    p->maxanglediff = 10.0f;
+    p->thetascale = 50.0f;
+    p->pd_iterations = 250;
+    p->color_weight = 26.0f;
+    p->color_alpha = 0.05f;
+    p->color_maxdiff = 0.04f;
+    p->grad_maxdiff = 0.01f;
+    p->weight_profile = CVTPM_PROFILE_SMOOTHSTEP;
+    p->rng = CVTPM_RNG_MWC64X;
+    p->seed = 0;
+    p->arith = CVTPM_ARITH_EXACT;
+    p->schedule = CVTPM_SCHEDULE_JACOBI;
+    if (preset == CVTPM_PRESET_BASELINE) {
+        p->color_weight = 25.5f;
+        p->weight_profile = CVTPM_PROFILE_CONSTANT;
+        p->color_alpha = 0.1f;
+        p->color_maxdiff = 10.0f / 255.0f;
+        p->grad_maxdiff = 2.0f / 255.0f;
+        p->rng = CVTPM_RNG_PHILOX;
+        p->seed = 0x5EED0000CAFEull;
+        p->arith = CVTPM_ARITH_FAST;
+    } else if (preset != CVTPM_PRESET_REFERENCE) {
+        return CVTPM_ERR_INVALID_ARGUMENT;
+    }
+    return CVTPM_OK;
+}
+
+cvtpm_status cvtpm_create(cvtpm_ctx** out, int device) {
+    if (!out) return CVTPM_ERR_INVALID_ARGUMENT;
+    *out = nullptr;
+    int n = 0;
+    cudaError_t e = cudaGetDeviceCount(&n);
+    if (e != cudaSuccess) return CVTPM_ERR_CUDA;
+    if (device < 0 || device >= n) return CVTPM_ERR_INVALID_ARGUMENT;
+    cvtpm_ctx* c = new (std::nothrow) cvtpm_ctx();
+    if (!c) return CVTPM_ERR_ALLOC;
+    c->device = device;
+    cvtpm_params_default(&c->prm, CVTPM_PRESET_REFERENCE);
+    *out = c;
+    return CVTPM_OK;
+}
+
+cvtpm_status cvtpm_destroy(cvtpm_ctx* ctx) {
+    if (!ctx) return CVTPM_ERR_INVALID_ARGUMENT;
+    cudaSetDevice(ctx->device);
+    if (ctx->pool) cudaFree(ctx->pool);
+    if (ctx->stage) cudaFree(ctx->stage);
+    delete ctx;
+    return CVTPM_OK;
+}
+
+cvtpm_status cvtpm_set_params(cvtpm_ctx* ctx, const cvtpm_params* p) {
+    if (!ctx || !p) return CVTPM_ERR_INVALID_ARGUMENT;
+    cvtpm_status s = check_params(ctx, *p);
+    if (s != CVTPM_OK) return s;
+    ctx->prm = *p;
+    return CVTPM_OK;
+}
+
+cvtpm_status cvtpm_get_params(const cvtpm_ctx* ctx, cvtpm_params* p) {
+    if (!ctx || !p) return CVTPM_ERR_INVALID_ARGUMENT;
+    *p = ctx->prm;
+    return CVTPM_OK;
+}
+
+const char* cvtpm_last_error(const cvtpm_ctx* ctx) { return ctx ? ctx->err.c_str() : "null context"; }
+
+cvtpm_status cvtpm_synchronize(cvtpm_ctx* ctx, void* stream) {
+    if (!ctx) return CVTPM_ERR_INVALID_ARGUMENT;
+    CK(cudaStreamSynchronize((cudaStream_t)stream), "synchronize");
+    return CVTPM_OK;
+}
+
+cvtpm_status cvtpm_depthmap(cvtpm_ctx* ctx, float* dmap, size_t dmap_pitch, const float* left, const float* right,
+                            int width, int height, size_t pitch, int patchsize, float depthmax, int iterations,
+                            int viewsamples, float dscale, float* normalmap, size_t normalmap_pitch,
+                            const cvtpm_trace* trace, void* stream) {
+    if (!ctx) return CVTPM_ERR_INVALID_ARGUMENT;
+    (void)viewsamples;   /* ignored, as in the reference (4 slots, pmhstereo.cl:40) */
+    cvtpm_params p = ctx->prm;
+    p.patchsize = patchsize;
+    p.depthmax = depthmax;
+    p.iterations = iterations;
+    p.dscale = dscale;
+    return run_depthmap(ctx, p, dmap, dmap_pitch, left, right, width, height, pitch, normalmap, normalmap_pitch,
+                        trace, (cudaStream_t)stream);
+}
+
+cvtpm_status cvtpm_depthmap_host(cvtpm_ctx* ctx, float* dmap, size_t dmap_pitch, const float* left,
+                                 const float* right, int width, int height, size_t pitch, int patchsize,
+                                 float depthmax, int iterations, int viewsamples, float dscale, float* normalmap,
+                                 size_t normalmap_pitch, void* stream) {
+    if (!ctx) return CVTPM_ERR_INVALID_ARGUMENT;
+    if (!left || !right || !dmap) return fail(ctx, CVTPM_ERR_INVALID_ARGUMENT, "null host pointer");
+    if (width < 1 || height < 1 || width > PM_MAX_WIDTH || height > 65535) return fail(ctx, CVTPM_ERR_SIZE, "image size out of range");
+    if (pitch < (size_t)width * 16 || dmap_pitch < (size_t)width * 4) return fail(ctx, CVTPM_ERR_INVALID_ARGUMENT, "pitch");
+    if (normalmap && normalmap_pitch < (size_t)width * 16) return fail(ctx, CVTPM_ERR_INVALID_ARGUMENT, "normalmap pitch");
+    cudaStream_t st = (cudaStream_t)stream;
+    CK(cudaSetDevice(ctx->device), "cudaSetDevice");
+    const size_t n = (size_t)width * height;
+    const size_t need = n * 16 * 2 + n * 4 + (normalmap ? n * 16 : 0) + 1024;
+    if (need > ctx->stage_bytes) {
+        if (ctx->stage) { cudaFree(ctx->stage); ctx->stage = nullptr; ctx->stage_bytes = 0; }
+        cudaError_t e = cudaMalloc(&ctx->stage, need);
+        if (e != cudaSuccess) { ctx->stage = nullptr; return fail(ctx, CVTPM_ERR_ALLOC, "staging allocation"); }
+        ctx->stage_bytes = need;
+    }
+    float* dL = (float*)ctx->stage;
+    float* dR = dL + n * 4;
+    float* dD = dR + n * 4;
+    float* dN = normalmap ? (float*)((char*)ctx->stage + align_up((n * 16 * 2 + n * 4), 256)) : nullptr;
+    const size_t row = (size_t)width * 16;
+    CK(cudaMemcpy2DAsync(dL, row, left, pitch, row, height, cudaMemcpyHostToDevice, st), "H2D left");
+    CK(cudaMemcpy2DAsync(dR, row, right, pitch, row, height, cudaMemcpyHostToDevice, st), "H2D right");
+    cvtpm_status s = cvtpm_depthmap(ctx, dD, (size_t)width * 4, dL, dR, width, height, row, patchsize, depthmax,
+                                    iterations, viewsamples, dscale, dN, row, nullptr, stream);
+    if (s != CVTPM_OK) return s;
+    CK(cudaMemcpy2DAsync(dmap, dmap_pitch, dD, (size_t)width * 4, (size_t)width * 4, height, cudaMemcpyDeviceToHost, st), "D2H dmap");
+    if (normalmap)
+        CK(cudaMemcpy2DAsync(normalmap, normalmap_pitch, dN, row, row, height, cudaMemcpyDeviceToHost, st), "D2H normalmap");
+    CK(cudaStreamSynchronize(st), "synchronize");
+    return CVTPM_OK;
+}
+
+cvtpm_status cvtpm_cost_eval(cvtpm_ctx* ctx, const float* img1, const float* img2, int width, int height,
+                             size_t pitch, const float* states, int lr, float* cost, void* stream) {
+    if (!ctx) return CVTPM_ERR_INVALID_ARGUMENT;
+    cvtpm_status s;
+    const cvtpm_params& p = ctx->prm;
+    if ((s = check_params(ctx, p)) != CVTPM_OK) return s;
+    if ((s = check_image(ctx, img1, width, height, pitch, "img1")) != CVTPM_OK) return s;
+    if ((s = check_image(ctx, img2, width, height, pitch, "img2")) != CVTPM_OK) return s;
+    if (!states || !cost) return fail(ctx, CVTPM_ERR_INVALID_ARGUMENT, "null states/cost");
+    (void)lr;   /* the cost does not depend on the view flag (pmhstereo.cl:170-228) */
+    cudaStream_t st = (cudaStream_t)stream;
+    CK(cudaSetDevice(ctx->device), "cudaSetDevice");
+    if ((s = ensure_buffers(ctx, width, height)) != CVTPM_OK) return s;
+    if ((s = ensure_tables(ctx, p, st)) != CVTPM_OK) return s;
+    if ((s = prep_views(ctx, p, img1, img2, width, height, pitch, st)) != CVTPM_OK) return s;
+    PmPassArgs a = base_args(ctx, p, width, height, 0);
+    CK(pm_launch_cost_field(a, p.arith == CVTPM_ARITH_EXACT, (const float4*)states, cost, st), "cost field");
+    return CVTPM_OK;
+}
+
+cvtpm_status cvtpm_cost_adjoint(cvtpm_ctx* ctx, const float*, const float*, int, int, size_t, const float*, int,
+                                const float*, float*, float*, float*, float*, void*) {
+    return fail(ctx, CVTPM_ERR_NOT_SUPPORTED, "cost adjoint not built yet");
+}
+
+cvtpm_status cvtpm_depthmap_batched(cvtpm_ctx* ctx, const cvtpm_pair*, int, void*) {
+    return fail(ctx, CVTPM_ERR_NOT_SUPPORTED, "batched path not built yet");
+}
+
+}  // extern "C"

@@ -1,0 +1,317 @@
+/*
+ * pm_device.cuh — device-side building blocks of the PatchMatch kernels:
+ * float4 helpers, the plane-state algebra of cvt/cl/kernel/pmhstereo.cl,
+ * the two random streams and the aggregated ASW cost.
+ *
+ * All of it is compiled with -fmad=false: an expression such as a*b + c is two
+ * IEEE operations, exactly as in the reference's OpenCL source read literally;
+ * fused multiply-adds appear only where fmaf() is written.
+ */
+#ifndef CVT_GB300_PM_DEVICE_CUH
+#define CVT_GB300_PM_DEVICE_CUH
+
+#include <stdint.h>
+#include <cuda_runtime.h>
+#include "pm_math.h"
+
+#define PM_DEV __device__ __forceinline__
+
+/* ------------------------------------------------------------ float4 -- */
+PM_DEV float4 f4(float x, float y, float z, float w) { return make_float4(x, y, z, w); }
+PM_DEV float4 f4s(float s) { return make_float4(s, s, s, s); }
+PM_DEV float4 operator+(float4 a, float4 b) { return f4(a.x + b.x, a.y + b.y, a.z + b.z, a.w + b.w); }
+PM_DEV float4 operator-(float4 a, float4 b) { return f4(a.x - b.x, a.y - b.y, a.z - b.z, a.w - b.w); }
+PM_DEV float4 operator*(float4 a, float4 b) { return f4(a.x * b.x, a.y * b.y, a.z * b.z, a.w * b.w); }
+PM_DEV float4 operator/(float4 a, float4 b) { return f4(a.x / b.x, a.y / b.y, a.z / b.z, a.w / b.w); }
+PM_DEV float4 operator*(float s, float4 a) { return f4(s * a.x, s * a.y, s * a.z, s * a.w); }
+PM_DEV bool finite3(float4 s) { return isfinite(s.x) && isfinite(s.y) && isfinite(s.z); }
+PM_DEV float len4(float4 a) { return pm_sqrt(((a.x * a.x + a.y * a.y) + a.z * a.z) + a.w * a.w); }
+PM_DEV float len3(float4 a) { return pm_sqrt((a.x * a.x + a.y * a.y) + a.z * a.z); }
+PM_DEV float dot4(float4 a, float4 b) { return ((a.x * b.x + a.y * b.y) + a.z * b.z) + a.w * b.w; }
+PM_DEV int clampi(int v, int lo, int hi) { return v < lo ? lo : (v > hi ? hi : v); }
+PM_DEV int f2i_nan0(float v) { return (v != v) ? 0 : (int)v; }
+
+/* ---------------------------------------------------------------- RNG -- */
+/* MWC64X (cvt/cl/kernel/RNG.cl:35-156).  The skip-ahead A^d mod M
+ * (RNG.cl:66-84) multiplies table entries A^(2^k) mod M for the set bits of d;
+ * each 64x64 -> 128-bit product is reduced with 2^64 = M + E exactly, so the
+ * residue equals the reference's bit-serial MulMod64. */
+#define PM_MWC_A 4294883355u
+#define PM_MWC_M 18446383549859758079ull
+#define PM_MWC_E 360523849793537ull   /* 2^64 - M */
+#define PM_MWC_BASEID 4077358422479273989ull
+
+/* The constant tables are defined in the kernels' translation unit only
+ * (pm_kernels.cu defines PM_KERNELS_TU); other units include this header for
+ * the host-visible types. */
+#ifdef PM_KERNELS_TU
+__constant__ unsigned long long c_mwc_pow2[64];   /* A^(2^k) mod M */
+#endif
+
+PM_DEV unsigned long long mwc_mulmod(unsigned long long a, unsigned long long b) {
+    unsigned long long lo = a * b;
+    unsigned long long hi = __umul64hi(a, b);
+#pragma unroll 1
+    for (int i = 0; i < 8 && hi != 0ull; ++i) {      /* hi*2^64 == hi*E (mod M) */
+        unsigned long long l = hi * PM_MWC_E;
+        unsigned long long h = __umul64hi(hi, PM_MWC_E);
+        unsigned long long s = lo + l;
+        h += (s < lo) ? 1ull : 0ull;
+        lo = s;
+        hi = h;
+    }
+    if (lo >= PM_MWC_M) lo -= PM_MWC_M;
+    return lo;
+}
+
+struct PmRng {
+    uint32_t a, b;          /* MWC64X: x, c.  Philox: draw index, unused */
+    uint32_t ctr0, ctr1, ctr2, key0, key1;
+    uint32_t buf[4];
+    int kind;
+};
+
+#ifdef PM_KERNELS_TU
+PM_DEV void mwc_seed(PmRng& r, unsigned long long distance) {
+    unsigned long long m = 1ull;
+#pragma unroll 1
+    for (int k = 0; k < 64 && distance != 0ull; ++k, distance >>= 1)
+        if (distance & 1ull) m = mwc_mulmod(m, c_mwc_pow2[k]);
+    unsigned long long v = mwc_mulmod(PM_MWC_BASEID, m);
+    r.kind = 0;
+    r.a = (uint32_t)(v / PM_MWC_A);
+    r.b = (uint32_t)(v % PM_MWC_A);
+}
+#endif
+
+PM_DEV void philox10(uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3, uint32_t k0, uint32_t k1, uint32_t out[4]) {
+#pragma unroll
+    for (int r = 0; r < 10; ++r) {
+        uint32_t hi0 = __umulhi(0xD2511F53u, c0), lo0 = 0xD2511F53u * c0;
+        uint32_t hi1 = __umulhi(0xCD9E8D57u, c2), lo1 = 0xCD9E8D57u * c2;
+        uint32_t n0 = hi1 ^ c1 ^ k0, n2 = hi0 ^ c3 ^ k1;
+        c0 = n0; c1 = lo1; c2 = n2; c3 = lo0;
+        k0 += 0x9E3779B9u; k1 += 0xBB67AE85u;
+    }
+    out[0] = c0; out[1] = c1; out[2] = c2; out[3] = c3;
+}
+
+#define PM_PHILOX_TAG_INIT 0xFFFFFFFFu
+
+PM_DEV void philox_seed(PmRng& r, uint32_t key0, uint32_t key1, uint32_t pixel, uint32_t tag, uint32_t view) {
+    r.kind = 1;
+    r.a = 0;
+    r.ctr0 = pixel; r.ctr1 = tag; r.ctr2 = view;
+    r.key0 = key0; r.key1 = key1;
+}
+
+PM_DEV float rng_float(PmRng& r) {
+    uint32_t res;
+    if (r.kind == 0) {                                  /* RNG.cl:108-118,142-147 */
+        uint32_t X = r.a, C = r.b;
+        res = X ^ C;
+        uint32_t Xn = PM_MWC_A * X + C;
+        uint32_t carry = (uint32_t)(Xn < C);
+        r.b = __umulhi(PM_MWC_A, X) + carry;
+        r.a = Xn;
+    } else {
+        if ((r.a & 3u) == 0u) philox10(r.ctr0, r.ctr1, r.ctr2, r.a >> 2, r.key0, r.key1, r.buf);
+        uint32_t i = r.a & 3u;
+        res = (i == 0) ? r.buf[0] : (i == 1) ? r.buf[1] : (i == 2) ? r.buf[2] : r.buf[3];
+        r.a++;
+    }
+    return 2.3283064365386962890625e-10f * __uint2float_rn(res);
+}
+
+/* ------------------------------------------------------ plane algebra -- */
+PM_DEV float4 viewprop(float4 n) { return f4(1.0f / n.x, -n.y / n.x, -n.z / n.x, 0.0f); }   /* :119-124 */
+PM_DEV float transform_x(float4 s, float cx, float cy) { return s.x * cx + s.y * cy + s.z; } /* :126-129 */
+
+PM_DEV float4 state_init(PmRng& rng, float cx, float cy, int lr, float normmul, float depthmax) { /* :50-68 */
+    float z = rng_float(rng) * depthmax;
+    float nx = (rng_float(rng) - 0.5f) * normmul * 0.95f;
+    float ny = (rng_float(rng) - 0.5f) * normmul * 0.95f;
+    nx = pm_clamp(nx, -0.95f, 0.95f);
+    ny = pm_clamp(ny, -0.95f, 0.95f);
+    float nfactor = fmaxf(pm_sqrt(nx * nx + ny * ny) + 0.001f, 1.0f);
+    nx = nx / nfactor; ny = ny / nfactor;
+    float nz = pm_sqrt(1.0f - nx * nx - ny * ny);
+    float4 ret = f4(1.0f - (-nx / nz), 0.0f - (-ny / nz), 0.0f - ((nx * cx + ny * cy) / nz + z), 0.0f - 0.0f);
+    if (!lr) ret = viewprop(ret);
+    return ret;
+}
+
+PM_DEV float4 to_ref_normal_depth(float4 state, float cx, float cy, int lr) {       /* :70-86 */
+    float4 s = lr ? state : viewprop(state);
+    s = f4(1.0f - s.x, 0.0f - s.y, 0.0f - s.z, 0.0f - s.w);
+    float4 ret;
+    ret.w = s.x * cx + s.y * cy + s.z;
+    ret.z = pm_rsqrt(s.x * s.x + s.y * s.y + 1.0f);
+    ret.x = -s.x * ret.z;
+    ret.y = -s.y * ret.z;
+    if (!finite3(ret)) return f4(0.0f, 0.0f, 1.0f, 0.0f);
+    return ret;
+}
+
+PM_DEV float4 state_refine(PmRng& rng, float4 in, float cx, float cy, float depthmax, int lr) { /* :88-117 */
+    float4 state = lr ? in : viewprop(in);
+    state = f4(1.0f - state.x, 0.0f - state.y, 0.0f - state.z, 0.0f - state.w);
+    float z = state.x * cx + state.y * cy + state.z;
+    float nz = pm_rsqrt(state.x * state.x + state.y * state.y + 1.0f);
+    float nx = -state.x * nz;
+    float ny = -state.y * nz;
+    z += (rng_float(rng) - 0.5f) * 2.0f;
+    z = pm_clamp(z, 0.0f, depthmax);
+    nx += (rng_float(rng) - 0.5f) * 0.1f;
+    ny += (rng_float(rng) - 0.5f) * 0.1f;
+    nx = pm_clamp(nx, -0.95f, 0.95f);
+    ny = pm_clamp(ny, -0.95f, 0.95f);
+    float nfactor = fmaxf(pm_sqrt(nx * nx + ny * ny) + 0.001f, 1.0f);
+    nx = nx / nfactor; ny = ny / nfactor;
+    nz = pm_sqrt(1.0f - nx * nx - ny * ny);
+    float4 ret = f4(-nx / nz, -ny / nz, (nx * cx + ny * cy) / nz + z, 0.0f);
+    ret = f4(1.0f - ret.x, 0.0f - ret.y, 0.0f - ret.z, 0.0f - ret.w);
+    if (!lr) return viewprop(state);   /* the reference's right-view branch (:114-115) */
+    return ret;
+}
+
+PM_DEV void to_normal(float4 st, float& nx, float& ny, float& nz) {               /* :144-153 */
+    float4 s = f4(1.0f - st.x, 0.0f - st.y, 0.0f - st.z, 0.0f - st.w);
+    nz = pm_rsqrt(s.x * s.x + s.y * s.y + 1.0f);
+    nx = -s.x * nz;
+    ny = -s.y * nz;
+}
+
+PM_DEV void smooth_distance(float4 sa, float4 sb, float4 smooth, float cx, float cy, float depthmax,
+                            int lr, float& dA, float& dB) {                      /* :266-283 */
+    float4 a = to_ref_normal_depth(sa, cx, cy, lr);
+    float4 b = to_ref_normal_depth(sb, cx, cy, lr);
+    float4 diag = f4(1.0f, 1.0f, 0.0f, 1.0f / (depthmax * depthmax));
+    if (!finite3(sa) || !finite3(sb)) { dA = 0.0f; dB = 0.0f; return; }
+    float4 da = a - smooth;
+    dA = dot4(da, diag * da);
+    float4 db = b - smooth;
+    dB = dot4(db, diag * db);
+}
+
+/* -------------------------------------------------------------- cost -- */
+/* Spatial ASW profile, indexed (dy+31)*63 + (dx+31). */
+#define PM_PMAX 31
+#define PM_PROF_N (2 * PM_PMAX + 1)
+#ifdef PM_KERNELS_TU
+__constant__ float c_prof[PM_PROF_N * PM_PROF_N];
+#endif
+
+struct PmView {
+    const float4* col;    /* RGBA, tight rows          */
+    const float4* grad;   /* (dx, dy, dxy, dyx)         */
+    const float4* recA;   /* fast records: (c0,c1,c2,g0) */
+    const float4* recB;   /*               (g1,g2,g3,dc0) */
+    const float4* recC;   /*               (dc1,dc2,dg0,dg1) */
+    const float2* recD;   /*               (dg2,dg3)      */
+};
+
+struct PmCostConsts {
+    int W, H, P;
+    float Wf, Hf;
+    float alpha, oma, cmax, gmax;
+};
+
+#ifdef PM_KERNELS_TU
+/* Aggregated ASW cost (patch_eval_color_grad_weighted, pmhstereo.cl:170-228)
+ * of K candidate planes at pixel (x, y), sharing the image-1 reads and the
+ * bilateral weight of every tap.  Each candidate's sum is accumulated in the
+ * reference's tap order, so its value equals a separate evaluation.
+ * Candidates with act[k] == false contribute nothing and return 1e5. */
+template <int K, bool EXACT>
+PM_DEV void eval_costs(const PmCostConsts& k, const PmView& v1, const PmView& v2, int x, int y,
+                       const float4 (&s)[K], const bool (&act)[K], float (&cost)[K]) {
+    float sx[K], sy[K], sz[K];
+    bool live[K];
+#pragma unroll
+    for (int c = 0; c < K; ++c) {
+        live[c] = act[c] && finite3(s[c]);
+        sx[c] = live[c] ? s[c].x : 0.0f;
+        sy[c] = live[c] ? s[c].y : 0.0f;
+        sz[c] = live[c] ? s[c].z : -1.0e30f;    /* never inside [0, W) */
+    }
+    float ws[K], r1[K], r2[K];
+#pragma unroll
+    for (int c = 0; c < K; ++c) { ws[c] = 0.0f; r1[c] = 0.0f; r2[c] = 0.0f; }
+    const float4 vc = __ldg(&v1.col[(size_t)y * k.W + x]);
+    const int P = k.P;
+    for (int dy = -P; dy <= P; ++dy) {
+        const int qy = y + dy;
+        if (qy < 0 || qy >= k.H) continue;
+        const float qyf = (float)qy;
+        const float4* c1row = v1.col + (size_t)qy * k.W;
+        const float4* g1row = v1.grad + (size_t)qy * k.W;
+        const float* prow = c_prof + (dy + PM_PMAX) * PM_PROF_N + PM_PMAX;
+        float rowb[K];
+        if (!EXACT) {
+#pragma unroll
+            for (int c = 0; c < K; ++c) rowb[c] = fmaf(sy[c], qyf, sz[c]);
+        }
+        for (int dx = -P; dx <= P; ++dx) {
+            const int qx = x + dx;
+            if (qx < 0 || qx >= k.W) continue;
+            const float qxf = (float)qx;
+            const float4 a1 = __ldg(&c1row[qx]);
+            const float4 g1 = __ldg(&g1row[qx]);
+            const float d = (fabsf(vc.x - a1.x) + fabsf(vc.y - a1.y)) + fabsf(vc.z - a1.z);
+            const float w1 = pm_exp(-d * prow[dx]);
+#pragma unroll
+            for (int c = 0; c < K; ++c) {
+                if (EXACT) {
+                    const float xp = sx[c] * qxf + sy[c] * qyf + sz[c];
+                    if (!(xp >= 0.0f && xp < k.Wf)) continue;
+                    ws[c] += w1;
+                    const float u = xp + 0.5f;
+                    const float t = u - 0.5f;
+                    const float fi = floorf(t);
+                    const float a = t - fi;
+                    const int i0 = clampi((int)fi, 0, k.W - 1);
+                    const int i1 = clampi((int)fi + 1, 0, k.W - 1);
+                    const size_t rb = (size_t)qy * k.W;
+                    const float4 c0 = __ldg(&v2.col[rb + i0]), cc1 = __ldg(&v2.col[rb + i1]);
+                    const float4 h0 = __ldg(&v2.grad[rb + i0]), h1 = __ldg(&v2.grad[rb + i1]);
+                    const float oa = 1.0f - a;
+                    const float a2x = oa * c0.x + a * cc1.x, a2y = oa * c0.y + a * cc1.y, a2z = oa * c0.z + a * cc1.z;
+                    const float g2x = oa * h0.x + a * h1.x, g2y = oa * h0.y + a * h1.y;
+                    const float g2z = oa * h0.z + a * h1.z, g2w = oa * h0.w + a * h1.w;
+                    const float cc = (fminf(fabsf(a1.x - a2x), k.cmax) + fminf(fabsf(a1.y - a2y), k.cmax)) + fminf(fabsf(a1.z - a2z), k.cmax);
+                    const float gc = ((fminf(fabsf(g1.x - g2x), k.gmax) + fminf(fabsf(g1.y - g2y), k.gmax)) + fminf(fabsf(g1.z - g2z), k.gmax)) + fminf(fabsf(g1.w - g2w), k.gmax);
+                    const float C = k.alpha * cc + k.oma * gc;
+                    r1[c] += w1 * C;
+                } else {
+                    const float xp = fmaf(sx[c], qxf, rowb[c]);
+                    if (!(xp >= 0.0f && xp < k.Wf)) continue;
+                    const float fi = floorf(xp);
+                    const float a = xp - fi;
+                    const size_t j = (size_t)qy * k.W + (int)fi;
+                    const float4 A = __ldg(&v2.recA[j]);
+                    const float4 B = __ldg(&v2.recB[j]);
+                    const float4 Cc = __ldg(&v2.recC[j]);
+                    const float2 D = __ldg(&v2.recD[j]);
+                    const float v0 = fmaf(a, B.w, A.x), v1c = fmaf(a, Cc.x, A.y), v2c = fmaf(a, Cc.y, A.z);
+                    const float u0 = fmaf(a, Cc.z, A.w), u1 = fmaf(a, Cc.w, B.x), u2 = fmaf(a, D.x, B.y), u3 = fmaf(a, D.y, B.z);
+                    const float cc = (fminf(fabsf(a1.x - v0), k.cmax) + fminf(fabsf(a1.y - v1c), k.cmax)) + fminf(fabsf(a1.z - v2c), k.cmax);
+                    const float gc = ((fminf(fabsf(g1.x - u0), k.gmax) + fminf(fabsf(g1.y - u1), k.gmax)) + fminf(fabsf(g1.z - u2), k.gmax)) + fminf(fabsf(g1.w - u3), k.gmax);
+                    r1[c] = fmaf(w1, cc, r1[c]);
+                    r2[c] = fmaf(w1, gc, r2[c]);
+                    ws[c] = ws[c] + w1;
+                }
+            }
+        }
+    }
+#pragma unroll
+    for (int c = 0; c < K; ++c) {
+        float v;
+        if (EXACT) v = r1[c] / ws[c];
+        else v = fmaf(k.alpha, r1[c], k.oma * r2[c]) / ws[c];
+        cost[c] = (!live[c] || ws[c] <= 1.1f) ? 1e5f : v;
+    }
+}
+#endif
+
+#endif

@@ -1,0 +1,498 @@
+/*
+ * pm_kernels.cu — CUDA kernels of the plain PatchMatch path (sm_103a).
+ *
+ * Kernel                 reference
+ *  k_prep               pmhstereo_gradxy + pmhstereo_weight (pmhstereo.cl:737-831), input copy
+ *  k_records            (fast arithmetic only) value/forward-difference records of a view
+ *  k_init<EXACT>        pmhstereo_init (:230-248)
+ *  k_propagate<EXACT>   pmhstereo_propagate_view (:286-404) without the scatter
+ *  k_view_list          the scatter of :391-400, made deterministic (smallest source x first)
+ *  k_consistency        pmhstereo_consistency (:428-464)
+ *  k_fill_state         pmhstereo_fill_state (:466-510)
+ *  k_pd_step            PDHuberWeighted (PDHuberWeighted.cl:34-104)
+ *  k_fill_output        pmhstereo_fill_depthmap / fill_normalmap (:512-603)
+ *  k_cost_field<EXACT>  the cost of a fixed state field (test/adjoint entry)
+ */
+#define PM_KERNELS_TU 1
+#include "pm_kernels.cuh"
+
+
+/* ------------------------------------------------------------- prep -- */
+#define PREP_T 16
+__global__ void __launch_bounds__(PREP_T * PREP_T)
+k_prep(const float4* __restrict__ img, size_t pitch4, int W, int H,
+       float4* __restrict__ col, float4* __restrict__ grad, float* __restrict__ wgt) {
+    __shared__ float g[PREP_T + 2][PREP_T + 2];
+    const int bx = blockIdx.x * PREP_T - 1, by = blockIdx.y * PREP_T - 1;
+    for (int i = threadIdx.y * PREP_T + threadIdx.x; i < (PREP_T + 2) * (PREP_T + 2); i += PREP_T * PREP_T) {
+        int lx = i % (PREP_T + 2), ly = i / (PREP_T + 2);
+        int x = bx + lx, y = by + ly;
+        float v = 0.0f;                                   /* CLK_ADDRESS_CLAMP: zero outside */
+        if (x >= 0 && y >= 0 && x < W && y < H) {
+            float4 c = img[(size_t)y * pitch4 + x];
+            v = ((c.x * 0.2126f + c.y * 0.7152f) + c.z * 0.0722f) + c.w * 0.0f;
+        }
+        g[ly][lx] = v;
+    }
+    __syncthreads();
+    const int x = blockIdx.x * PREP_T + threadIdx.x, y = blockIdx.y * PREP_T + threadIdx.y;
+    if (x >= W || y >= H) return;
+    const int lx = threadIdx.x + 1, ly = threadIdx.y + 1;
+#define B(dx_, dy_) g[ly + (dy_)][lx + (dx_)]
+    float dx = (B(1, 0) - B(-1, 0)) * 0.5f + (B(1, -1) - B(-1, -1)) * 0.25f + (B(1, 1) - B(-1, 1)) * 0.25f;
+    float dy = (B(0, 1) - B(0, -1)) * 0.5f + (B(-1, 1) - B(-1, -1)) * 0.25f + (B(1, 1) - B(1, -1)) * 0.25f;
+    float dxy = B(1, 1) - B(-1, -1);
+    float dyx = B(-1, 1) - B(1, -1);
+    float ex = B(1, 0) - B(-1, 0);
+    float ey = B(0, -1) - B(0, -1);
+#undef B
+    size_t o = (size_t)y * W + x;
+    col[o] = img[(size_t)y * pitch4 + x];
+    grad[o] = f4(dx, dy, dxy, dyx);
+    wgt[o] = pm_exp(-3.0f * pm_pow(pm_sqrt(ex * ex + ey * ey), 0.8f)) + 0.0001f;
+}
+
+__global__ void k_records(const float4* __restrict__ col, const float4* __restrict__ grad, int W, int H,
+                          float4* __restrict__ A, float4* __restrict__ Bq, float4* __restrict__ C,
+                          float2* __restrict__ D) {
+    const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y;
+    if (x >= W || y >= H) return;
+    const size_t o = (size_t)y * W + x;
+    const size_t o1 = (size_t)y * W + min(x + 1, W - 1);
+    float4 c0 = col[o], c1 = col[o1], g0 = grad[o], g1 = grad[o1];
+    A[o] = f4(c0.x, c0.y, c0.z, g0.x);
+    Bq[o] = f4(g0.y, g0.z, g0.w, c1.x - c0.x);
+    C[o] = f4(c1.y - c0.y, c1.z - c0.z, g1.x - g0.x, g1.y - g0.y);
+    D[o] = make_float2(g1.z - g0.z, g1.w - g0.w);
+}
+
+/* ------------------------------------------------------- init / cost -- */
+PM_DEV void seed_rng(PmRng& rng, const PmPassArgs& a, int x, int y, bool init) {
+    const uint32_t p = (uint32_t)(y * a.k.W + x);
+    if (a.rng == CVTPM_RNG_PHILOX)
+        philox_seed(rng, a.key0, a.key1, p, init ? PM_PHILOX_TAG_INIT : (uint32_t)a.iter, a.lr ? 0u : 1u);
+    else
+        mwc_seed(rng, init ? (unsigned long long)p * 3ull : ((unsigned long long)p + (unsigned long long)a.iter) * 45ull);
+}
+
+template <bool EXACT>
+__global__ void __launch_bounds__(256) k_init(PmPassArgs a) {
+    const int x = blockIdx.x * 32 + threadIdx.x, y = blockIdx.y * 8 + threadIdx.y;
+    if (x >= a.k.W || y >= a.k.H) return;
+    PmRng rng;
+    seed_rng(rng, a, x, y, true);
+    float4 s[1] = {state_init(rng, (float)x, (float)y, a.lr, 1.0f, a.depthmax)};
+    bool act[1] = {true};
+    float c[1];
+    eval_costs<1, EXACT>(a.k, a.v1, a.v2, x, y, s, act, c);
+    s[0].w = c[0];
+    a.out[(size_t)y * a.k.W + x] = s[0];
+}
+
+template <bool EXACT>
+__global__ void __launch_bounds__(256) k_cost_field(PmPassArgs a, const float4* __restrict__ states,
+                                                   float* __restrict__ cost) {
+    const int x = blockIdx.x * 32 + threadIdx.x, y = blockIdx.y * 8 + threadIdx.y;
+    if (x >= a.k.W || y >= a.k.H) return;
+    float4 s[1] = {states[(size_t)y * a.k.W + x]};
+    bool act[1] = {true};
+    float c[1];
+    eval_costs<1, EXACT>(a.k, a.v1, a.v2, x, y, s, act, c);
+    cost[(size_t)y * a.k.W + x] = c[0];
+}
+
+/* --------------------------------------------------------- propagate -- */
+template <bool EXACT>
+__global__ void __launch_bounds__(256) k_propagate(PmPassArgs a) {
+    const int W = a.k.W, H = a.k.H;
+    const int x = blockIdx.x * 32 + threadIdx.x, y = blockIdx.y * 8 + threadIdx.y;
+    const bool inside = x < W && y < H;
+    const int xc = min(x, W - 1), yc = min(y, H - 1);   /* lanes outside still follow the warp */
+    const float cx = (float)xc, cy = (float)yc;
+    const float dmax = a.depthmax, theta = a.theta;
+    const int lr = a.lr;
+    const size_t o = (size_t)yc * W + xc;
+
+    float4 sm = a.smooth[o];                                               /* :320-323 */
+    float nf = fmaxf(pm_sqrt(sm.x * sm.x + sm.y * sm.y) + 0.001f, 1.0f);
+    float smx = sm.x / nf, smy = sm.y / nf;
+    const float4 smooth = f4(smx, smy, pm_sqrt(1.0f - smx * smx - smy * smy), sm.z * dmax);
+    float4 self = a.old[o];
+    int win = 0;
+    PmRng rng;
+    seed_rng(rng, a, xc, yc, false);
+
+    auto accept = [&](float4 cand, float cost, int idx) {
+        cand.w = cost;
+        float da, db;
+        smooth_distance(cand, self, smooth, cx, cy, dmax, lr, da, db);
+        if (cand.w + theta * da <= self.w + theta * db) { self = cand; win = idx; }
+    };
+
+    /* candidates 1-8: the 3x3 neighbourhood of `old`, clamped to the edge (:330-342) */
+#pragma unroll 1
+    for (int b = 0; b < 2; ++b) {
+        float4 s[4]; bool act[4]; float c[4];
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+            int n = b * 4 + i;                 /* 0..7 over the 8 neighbours in raster order */
+            int nn = n < 4 ? n : n + 1;        /* skip the centre */
+            int px = nn % 3 - 1, py = nn / 3 - 1;
+            s[i] = a.old[(size_t)clampi(yc + py, 0, H - 1) * W + clampi(xc + px, 0, W - 1)];
+            act[i] = true;
+        }
+        eval_costs<4, EXACT>(a.k, a.v1, a.v2, xc, yc, s, act, c);
+#pragma unroll
+        for (int i = 0; i < 4; ++i) accept(s[i], c[i], 1 + b * 4 + i);
+    }
+    /* candidate 9: the smoothed plane (:345-352); 10-12: random neighbours (:355-361) */
+    {
+        float4 s[4]; bool act[4] = {true, true, true, true}; float c[4];
+        float4 sc = f4(1.0f - (-smooth.x / smooth.z), 0.0f - (-smooth.y / smooth.z),
+                       0.0f - ((smooth.x * cx + smooth.y * cy) / smooth.z + smooth.w), 0.0f - 0.0f);
+        s[0] = lr ? sc : viewprop(sc);
+#pragma unroll
+        for (int i = 1; i < 4; ++i) {
+            int ox = (int)(rng_float(rng) * 7.0f + 0.5f);
+            int oy = (int)(rng_float(rng) * 7.0f + 0.5f);
+            s[i] = a.old[(size_t)clampi(yc + oy, 0, H - 1) * W + clampi(xc + ox, 0, W - 1)];
+        }
+        eval_costs<4, EXACT>(a.k, a.v1, a.v2, xc, yc, s, act, c);
+#pragma unroll
+        for (int i = 0; i < 4; ++i) accept(s[i], c[i], 9 + i);
+    }
+    /* 13-15: random neighbours; 16: a fresh random plane (:364-368) */
+    {
+        float4 s[4]; bool act[4] = {true, true, true, true}; float c[4];
+#pragma unroll
+        for (int i = 0; i < 3; ++i) {
+            int ox = (int)(rng_float(rng) * 7.0f + 0.5f);
+            int oy = (int)(rng_float(rng) * 7.0f + 0.5f);
+            s[i] = a.old[(size_t)clampi(yc + oy, 0, H - 1) * W + clampi(xc + ox, 0, W - 1)];
+        }
+        s[3] = state_init(rng, cx, cy, lr, 2.0f, dmax);
+        eval_costs<4, EXACT>(a.k, a.v1, a.v2, xc, yc, s, act, c);
+#pragma unroll
+        for (int i = 0; i < 4; ++i) accept(s[i], c[i], 13 + i);
+    }
+    /* 17-20: candidates from the other view (:372-379) */
+    if (a.viewin) {
+        short4 l = a.viewin[o];
+        short li[4] = {l.x, l.y, l.z, l.w};
+        int nview = (li[0] < 0) ? 0 : (li[1] < 0) ? 1 : (li[2] < 0) ? 2 : (li[3] < 0) ? 3 : 4;
+        if (!inside) nview = 0;
+        if (__any_sync(0xffffffffu, nview > 0)) {
+            float4 s[4]; bool act[4]; float c[4];
+#pragma unroll
+            for (int i = 0; i < 4; ++i) {
+                act[i] = i < nview;
+                s[i] = act[i] ? viewprop(a.viewsrc[(size_t)yc * W + li[i]]) : f4s(0.0f);
+            }
+            eval_costs<4, EXACT>(a.k, a.v1, a.v2, xc, yc, s, act, c);
+#pragma unroll
+            for (int i = 0; i < 4; ++i)
+                if (act[i]) accept(s[i], c[i], 17 + i);
+        }
+    }
+    /* 21-22: random refinements of the current best (:383-389) */
+#pragma unroll 1
+    for (int i = 0; i < 2; ++i) {
+        float4 s[1] = {state_refine(rng, self, cx, cy, dmax, lr)};
+        bool act[1] = {true};
+        float c[1];
+        eval_costs<1, EXACT>(a.k, a.v1, a.v2, xc, yc, s, act, c);
+        accept(s[0], c[0], 21 + i);
+    }
+    if (inside) {
+        a.out[o] = self;
+        if (a.winners) a.winners[o] = (uint8_t)win;
+    }
+}
+
+/* -------------------------------------------------------- view lists -- */
+/* One warp per row.  Sources are visited in increasing x; the first four
+ * that map to a target pixel fill its slots in that order (pmhstereo.cl:394-400
+ * executed in raster order). */
+__global__ void __launch_bounds__(32) k_view_list(const float4* __restrict__ src, int W, int H,
+                                                  short4* __restrict__ list) {
+    extern __shared__ int cnt[];
+    const int y = blockIdx.x;
+    const int lane = threadIdx.x;
+    if (y >= H) return;
+    short4* row = list + (size_t)y * W;
+    for (int x = lane; x < W; x += 32) { cnt[x] = 0; row[x] = make_short4(-1, -1, -1, -1); }
+    __syncwarp();
+    const unsigned lt = (1u << lane) - 1u;
+    for (int x0 = 0; x0 < W; x0 += 32) {
+        const int x = x0 + lane;
+        int d = -1;
+        if (x < W) {
+            float4 s = src[(size_t)y * W + x];
+            float v = transform_x(s, (float)x, (float)y) + 0.5f;
+            if (v > -1.0f && v < (float)W) d = (int)v;
+        }
+        const unsigned peers = __match_any_sync(0xffffffffu, d);
+        const int rank = __popc(peers & lt);
+        int base = (d >= 0) ? cnt[d] : 0;
+        __syncwarp();
+        if (d >= 0) {
+            int slot = base + rank;
+            if (slot < 4) reinterpret_cast<short*>(&row[d])[slot] = (short)x;
+            if (rank == 0) cnt[d] = base + __popc(peers);
+        }
+        __syncwarp();
+    }
+}
+
+/* ------------------------------------------------------- consistency -- */
+__global__ void k_consistency(const float4* __restrict__ L, const float4* __restrict__ R, int W, int H,
+                              float maxdisp, float athr, int lr, float4* __restrict__ out,
+                              uint8_t* __restrict__ valid) {
+    const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
+    if (x >= W || y >= H) return;
+    const size_t o = (size_t)y * W + x;
+    float4 sl = L[o];
+    float x2 = transform_x(sl, (float)x, (float)y);
+    float4 sr;
+    if (x2 < 0 || x2 >= (float)W) sr = f4s(1e5f);
+    else sr = R[(size_t)y * W + clampi(f2i_nan0(roundf(x2)), 0, W - 1)];
+    float ax, ay, az, bx, by, bz;
+    if (lr) { to_normal(sl, ax, ay, az); to_normal(viewprop(sr), bx, by, bz); }
+    else { to_normal(sr, ax, ay, az); to_normal(viewprop(sl), bx, by, bz); }
+    float ndiff = (ax * bx + ay * by) + az * bz;
+    float dm = fabsf((float)x - transform_x(sr, x2, (float)y));
+    bool bad = (dm >= maxdisp) || (pm_acospi(ndiff) >= athr);
+    out[o] = bad ? f4s(0.0f) : sl;
+    if (valid) valid[o] = bad ? 0 : 1;
+}
+
+/* ------------------------------------------------- row scans / fills -- */
+/* For every x of the row: the nearest index to the left (lft, in shared
+ * memory) whose value passes ok(); then, right to left, the nearest to the
+ * right, handed with lft to emit(x, lft, rgt).  -1 means none. */
+template <class OK, class EMIT>
+PM_DEV void row_scan(const float4* row, int W, int* lftbuf, OK ok, EMIT emit) {
+    const int lane = threadIdx.x;
+    const unsigned lt = (1u << lane) - 1u;
+    const unsigned gt = ~((2u << lane) - 1u);
+    int carry = -1;
+    for (int x0 = 0; x0 < W; x0 += 32) {
+        const int x = x0 + lane;
+        bool v = x < W && ok(row[x]);
+        unsigned bal = __ballot_sync(0xffffffffu, v);
+        unsigned below = bal & lt;
+        if (x < W) lftbuf[x] = below ? (x0 + 31 - __clz(below)) : carry;
+        if (bal) carry = x0 + 31 - __clz(bal);
+    }
+    __syncwarp();
+    carry = -1;
+    for (int x0 = ((W - 1) / 32) * 32; x0 >= 0; x0 -= 32) {
+        const int x = x0 + lane;
+        bool v = x < W && ok(row[x]);
+        unsigned bal = __ballot_sync(0xffffffffu, v);
+        unsigned above = bal & gt;
+        int rgt = above ? (x0 + __ffs(above) - 1) : carry;
+        if (bal) carry = x0 + __ffs(bal) - 1;
+        if (x < W) emit(x, lftbuf[x], rgt);
+    }
+}
+
+__global__ void __launch_bounds__(32) k_fill_state(const float4* __restrict__ in, int W, int H, float depthmax,
+                                                   int lr, float4* __restrict__ out) {
+    extern __shared__ int lftbuf[];
+    const int y = blockIdx.x;
+    if (y >= H) return;
+    const float4* row = in + (size_t)y * W;
+    const float cy = (float)y;
+    row_scan(row, W, lftbuf, [](float4 v) { return !(len4(v) < 1e-1f); },
+             [&](int x, int li, int ri) {
+                 const float cx = (float)x;
+                 float4 st = row[x], val;
+                 if (len4(st) < 1e-1f) {                                  /* :478-502 */
+                     float4 l = li >= 0 ? row[li] : f4s(1e5f);
+                     float4 r = ri >= 0 ? row[ri] : f4s(1e5f);
+                     l.w = fabsf(transform_x(l, cx, cy) - cx);
+                     r.w = fabsf(transform_x(r, cx, cy) - cx);
+                     val = (l.w < r.w) ? l : r;
+                 } else {
+                     val = st;
+                 }
+                 val = to_ref_normal_depth(val, cx, cy, lr);
+                 out[(size_t)y * W + x] = f4(val.x, val.y, val.w / depthmax, 1.0f);
+             });
+}
+
+__global__ void __launch_bounds__(32) k_fill_output(const float4* __restrict__ in, int W, int H, float scale,
+                                                    float* __restrict__ dmap, size_t dpitch,
+                                                    float4* __restrict__ nmap, size_t npitch) {
+    extern __shared__ int lftbuf[];
+    const int y = blockIdx.x;
+    if (y >= H) return;
+    const float4* row = in + (size_t)y * W;
+    const float cy = (float)y;
+    row_scan(row, W, lftbuf, [](float4 v) { return !(len3(v) < 1e-1f); },
+             [&](int x, int li, int ri) {
+                 const float cx = (float)x;
+                 float4 st = row[x];
+                 float v, nx, ny, nz;
+                 if (len3(st) < 1e-1f) {                                  /* :524-546, :569-595 */
+                     float4 l = li >= 0 ? row[li] : f4(-1e5f, -1e5f, -1e5f, 0.0f);
+                     float4 r = ri >= 0 ? row[ri] : f4(-1e5f, -1e5f, -1e5f, 0.0f);
+                     float lw = -(transform_x(l, cx, cy) - cx);
+                     float rw = -(transform_x(r, cx, cy) - cx);
+                     v = fminf(lw, rw);
+                     to_normal((lw < rw) ? l : r, nx, ny, nz);
+                 } else {
+                     v = fabsf(transform_x(st, cx, cy) - cx);
+                     to_normal(st, nx, ny, nz);
+                 }
+                 dmap[(size_t)y * dpitch + x] = v * scale;
+                 if (nmap) nmap[(size_t)y * npitch + x] = f4(nx, ny, nz, 0.0f);
+             });
+}
+
+/* ------------------------------------------------------------ PD step -- */
+/* One weighted Huber-ROF primal-dual step (PDHuberWeighted.cl:34-104):
+ * dual ascent with Huber smoothing and projection, primal descent, over-
+ * relaxation.  The dual of the pixel to the left and above is recomputed by
+ * the block edge threads, as the reference's work-group halo does. */
+PM_DEV void pd_dual(const float4* __restrict__ last, const float4* __restrict__ pin, const float* __restrict__ wgt,
+                    int W, int H, int qx, int qy, float4& lo, float4& hi) {
+    const float SIGMA = 1.0f / pm_sqrt(8.0f), ALPHA = 0.001f;
+    const bool in = qx >= 0 && qy >= 0 && qx < W && qy < H;
+    const float w = in ? wgt[(size_t)qy * W + qx] : 0.0f;
+    const int cx0 = clampi(qx, 0, W - 1), cy0 = clampi(qy, 0, H - 1);
+    const float4 uq = last[(size_t)cy0 * W + cx0];
+    const float4 ux = last[(size_t)cy0 * W + clampi(qx + 1, 0, W - 1)];
+    const float4 uy = last[(size_t)clampi(qy + 1, 0, H - 1) * W + cx0];
+    const float4 dx = w * (uq - ux);
+    const float4 dy = w * (uq - uy);
+    const float4 plo = in ? pin[((size_t)qy * W + qx) * 2] : f4s(0.0f);
+    const float4 phi = in ? pin[((size_t)qy * W + qx) * 2 + 1] : f4s(0.0f);
+    const float den = 1.0f + SIGMA * ALPHA / w;
+    const float4 l = (plo + SIGMA * dx) / f4s(den);
+    const float4 h = (phi + SIGMA * dy) / f4s(den);
+    const float4 pt = l * l + h * h;
+    const float sxy = pm_sqrt(pt.x + pt.y);
+    const float4 pproj = f4(fmaxf(1.0f, sxy), fmaxf(1.0f, sxy), fmaxf(1.0f, pm_sqrt(pt.z)), fmaxf(1.0f, pm_sqrt(0.0f)));
+    lo = l / pproj;
+    hi = h / pproj;
+}
+
+#define PD_TX 32
+#define PD_TY 8
+__global__ void __launch_bounds__(PD_TX * PD_TY)
+k_pd_step(float4* __restrict__ uout, float4* __restrict__ pout, const float4* __restrict__ last,
+          const float4* __restrict__ pin, const float4* __restrict__ f, const float* __restrict__ wgt,
+          float lambda, int W, int H) {
+    __shared__ float4 slo[PD_TY + 1][PD_TX + 1];
+    __shared__ float4 shi[PD_TY + 1][PD_TX + 1];
+    const int tx = threadIdx.x, ty = threadIdx.y;
+    const int x = blockIdx.x * PD_TX + tx, y = blockIdx.y * PD_TY + ty;
+    float4 lo, hi;
+    pd_dual(last, pin, wgt, W, H, x, y, lo, hi);
+    slo[ty + 1][tx + 1] = lo; shi[ty + 1][tx + 1] = hi;
+    if (tx == 0) { float4 l2, h2; pd_dual(last, pin, wgt, W, H, x - 1, y, l2, h2); slo[ty + 1][0] = l2; shi[ty + 1][0] = h2; }
+    if (ty == 0) { float4 l2, h2; pd_dual(last, pin, wgt, W, H, x, y - 1, l2, h2); slo[0][tx + 1] = l2; shi[0][tx + 1] = h2; }
+    __syncthreads();
+    if (x >= W || y >= H) return;
+    const float TAU = 1.0f / pm_sqrt(8.0f), THETA = 0.5f;
+    const float4 div = slo[ty + 1][tx + 1] - slo[ty + 1][tx] + shi[ty + 1][tx + 1] - shi[ty][tx + 1];
+    const size_t o = (size_t)y * W + x;
+    const float4 img = f[o];
+    const float4 uc = last[o];
+    const float wc = wgt[o];
+    const float4 lam = f4s(lambda);
+    float4 un = (uc + TAU * (lam * img - wc * div)) / (f4s(1.0f) + TAU * lam);
+    un = un + THETA * (un - uc);
+    un.w = 1.0f;
+    uout[o] = un;
+    pout[o * 2] = lo;
+    pout[o * 2 + 1] = hi;
+}
+
+/* ---------------------------------------------------------- launchers -- */
+#define PM_LAUNCH_CHECK() do { cudaError_t e_ = cudaGetLastError(); if (e_ != cudaSuccess) return e_; } while (0)
+
+cudaError_t pm_upload_tables(const unsigned long long* pow2, const float* prof, cudaStream_t st) {
+    cudaError_t e = cudaMemcpyToSymbolAsync(c_mwc_pow2, pow2, sizeof(unsigned long long) * 64, 0,
+                                            cudaMemcpyHostToDevice, st);
+    if (e != cudaSuccess) return e;
+    return cudaMemcpyToSymbolAsync(c_prof, prof, sizeof(float) * PM_PROF_N * PM_PROF_N, 0,
+                                   cudaMemcpyHostToDevice, st);
+}
+
+cudaError_t pm_launch_prep(const float4* img, size_t pitch4, int W, int H, float4* col, float4* grad,
+                           float* wgt, cudaStream_t st) {
+    dim3 b(PREP_T, PREP_T), g((W + PREP_T - 1) / PREP_T, (H + PREP_T - 1) / PREP_T);
+    k_prep<<<g, b, 0, st>>>(img, pitch4, W, H, col, grad, wgt);
+    PM_LAUNCH_CHECK();
+    return cudaSuccess;
+}
+
+cudaError_t pm_launch_records(const float4* col, const float4* grad, int W, int H, float4* A, float4* B,
+                              float4* C, float2* D, cudaStream_t st) {
+    dim3 b(128), g((W + 127) / 128, H);
+    k_records<<<g, b, 0, st>>>(col, grad, W, H, A, B, C, D);
+    PM_LAUNCH_CHECK();
+    return cudaSuccess;
+}
+
+static inline dim3 pix_grid(int W, int H) { return dim3((W + 31) / 32, (H + 7) / 8); }
+
+cudaError_t pm_launch_init(const PmPassArgs& a, bool exact, cudaStream_t st) {
+    if (exact) k_init<true><<<pix_grid(a.k.W, a.k.H), dim3(32, 8), 0, st>>>(a);
+    else k_init<false><<<pix_grid(a.k.W, a.k.H), dim3(32, 8), 0, st>>>(a);
+    PM_LAUNCH_CHECK();
+    return cudaSuccess;
+}
+
+cudaError_t pm_launch_cost_field(const PmPassArgs& a, bool exact, const float4* states, float* cost, cudaStream_t st) {
+    if (exact) k_cost_field<true><<<pix_grid(a.k.W, a.k.H), dim3(32, 8), 0, st>>>(a, states, cost);
+    else k_cost_field<false><<<pix_grid(a.k.W, a.k.H), dim3(32, 8), 0, st>>>(a, states, cost);
+    PM_LAUNCH_CHECK();
+    return cudaSuccess;
+}
+
+cudaError_t pm_launch_propagate(const PmPassArgs& a, bool exact, cudaStream_t st) {
+    if (exact) k_propagate<true><<<pix_grid(a.k.W, a.k.H), dim3(32, 8), 0, st>>>(a);
+    else k_propagate<false><<<pix_grid(a.k.W, a.k.H), dim3(32, 8), 0, st>>>(a);
+    PM_LAUNCH_CHECK();
+    return cudaSuccess;
+}
+
+cudaError_t pm_launch_view_list(const float4* src, int W, int H, short4* list, cudaStream_t st) {
+    k_view_list<<<H, 32, sizeof(int) * W, st>>>(src, W, H, list);
+    PM_LAUNCH_CHECK();
+    return cudaSuccess;
+}
+
+cudaError_t pm_launch_consistency(const float4* L, const float4* R, int W, int H, float maxdisp, float maxangle,
+                                  int lr, float4* out, uint8_t* valid, cudaStream_t st) {
+    dim3 b(32, 8), g((W + 31) / 32, (H + 7) / 8);
+    k_consistency<<<g, b, 0, st>>>(L, R, W, H, maxdisp, maxangle / 180.0f, lr, out, valid);
+    PM_LAUNCH_CHECK();
+    return cudaSuccess;
+}
+
+cudaError_t pm_launch_fill_state(const float4* in, int W, int H, float depthmax, int lr, float4* out,
+                                 cudaStream_t st) {
+    k_fill_state<<<H, 32, sizeof(int) * W, st>>>(in, W, H, depthmax, lr, out);
+    PM_LAUNCH_CHECK();
+    return cudaSuccess;
+}
+
+cudaError_t pm_launch_fill_output(const float4* in, int W, int H, float scale, float* dmap, size_t dpitch,
+                                  float4* nmap, size_t npitch, cudaStream_t st) {
+    k_fill_output<<<H, 32, sizeof(int) * W, st>>>(in, W, H, scale, dmap, dpitch, nmap, npitch);
+    PM_LAUNCH_CHECK();
+    return cudaSuccess;
+}
+
+cudaError_t pm_launch_pd_step(float4* uout, float4* pout, const float4* last, const float4* pin, const float4* f,
+                              const float* wgt, float lambda, int W, int H, cudaStream_t st) {
+    dim3 b(PD_TX, PD_TY), g((W + PD_TX - 1) / PD_TX, (H + PD_TY - 1) / PD_TY);
+    k_pd_step<<<g, b, 0, st>>>(uout, pout, last, pin, f, wgt, lambda, W, H);
+    PM_LAUNCH_CHECK();
+    return cudaSuccess;
+}

@@ -1,0 +1,48 @@
+/*
+ * pm_kernels.cuh — launch interface between the host schedule (pm_capi.cu)
+ * and the kernels (pm_kernels.cu).
+ */
+#ifndef CVT_GB300_PM_KERNELS_CUH
+#define CVT_GB300_PM_KERNELS_CUH
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include "cvtpm.h"
+#include "pm_device.cuh"
+
+/* Everything one init / propagation / cost launch needs. */
+struct PmPassArgs {
+    PmCostConsts k;
+    PmView v1, v2;             /* v1: the view being estimated; v2: the other view */
+    int lr, iter, rng;
+    uint32_t key0, key1;
+    float depthmax, theta;
+    const float4* old;         /* previous states of v1            */
+    const float4* smooth;      /* PD-smoothed (nx, ny, d/dmax, 1)  */
+    const short4* viewin;      /* up to 4 source x per pixel, or NULL */
+    const float4* viewsrc;     /* states the view list refers to    */
+    float4* out;
+    uint8_t* winners;
+};
+
+cudaError_t pm_upload_tables(const unsigned long long* pow2, const float* prof, cudaStream_t st);
+cudaError_t pm_launch_prep(const float4* img, size_t pitch4, int W, int H, float4* col, float4* grad,
+                           float* wgt, cudaStream_t st);
+cudaError_t pm_launch_records(const float4* col, const float4* grad, int W, int H, float4* A, float4* B,
+                              float4* C, float2* D, cudaStream_t st);
+cudaError_t pm_launch_init(const PmPassArgs& a, bool exact, cudaStream_t st);
+cudaError_t pm_launch_cost_field(const PmPassArgs& a, bool exact, const float4* states, float* cost,
+                                 cudaStream_t st);
+cudaError_t pm_launch_propagate(const PmPassArgs& a, bool exact, cudaStream_t st);
+cudaError_t pm_launch_view_list(const float4* src, int W, int H, short4* list, cudaStream_t st);
+cudaError_t pm_launch_consistency(const float4* L, const float4* R, int W, int H, float maxdisp,
+                                  float maxangle, int lr, float4* out, uint8_t* valid, cudaStream_t st);
+cudaError_t pm_launch_fill_state(const float4* in, int W, int H, float depthmax, int lr, float4* out,
+                                 cudaStream_t st);
+cudaError_t pm_launch_fill_output(const float4* in, int W, int H, float scale, float* dmap, size_t dpitch,
+                                  float4* nmap, size_t npitch, cudaStream_t st);
+cudaError_t pm_launch_pd_step(float4* uout, float4* pout, const float4* last, const float4* pin,
+                              const float4* f, const float* wgt, float lambda, int W, int H,
+                              cudaStream_t st);
+
+#endif

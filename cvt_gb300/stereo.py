@@ -1,0 +1,154 @@
+"""Python mirror of ``cvt::PMHuberStereo`` (cvt/vision/PMHuberStereo.h:35-59)
+over libcvtpm.so, for torch tensors on a CUDA device.
+
+    stereo = PMHuberStereo()
+    dmap = torch.empty(0, device="cuda")
+    stereo.depthMap(dmap, left, right, patchsize=17, depthmax=64,
+                    iterations=3, viewsamples=4)
+
+``left``/``right`` are (H, W, 4) float32 RGBA CUDA tensors (the reference's
+IFormat::RGBA_FLOAT images).  ``dmap`` is resized to (H, W) like the
+reference's ``dmap.reallocate(...)`` (PMHuberStereo.cpp:278), and so is
+``normalmap`` to (H, W, 4) (:286).  Size mismatches raise CVTException with
+the reference's message (:66-68); every other failure raises CvtpmError.
+Work runs on torch's current CUDA stream.
+"""
+from __future__ import annotations
+
+import ctypes
+
+import torch
+
+from . import _lib
+from .params import CvtpmParams, default_params, PRESET_REFERENCE
+
+
+class CVTException(RuntimeError):
+    """The reference's cvt::CVTException for inconsistent inputs."""
+
+
+def _stream_ptr(t: torch.Tensor):
+    return ctypes.c_void_p(torch.cuda.current_stream(t.device).cuda_stream)
+
+
+def _check_img(t: torch.Tensor, name: str):
+    if not isinstance(t, torch.Tensor) or not t.is_cuda or t.dtype != torch.float32:
+        raise CVTException(f"{name} must be a float32 CUDA tensor")
+    if t.dim() != 3 or t.shape[2] != 4:
+        raise CVTException(f"{name} must be an (H, W, 4) RGBA image")
+    if t.stride(2) != 1 or t.stride(1) != 4:
+        raise CVTException(f"{name} rows must be contiguous RGBA pixels")
+
+
+class PMHuberStereo:
+    def __init__(self, device: int | None = None, params: CvtpmParams | None = None):
+        L = _lib.lib()
+        if device is None:
+            device = torch.cuda.current_device()
+        self.device = int(device)
+        h = ctypes.c_void_p()
+        rc = L.cvtpm_create(ctypes.byref(h), self.device)
+        if rc:
+            raise _lib.CvtpmError(rc, _lib.status_string(rc))
+        self._h = h
+        self.params = params if params is not None else default_params(PRESET_REFERENCE)
+        self.set_params(self.params)
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None and h.value:
+            try:
+                _lib.lib().cvtpm_destroy(h)
+            except Exception:
+                pass
+            self._h = None
+
+    def _check(self, rc: int):
+        if rc:
+            msg = _lib.lib().cvtpm_last_error(self._h).decode()
+            raise _lib.CvtpmError(rc, msg)
+
+    def set_params(self, params: CvtpmParams):
+        self._check(_lib.lib().cvtpm_set_params(self._h, ctypes.byref(params)))
+        self.params = params
+
+    def get_params(self) -> CvtpmParams:
+        p = CvtpmParams()
+        self._check(_lib.lib().cvtpm_get_params(self._h, ctypes.byref(p)))
+        return p
+
+    def depthMap(self, dmap: torch.Tensor, left: torch.Tensor, right: torch.Tensor, patchsize: int,
+                 depthmax: float, iterations: int, viewsamples: int, dscale: float = -1.0,
+                 normalmap: torch.Tensor | None = None, trace: dict | None = None) -> torch.Tensor:
+        """PMHuberStereo::depthMap.  If ``trace`` is a dict it receives the
+        integer outputs: 'winners' (2, H, W) uint8, 'valid' (H, W) uint8 and
+        'states' (2, H, W, 4) float32."""
+        _check_img(left, "left")
+        _check_img(right, "right")
+        if left.shape != right.shape:
+            raise CVTException("Left/Right stereo images inconsistent or incompatible memory type")
+        if left.device != right.device or left.device.index != self.device:
+            raise CVTException("Left/Right stereo images inconsistent or incompatible memory type")
+        if left.stride(0) != right.stride(0):
+            right = right.contiguous()
+            left = left.contiguous()
+        H, W = left.shape[:2]
+        if dmap is None:
+            dmap = torch.empty((H, W), dtype=torch.float32, device=left.device)
+        if dmap.shape != (H, W) or dmap.dtype != torch.float32 or not dmap.is_contiguous() or dmap.device != left.device:
+            if dmap.device != left.device or dmap.dtype != torch.float32:
+                raise CVTException("dmap must be a float32 tensor on the images' device")
+            dmap.resize_(H, W)
+        nm_ptr, nm_pitch = None, 0
+        if normalmap is not None:
+            if normalmap.device != left.device or normalmap.dtype != torch.float32:
+                raise CVTException("normalmap must be a float32 tensor on the images' device")
+            if normalmap.shape != (H, W, 4) or not normalmap.is_contiguous():
+                normalmap.resize_(H, W, 4)
+            nm_ptr, nm_pitch = normalmap.data_ptr(), W * 16
+        tr = None
+        if trace is not None:
+            trace["winners"] = torch.empty((2, H, W), dtype=torch.uint8, device=left.device)
+            trace["valid"] = torch.empty((H, W), dtype=torch.uint8, device=left.device)
+            trace["states"] = torch.empty((2, H, W, 4), dtype=torch.float32, device=left.device)
+            tr = _lib.CvtpmTrace(trace["winners"].data_ptr(), trace["valid"].data_ptr(), trace["states"].data_ptr())
+        rc = _lib.lib().cvtpm_depthmap(
+            self._h, dmap.data_ptr(), W * 4, left.data_ptr(), right.data_ptr(), W, H, left.stride(0) * 4,
+            int(patchsize), float(depthmax), int(iterations), int(viewsamples), float(dscale),
+            nm_ptr, nm_pitch, ctypes.byref(tr) if tr is not None else None, _stream_ptr(left))
+        self._check(rc)
+        return dmap
+
+    def depthMapHost(self, left, right, patchsize: int, depthmax: float, iterations: int, viewsamples: int,
+                     dscale: float = -1.0, dmap=None):
+        """depthMap on host (numpy / CPU torch) buffers: copies in, runs,
+        copies out and synchronizes.  Returns the (H, W) disparity map."""
+        import numpy as np
+        left = np.ascontiguousarray(left, np.float32)
+        right = np.ascontiguousarray(right, np.float32)
+        if left.shape != right.shape or left.ndim != 3 or left.shape[2] != 4:
+            raise CVTException("Left/Right stereo images inconsistent or incompatible memory type")
+        H, W = left.shape[:2]
+        if dmap is None:
+            dmap = np.empty((H, W), np.float32)
+        stream = ctypes.c_void_p(torch.cuda.current_stream(self.device).cuda_stream)
+        rc = _lib.lib().cvtpm_depthmap_host(
+            self._h, dmap.ctypes.data, W * 4, left.ctypes.data, right.ctypes.data, W, H, W * 16,
+            int(patchsize), float(depthmax), int(iterations), int(viewsamples), float(dscale), None, 0, stream)
+        self._check(rc)
+        return dmap
+
+    def cost(self, img1: torch.Tensor, img2: torch.Tensor, states: torch.Tensor, lr: int = 1) -> torch.Tensor:
+        """Aggregated ASW cost of every pixel for a fixed state field
+        (H, W, 4) (s0, s1, s2, -): x_other = s0*x + s1*y + s2."""
+        _check_img(img1, "img1")
+        _check_img(img2, "img2")
+        if img1.shape != img2.shape or states.shape != img1.shape:
+            raise CVTException("img1/img2/states shapes differ")
+        states = states.contiguous()
+        H, W = img1.shape[:2]
+        out = torch.empty((H, W), dtype=torch.float32, device=img1.device)
+        rc = _lib.lib().cvtpm_cost_eval(self._h, img1.data_ptr(), img2.data_ptr(), W, H, img1.stride(0) * 4,
+                                        states.data_ptr(), int(lr), out.data_ptr(), _stream_ptr(img1))
+        self._check(rc)
+        return out

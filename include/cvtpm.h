@@ -1,0 +1,176 @@
+/*
+ * cvtpm.h — C ABI of the GB300 slanted-plane PatchMatch stereo library
+ * (libcvtpm.so).  Plain C: pointers, sizes and status codes; no C++ or torch
+ * types cross this boundary and no exception escapes it.
+ *
+ * It replaces the OpenCL path behind
+ *   cvt::PMHuberStereo::depthMap(Image& dmap, const Image& left,
+ *       const Image& right, size_t patchsize, float depthmax,
+ *       size_t iterations, size_t viewsamples, float dscale = -1.0f,
+ *       Image* normalmap = NULL)
+ * declared at cvt/vision/PMHuberStereo.h:40 and implemented at
+ * cvt/vision/PMHuberStereo.cpp:64-291 (kernels in cvt/cl/kernel/pmhstereo.cl,
+ * cvt/cl/kernel/PDHuberWeighted.cl, cvt/cl/kernel/RNG.cl; smoother in
+ * cvt/gfx/PDROF.h:50-96).
+ *
+ * Conventions
+ *  - Images are row-major RGBA float32 (4 floats per pixel, the reference's
+ *    IFormat::RGBA_FLOAT), with a row pitch in BYTES that is a multiple of 16.
+ *    The disparity map is GRAY float32 (IFormat::GRAY_FLOAT) with its own pitch.
+ *  - Device pointers belong to the caller.  Scratch memory belongs to the
+ *    context, is allocated on first use for a given size and reused.
+ *  - Work is stream-ordered on the cudaStream_t passed as `void* stream`
+ *    (NULL = legacy default stream).  Only the *_host entry points and
+ *    cvtpm_synchronize block the calling thread.
+ *  - One context per host thread at a time; contexts are independent.
+ */
+#ifndef CVTPM_H
+#define CVTPM_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum cvtpm_status {
+    CVTPM_OK = 0,
+    CVTPM_ERR_INVALID_ARGUMENT = 1, /* null pointer, bad pitch, bad enum      */
+    CVTPM_ERR_SIZE = 2,             /* width/height/patchsize out of range    */
+    CVTPM_ERR_INCONSISTENT = 3,     /* left/right sizes differ (the reference
+                                       throws CVTException, PMHuberStereo.cpp:66-68) */
+    CVTPM_ERR_CUDA = 4,             /* a CUDA runtime call failed             */
+    CVTPM_ERR_ALLOC = 5,            /* device allocation failed               */
+    CVTPM_ERR_TIMEOUT = 6,          /* a bounded device wait gave up          */
+    CVTPM_ERR_NOT_SUPPORTED = 7
+} cvtpm_status;
+
+enum { CVTPM_RNG_MWC64X = 0, CVTPM_RNG_PHILOX = 1 };
+/* EXACT: the reference's operation order, no contraction (bit-faithful to the
+ * .cl arithmetic).  FAST: FMA-contracted tap arithmetic with a precomputed
+ * (value, forward difference) layout of the other view; its CPU mirror is the
+ * oracle run with the same setting. */
+enum { CVTPM_ARITH_EXACT = 0, CVTPM_ARITH_FAST = 1 };
+enum { CVTPM_SCHEDULE_JACOBI = 0, CVTPM_SCHEDULE_REDBLACK = 1 };
+enum { CVTPM_PROFILE_SMOOTHSTEP = 0, CVTPM_PROFILE_CONSTANT = 1 };
+enum { CVTPM_PRESET_REFERENCE = 0, CVTPM_PRESET_BASELINE = 1 };
+
+/* Every constant of the path.  cvtpm_params_default() fills them. */
+typedef struct cvtpm_params {
+    int   patchsize;        /* window radius P, window (2P+1)^2; 1..31      */
+    float depthmax;         /* maximum disparity in pixels (> 0)            */
+    int   iterations;       /* PatchMatch iterations (>= 1)                 */
+    int   viewsamples;      /* accepted and ignored: 4 slots, as in the
+                               reference (pmhstereo.cl:40)                  */
+    float dscale;           /* output scale; <= 0 means 1/depthmax
+                               (PMHuberStereo.cpp:75-76)                    */
+    float maxdispdiff;      /* LR check, px (PMHuberStereo.cpp:70: 0.5)     */
+    float maxanglediff;     /* LR check, degrees (:71: 10)                  */
+    float thetascale;       /* PD lambda = theta*thetascale + 5 (:72,:243)  */
+    int   pd_iterations;    /* PD steps per view per iteration (:243: 250)  */
+    float color_weight;     /* COLORWEIGHT (pmhstereo.cl:34: 26)            */
+    float color_alpha;      /* COLORGRADALPHA, colour share (:35: 0.05)     */
+    float color_maxdiff;    /* COLORMAXDIFF (:36: 0.04)                     */
+    float grad_maxdiff;     /* GRADMAXDIFF (:37: 0.01)                      */
+    int   weight_profile;   /* CVTPM_PROFILE_*                              */
+    int   rng;              /* CVTPM_RNG_*                                  */
+    uint64_t seed;          /* Philox key (ignored by MWC64X)               */
+    int   arith;            /* CVTPM_ARITH_*                                */
+    int   schedule;         /* CVTPM_SCHEDULE_*                             */
+} cvtpm_params;
+
+/* Per-pixel integer outputs of a run, for bit-exact comparison. */
+typedef struct cvtpm_trace {
+    uint8_t* winners;       /* 2*W*H: index of the winning hypothesis in the
+                               last propagation pass, left view then right;
+                               0 kept, 1-8 neighbours, 9 smooth, 10-15 random
+                               neighbours, 16 random plane, 17-20 view,
+                               21-22 refinements                            */
+    uint8_t* valid;         /* W*H: final LR-consistency mask of the left view */
+    float*   states;        /* 2*W*H*4: final plane states (s0,s1,s2,cost),
+                               left then right                              */
+} cvtpm_trace;
+
+typedef struct cvtpm_ctx cvtpm_ctx;
+
+/* One stereo pair of a batch. */
+typedef struct cvtpm_pair {
+    const float* left;      /* device RGBA f32 */
+    const float* right;
+    int width, height;
+    size_t pitch;           /* bytes, both images */
+    float depthmax;
+    float* dmap;            /* device GRAY f32 out */
+    size_t dmap_pitch;      /* bytes */
+} cvtpm_pair;
+
+const char*  cvtpm_version(void);
+const char*  cvtpm_status_string(cvtpm_status s);
+cvtpm_status cvtpm_params_default(cvtpm_params* p, int preset);
+
+/* Context (replaces the CLKernel members built in PMHuberStereo's
+ * constructor, PMHuberStereo.cpp:42-58). */
+cvtpm_status cvtpm_create(cvtpm_ctx** ctx, int device);
+cvtpm_status cvtpm_destroy(cvtpm_ctx* ctx);
+cvtpm_status cvtpm_set_params(cvtpm_ctx* ctx, const cvtpm_params* p);
+cvtpm_status cvtpm_get_params(const cvtpm_ctx* ctx, cvtpm_params* p);
+const char*  cvtpm_last_error(const cvtpm_ctx* ctx);
+cvtpm_status cvtpm_synchronize(cvtpm_ctx* ctx, void* stream);
+
+/* PMHuberStereo::depthMap (PMHuberStereo.h:40, PMHuberStereo.cpp:64-291).
+ * patchsize, depthmax, iterations, viewsamples and dscale override the
+ * context's parameters for this call, as the reference's arguments do.
+ * normalmap may be NULL (reference default).  trace may be NULL. */
+cvtpm_status cvtpm_depthmap(cvtpm_ctx* ctx,
+                            float* dmap, size_t dmap_pitch,
+                            const float* left, const float* right,
+                            int width, int height, size_t pitch,
+                            int patchsize, float depthmax, int iterations,
+                            int viewsamples, float dscale,
+                            float* normalmap, size_t normalmap_pitch,
+                            const cvtpm_trace* trace, void* stream);
+
+/* The same call on HOST buffers: copies in, runs, copies out, synchronizes. */
+cvtpm_status cvtpm_depthmap_host(cvtpm_ctx* ctx,
+                                 float* dmap, size_t dmap_pitch,
+                                 const float* left, const float* right,
+                                 int width, int height, size_t pitch,
+                                 int patchsize, float depthmax, int iterations,
+                                 int viewsamples, float dscale,
+                                 float* normalmap, size_t normalmap_pitch,
+                                 void* stream);
+
+/* Fixed-plane cost evaluator: the aggregated ASW cost
+ * patch_eval_color_grad_weighted (pmhstereo.cl:170-228) of every pixel of
+ * view `lr` (1 = left is image 1, 0 = right is image 1) for the given state
+ * field (float4 s0,s1,s2,unused per pixel, x_other = s0*x + s1*y + s2).
+ * img1/img2 are RGBA f32 device images; gradients are computed internally
+ * (pmhstereo_gradxy, pmhstereo.cl:785-831).  cost is W*H floats. */
+cvtpm_status cvtpm_cost_eval(cvtpm_ctx* ctx,
+                             const float* img1, const float* img2,
+                             int width, int height, size_t pitch,
+                             const float* states, int lr, float* cost,
+                             void* stream);
+
+/* Adjoint of cvtpm_cost_eval with respect to the planes and both images.
+ * planes are per-pixel (a, b, c, unused) in the disparity convention
+ * d = a*x + b*y + c of view 1 (x_other = x - d for lr = 1, x + d for lr = 0).
+ * dcost is W*H; dplanes W*H*4 (a, b, c, 0); dimg1/dimg2 W*H*4 RGBA (alpha 0).
+ * Any output may be NULL.  Window weights are recomputed, not stored. */
+cvtpm_status cvtpm_cost_adjoint(cvtpm_ctx* ctx,
+                                const float* img1, const float* img2,
+                                int width, int height, size_t pitch,
+                                const float* planes, int lr,
+                                const float* dcost,
+                                float* cost, float* dplanes,
+                                float* dimg1, float* dimg2, void* stream);
+
+/* Many pairs of uneven size in one graph-captured launch sequence. */
+cvtpm_status cvtpm_depthmap_batched(cvtpm_ctx* ctx, const cvtpm_pair* pairs,
+                                    int npairs, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

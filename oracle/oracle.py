@@ -1,0 +1,209 @@
+"""TEST INFRASTRUCTURE: ctypes front end of the CPU oracle (liboracle.so).
+
+Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline / reference
+arm use this module, as the checker or as the timed CPU baseline.  The
+product never imports it.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+from cvt_gb300.params import CvtpmParams
+
+from . import build_oracle
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        path = build_oracle.LIB
+        if not os.path.exists(path):
+            build_oracle.build()
+        L = ctypes.CDLL(path)
+        f32p = np.ctypeslib.ndpointer(np.float32, flags="C_CONTIGUOUS")
+        i16p = np.ctypeslib.ndpointer(np.int16, flags="C_CONTIGUOUS")
+        u8p = np.ctypeslib.ndpointer(np.uint8, flags="C_CONTIGUOUS")
+        P = ctypes.POINTER(CvtpmParams)
+        c_int, c_float = ctypes.c_int, ctypes.c_float
+        L.orc_set_threads.argtypes = [c_int]
+        L.orc_max_threads.restype = c_int
+        L.orc_gradxy.argtypes = [f32p, c_int, c_int, f32p]
+        L.orc_edge_weight.argtypes = [f32p, c_int, c_int, f32p]
+        for n in ("orc_exp", "orc_acospi"):
+            getattr(L, n).argtypes = [c_float]
+            getattr(L, n).restype = c_float
+        L.orc_pow.argtypes = [c_float, c_float]
+        L.orc_pow.restype = c_float
+        L.orc_exp_array.argtypes = [f32p, f32p, ctypes.c_long]
+        L.orc_acospi_array.argtypes = [f32p, f32p, ctypes.c_long]
+        L.orc_pow_array.argtypes = [f32p, c_float, f32p, ctypes.c_long]
+        L.orc_mwc_mulmod_serial.argtypes = [ctypes.c_uint64, ctypes.c_uint64]
+        L.orc_mwc_mulmod_serial.restype = ctypes.c_uint64
+        L.orc_mwc_mulmod.argtypes = [ctypes.c_uint64, ctypes.c_uint64]
+        L.orc_mwc_mulmod.restype = ctypes.c_uint64
+        L.orc_mwc_stream.argtypes = [ctypes.c_uint64, c_int, f32p]
+        L.orc_mwc_state.argtypes = [ctypes.c_uint64, ctypes.POINTER(ctypes.c_uint32), ctypes.POINTER(ctypes.c_uint32)]
+        u32p = np.ctypeslib.ndpointer(np.uint32, flags="C_CONTIGUOUS")
+        L.orc_philox.argtypes = [u32p, u32p, u32p]
+        L.orc_philox_stream.argtypes = [ctypes.c_uint64, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32, c_int, f32p]
+        L.orc_cost_field.argtypes = [P, f32p, f32p, c_int, c_int, f32p, f32p]
+        L.orc_cost_field.restype = c_int
+        L.orc_init.argtypes = [P, f32p, f32p, c_int, c_int, c_int, f32p]
+        L.orc_init.restype = c_int
+        opt_i16 = ctypes.c_void_p
+        L.orc_propagate.argtypes = [P, f32p, f32p, c_int, c_int, c_int, c_int, c_float, f32p, f32p,
+                                    opt_i16, ctypes.c_void_p, f32p, ctypes.c_void_p]
+        L.orc_propagate.restype = c_int
+        L.orc_view_list.argtypes = [f32p, c_int, c_int, i16p]
+        L.orc_consistency.argtypes = [f32p, f32p, c_int, c_int, c_float, c_float, c_int, f32p, ctypes.c_void_p]
+        L.orc_fill_state.argtypes = [f32p, c_int, c_int, c_float, c_int, f32p]
+        L.orc_fill_depthmap.argtypes = [f32p, c_int, c_int, c_float, f32p]
+        L.orc_fill_normalmap.argtypes = [f32p, c_int, c_int, f32p]
+        L.orc_pd_step.argtypes = [f32p, f32p, f32p, f32p, f32p, f32p, c_float, c_int, c_int]
+        L.orc_pd_apply.argtypes = [f32p, f32p, f32p, c_float, c_int, c_int, c_int]
+        L.orc_depthmap.argtypes = [P, f32p, f32p, c_int, c_int, f32p, ctypes.c_void_p, ctypes.c_void_p,
+                                   ctypes.c_void_p, ctypes.c_void_p]
+        L.orc_depthmap.restype = c_int
+        _lib = L
+    return _lib
+
+
+def _f32(a):
+    return np.ascontiguousarray(a, dtype=np.float32)
+
+
+def _ptr(a):
+    return None if a is None else a.ctypes.data_as(ctypes.c_void_p)
+
+
+def set_threads(n: int) -> None:
+    lib().orc_set_threads(int(n))
+
+
+def max_threads() -> int:
+    return int(lib().orc_max_threads())
+
+
+def gradxy(img):
+    img = _f32(img)
+    h, w = img.shape[:2]
+    out = np.empty((h, w, 4), np.float32)
+    lib().orc_gradxy(img, w, h, out)
+    return out
+
+
+def edge_weight(img):
+    img = _f32(img)
+    h, w = img.shape[:2]
+    out = np.empty((h, w), np.float32)
+    lib().orc_edge_weight(img, w, h, out)
+    return out
+
+
+def cost_field(params: CvtpmParams, img1, img2, states):
+    img1, img2, states = _f32(img1), _f32(img2), _f32(states)
+    h, w = img1.shape[:2]
+    out = np.empty((h, w), np.float32)
+    rc = lib().orc_cost_field(ctypes.byref(params), img1, img2, w, h, states, out)
+    assert rc == 0, rc
+    return out
+
+
+def init(params: CvtpmParams, img1, img2, lr: int):
+    img1, img2 = _f32(img1), _f32(img2)
+    h, w = img1.shape[:2]
+    out = np.empty((h, w, 4), np.float32)
+    rc = lib().orc_init(ctypes.byref(params), img1, img2, w, h, int(lr), out)
+    assert rc == 0, rc
+    return out
+
+
+def propagate(params, img1, img2, lr, it, theta, old, smooth, viewin=None, viewsrc=None):
+    img1, img2, old, smooth = _f32(img1), _f32(img2), _f32(old), _f32(smooth)
+    h, w = img1.shape[:2]
+    out = np.empty((h, w, 4), np.float32)
+    win = np.empty((h, w), np.uint8)
+    vi = None if viewin is None else np.ascontiguousarray(viewin, np.int16)
+    vs = None if viewsrc is None else _f32(viewsrc)
+    rc = lib().orc_propagate(ctypes.byref(params), img1, img2, w, h, int(lr), int(it), float(theta),
+                             old, smooth, _ptr(vi), _ptr(vs), out, _ptr(win))
+    assert rc == 0, rc
+    return out, win
+
+
+def view_list(src):
+    src = _f32(src)
+    h, w = src.shape[:2]
+    out = np.empty((h, w, 4), np.int16)
+    lib().orc_view_list(src, w, h, out)
+    return out
+
+
+def consistency(L, R, maxdisp, maxangle, lr):
+    L, R = _f32(L), _f32(R)
+    h, w = L.shape[:2]
+    out = np.empty((h, w, 4), np.float32)
+    valid = np.empty((h, w), np.uint8)
+    lib().orc_consistency(L, R, w, h, float(maxdisp), float(maxangle), int(lr), out, _ptr(valid))
+    return out, valid
+
+
+def fill_state(inp, depthmax, lr):
+    inp = _f32(inp)
+    h, w = inp.shape[:2]
+    out = np.empty((h, w, 4), np.float32)
+    lib().orc_fill_state(inp, w, h, float(depthmax), int(lr), out)
+    return out
+
+
+def fill_depthmap(inp, scale):
+    inp = _f32(inp)
+    h, w = inp.shape[:2]
+    out = np.empty((h, w), np.float32)
+    lib().orc_fill_depthmap(inp, w, h, float(scale), out)
+    return out
+
+
+def fill_normalmap(inp):
+    inp = _f32(inp)
+    h, w = inp.shape[:2]
+    out = np.empty((h, w, 4), np.float32)
+    lib().orc_fill_normalmap(inp, w, h, out)
+    return out
+
+
+def pd_step(last, pin, f, wgt, lam):
+    last, pin, f, wgt = _f32(last), _f32(pin), _f32(f), _f32(wgt)
+    h, w = last.shape[:2]
+    uout = np.empty((h, w, 4), np.float32)
+    pout = np.empty((h, w, 8), np.float32)
+    lib().orc_pd_step(uout, pout, last, pin, f, wgt, float(lam), w, h)
+    return uout, pout
+
+
+def pd_apply(output, inp, wgt, lam, iters):
+    out = _f32(output).copy()
+    inp, wgt = _f32(inp), _f32(wgt)
+    h, w = inp.shape[:2]
+    lib().orc_pd_apply(out, inp, wgt, float(lam), int(iters), w, h)
+    return out
+
+
+def depthmap(params: CvtpmParams, left, right, normalmap: bool = False, trace: bool = False):
+    """PMHuberStereo::depthMap on the CPU.  Returns (dmap, extras) with extras
+    holding 'normalmap', 'states' (2,H,W,4), 'winners' (2,H,W), 'valid' (H,W)."""
+    left, right = _f32(left), _f32(right)
+    h, w = left.shape[:2]
+    dmap = np.empty((h, w), np.float32)
+    nm = np.empty((h, w, 4), np.float32) if normalmap else None
+    st = np.empty((2, h, w, 4), np.float32) if trace else None
+    win = np.empty((2, h, w), np.uint8) if trace else None
+    val = np.empty((h, w), np.uint8) if trace else None
+    rc = lib().orc_depthmap(ctypes.byref(params), left, right, w, h, dmap, _ptr(nm), _ptr(st), _ptr(win), _ptr(val))
+    assert rc == 0, rc
+    return dmap, {"normalmap": nm, "states": st, "winners": win, "valid": val}

@@ -1,0 +1,844 @@
+/*
+ * pm_oracle.cpp — TEST INFRASTRUCTURE: the CPU oracle of the slanted-plane
+ * PatchMatch stereo path.  Only tests/, __graft_entry__.smoke() and bench.py's
+ * CPU-baseline / reference arm load it, and only as a checker or as the timed
+ * CPU baseline.  The product (cvt_gb300/, libcvtpm.so) never links it.
+ *
+ * It restates, in plain C++17 FP32 (no contraction, IEEE division and sqrt, no
+ * flush-to-zero), the reference's OpenCL path:
+ *   cvt/cl/kernel/pmhstereo.cl      kernels and plane algebra
+ *   cvt/cl/kernel/RNG.cl            MWC64X generator
+ *   cvt/cl/kernel/PDHuberWeighted.cl + cvt/gfx/PDROF.h   Huber-TV smoother
+ *   cvt/vision/PMHuberStereo.cpp:64-291                 the depthMap schedule
+ * Each function names the lines it follows.
+ *
+ * Choices where the reference is not deterministic or not defined:
+ *  - native_exp / exp / pow / acospi use the project's functions
+ *    (cvt_gb300/csrc/pm_math.h); native_sqrt / native_rsqrt are IEEE sqrt and
+ *    1/sqrt.  OpenCL leaves their accuracy to the implementation.
+ *  - The view-candidate scatter (pmhstereo.cl:394-400) races on atomic_inc;
+ *    here the up-to-4 survivors of a target pixel are the sources with the
+ *    smallest x, in increasing x — the order a sequential execution of the
+ *    reference's 16x16 work-groups (row-major groups, raster order inside a
+ *    group) produces, because only sources of the same row compete.
+ *  - Vector literals evaluate their components left to right (the random
+ *    neighbour offsets draw x before y, pmhstereo.cl:356).
+ *  - Non-finite sample positions are treated as outside the image, and a NaN
+ *    converted to int is 0 (the NVIDIA conversion).  These only arise for
+ *    non-finite plane states.
+ * The bilinear sampler is the OpenCL specification's formula at full FP32
+ * precision (no 8-bit fraction quantisation as texture hardware has).
+ *
+ * ARITH_FAST selects the tap arithmetic of the CUDA fast kernel instead
+ * (FMA forms, (value, forward-difference) records of the other view,
+ * separate colour/gradient accumulators); it is the bit-exact CPU mirror of
+ * that kernel.
+ */
+#include "cvtpm.h"
+#include "pm_math.h"
+
+#include <algorithm>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <vector>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+namespace {
+
+struct F4 { float x, y, z, w; };
+static inline F4 f4(float x, float y, float z, float w) { F4 r = {x, y, z, w}; return r; }
+static inline F4 f4s(float s) { return f4(s, s, s, s); }
+static inline F4 operator+(F4 a, F4 b) { return f4(a.x + b.x, a.y + b.y, a.z + b.z, a.w + b.w); }
+static inline F4 operator-(F4 a, F4 b) { return f4(a.x - b.x, a.y - b.y, a.z - b.z, a.w - b.w); }
+static inline F4 operator*(F4 a, F4 b) { return f4(a.x * b.x, a.y * b.y, a.z * b.z, a.w * b.w); }
+static inline F4 operator/(F4 a, F4 b) { return f4(a.x / b.x, a.y / b.y, a.z / b.z, a.w / b.w); }
+static inline F4 operator*(float s, F4 a) { return f4(s * a.x, s * a.y, s * a.z, s * a.w); }
+static inline bool finite3(F4 s) { return std::isfinite(s.x) && std::isfinite(s.y) && std::isfinite(s.z); }
+static inline float len4(F4 a) { return sqrtf(((a.x * a.x + a.y * a.y) + a.z * a.z) + a.w * a.w); }
+static inline float len3(F4 a) { return sqrtf((a.x * a.x + a.y * a.y) + a.z * a.z); }
+static inline int clampi(int v, int lo, int hi) { return v < lo ? lo : (v > hi ? hi : v); }
+static inline int f2i_nan0(float v) { return (v != v) ? 0 : (int)v; }
+
+/* ------------------------------------------------------------------ RNG -- */
+/* MWC64X, RNG.cl:35-156.  MulMod64 is evaluated with a 128-bit product; it
+ * returns the same residue as the bit-serial loop of RNG.cl:49-59
+ * (orc_mwc_mulmod_serial keeps that loop for the known-answer test). */
+const uint32_t MWC_A = 4294883355u;
+const uint64_t MWC_M = 18446383549859758079ull;
+const uint64_t MWC_BASEID = 4077358422479273989ull;
+
+static inline uint64_t mwc_addmod(uint64_t a, uint64_t b, uint64_t M) {  /* RNG.cl:35-41 */
+    uint64_t v = a + b;
+    if ((v >= M) || (v < a)) v = v - M;
+    return v;
+}
+static uint64_t mwc_mulmod_serial(uint64_t a, uint64_t b, uint64_t M) { /* RNG.cl:49-59 */
+    uint64_t r = 0;
+    while (a != 0) {
+        if (a & 1) r = mwc_addmod(r, b, M);
+        b = mwc_addmod(b, b, M);
+        a = a >> 1;
+    }
+    return r;
+}
+static inline uint64_t mwc_mulmod(uint64_t a, uint64_t b, uint64_t M) {
+    return (uint64_t)(((unsigned __int128)a * b) % M);
+}
+static uint64_t mwc_powmod(uint64_t a, uint64_t e, uint64_t M) {       /* RNG.cl:66-76 */
+    uint64_t sqr = a, acc = 1;
+    while (e != 0) {
+        if (e & 1) acc = mwc_mulmod(acc, sqr, M);
+        sqr = mwc_mulmod(sqr, sqr, M);
+        e = e >> 1;
+    }
+    return acc;
+}
+
+struct Rng {
+    int kind;
+    uint32_t x, c;                  /* MWC64X */
+    uint32_t ctr[4], key[2], buf[4];/* Philox */
+    uint32_t n;
+};
+
+/* RNG_init(rng, linpos, numdraws) = SeedStreams(0, 0) then Skip(linpos*numdraws),
+ * RNG.cl:151-154 with RNG.cl:78-100,120-132. */
+static void mwc_init(Rng& r, uint64_t distance) {
+    uint64_t m0 = mwc_powmod(MWC_A, 0, MWC_M);           /* dist = 0 + gid*1*0 */
+    uint64_t x = mwc_mulmod(MWC_BASEID, m0, MWC_M);
+    uint32_t sx = (uint32_t)(x / MWC_A), sc = (uint32_t)(x % MWC_A);
+    uint64_t m = mwc_powmod(MWC_A, distance, MWC_M);
+    uint64_t v = (uint64_t)sx * (uint64_t)MWC_A + sc;
+    v = mwc_mulmod(v, m, MWC_M);
+    r.kind = CVTPM_RNG_MWC64X;
+    r.x = (uint32_t)(v / MWC_A);
+    r.c = (uint32_t)(v % MWC_A);
+}
+static inline float mwc_float(Rng& r) {                                /* RNG.cl:108-118,142-147 */
+    uint32_t res = r.x ^ r.c;
+    uint32_t X = r.x, C = r.c;
+    uint32_t Xn = MWC_A * X + C;
+    uint32_t carry = (uint32_t)(Xn < C);
+    uint32_t Cn = (uint32_t)(((uint64_t)MWC_A * X) >> 32) + carry;    /* mad_hi */
+    r.x = Xn; r.c = Cn;
+    return 2.3283064365386962890625e-10f * (float)res;
+}
+
+/* Philox4x32-10 (Salmon, Moraes, Dror, Shaw, SC'11): counter (pixel, tag,
+ * view, block), key = seed.  Draw k is word k%4 of block k/4. */
+static inline void philox10(const uint32_t in[4], const uint32_t key[2], uint32_t out[4]) {
+    uint32_t c0 = in[0], c1 = in[1], c2 = in[2], c3 = in[3];
+    uint32_t k0 = key[0], k1 = key[1];
+    for (int r = 0; r < 10; ++r) {
+        uint64_t p0 = (uint64_t)0xD2511F53u * c0;
+        uint64_t p1 = (uint64_t)0xCD9E8D57u * c2;
+        uint32_t n0 = (uint32_t)(p1 >> 32) ^ c1 ^ k0;
+        uint32_t n1 = (uint32_t)p1;
+        uint32_t n2 = (uint32_t)(p0 >> 32) ^ c3 ^ k1;
+        uint32_t n3 = (uint32_t)p0;
+        c0 = n0; c1 = n1; c2 = n2; c3 = n3;
+        k0 += 0x9E3779B9u; k1 += 0xBB67AE85u;
+    }
+    out[0] = c0; out[1] = c1; out[2] = c2; out[3] = c3;
+}
+const uint32_t PHILOX_TAG_INIT = 0xFFFFFFFFu;
+static void philox_init(Rng& r, uint64_t seed, uint32_t pixel, uint32_t tag, uint32_t view) {
+    r.kind = CVTPM_RNG_PHILOX;
+    r.ctr[0] = pixel; r.ctr[1] = tag; r.ctr[2] = view; r.ctr[3] = 0;
+    r.key[0] = (uint32_t)seed; r.key[1] = (uint32_t)(seed >> 32);
+    r.n = 0;
+}
+static inline float philox_float(Rng& r) {
+    if ((r.n & 3u) == 0) { r.ctr[3] = r.n >> 2; philox10(r.ctr, r.key, r.buf); }
+    uint32_t u = r.buf[r.n & 3u];
+    r.n++;
+    return 2.3283064365386962890625e-10f * (float)u;
+}
+static inline float rng_float(Rng& r) { return r.kind == CVTPM_RNG_PHILOX ? philox_float(r) : mwc_float(r); }
+
+/* ------------------------------------------------------- plane algebra -- */
+static inline F4 viewprop(F4 n) {                                      /* pmhstereo.cl:119-124 */
+    return f4(1.0f / n.x, -n.y / n.x, -n.z / n.x, 0.0f);
+}
+static inline float transform_x(F4 s, float cx, float cy) {            /* :126-129 */
+    return s.x * cx + s.y * cy + s.z;
+}
+static F4 state_init(Rng& rng, float cx, float cy, int lr, float normmul, float depthmax) {  /* :50-68 */
+    float z = rng_float(rng) * depthmax;
+    float nx = (rng_float(rng) - 0.5f) * normmul * 0.95f;
+    float ny = (rng_float(rng) - 0.5f) * normmul * 0.95f;
+    nx = pm_clamp(nx, -0.95f, 0.95f);
+    ny = pm_clamp(ny, -0.95f, 0.95f);
+    float nfactor = fmaxf(sqrtf(nx * nx + ny * ny) + 0.001f, 1.0f);
+    nx = nx / nfactor; ny = ny / nfactor;
+    float nz = sqrtf(1.0f - nx * nx - ny * ny);
+    F4 ret = f4(1.0f - (-nx / nz), 0.0f - (-ny / nz), 0.0f - ((nx * cx + ny * cy) / nz + z), 0.0f - 0.0f);
+    if (!lr) ret = viewprop(ret);
+    return ret;
+}
+static F4 to_ref_normal_depth(F4 state, float cx, float cy, int lr) {  /* :70-86 */
+    F4 s = lr ? state : viewprop(state);
+    s = f4(1.0f - s.x, 0.0f - s.y, 0.0f - s.z, 0.0f - s.w);
+    F4 ret;
+    ret.w = s.x * cx + s.y * cy + s.z;
+    ret.z = pm_rsqrt(s.x * s.x + s.y * s.y + 1.0f);
+    ret.x = -s.x * ret.z;
+    ret.y = -s.y * ret.z;
+    if (!finite3(ret)) return f4(0.0f, 0.0f, 1.0f, 0.0f);
+    return ret;
+}
+static F4 state_refine(Rng& rng, F4 in, float cx, float cy, float depthmax, int lr) {  /* :88-117 */
+    F4 state = lr ? in : viewprop(in);
+    state = f4(1.0f - state.x, 0.0f - state.y, 0.0f - state.z, 0.0f - state.w);
+    float z = state.x * cx + state.y * cy + state.z;
+    float nz = pm_rsqrt(state.x * state.x + state.y * state.y + 1.0f);
+    float nx = -state.x * nz;
+    float ny = -state.y * nz;
+    z += (rng_float(rng) - 0.5f) * 2.0f;
+    z = pm_clamp(z, 0.0f, depthmax);
+    nx += (rng_float(rng) - 0.5f) * 0.1f;
+    ny += (rng_float(rng) - 0.5f) * 0.1f;
+    nx = pm_clamp(nx, -0.95f, 0.95f);
+    ny = pm_clamp(ny, -0.95f, 0.95f);
+    float nfactor = fmaxf(sqrtf(nx * nx + ny * ny) + 0.001f, 1.0f);
+    nx = nx / nfactor; ny = ny / nfactor;
+    nz = sqrtf(1.0f - nx * nx - ny * ny);
+    F4 ret = f4(-nx / nz, -ny / nz, (nx * cx + ny * cy) / nz + z, 0.0f);
+    ret = f4(1.0f - ret.x, 0.0f - ret.y, 0.0f - ret.z, 0.0f - ret.w);
+    if (!lr) return viewprop(state);   /* the reference returns the unperturbed state here (:114-115) */
+    return ret;
+}
+static inline void to_normal(F4 st, float n[3]) {                     /* :144-153 */
+    F4 s = f4(1.0f - st.x, 0.0f - st.y, 0.0f - st.z, 0.0f - st.w);
+    n[2] = pm_rsqrt(s.x * s.x + s.y * s.y + 1.0f);
+    n[0] = -s.x * n[2];
+    n[1] = -s.y * n[2];
+}
+static inline float dot4(F4 a, F4 b) { return ((a.x * b.x + a.y * b.y) + a.z * b.z) + a.w * b.w; }
+static void smooth_distance(F4 sa, F4 sb, F4 smooth, float cx, float cy, float depthmax, int lr,
+                            float* dA, float* dB) {                  /* :266-283 */
+    F4 a = to_ref_normal_depth(sa, cx, cy, lr);
+    F4 b = to_ref_normal_depth(sb, cx, cy, lr);
+    F4 diag = f4(1.0f, 1.0f, 0.0f, 1.0f / (depthmax * depthmax));
+    if (!finite3(sa) || !finite3(sb)) { *dA = 0.0f; *dB = 0.0f; return; }
+    F4 da = a - smooth;
+    *dA = dot4(da, diag * da);
+    F4 db = b - smooth;
+    *dB = dot4(db, diag * db);
+}
+
+/* -------------------------------------------------------- view images -- */
+struct View {
+    int W, H;
+    const F4* col;    /* RGBA input                       */
+    const F4* grad;   /* (dx, dy, dxy, dyx), :785-831      */
+    std::vector<float> rec; /* FAST: 14 floats per pixel: T(x) then T(x+1)-T(x) */
+};
+
+static void build_records(View& v) {
+    int W = v.W, H = v.H;
+    v.rec.assign((size_t)W * H * 14, 0.0f);
+    for (int y = 0; y < H; ++y)
+        for (int x = 0; x < W; ++x) {
+            const F4& c0 = v.col[(size_t)y * W + x];
+            const F4& g0 = v.grad[(size_t)y * W + x];
+            int x1 = std::min(x + 1, W - 1);
+            const F4& c1 = v.col[(size_t)y * W + x1];
+            const F4& g1 = v.grad[(size_t)y * W + x1];
+            float T0[7] = {c0.x, c0.y, c0.z, g0.x, g0.y, g0.z, g0.w};
+            float T1[7] = {c1.x, c1.y, c1.z, g1.x, g1.y, g1.z, g1.w};
+            float* r = &v.rec[((size_t)y * W + x) * 14];
+            for (int k = 0; k < 7; ++k) { r[k] = T0[k]; r[7 + k] = T1[k] - T0[k]; }
+        }
+}
+
+struct CostCfg {
+    int P;
+    float alpha, one_m_alpha, cmax, gmax;
+    int arith;
+    std::vector<float> prof;   /* (2P+1)^2 spatial profile */
+};
+
+static CostCfg make_cost_cfg(const cvtpm_params* p) {
+    CostCfg c;
+    c.P = p->patchsize;
+    c.alpha = p->color_alpha;
+    c.one_m_alpha = 1.0f - p->color_alpha;
+    c.cmax = p->color_maxdiff;
+    c.gmax = p->grad_maxdiff;
+    c.arith = p->arith;
+    int n = 2 * c.P + 1;
+    c.prof.resize((size_t)n * n);
+    for (int dy = -c.P; dy <= c.P; ++dy)
+        for (int dx = -c.P; dx <= c.P; ++dx)
+            c.prof[(size_t)(dy + c.P) * n + (dx + c.P)] = pm_profile(dx, dy, p->color_weight, p->weight_profile);
+    return c;
+}
+
+/* patch_eval_color_grad_weighted, pmhstereo.cl:170-228. */
+static float cost_eval(const CostCfg& k, const View& v1, const View& v2, int cx, int cy, F4 s) {
+    if (!finite3(s)) return 1e5f;
+    const int W = v1.W, H = v1.H, P = k.P, n = 2 * P + 1;
+    const float Wf = (float)W, Hf = (float)H;
+    const F4 vc = v1.col[(size_t)cy * W + cx];
+    if (k.arith == CVTPM_ARITH_EXACT) {
+        float wsum = 0.0f, ret = 0.0f;
+        for (int dy = -P; dy <= P; ++dy) {
+            for (int dx = -P; dx <= P; ++dx) {
+                float px = (float)cx + (float)dx, py = (float)cy + (float)dy;
+                if (px < 0 || px >= Wf || py < 0 || py >= Hf) continue;
+                const F4 a1 = v1.col[(size_t)(int)py * W + (int)px];
+                const F4 g1 = v1.grad[(size_t)(int)py * W + (int)px];
+                float d = (fabsf(vc.x - a1.x) + fabsf(vc.y - a1.y)) + fabsf(vc.z - a1.z);
+                float w1 = pm_exp(-d * k.prof[(size_t)(dy + P) * n + (dx + P)]);
+                float xp = s.x * px + s.y * py + s.z;
+                if (!(xp >= 0.0f && xp < Wf)) continue;
+                wsum += w1;
+                /* read_imagef(SAMPLER_BILINEAR, (xp+0.5, py+0.5)): the row is exact,
+                 * so the spec formula reduces to (1-a)*T0 + a*T1 */
+                float u = xp + 0.5f;
+                float t = u - 0.5f;
+                float fi = floorf(t);
+                float a = t - fi;
+                int i0 = clampi((int)fi, 0, W - 1);
+                int i1 = clampi((int)fi + 1, 0, W - 1);
+                const F4 c0 = v2.col[(size_t)(int)py * W + i0], c1 = v2.col[(size_t)(int)py * W + i1];
+                const F4 h0 = v2.grad[(size_t)(int)py * W + i0], h1 = v2.grad[(size_t)(int)py * W + i1];
+                float oa = 1.0f - a;
+                F4 a2 = f4(oa * c0.x + a * c1.x, oa * c0.y + a * c1.y, oa * c0.z + a * c1.z, 0.0f);
+                F4 g2 = f4(oa * h0.x + a * h1.x, oa * h0.y + a * h1.y, oa * h0.z + a * h1.z, oa * h0.w + a * h1.w);
+                float cc = (fminf(fabsf(a1.x - a2.x), k.cmax) + fminf(fabsf(a1.y - a2.y), k.cmax)) + fminf(fabsf(a1.z - a2.z), k.cmax);
+                float gc = ((fminf(fabsf(g1.x - g2.x), k.gmax) + fminf(fabsf(g1.y - g2.y), k.gmax)) + fminf(fabsf(g1.z - g2.z), k.gmax)) + fminf(fabsf(g1.w - g2.w), k.gmax);
+                float C = k.alpha * cc + k.one_m_alpha * gc;
+                ret += w1 * C;
+            }
+        }
+        if (wsum <= 1.1f) return 1e5f;
+        return ret / wsum;
+    }
+    /* ARITH_FAST: mirror of the CUDA fast kernel. */
+    float wsum = 0.0f, rc = 0.0f, rg = 0.0f;
+    for (int dy = -P; dy <= P; ++dy) {
+        int qy = cy + dy;
+        if (qy < 0 || qy >= H) continue;
+        float rowb = fmaf(s.y, (float)qy, s.z);
+        const float* rrow = &v2.rec[(size_t)qy * W * 14];
+        for (int dx = -P; dx <= P; ++dx) {
+            int qx = cx + dx;
+            if (qx < 0 || qx >= W) continue;
+            const F4 a1 = v1.col[(size_t)qy * W + qx];
+            const F4 g1 = v1.grad[(size_t)qy * W + qx];
+            float d = (fabsf(vc.x - a1.x) + fabsf(vc.y - a1.y)) + fabsf(vc.z - a1.z);
+            float w1 = pm_exp(-d * k.prof[(size_t)(dy + P) * n + (dx + P)]);
+            float xp = fmaf(s.x, (float)qx, rowb);
+            if (!(xp >= 0.0f && xp < Wf)) continue;
+            float fi = floorf(xp);
+            float a = xp - fi;
+            const float* r = rrow + (size_t)(int)fi * 14;
+            float v[7];
+            for (int c = 0; c < 7; ++c) v[c] = fmaf(a, r[7 + c], r[c]);
+            float cc = (fminf(fabsf(a1.x - v[0]), k.cmax) + fminf(fabsf(a1.y - v[1]), k.cmax)) + fminf(fabsf(a1.z - v[2]), k.cmax);
+            float gc = ((fminf(fabsf(g1.x - v[3]), k.gmax) + fminf(fabsf(g1.y - v[4]), k.gmax)) + fminf(fabsf(g1.z - v[5]), k.gmax)) + fminf(fabsf(g1.w - v[6]), k.gmax);
+            rc = fmaf(w1, cc, rc);
+            rg = fmaf(w1, gc, rg);
+            wsum = wsum + w1;
+        }
+    }
+    if (wsum <= 1.1f) return 1e5f;
+    return fmaf(k.alpha, rc, k.one_m_alpha * rg) / wsum;
+}
+
+/* ------------------------------------------------------ preprocessing -- */
+static inline float gray_at(const F4* img, int W, int H, int x, int y) {
+    if (x < 0 || y < 0 || x >= W || y >= H) return 0.0f;             /* CLK_ADDRESS_CLAMP */
+    F4 c = img[(size_t)y * W + x];
+    return ((c.x * 0.2126f + c.y * 0.7152f) + c.z * 0.0722f) + c.w * 0.0f;
+}
+static void gradxy(const F4* img, int W, int H, F4* out) {             /* :785-831 */
+#pragma omp parallel for schedule(static)
+    for (int y = 0; y < H; ++y)
+        for (int x = 0; x < W; ++x) {
+#define B(dx_, dy_) gray_at(img, W, H, x + (dx_), y + (dy_))
+            float dx = (B(1, 0) - B(-1, 0)) * 0.5f + (B(1, -1) - B(-1, -1)) * 0.25f + (B(1, 1) - B(-1, 1)) * 0.25f;
+            float dy = (B(0, 1) - B(0, -1)) * 0.5f + (B(-1, 1) - B(-1, -1)) * 0.25f + (B(1, 1) - B(1, -1)) * 0.25f;
+            float dxy = B(1, 1) - B(-1, -1);
+            float dyx = B(-1, 1) - B(1, -1);
+#undef B
+            out[(size_t)y * W + x] = f4(dx, dy, dxy, dyx);
+        }
+}
+static void edge_weight(const F4* img, int W, int H, float* out) {     /* :737-783 */
+#pragma omp parallel for schedule(static)
+    for (int y = 0; y < H; ++y)
+        for (int x = 0; x < W; ++x) {
+            float dx = gray_at(img, W, H, x + 1, y) - gray_at(img, W, H, x - 1, y);
+            float gy = gray_at(img, W, H, x, y - 1);
+            float dy = gy - gy;                                        /* the reference's dy (:769) */
+            out[(size_t)y * W + x] = pm_exp(-3.0f * pm_pow(sqrtf(dx * dx + dy * dy), 0.8f)) + 0.0001f;
+        }
+}
+
+/* ----------------------------------------------------------- view lists -- */
+/* Up to 4 source x per target pixel, smallest source x first; -1 = empty.
+ * Restates the scatter of pmhstereo.cl:394-400 (see the header). */
+static void build_view_list(const F4* src, int W, int H, int16_t* list) {
+#pragma omp parallel for schedule(static)
+    for (int y = 0; y < H; ++y) {
+        std::vector<uint8_t> cnt(W, 0);
+        int16_t* row = list + (size_t)y * W * 4;
+        for (int i = 0; i < W * 4; ++i) row[i] = -1;
+        for (int x = 0; x < W; ++x) {
+            F4 s = src[(size_t)y * W + x];
+            float v = transform_x(s, (float)x, (float)y) + 0.5f;
+            if (v > -1.0f && v < (float)W) {
+                int d = (int)v;
+                if (cnt[d] < 4) row[d * 4 + cnt[d]++] = (int16_t)x;
+            }
+        }
+    }
+}
+
+/* --------------------------------------------------------- init/prop -- */
+struct Pass {
+    const View* v1; const View* v2;
+    const CostCfg* k;
+    int lr, iter, rngkind; uint64_t seed;
+    float depthmax, theta;
+};
+
+static inline uint32_t view_id(int lr) { return lr ? 0u : 1u; }
+
+static void init_pass(const Pass& ps, F4* out) {                      /* :230-248 */
+    const int W = ps.v1->W, H = ps.v1->H;
+#pragma omp parallel for schedule(dynamic, 1)
+    for (int y = 0; y < H; ++y)
+        for (int x = 0; x < W; ++x) {
+            Rng rng;
+            uint32_t p = (uint32_t)(y * W + x);
+            if (ps.rngkind == CVTPM_RNG_PHILOX) philox_init(rng, ps.seed, p, PHILOX_TAG_INIT, view_id(ps.lr));
+            else mwc_init(rng, (uint64_t)p * 3u);
+            F4 s = state_init(rng, (float)x, (float)y, ps.lr, 1.0f, ps.depthmax);
+            s.w = cost_eval(*ps.k, *ps.v1, *ps.v2, x, y, s);
+            out[(size_t)y * W + x] = s;
+        }
+}
+
+/* pmhstereo_propagate_view, pmhstereo.cl:286-404, without the scatter
+ * (build_view_list runs after the pass). */
+static void propagate_pass(const Pass& ps, const F4* old, const F4* smoothimg,
+                           const int16_t* viewin, const F4* viewsrc, F4* out, uint8_t* winners) {
+    const int W = ps.v1->W, H = ps.v1->H;
+    const float dmax = ps.depthmax, theta = ps.theta;
+    const int lr = ps.lr;
+#pragma omp parallel for schedule(dynamic, 1)
+    for (int y = 0; y < H; ++y)
+        for (int x = 0; x < W; ++x) {
+            const float cx = (float)x, cy = (float)y;
+            F4 sm = smoothimg[(size_t)y * W + x];                       /* :320-323 */
+            float nf = fmaxf(sqrtf(sm.x * sm.x + sm.y * sm.y) + 0.001f, 1.0f);
+            float smx = sm.x / nf, smy = sm.y / nf;
+            F4 smooth = f4(smx, smy, sqrtf(1.0f - smx * smx - smy * smy), sm.z * dmax);
+            F4 self = old[(size_t)y * W + x];                           /* :325 */
+            int win = 0;
+            Rng rng;                                                     /* :327 */
+            uint32_t p = (uint32_t)(y * W + x);
+            if (ps.rngkind == CVTPM_RNG_PHILOX) philox_init(rng, ps.seed, p, (uint32_t)ps.iter, view_id(lr));
+            else mwc_init(rng, ((uint64_t)p + (uint64_t)ps.iter) * 45u);
+            auto consider = [&](F4 cand, int idx) {
+                cand.w = cost_eval(*ps.k, *ps.v1, *ps.v2, x, y, cand);
+                float da, db;
+                smooth_distance(cand, self, smooth, cx, cy, dmax, lr, &da, &db);
+                if (cand.w + theta * da <= self.w + theta * db) { self = cand; win = idx; }
+            };
+            int idx = 1;
+            for (int py = -1; py <= 1; ++py)                             /* :330-342 */
+                for (int px = -1; px <= 1; ++px) {
+                    if (px == 0 && py == 0) continue;
+                    int nx = clampi(x + px, 0, W - 1), ny = clampi(y + py, 0, H - 1);
+                    consider(old[(size_t)ny * W + nx], idx++);
+                }
+            {                                                            /* :345-352 */
+                F4 c = f4(1.0f - (-smooth.x / smooth.z), 0.0f - (-smooth.y / smooth.z),
+                          0.0f - ((smooth.x * cx + smooth.y * cy) / smooth.z + smooth.w), 0.0f - 0.0f);
+                if (!lr) c = viewprop(c);
+                consider(c, 9);
+            }
+            for (int i = 0; i < 6; ++i) {                                /* :355-361 */
+                int ox = (int)(rng_float(rng) * 7.0f + 0.5f);
+                int oy = (int)(rng_float(rng) * 7.0f + 0.5f);
+                int nx = clampi(x + ox, 0, W - 1), ny = clampi(y + oy, 0, H - 1);
+                consider(old[(size_t)ny * W + nx], 10 + i);
+            }
+            consider(state_init(rng, cx, cy, lr, 2.0f, dmax), 16);      /* :364-368 */
+            if (viewin) {                                                /* :372-379 */
+                const int16_t* l = viewin + ((size_t)y * W + x) * 4;
+                for (int i = 0; i < 4 && l[i] >= 0; ++i)
+                    consider(viewprop(viewsrc[(size_t)y * W + l[i]]), 17 + i);
+            }
+            for (int i = 0; i < 2; ++i)                                  /* :383-389 */
+                consider(state_refine(rng, self, cx, cy, dmax, lr), 21 + i);
+            out[(size_t)y * W + x] = self;
+            if (winners) winners[(size_t)y * W + x] = (uint8_t)win;
+        }
+}
+
+/* ------------------------------------------------- consistency / fill -- */
+static void consistency(const F4* L, const F4* R, int W, int H, float maxdisp, float maxangle,
+                        int lr, F4* out, uint8_t* valid) {             /* :428-464 */
+    const float athr = maxangle / 180.0f;
+#pragma omp parallel for schedule(static)
+    for (int y = 0; y < H; ++y)
+        for (int x = 0; x < W; ++x) {
+            F4 sl = L[(size_t)y * W + x];
+            float x2 = transform_x(sl, (float)x, (float)y);
+            F4 sr;
+            if (x2 < 0 || x2 >= (float)W) sr = f4s(1e5f);
+            else sr = R[(size_t)y * W + clampi(f2i_nan0(roundf(x2)), 0, W - 1)];
+            float na[3], nb[3];
+            if (lr) { to_normal(sl, na); to_normal(viewprop(sr), nb); }
+            else { to_normal(sr, na); to_normal(viewprop(sl), nb); }
+            float ndiff = (na[0] * nb[0] + na[1] * nb[1]) + na[2] * nb[2];
+            float dm = fabsf((float)x - transform_x(sr, x2, (float)y));
+            bool bad = (dm >= maxdisp) || (pm_acospi(ndiff) >= athr);
+            out[(size_t)y * W + x] = bad ? f4s(0.0f) : sl;
+            if (valid) valid[(size_t)y * W + x] = bad ? 0 : 1;
+        }
+}
+
+/* nearest index to the left/right of each x whose value passes `ok` */
+template <class OK>
+static void row_neighbours(const F4* row, int W, OK ok, std::vector<int>& lft, std::vector<int>& rgt) {
+    lft.assign(W, -1); rgt.assign(W, -1);
+    int last = -1;
+    for (int x = 0; x < W; ++x) { lft[x] = last; if (ok(row[x])) last = x; }
+    last = -1;
+    for (int x = W - 1; x >= 0; --x) { rgt[x] = last; if (ok(row[x])) last = x; }
+}
+
+static void fill_state(const F4* in, int W, int H, float depthmax, int lr, F4* out) {  /* :466-510 */
+#pragma omp parallel for schedule(static)
+    for (int y = 0; y < H; ++y) {
+        const F4* row = in + (size_t)y * W;
+        std::vector<int> lft, rgt;
+        row_neighbours(row, W, [](F4 v) { return !(len4(v) < 1e-1f); }, lft, rgt);
+        for (int x = 0; x < W; ++x) {
+            F4 st = row[x], val;
+            const float cx = (float)x, cy = (float)y;
+            if (len4(st) < 1e-1f) {
+                F4 l = lft[x] >= 0 ? row[lft[x]] : f4s(1e5f);
+                F4 r = rgt[x] >= 0 ? row[rgt[x]] : f4s(1e5f);
+                l.w = fabsf(transform_x(l, cx, cy) - cx);
+                r.w = fabsf(transform_x(r, cx, cy) - cx);
+                val = (l.w < r.w) ? l : r;
+            } else {
+                val = st;
+            }
+            val = to_ref_normal_depth(val, cx, cy, lr);
+            out[(size_t)y * W + x] = f4(val.x, val.y, val.w / depthmax, 1.0f);
+        }
+    }
+}
+
+static void fill_depthmap(const F4* in, int W, int H, float scale, float* out) {  /* :512-555 */
+#pragma omp parallel for schedule(static)
+    for (int y = 0; y < H; ++y) {
+        const F4* row = in + (size_t)y * W;
+        std::vector<int> lft, rgt;
+        row_neighbours(row, W, [](F4 v) { return !(len3(v) < 1e-1f); }, lft, rgt);
+        for (int x = 0; x < W; ++x) {
+            F4 st = row[x];
+            const float cx = (float)x, cy = (float)y;
+            float v;
+            if (len3(st) < 1e-1f) {
+                F4 l = lft[x] >= 0 ? row[lft[x]] : f4(-1e5f, -1e5f, -1e5f, row[0].w);
+                F4 r = rgt[x] >= 0 ? row[rgt[x]] : f4(-1e5f, -1e5f, -1e5f, row[W - 1].w);
+                float lw = -(transform_x(l, cx, cy) - cx);
+                float rw = -(transform_x(r, cx, cy) - cx);
+                v = fminf(lw, rw);
+            } else {
+                v = fabsf(transform_x(st, cx, cy) - cx);
+            }
+            out[(size_t)y * W + x] = v * scale;
+        }
+    }
+}
+
+static void fill_normalmap(const F4* in, int W, int H, F4* out) {      /* :557-603 */
+#pragma omp parallel for schedule(static)
+    for (int y = 0; y < H; ++y) {
+        const F4* row = in + (size_t)y * W;
+        std::vector<int> lft, rgt;
+        row_neighbours(row, W, [](F4 v) { return !(len3(v) < 1e-1f); }, lft, rgt);
+        for (int x = 0; x < W; ++x) {
+            F4 st = row[x];
+            const float cx = (float)x, cy = (float)y;
+            float n[3];
+            if (len3(st) < 1e-1f) {
+                F4 l = lft[x] >= 0 ? row[lft[x]] : f4(-1e5f, -1e5f, -1e5f, 0.0f);
+                F4 r = rgt[x] >= 0 ? row[rgt[x]] : f4(-1e5f, -1e5f, -1e5f, 0.0f);
+                float lw = -(transform_x(l, cx, cy) - cx);
+                float rw = -(transform_x(r, cx, cy) - cx);
+                to_normal((lw < rw) ? l : r, n);
+            } else {
+                to_normal(st, n);
+            }
+            out[(size_t)y * W + x] = f4(n[0], n[1], n[2], 0.0f);
+        }
+    }
+}
+
+/* ------------------------------------------------------------ PD ROF -- */
+/* One PDHuberWeighted launch, PDHuberWeighted.cl:34-104. */
+static void pd_step(F4* uout, F4* pout, const F4* last, const F4* pin, const F4* f,
+                    const float* wgt, float lambda, int W, int H) {
+    const float SIGMA = 1.0f / sqrtf(8.0f), TAU = 1.0f / sqrtf(8.0f);
+    const float THETA = 0.5f, ALPHA = 0.001f;
+    auto U = [&](int x, int y) { return last[(size_t)clampi(y, 0, H - 1) * W + clampi(x, 0, W - 1)]; };
+    auto pnew = [&](int qx, int qy, F4* lo, F4* hi) {                 /* :49-68 */
+        bool in = qx >= 0 && qy >= 0 && qx < W && qy < H;
+        float w = in ? wgt[(size_t)qy * W + qx] : 0.0f;
+        F4 uq = U(qx, qy);
+        F4 dx = w * (uq - U(qx + 1, qy));
+        F4 dy = w * (uq - U(qx, qy + 1));
+        F4 plo = in ? pin[((size_t)qy * W + qx) * 2] : f4s(0.0f);
+        F4 phi = in ? pin[((size_t)qy * W + qx) * 2 + 1] : f4s(0.0f);
+        float den = 1.0f + SIGMA * ALPHA / w;
+        F4 l = (plo + SIGMA * dx) / f4s(den);
+        F4 h = (phi + SIGMA * dy) / f4s(den);
+        F4 pt = l * l + h * h;
+        float sxy = sqrtf(pt.x + pt.y);
+        F4 pproj = f4(fmaxf(1.0f, sxy), fmaxf(1.0f, sxy), fmaxf(1.0f, sqrtf(pt.z)), fmaxf(1.0f, sqrtf(0.0f)));
+        *lo = l / pproj; *hi = h / pproj;
+    };
+#pragma omp parallel for schedule(static)
+    for (int y = 0; y < H; ++y)
+        for (int x = 0; x < W; ++x) {
+            F4 lo, hi, lol, hil, lou, hiu;
+            pnew(x, y, &lo, &hi);
+            pnew(x - 1, y, &lol, &hil);
+            pnew(x, y - 1, &lou, &hiu);
+            F4 div = lo - lol + hi - hiu;                                 /* :73-74 */
+            F4 img = f[(size_t)y * W + x];
+            F4 uc = last[(size_t)y * W + x];
+            float wc = wgt[(size_t)y * W + x];
+            F4 lam = f4s(lambda);
+            F4 un = (uc + TAU * (lam * img - wc * div)) / (f4s(1.0f) + TAU * lam);  /* :76 */
+            un = un + THETA * (un - uc);
+            un.w = 1.0f;
+            uout[(size_t)y * W + x] = un;
+            pout[((size_t)y * W + x) * 2] = lo;
+            pout[((size_t)y * W + x) * 2 + 1] = hi;
+        }
+}
+
+/* PDROF::apply, cvt/gfx/PDROF.h:50-96.  `output` is read as the warm start. */
+static void pd_apply(F4* output, const F4* input, const float* wgt, float lambda, int iters, int W, int H) {
+    size_t n = (size_t)W * H;
+    std::vector<F4> tmp(input, input + n);
+    std::vector<F4> p1(2 * n, f4s(0.0f)), p2(2 * n, f4s(0.0f));
+    F4* img[2] = {tmp.data(), output};
+    F4* pp[2] = {p1.data(), p2.data()};
+    int swap = 0;
+    for (int i = 0; i < iters; ++i) {
+        swap = i & 1;
+        pd_step(img[swap], pp[swap], img[1 - swap], pp[1 - swap], input, wgt, lambda, W, H);
+    }
+    if (!swap) pd_step(img[1], pp[1], img[0], pp[0], input, wgt, lambda, W, H);
+}
+
+static float smoothstep01(float x) {                                   /* cvt/math/Math.h:88-92 */
+    float t = (x < 0.0f) ? 0.0f : (x > 1.0f) ? 1.0f : x;
+    return t * t * (3.0f - 2.0f * t);
+}
+
+static bool check_params(const cvtpm_params* p) {
+    return p && p->patchsize >= 1 && p->patchsize <= 31 && p->depthmax > 0.0f && p->iterations >= 1 &&
+           p->pd_iterations >= 0 && (p->arith == CVTPM_ARITH_EXACT || p->arith == CVTPM_ARITH_FAST) &&
+           (p->rng == CVTPM_RNG_MWC64X || p->rng == CVTPM_RNG_PHILOX);
+}
+
+struct Views {
+    std::vector<F4> gl, gr;
+    View L, R;
+};
+
+static void make_views(const float* left, const float* right, int W, int H, int arith, Views& v) {
+    size_t n = (size_t)W * H;
+    v.gl.resize(n); v.gr.resize(n);
+    gradxy((const F4*)left, W, H, v.gl.data());
+    gradxy((const F4*)right, W, H, v.gr.data());
+    v.L.W = v.R.W = W; v.L.H = v.R.H = H;
+    v.L.col = (const F4*)left; v.R.col = (const F4*)right;
+    v.L.grad = v.gl.data(); v.R.grad = v.gr.data();
+    if (arith == CVTPM_ARITH_FAST) { build_records(v.L); build_records(v.R); }
+}
+
+}  // namespace
+
+/* ===================================================== extern "C" API == */
+extern "C" {
+
+void orc_set_threads(int n) {
+#ifdef _OPENMP
+    if (n > 0) omp_set_num_threads(n);
+#else
+    (void)n;
+#endif
+}
+int orc_max_threads(void) {
+#ifdef _OPENMP
+    return omp_get_max_threads();
+#else
+    return 1;
+#endif
+}
+
+void orc_gradxy(const float* img, int W, int H, float* out) { gradxy((const F4*)img, W, H, (F4*)out); }
+void orc_edge_weight(const float* img, int W, int H, float* out) { edge_weight((const F4*)img, W, H, out); }
+
+float orc_exp(float x) { return pm_exp(x); }
+float orc_pow(float x, float y) { return pm_pow(x, y); }
+float orc_acospi(float x) { return pm_acospi(x); }
+void orc_exp_array(const float* x, float* y, long n) { for (long i = 0; i < n; ++i) y[i] = pm_exp(x[i]); }
+void orc_pow_array(const float* x, float e, float* y, long n) { for (long i = 0; i < n; ++i) y[i] = pm_pow(x[i], e); }
+void orc_acospi_array(const float* x, float* y, long n) { for (long i = 0; i < n; ++i) y[i] = pm_acospi(x[i]); }
+
+uint64_t orc_mwc_mulmod_serial(uint64_t a, uint64_t b) { return mwc_mulmod_serial(a, b, MWC_M); }
+uint64_t orc_mwc_mulmod(uint64_t a, uint64_t b) { return mwc_mulmod(a, b, MWC_M); }
+/* n consecutive floats of the stream RNG_init(linpos, numdraws) */
+void orc_mwc_stream(uint64_t distance, int n, float* out) {
+    Rng r; mwc_init(r, distance);
+    for (int i = 0; i < n; ++i) out[i] = mwc_float(r);
+}
+/* state (x, c) after skipping `distance` steps */
+void orc_mwc_state(uint64_t distance, uint32_t* x, uint32_t* c) {
+    Rng r; mwc_init(r, distance); *x = r.x; *c = r.c;
+}
+void orc_philox(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]) { philox10(ctr, key, out); }
+void orc_philox_stream(uint64_t seed, uint32_t pixel, uint32_t tag, uint32_t view, int n, float* out) {
+    Rng r; philox_init(r, seed, pixel, tag, view);
+    for (int i = 0; i < n; ++i) out[i] = philox_float(r);
+}
+
+/* Aggregated cost of every pixel for a fixed state field (float4 per pixel). */
+int orc_cost_field(const cvtpm_params* prm, const float* img1, const float* img2, int W, int H,
+                   const float* states, float* cost) {
+    if (!check_params(prm)) return CVTPM_ERR_INVALID_ARGUMENT;
+    Views v;
+    make_views(img1, img2, W, H, prm->arith, v);
+    CostCfg k = make_cost_cfg(prm);
+#pragma omp parallel for schedule(dynamic, 1)
+    for (int y = 0; y < H; ++y)
+        for (int x = 0; x < W; ++x) {
+            const float* s = states + ((size_t)y * W + x) * 4;
+            cost[(size_t)y * W + x] = cost_eval(k, v.L, v.R, x, y, f4(s[0], s[1], s[2], s[3]));
+        }
+    return CVTPM_OK;
+}
+
+/* pmhstereo_init for view lr (img1 = that view). */
+int orc_init(const cvtpm_params* prm, const float* img1, const float* img2, int W, int H, int lr, float* out) {
+    if (!check_params(prm)) return CVTPM_ERR_INVALID_ARGUMENT;
+    Views v;
+    make_views(img1, img2, W, H, prm->arith, v);
+    CostCfg k = make_cost_cfg(prm);
+    Pass ps = {&v.L, &v.R, &k, lr, 0, prm->rng, prm->seed, prm->depthmax, 0.0f};
+    init_pass(ps, (F4*)out);
+    return CVTPM_OK;
+}
+
+/* One propagation pass of view lr (img1 = that view) with optional view list
+ * (W*H*4 int16, sources in viewsrc, the other view's states). */
+int orc_propagate(const cvtpm_params* prm, const float* img1, const float* img2, int W, int H, int lr,
+                  int iter, float theta, const float* old, const float* smooth,
+                  const int16_t* viewin, const float* viewsrc, float* out, uint8_t* winners) {
+    if (!check_params(prm)) return CVTPM_ERR_INVALID_ARGUMENT;
+    Views v;
+    make_views(img1, img2, W, H, prm->arith, v);
+    CostCfg k = make_cost_cfg(prm);
+    Pass ps = {&v.L, &v.R, &k, lr, iter, prm->rng, prm->seed, prm->depthmax, theta};
+    propagate_pass(ps, (const F4*)old, (const F4*)smooth, viewin, (const F4*)viewsrc, (F4*)out, winners);
+    return CVTPM_OK;
+}
+
+void orc_view_list(const float* src, int W, int H, int16_t* list) { build_view_list((const F4*)src, W, H, list); }
+
+void orc_consistency(const float* L, const float* R, int W, int H, float maxdisp, float maxangle, int lr,
+                     float* out, uint8_t* valid) {
+    consistency((const F4*)L, (const F4*)R, W, H, maxdisp, maxangle, lr, (F4*)out, valid);
+}
+void orc_fill_state(const float* in, int W, int H, float depthmax, int lr, float* out) {
+    fill_state((const F4*)in, W, H, depthmax, lr, (F4*)out);
+}
+void orc_fill_depthmap(const float* in, int W, int H, float scale, float* out) {
+    fill_depthmap((const F4*)in, W, H, scale, out);
+}
+void orc_fill_normalmap(const float* in, int W, int H, float* out) {
+    fill_normalmap((const F4*)in, W, H, (F4*)out);
+}
+void orc_pd_step(float* uout, float* pout, const float* last, const float* pin, const float* f,
+                 const float* wgt, float lambda, int W, int H) {
+    pd_step((F4*)uout, (F4*)pout, (const F4*)last, (const F4*)pin, (const F4*)f, wgt, lambda, W, H);
+}
+void orc_pd_apply(float* output, const float* input, const float* wgt, float lambda, int iters, int W, int H) {
+    pd_apply((F4*)output, (const F4*)input, wgt, lambda, iters, W, H);
+}
+
+/* PMHuberStereo::depthMap, PMHuberStereo.cpp:64-291. */
+int orc_depthmap(const cvtpm_params* prm, const float* left, const float* right, int W, int H,
+                 float* dmap, float* normalmap, float* states_out, uint8_t* winners, uint8_t* valid) {
+    if (!check_params(prm) || !left || !right || !dmap || W < 1 || H < 1) return CVTPM_ERR_INVALID_ARGUMENT;
+    const size_t n = (size_t)W * H;
+    const int N = prm->iterations;
+    const float dmax = prm->depthmax;
+    const float dscale = prm->dscale <= 0.0f ? 1.0f / dmax : prm->dscale;
+    Views v;
+    make_views(left, right, W, H, prm->arith, v);
+    CostCfg k = make_cost_cfg(prm);
+    std::vector<float> wl(n), wr(n);                                   /* :99-106 */
+    edge_weight((const F4*)left, W, H, wl.data());
+    edge_weight((const F4*)right, W, H, wr.data());
+    std::vector<F4> smL(n, f4s(0.0f)), smR(n, f4s(0.0f));              /* :108-113 */
+    std::vector<F4> SL[2] = {std::vector<F4>(n), std::vector<F4>(n)};
+    std::vector<F4> SR[2] = {std::vector<F4>(n), std::vector<F4>(n)};
+    std::vector<F4> tmp(n), tmp2(n);
+    std::vector<int16_t> list1(n * 4, -1), list2(n * 4, -1);
+    std::vector<uint8_t> winL(n, 0), winR(n, 0);
+    Pass pl = {&v.L, &v.R, &k, 1, 0, prm->rng, prm->seed, dmax, 0.0f};
+    Pass pr = {&v.R, &v.L, &k, 0, 0, prm->rng, prm->seed, dmax, 0.0f};
+    init_pass(pl, SL[0].data());                                       /* :124-143 */
+    init_pass(pr, SR[0].data());
+    float theta = 0.0f;
+    for (int iter = 0; iter < N; ++iter) {                             /* :151-266 */
+        int swap = iter & 1;
+        pl.iter = pr.iter = iter;
+        pl.theta = pr.theta = theta;
+        propagate_pass(pl, SL[swap].data(), smL.data(), list2.data(), SR[swap].data(), SL[1 - swap].data(), winL.data());
+        build_view_list(SL[1 - swap].data(), W, H, list1.data());
+        propagate_pass(pr, SR[swap].data(), smR.data(), list1.data(), SL[1 - swap].data(), SR[1 - swap].data(), winR.data());
+        build_view_list(SR[1 - swap].data(), W, H, list2.data());
+        float lambda = theta * prm->thetascale + 5.0f;
+        consistency(SL[1 - swap].data(), SR[1 - swap].data(), W, H, prm->maxdispdiff, prm->maxanglediff, 1, tmp.data(), nullptr);
+        fill_state(tmp.data(), W, H, dmax, 1, tmp2.data());
+        pd_apply(smL.data(), tmp2.data(), wl.data(), lambda, prm->pd_iterations, W, H);
+        consistency(SR[1 - swap].data(), SL[1 - swap].data(), W, H, prm->maxdispdiff, prm->maxanglediff, 0, tmp.data(), nullptr);
+        fill_state(tmp.data(), W, H, dmax, 0, tmp2.data());
+        pd_apply(smR.data(), tmp2.data(), wr.data(), lambda, prm->pd_iterations, W, H);
+        if (iter >= 5) theta = smoothstep01(((float)iter - 5.0f) / ((float)N - 5.0f)) * 1.0f;
+    }
+    int fin = 1 - ((N - 1) & 1);
+    consistency(SL[fin].data(), SR[fin].data(), W, H, prm->maxdispdiff, prm->maxanglediff, 1, tmp.data(), valid);
+    fill_depthmap(tmp.data(), W, H, dscale, dmap);
+    if (normalmap) fill_normalmap(tmp.data(), W, H, (F4*)normalmap);
+    if (states_out) {
+        memcpy(states_out, SL[fin].data(), n * sizeof(F4));
+        memcpy(states_out + 4 * n, SR[fin].data(), n * sizeof(F4));
+    }
+    if (winners) { memcpy(winners, winL.data(), n); memcpy(winners + n, winR.data(), n); }
+    return CVTPM_OK;
+}
+
+}  // extern "C"

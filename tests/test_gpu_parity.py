@@ -1,0 +1,145 @@
+"""GPU parity: libcvtpm.so (through the C ABI) against the CPU oracle on the
+same seeded inputs.  Integer outputs (winning hypothesis, validity mask) and
+every float output are compared bit for bit: both sides use the same
+arithmetic (EXACT = the reference's operation order; FAST = the fused form the
+oracle mirrors)."""
+import numpy as np
+import pytest
+import torch
+
+from cvt_gb300 import scenes
+from cvt_gb300.params import (default_params, PRESET_REFERENCE, PRESET_BASELINE, ARITH_EXACT, ARITH_FAST,
+                              RNG_MWC64X, RNG_PHILOX)
+
+pytestmark = pytest.mark.gpu
+
+MODES = [(ARITH_EXACT, RNG_MWC64X), (ARITH_FAST, RNG_PHILOX), (ARITH_EXACT, RNG_PHILOX), (ARITH_FAST, RNG_MWC64X)]
+MODE_IDS = ["exact-mwc64x", "fast-philox", "exact-philox", "fast-mwc64x"]
+
+
+def bits(a):
+    a = np.ascontiguousarray(a)
+    return a.view(np.uint32) if a.dtype == np.float32 else a
+
+
+def assert_bitexact(got, want, what):
+    got, want = np.asarray(got), np.asarray(want)
+    assert got.shape == want.shape, what
+    diff = bits(got) != bits(want)
+    assert not diff.any(), f"{what}: {int(diff.sum())} of {diff.size} differ, first at {np.argwhere(diff)[0]}"
+
+
+@pytest.fixture(scope="module")
+def stereo(cuda):
+    from cvt_gb300.stereo import PMHuberStereo
+    return PMHuberStereo(0)
+
+
+def to_dev(a):
+    return torch.from_numpy(np.ascontiguousarray(a, np.float32)).cuda()
+
+
+def plane_states(sc, rng, lr=1):
+    """Ground-truth planes as reference states, perturbed, plus random and
+    non-finite entries."""
+    H, W = sc.labels.shape
+    pf = sc.plane_field().astype(np.float64)
+    a = pf[..., 0] + rng.normal(0, 0.01, (H, W))
+    b = pf[..., 1] + rng.normal(0, 0.01, (H, W))
+    c = pf[..., 2] + rng.normal(0, 1.0, (H, W))
+    s = np.zeros((H, W, 4), np.float32)
+    s[..., 0], s[..., 1], s[..., 2] = 1.0 - a, -b, -c        # x' = x - d
+    m = rng.random((H, W)) < 0.05
+    s[m, 0] = rng.uniform(-1, 3, m.sum())
+    s[m, 2] = rng.uniform(-100, 100, m.sum())
+    s[0, 0, 0] = np.inf
+    s[0, 1, 2] = np.nan
+    return s
+
+
+@pytest.mark.parametrize("arith", [ARITH_EXACT, ARITH_FAST], ids=["exact", "fast"])
+@pytest.mark.parametrize("preset", [PRESET_REFERENCE, PRESET_BASELINE], ids=["ref", "baseline"])
+def test_cost_field_bitexact(stereo, oracle, arith, preset):
+    sc = scenes.make_scene(83, 61, 5, 20.0, seed=21)
+    st = plane_states(sc, np.random.default_rng(3))
+    p = default_params(preset, arith=arith, patchsize=17, depthmax=20.0)
+    stereo.set_params(p)
+    got = stereo.cost(to_dev(sc.left), to_dev(sc.right), to_dev(st)).cpu().numpy()
+    want = oracle.cost_field(p, sc.left, sc.right, st)
+    assert_bitexact(got, want, "cost")
+    assert (got[0, 0] == 1e5) and (got[0, 1] == 1e5)
+
+
+def run_both(stereo, oracle, sc, p, normalmap=True):
+    stereo.set_params(p)
+    dm = torch.empty(0, device="cuda")
+    nm = torch.empty(0, device="cuda") if normalmap else None
+    tr = {}
+    stereo.depthMap(dm, to_dev(sc.left), to_dev(sc.right), p.patchsize, p.depthmax, p.iterations, 4,
+                    p.dscale, nm, trace=tr)
+    torch.cuda.synchronize()
+    want, ex = oracle.depthmap(p, sc.left, sc.right, normalmap=normalmap, trace=True)
+    return dm.cpu().numpy(), (nm.cpu().numpy() if normalmap else None), {k: v.cpu().numpy() for k, v in tr.items()}, want, ex
+
+
+@pytest.mark.parametrize("mode", MODES, ids=MODE_IDS)
+def test_depthmap_bitexact(stereo, oracle, mode):
+    arith, rng = mode
+    sc = scenes.make_scene(96, 64, 4, 16.0, seed=5)
+    p = default_params(PRESET_REFERENCE, arith=arith, rng=rng, seed=99, patchsize=7, depthmax=16.0,
+                       iterations=3, pd_iterations=20)
+    dm, nm, tr, want, ex = run_both(stereo, oracle, sc, p)
+    assert_bitexact(tr["winners"], ex["winners"], "winners")
+    assert_bitexact(tr["valid"], ex["valid"], "valid")
+    assert_bitexact(tr["states"], ex["states"], "states")
+    assert_bitexact(dm, want, "dmap")
+    assert_bitexact(nm, ex["normalmap"], "normalmap")
+
+
+def test_depthmap_theta_ramp(stereo, oracle):
+    """7 iterations: the smoothness coupling theta becomes non-zero in the last
+    (PMHuberStereo.cpp:264-265)."""
+    sc = scenes.make_scene(72, 48, 3, 12.0, seed=8)
+    p = default_params(PRESET_REFERENCE, patchsize=5, depthmax=12.0, iterations=7, pd_iterations=12)
+    dm, _, tr, want, ex = run_both(stereo, oracle, sc, p, normalmap=False)
+    assert_bitexact(tr["winners"], ex["winners"], "winners")
+    assert_bitexact(tr["states"], ex["states"], "states")
+    assert_bitexact(dm, want, "dmap")
+
+
+@pytest.mark.parametrize("W,H,P", [(37, 29, 17), (1, 1, 3), (33, 9, 2), (130, 17, 4)])
+def test_depthmap_odd_sizes(stereo, oracle, W, H, P):
+    sc = scenes.make_scene(W, H, 2, 8.0, seed=W * 100 + H)
+    p = default_params(PRESET_BASELINE, patchsize=P, depthmax=8.0, iterations=2, pd_iterations=5)
+    dm, nm, tr, want, ex = run_both(stereo, oracle, sc, p)
+    assert_bitexact(tr["winners"], ex["winners"], "winners")
+    assert_bitexact(tr["states"], ex["states"], "states")
+    assert_bitexact(dm, want, "dmap")
+
+
+def test_pitched_input_and_host_entry(stereo, oracle):
+    sc = scenes.make_scene(50, 30, 3, 10.0, seed=4)
+    p = default_params(PRESET_BASELINE, patchsize=5, depthmax=10.0, iterations=2, pd_iterations=4)
+    stereo.set_params(p)
+    wide = torch.zeros((30, 64, 4), device="cuda")
+    wide[:, :50] = to_dev(sc.left)
+    wide2 = torch.zeros((30, 64, 4), device="cuda")
+    wide2[:, :50] = to_dev(sc.right)
+    dm = stereo.depthMap(None, wide[:, :50], wide2[:, :50], 5, 10.0, 2, 4)
+    want, _ = oracle.depthmap(p, sc.left, sc.right)
+    assert_bitexact(dm.cpu().numpy(), want, "dmap pitched")
+    host = stereo.depthMapHost(sc.left, sc.right, 5, 10.0, 2, 4)
+    assert_bitexact(host, want, "dmap host")
+
+
+def test_errors(stereo):
+    from cvt_gb300.stereo import CVTException
+    from cvt_gb300._lib import CvtpmError
+    a = torch.zeros((10, 12, 4), device="cuda")
+    b = torch.zeros((10, 13, 4), device="cuda")
+    with pytest.raises(CVTException):
+        stereo.depthMap(None, a, b, 3, 8.0, 1, 4)
+    with pytest.raises(CvtpmError):
+        stereo.depthMap(None, a, a, 40, 8.0, 1, 4)
+    with pytest.raises(CvtpmError):
+        stereo.depthMap(None, a, a, 3, -1.0, 1, 4)
