@@ -72,7 +72,11 @@ PM_DEV void seed_rng(PmRng& rng, const PmPassArgs& a, int x, int y, bool init) {
     if (a.rng == CVTPM_RNG_PHILOX)
         philox_seed(rng, a.key0, a.key1, p, init ? PM_PHILOX_TAG_INIT : (uint32_t)a.iter, a.lr ? 0u : 1u);
     else
-        mwc_seed(rng, init ? (unsigned long long)p * 3ull : ((unsigned long long)p + (unsigned long long)a.iter) * 45ull);
+        /* init: RNG_init(p, 3) (pmhstereo.cl:241).  propagate: RNG_init(p + iter, N)
+         * with N the unparenthesised ((3*3-1)+3)*3 + 2*6, i.e. distance
+         * 33(p + iter) + 12 (RNG.cl:151-154, pmhstereo.cl:327). */
+        mwc_seed(rng, init ? (unsigned long long)p * 3ull
+                           : ((unsigned long long)p + (unsigned long long)a.iter) * 33ull + 12ull);
 }
 
 template <bool EXACT>

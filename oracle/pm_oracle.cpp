@@ -446,7 +446,11 @@ static void propagate_pass(const Pass& ps, const F4* old, const F4* smoothimg,
             Rng rng;                                                     /* :327 */
             uint32_t p = (uint32_t)(y * W + x);
             if (ps.rngkind == CVTPM_RNG_PHILOX) philox_init(rng, ps.seed, p, (uint32_t)ps.iter, view_id(lr));
-            else mwc_init(rng, ((uint64_t)p + (uint64_t)ps.iter) * 45u);
+            /* RNG_init(&rng, p + iter, ((3*3-1) + 3)*3 + 2*6): the macro body
+             * `(linpos) * numdraws` takes numdraws unparenthesised, so the
+             * skip distance is (p + iter)*(8 + 3)*3 + 2*6 = 33(p + iter) + 12
+             * (RNG.cl:151-154, pmhstereo.cl:327). */
+            else mwc_init(rng, ((uint64_t)p + (uint64_t)ps.iter) * 33u + 12u);
             auto consider = [&](F4 cand, int idx) {
                 cand.w = cost_eval(*ps.k, *ps.v1, *ps.v2, x, y, cand);
                 float da, db;

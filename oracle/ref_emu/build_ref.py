@@ -1,0 +1,108 @@
+"""TEST INFRASTRUCTURE — build recipe of the emulated reference
+(oracle/_ref/libpmref.so).  Needs the reference sources (it reads them where
+they lie, under /root/reference, and copies none into the repository), so it
+runs only where they are present.
+
+  1. translate.py rewrites cvt/cl/kernel/{pmhstereo,RNG,PDHuberWeighted,fill}.cl
+     into _build/ref_gen/*.inc (generated, never committed);
+  2. one C++ unit per kernel file wraps its .inc in a namespace and registers
+     the kernels with clemu;
+  3. g++ compiles those, the runtime, the harness and the reference's own
+     cvt/vision/PMHuberStereo.cpp (which includes the reference's
+     PMHuberStereo.h, PDROF.h and PDROFInpaint.h) against the shims in
+     oracle/ref_emu/shim.
+"""
+from __future__ import annotations
+
+import os
+import subprocess
+import sys
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ORACLE = os.path.dirname(HERE)
+ROOT = os.path.dirname(ORACLE)
+REF = "/root/reference"
+GEN = os.path.join(ROOT, "_build", "ref_gen")
+OUT = os.path.join(ORACLE, "_ref")
+LIB = os.path.join(OUT, "libpmref.so")
+KERNEL_FILES = ["RNG", "pmhstereo", "PDHuberWeighted", "fill"]
+
+sys.path.insert(0, HERE)
+import translate  # noqa: E402
+
+
+def available() -> bool:
+    return os.path.isfile(os.path.join(REF, "cvt", "cl", "kernel", "pmhstereo.cl"))
+
+
+def generate():
+    os.makedirs(GEN, exist_ok=True)
+    units = []
+    for name in KERNEL_FILES:
+        src = open(os.path.join(REF, "cvt", "cl", "kernel", name + ".cl")).read()
+        tr = translate.translate(src)
+        with open(os.path.join(GEN, name + ".inc"), "w") as f:
+            f.write(tr)
+        if name == "RNG":
+            continue
+        ns = "k_" + name
+        lines = ['#include "clemu.h"', "namespace clemu { namespace %s {" % ns, '#include "%s.inc"' % name, "}}",
+                 "namespace {", "struct Reg { Reg() {"]
+        for k, barrier in translate.kernels(tr):
+            lines.append('  clemu::reg_kernel("%s", %s, &clemu::%s::%s);' % (k, "true" if barrier else "false", ns, k))
+        lines += ["} } reg_;", "}"]
+        if name == "pmhstereo":
+            lines += ["float clemu::pmh_patch_eval(Img* c1, Img* g1, Img* c2, Img* g2, float cx, float cy,",
+                      "                          const float st[4], int patchsize, int lr) {",
+                      "  return clemu::k_pmhstereo::patch_eval_color_grad_weighted(c1, g1, c2, g2, clemu::float2(cx, cy),",
+                      "      clemu::float4(st[0], st[1], st[2], st[3]), patchsize, lr);",
+                      "}"]
+        path = os.path.join(GEN, "unit_%s.cpp" % name)
+        with open(path, "w") as f:
+            f.write("\n".join(lines) + "\n")
+        units.append(path)
+    return units
+
+
+def build(force: bool = False, verbose: bool = False) -> str | None:
+    if not available():
+        return None
+    srcs = [os.path.join(HERE, f) for f in os.listdir(HERE) if f.endswith((".cpp", ".h", ".py"))]
+    srcs += [os.path.join(dp, f) for dp, _, fs in os.walk(os.path.join(HERE, "shim")) for f in fs]
+    srcs.append(os.path.join(ROOT, "cvt_gb300", "csrc", "pm_math.h"))
+    if not force and os.path.exists(LIB) and all(os.path.getmtime(s) <= os.path.getmtime(LIB) for s in srcs):
+        return LIB
+    os.makedirs(OUT, exist_ok=True)
+    units = generate()
+    base = ["g++", "-std=c++17", "-O2", "-fPIC", "-fopenmp", "-ffp-contract=off", "-fno-fast-math",
+            "-U_FORTIFY_SOURCE", "-D_FORTIFY_SOURCE=0", "-w",
+            "-I", os.path.join(HERE, "shim"), "-I", HERE, "-I", GEN, "-I", os.path.join(ROOT, "cvt_gb300", "csrc"),
+            "-I", REF]
+    jobs = []
+    objs = []
+    todo = [(u, []) for u in units]
+    todo += [(os.path.join(HERE, "clemu_rt.cpp"), []), (os.path.join(HERE, "ref_harness.cpp"), []),
+             (os.path.join(REF, "cvt", "vision", "PMHuberStereo.cpp"),
+              ["-include", os.path.join(HERE, "shim", "force_include.h")])]
+    for src, extra in todo:
+        obj = os.path.join(GEN, os.path.basename(src).replace(".cpp", ".o"))
+        cmd = base + extra + ["-c", src, "-o", obj]
+        if verbose:
+            print(" ".join(cmd), file=sys.stderr)
+        jobs.append((src, subprocess.Popen(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)))
+        objs.append(obj)
+    bad = []
+    for src, p in jobs:
+        out, _ = p.communicate()
+        if p.returncode:
+            print(out, file=sys.stderr)
+            bad.append(src)
+    if bad:
+        raise RuntimeError(f"emulated reference: compile failed for {bad}")
+    subprocess.run(["g++", "-shared", "-fopenmp", "-o", LIB + ".tmp", *objs], check=True)
+    os.replace(LIB + ".tmp", LIB)
+    return LIB
+
+
+if __name__ == "__main__":
+    print(build(force=True, verbose="-v" in sys.argv))
