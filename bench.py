@@ -1,0 +1,344 @@
+"""Benchmark of the plain PatchMatch stereo path on one GB300 (or N replicas).
+
+Workload (one step): PMHuberStereo::depthMap on one rectified pair of
+1242x375 RGBA float32 (16 slanted planes, disparity 0-128 px, 2% salt noise,
++/-5% gain/bias between the views), 35x35 window, 8 iterations, LR threshold
+1 px with fill-in, 250 PD steps per view and iteration.  Synthetic, seeded.
+
+Metric: Mpix-iter/s = W*H*iterations / time of the whole depthMap (both views,
+init through the final fill).  `value` is device-timed with the inputs
+resident in HBM; `e2e` is the same metric through the C ABI on pinned host
+buffers (cvtpm_depthmap_host: H2D of both images, the run, D2H of the map).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+`--impl reference` times the reference's algorithm on the host cores: the
+CPU restatement of pmhstereo.cl/PDHuberWeighted.cl/RNG.cl and the depthMap
+schedule (oracle/), EXACT arithmetic with MWC64X streams, all host threads,
+each step a bounded band of the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+W_CFG, H_CFG, DMAX, ITERS, PATCH = 1242, 375, 128.0, 8, 17
+WORKLOAD = "plain PatchMatch depthMap, 1 pair 1242x375 RGBA f32, 16 planes, dmax 128, 2% salt, +/-5% gain/bias, 35x35 ASW, 8 iterations, LR 1px + fill"
+METRIC = "PatchMatch Mpix-iter/s (plain depthMap, 1242x375, 8 iterations)"
+FLOPS_PER_TAP = 55.0          # per (pixel, candidate) window tap: plane, lerp, truncated L1, accumulate
+FLOPS_PER_WEIGHT_TAP = 20.0   # bilateral weight of a tap, once per pixel and launch
+PD_BYTES_PER_PX = 116.0       # u 16 + p 32 + f 16 + w 4 read; u 16 + p 32 written
+
+
+def params_for(impl: str):
+    from cvt_gb300.params import default_params, PRESET_BASELINE, ARITH_EXACT, RNG_MWC64X
+    p = default_params(PRESET_BASELINE, patchsize=PATCH, depthmax=DMAX, iterations=ITERS, maxdispdiff=1.0)
+    if impl == "reference":
+        p = p.replace(arith=ARITH_EXACT, rng=RNG_MWC64X)
+    return p
+
+
+def scene_for(rank: int):
+    from cvt_gb300 import scenes
+    return scenes.config_scene(2, pair=rank)
+
+
+def in_image_taps(W: int, H: int, P: int) -> int:
+    xs = np.arange(W)
+    nx = np.minimum(xs + P, W - 1) - np.maximum(xs - P, 0) + 1
+    ys = np.arange(H)
+    ny = np.minimum(ys + P, H - 1) - np.maximum(ys - P, 0) + 1
+    return int(nx.sum()) * int(ny.sum())
+
+
+def peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            d = json.load(f)
+        return float(d.get("hbm_gbs", 6800.0)), "measured"
+    return 6800.0, "fallback"
+
+
+def read_traffic():
+    path = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            return json.load(f)
+    return {}
+
+
+class ClockSampler:
+    """nvidia-smi samples during the timed region (SM clock, reasons)."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.file = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=self.file, stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        self.file.flush()
+        self.file.seek(0)
+        rows = [r.split(",") for r in self.file.read().strip().splitlines() if r.strip()]
+        os.unlink(self.file.name)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no nvidia-smi samples"], "samples": 0}
+        sm = [float(r[1]) for r in rows if r[1].strip().replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].strip().replace(".", "").isdigit()]
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            for n, v in zip(names, r[5:9]):
+                if "Active" in v and "Not" not in v:
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(rows)}
+
+
+def cpu_baseline(params, sc, rows: int, iters: int):
+    """The oracle (CPU restatement) on a band of `rows` rows for `iters`
+    iterations: Mpix-iter/s of the reference's algorithm on this host."""
+    from oracle import oracle as orc
+    p = params.replace(iterations=iters)
+    L = np.ascontiguousarray(sc.left[:rows])
+    R = np.ascontiguousarray(sc.right[:rows])
+    t0 = time.perf_counter()
+    orc.depthmap(p, L, R)
+    dt = time.perf_counter() - t0
+    return sc.width * rows * iters / dt / 1e6, dt, orc.max_threads()
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return 0
+    from oracle import oracle as orc
+    orc.lib()
+    p = params_for("reference")
+    sc = scene_for(0)
+    rows, iters = args.ref_rows, args.ref_iters
+    for _ in range(args.warmup):
+        cpu_baseline(p, sc, rows, iters)
+    vals, secs = [], 0.0
+    for _ in range(args.steps):
+        v, dt, cores = cpu_baseline(p, sc, rows, iters)
+        vals.append(v)
+        secs += dt
+    value = float(np.mean(vals))
+    sample = f"rows 0-{rows - 1} of the 1242x375 pair ({sc.width}x{rows}), {iters} iterations per step"
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "Mpix-iter/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * secs / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded Voronoi slanted planes, blurred noise texture)",
+            "config": {"workload": WORKLOAD, "arith": "exact (reference operation order)", "rng": "MWC64X"},
+            "cpu_baseline": {"value": value, "unit": "Mpix-iter/s", "cores": cores, "kind": "port", "sample": sample},
+            "e2e": {"value": value, "unit": "Mpix-iter/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_ours(args, rank, world, local_rank):
+    import torch
+    from cvt_gb300 import scenes, _lib
+    from cvt_gb300.stereo import PMHuberStereo
+    dist = world > 1
+    torch.cuda.set_device(local_rank)
+    dev = torch.device("cuda", local_rank)
+    if dist:
+        import torch.distributed as tdist
+
+    def barrier():
+        if dist:
+            tdist.barrier()
+        torch.cuda.synchronize()
+
+    p = params_for("ours")
+    sc = scene_for(rank)
+    W, H = sc.width, sc.height
+    st = PMHuberStereo(local_rank, p)
+    L = torch.from_numpy(sc.left).to(dev)
+    R = torch.from_numpy(sc.right).to(dev)
+    dmap = torch.empty((H, W), device=dev)
+    flush = torch.empty(64 * 1024 * 1024, device=dev)          # 256 MB > 129 MB L2
+    stream = torch.cuda.current_stream(dev)
+
+    fp32 = _lib.ctypes.c_float()
+    rc = _lib.lib().cvtpm_tool_fp32_peak(local_rank, _lib.ctypes.c_void_p(stream.cuda_stream), _lib.ctypes.byref(fp32))
+    fp32_tflops = float(fp32.value) if rc == 0 else None
+
+    for _ in range(args.warmup):
+        st.depthMap(dmap, L, R, PATCH, DMAX, ITERS, 4)
+    barrier()
+    st.reset_stats()
+    st.set_timing(True)
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    with ClockSampler(local_rank) as clk:
+        barrier()
+        t0 = time.perf_counter()
+        for i in range(args.steps):
+            flush.fill_(float(i))
+            ev[i][0].record(stream)
+            st.depthMap(dmap, L, R, PATCH, DMAX, ITERS, 4)
+            ev[i][1].record(stream)
+        barrier()
+        wall = time.perf_counter() - t0
+    st.set_timing(False)
+    stats = st.stats()
+    step_ms = [a.elapsed_time(b) for a, b in ev]
+    ms = float(np.mean(step_ms))
+    if dist:
+        t = torch.tensor([ms], device=dev)
+        tdist.all_reduce(t, op=tdist.ReduceOp.MAX)
+        ms = float(t.item())
+    value = world * W * H * ITERS / (ms * 1e-3) / 1e6
+    bad1 = scenes.bad_pixel_rate(dmap.cpu().numpy() * DMAX, sc)
+    epe = scenes.end_point_error(dmap.cpu().numpy() * DMAX, sc)
+
+    # ---- end to end through the C ABI on pinned host buffers
+    hl = torch.from_numpy(sc.left).pin_memory()
+    hr = torch.from_numpy(sc.right).pin_memory()
+    hd = torch.empty((H, W), dtype=torch.float32).pin_memory()
+    for _ in range(max(1, args.warmup // 2)):
+        st.depthMapHost(hl.numpy(), hr.numpy(), PATCH, DMAX, ITERS, 4, dmap=hd.numpy())
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        st.depthMapHost(hl.numpy(), hr.numpy(), PATCH, DMAX, ITERS, 4, dmap=hd.numpy())
+    barrier()
+    e2e_s = (time.perf_counter() - t0) / args.steps
+    if dist:
+        t = torch.tensor([e2e_s], device=dev)
+        tdist.all_reduce(t, op=tdist.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    e2e = world * W * H * ITERS / e2e_s / 1e6
+
+    if rank != 0:
+        return 0
+    # ---- roofline of the dominant kernel (propagation: FP32 CUDA cores)
+    nprop = max(1, stats["propagate_launches"])
+    prop_ms = stats["propagate_ms"] / nprop
+    flops_launch = (stats["cost_taps"] * FLOPS_PER_TAP) / nprop + in_image_taps(W, H, PATCH) * FLOPS_PER_WEIGHT_TAP
+    achieved = flops_launch / (prop_ms * 1e-3) / 1e12
+    traffic = read_traffic()
+    roofline = {"kernel": "k_propagate<fast>", "bound": "fp32", "achieved": achieved,
+                "peak": fp32_tflops, "unit": "TFLOP/s",
+                "frac": (achieved / fp32_tflops) if fp32_tflops else None,
+                "traffic": traffic.get("k_propagate_bytes_per_launch"),
+                "peak_source": "FFMA-chain probe run in this process (cvtpm_tool_fp32_peak), FMA = 2 flops",
+                "flops_per_launch": flops_launch, "launch_ms": prop_ms,
+                "share_of_step": stats["propagate_ms"] / max(1e-9, sum(step_ms))}
+    hbm_peak, hbm_src = peaks()
+    npd = max(1, stats["pd_launches"])
+    pd_ms = stats["pd_ms"] / npd
+    pd_bytes = PD_BYTES_PER_PX * W * H
+    roofline_pd = {"kernel": "k_pd_step", "bound": "hbm", "achieved": pd_bytes / (pd_ms * 1e-3) / 1e9,
+                   "peak": hbm_peak, "unit": "GB/s", "frac": pd_bytes / (pd_ms * 1e-3) / 1e9 / hbm_peak,
+                   "traffic": traffic.get("k_pd_step_bytes_per_launch"), "peak_source": hbm_src,
+                   "note": "the PD state (~21 MB/view) stays in the 129 MB L2 between steps, so this can exceed HBM"}
+    cpu = None
+    if not args.no_cpu_baseline:
+        from cvt_gb300.params import ARITH_EXACT, RNG_MWC64X
+        pv, dt, cores = cpu_baseline(p.replace(arith=ARITH_EXACT, rng=RNG_MWC64X), sc, args.ref_rows, args.ref_iters)
+        cpu = {"value": pv, "unit": "Mpix-iter/s", "cores": cores, "kind": "port",
+               "sample": f"rows 0-{args.ref_rows - 1} ({W}x{args.ref_rows}), {args.ref_iters} iterations, "
+                         f"exact arithmetic + MWC64X, {dt:.1f} s"}
+    line = {"metric": METRIC, "value": value, "unit": "Mpix-iter/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded Voronoi slanted planes, blurred noise texture); replica r uses pair seed 2000+r",
+            "config": {"workload": WORKLOAD, "arith": "fast (FMA, mirrored bit-exactly by the oracle)",
+                       "rng": "Philox4x32-10", "preset": "BASELINE (gamma 10, alpha 0.9, tau 10/255 and 2/255)",
+                       "l2": "flushed between steps (256 MB write)", "parallelism": "replicas" if world > 1 else "1 GPU"},
+            "e2e": {"value": e2e, "unit": "Mpix-iter/s", "h2d_bytes_per_step": 2 * W * H * 16,
+                    "d2h_bytes_per_step": W * H * 4},
+            "roofline": roofline, "roofline_pd": roofline_pd, "cpu_baseline": cpu,
+            "quality": {"bad1_nonocc_pct": bad1, "epe_nonocc_px": epe},
+            "clocks": clk.summary(), "gpu_launches": stats["launches"], "wall_s": wall}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_profile(args):
+    """A short run for ncu: one warm-up and one timed depthMap with
+    --profile-iters iterations on the same pair (device memory ~0.2 GB)."""
+    import torch
+    from cvt_gb300.stereo import PMHuberStereo
+    p = params_for("ours").replace(iterations=args.profile_iters)
+    sc = scene_for(0)
+    st = PMHuberStereo(0, p)
+    L = torch.from_numpy(sc.left).cuda()
+    R = torch.from_numpy(sc.right).cuda()
+    dmap = torch.empty((sc.height, sc.width), device="cuda")
+    for _ in range(2):
+        st.depthMap(dmap, L, R, PATCH, DMAX, args.profile_iters, 4)
+    torch.cuda.synchronize()
+    print(json.dumps({"profile_run": "ok", "iterations": args.profile_iters, "launches_per_step": st.stats()["launches"] // 2}))
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--ref-rows", type=int, default=96)
+    ap.add_argument("--ref-iters", type=int, default=2)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--profile", action="store_true", help="short run for ncu captures")
+    ap.add_argument("--profile-iters", type=int, default=1)
+    args = ap.parse_args()
+    if args.profile:
+        return run_profile(args)
+    if args.warmup < 3 and args.impl == "ours":
+        args.warmup = 3
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        return run_reference(args, rank, world)
+    if world > 1:
+        import torch
+        import torch.distributed as tdist
+        torch.cuda.set_device(local_rank)
+        tdist.init_process_group("nccl")
+    try:
+        return run_ours(args, rank, world, local_rank)
+    finally:
+        if world > 1:
+            import torch.distributed as tdist
+            tdist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -19,6 +19,7 @@ EXPORTS = (
     "cvtpm_version", "cvtpm_status_string", "cvtpm_params_default", "cvtpm_create", "cvtpm_destroy",
     "cvtpm_set_params", "cvtpm_get_params", "cvtpm_last_error", "cvtpm_synchronize", "cvtpm_depthmap",
     "cvtpm_depthmap_host", "cvtpm_cost_eval", "cvtpm_cost_adjoint", "cvtpm_depthmap_batched",
+    "cvtpm_set_timing", "cvtpm_reset_stats", "cvtpm_get_stats", "cvtpm_tool_fp32_peak",
 )
 
 
@@ -30,6 +31,15 @@ class CvtpmPair(ctypes.Structure):
     _fields_ = [("left", ctypes.c_void_p), ("right", ctypes.c_void_p), ("width", ctypes.c_int),
                 ("height", ctypes.c_int), ("pitch", ctypes.c_size_t), ("depthmax", ctypes.c_float),
                 ("dmap", ctypes.c_void_p), ("dmap_pitch", ctypes.c_size_t)]
+
+
+class CvtpmStats(ctypes.Structure):
+    _fields_ = [("calls", ctypes.c_uint64), ("launches", ctypes.c_uint64), ("propagate_launches", ctypes.c_uint64),
+                ("cost_evals", ctypes.c_uint64), ("cost_taps", ctypes.c_uint64), ("pd_launches", ctypes.c_uint64),
+                ("propagate_ms", ctypes.c_float), ("pd_ms", ctypes.c_float)]
+
+    def as_dict(self) -> dict:
+        return {name: getattr(self, name) for name, _ in self._fields_}
 
 
 class CvtpmError(RuntimeError):
@@ -66,6 +76,10 @@ def lib() -> ctypes.CDLL:
     L.cvtpm_cost_eval.argtypes = [vp, vp, vp, i, i, sz, vp, i, vp, vp]
     L.cvtpm_cost_adjoint.argtypes = [vp, vp, vp, i, i, sz, vp, i, vp, vp, vp, vp, vp, vp]
     L.cvtpm_depthmap_batched.argtypes = [vp, ctypes.POINTER(CvtpmPair), i, vp]
+    L.cvtpm_set_timing.argtypes = [vp, i]
+    L.cvtpm_reset_stats.argtypes = [vp]
+    L.cvtpm_get_stats.argtypes = [vp, ctypes.POINTER(CvtpmStats)]
+    L.cvtpm_tool_fp32_peak.argtypes = [i, vp, ctypes.POINTER(ctypes.c_float)]
     for name in EXPORTS:
         if name not in ("cvtpm_version", "cvtpm_status_string", "cvtpm_last_error"):
             getattr(L, name).restype = ctypes.c_int

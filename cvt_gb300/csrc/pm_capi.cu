@@ -20,6 +20,7 @@
 #include <vector>
 
 #include "cvtpm.h"
+#include "cvtpm_tools.h"
 #include "pm_kernels.cuh"
 
 #define CVTPM_VERSION "cvt-gb300 0.1.0 (sm_103a)"
@@ -46,6 +47,12 @@ struct cvtpm_ctx {
     /* staging for the *_host entry points */
     void* stage = nullptr;
     size_t stage_bytes = 0;
+    /* observability (cvtpm_get_stats) */
+    cvtpm_stats stats{};
+    bool timing = false;
+    unsigned long long* dcount = nullptr;            /* device counters: evaluations, taps */
+    std::vector<std::pair<cudaEvent_t, cudaEvent_t>> ev_prop, ev_pd;
+    std::vector<cudaEvent_t> ev_free;
 };
 
 namespace {
@@ -62,8 +69,33 @@ cvtpm_status cuda_fail(cvtpm_ctx* c, cudaError_t e, const char* where) {
     return fail(c, CVTPM_ERR_CUDA, std::string(where) + ": " + cudaGetErrorString(e));
 }
 #define CK(call, where) do { cudaError_t e_ = (call); if (e_ != cudaSuccess) return cuda_fail(ctx, e_, where); } while (0)
+/* a kernel launch: checked and counted */
+#define LK(call, where) do { CK(call, where); ++ctx->stats.launches; } while (0)
+
+cudaEvent_t take_event(cvtpm_ctx* ctx) {
+    if (!ctx->ev_free.empty()) { cudaEvent_t e = ctx->ev_free.back(); ctx->ev_free.pop_back(); return e; }
+    cudaEvent_t e = nullptr;
+    if (cudaEventCreate(&e) != cudaSuccess) return nullptr;
+    return e;
+}
+
+/* Records an event pair around a phase when timing is on. */
+struct PhaseTimer {
+    cvtpm_ctx* ctx; cudaStream_t st; std::vector<std::pair<cudaEvent_t, cudaEvent_t>>* list;
+    cudaEvent_t a = nullptr, b = nullptr;
+    PhaseTimer(cvtpm_ctx* c, cudaStream_t s, std::vector<std::pair<cudaEvent_t, cudaEvent_t>>& l) : ctx(c), st(s), list(&l) {
+        if (ctx->timing) { a = take_event(ctx); b = take_event(ctx); if (a) cudaEventRecord(a, st); }
+    }
+    void stop() {
+        if (a && b) { cudaEventRecord(b, st); list->push_back({a, b}); a = b = nullptr; }
+    }
+};
 
 size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
+
+/* Row pitch (elements) of the record planes: even and two columns past the
+ * row, so 16-byte chunks of the float2 plane never leave a row. */
+int rec_pitch(int W) { return (int)align_up((size_t)W + 2, 4); }
 
 void mwc_pow2_table(unsigned long long* t) {
     const unsigned __int128 M = 18446383549859758079ull;
@@ -98,16 +130,17 @@ cvtpm_status ensure_buffers(cvtpm_ctx* ctx, int W, int H) {
         /* reuse: the carve below depends only on n = W*H, recompute it */
     }
     const size_t n = (size_t)W * H;
+    const size_t nr = (size_t)rec_pitch(W) * H;
     size_t off = 0;
     std::vector<std::pair<void**, size_t>> parts;
     auto add = [&](void** p, size_t bytes) { parts.push_back({p, bytes}); off = align_up(off, 256) + bytes; };
     for (int v = 0; v < 2; ++v) {
         add((void**)&ctx->col[v], n * 16);
         add((void**)&ctx->grad[v], n * 16);
-        add((void**)&ctx->recA[v], n * 16);
-        add((void**)&ctx->recB[v], n * 16);
-        add((void**)&ctx->recC[v], n * 16);
-        add((void**)&ctx->recD[v], n * 8);
+        add((void**)&ctx->recA[v], nr * 16);
+        add((void**)&ctx->recB[v], nr * 16);
+        add((void**)&ctx->recC[v], nr * 16);
+        add((void**)&ctx->recD[v], nr * 8);
         add((void**)&ctx->wgt[v], n * 4);
         add((void**)&ctx->S[v][0], n * 16);
         add((void**)&ctx->S[v][1], n * 16);
@@ -161,6 +194,12 @@ PmPassArgs base_args(cvtpm_ctx* ctx, const cvtpm_params& p, int W, int H, int v1
     a.k.Wf = (float)W; a.k.Hf = (float)H;
     a.k.alpha = p.color_alpha; a.k.oma = 1.0f - p.color_alpha;
     a.k.cmax = p.color_maxdiff; a.k.gmax = p.grad_maxdiff;
+    a.k.rp = rec_pitch(W);
+    a.k.n = 2 * p.patchsize + 1;
+    a.k.ntaps = a.k.n * a.k.n;
+    a.k.ni = (a.k.ntaps + 31) / 32;
+    a.k.kstep = 32 / a.k.n;
+    a.k.rstep = 32 % a.k.n;
     const int v2 = 1 - v1;
     a.v1 = {ctx->col[v1], ctx->grad[v1], ctx->recA[v1], ctx->recB[v1], ctx->recC[v1], ctx->recD[v1]};
     a.v2 = {ctx->col[v2], ctx->grad[v2], ctx->recA[v2], ctx->recB[v2], ctx->recC[v2], ctx->recD[v2]};
@@ -175,9 +214,9 @@ cvtpm_status prep_views(cvtpm_ctx* ctx, const cvtpm_params& p, const float* img0
                         size_t pitch, cudaStream_t st) {
     const float* im[2] = {img0, img1};
     for (int v = 0; v < 2; ++v) {
-        CK(pm_launch_prep((const float4*)im[v], pitch / 16, W, H, ctx->col[v], ctx->grad[v], ctx->wgt[v], st), "prep");
+        LK(pm_launch_prep((const float4*)im[v], pitch / 16, W, H, ctx->col[v], ctx->grad[v], ctx->wgt[v], st), "prep");
         if (p.arith == CVTPM_ARITH_FAST)
-            CK(pm_launch_records(ctx->col[v], ctx->grad[v], W, H, ctx->recA[v], ctx->recB[v], ctx->recC[v], ctx->recD[v], st), "records");
+            LK(pm_launch_records(ctx->col[v], ctx->grad[v], W, H, rec_pitch(W), ctx->recA[v], ctx->recB[v], ctx->recC[v], ctx->recD[v], st), "records");
     }
     return CVTPM_OK;
 }
@@ -191,12 +230,18 @@ cvtpm_status pd_apply(cvtpm_ctx* ctx, float4* output, const float4* input, const
     CK(cudaMemsetAsync(ctx->pdP[1], 0, n * 32, st), "pd clear");
     float4* img[2] = {ctx->pdT, output};
     float4* pp[2] = {ctx->pdP[0], ctx->pdP[1]};
+    PhaseTimer tm(ctx, st, ctx->ev_pd);
     int swap = 0;
     for (int i = 0; i < iters; ++i) {
         swap = i & 1;
-        CK(pm_launch_pd_step(img[swap], pp[swap], img[1 - swap], pp[1 - swap], input, wgt, lambda, W, H, st), "pd step");
+        LK(pm_launch_pd_step(img[swap], pp[swap], img[1 - swap], pp[1 - swap], input, wgt, lambda, W, H, st), "pd step");
+        ++ctx->stats.pd_launches;
     }
-    if (!swap) CK(pm_launch_pd_step(img[1], pp[1], img[0], pp[0], input, wgt, lambda, W, H, st), "pd step");
+    if (!swap) {
+        LK(pm_launch_pd_step(img[1], pp[1], img[0], pp[0], input, wgt, lambda, W, H, st), "pd step");
+        ++ctx->stats.pd_launches;
+    }
+    tm.stop();
     return CVTPM_OK;
 }
 
@@ -226,11 +271,16 @@ cvtpm_status run_depthmap(cvtpm_ctx* ctx, const cvtpm_params& p, float* dmap, si
     const float dscale = p.dscale <= 0.0f ? 1.0f / dmax : p.dscale;
     const int N = p.iterations;
     PmPassArgs aL = base_args(ctx, p, W, H, 0), aR = base_args(ctx, p, W, H, 1);
+    if (!ctx->dcount) {
+        CK(cudaMalloc(&ctx->dcount, 2 * sizeof(unsigned long long)), "counters");
+        CK(cudaMemset(ctx->dcount, 0, 2 * sizeof(unsigned long long)), "counters");
+    }
+    ++ctx->stats.calls;
 
     aL.out = ctx->S[0][0];                                         /* :124-143 */
-    CK(pm_launch_init(aL, exact, st), "init");
+    LK(pm_launch_init(aL, exact, st), "init");
     aR.out = ctx->S[1][0];
-    CK(pm_launch_init(aR, exact, st), "init");
+    LK(pm_launch_init(aR, exact, st), "init");
     CK(cudaMemsetAsync(ctx->smooth[0], 0, n * 16, st), "clear");   /* :108-113 */
     CK(cudaMemsetAsync(ctx->smooth[1], 0, n * 16, st), "clear");
     CK(cudaMemsetAsync(ctx->list[1], 0xFF, n * 8, st), "clear");   /* :145-149 */
@@ -242,26 +292,36 @@ cvtpm_status run_depthmap(cvtpm_ctx* ctx, const cvtpm_params& p, float* dmap, si
         aL.theta = aR.theta = theta;
         aL.old = ctx->S[0][sw]; aL.out = ctx->S[0][1 - sw]; aL.smooth = ctx->smooth[0];
         aL.viewin = ctx->list[1]; aL.viewsrc = ctx->S[1][sw]; aL.winners = ctx->win[0];
-        CK(pm_launch_propagate(aL, exact, st), "propagate left");
-        CK(pm_launch_view_list(ctx->S[0][1 - sw], W, H, ctx->list[0], st), "view list");
+        aL.counters = aR.counters = ctx->dcount;
+        {
+            PhaseTimer tm(ctx, st, ctx->ev_prop);
+            LK(pm_launch_propagate(aL, exact, st), "propagate left");
+            tm.stop();
+        }
+        LK(pm_launch_view_list(ctx->S[0][1 - sw], W, H, ctx->list[0], st), "view list");
         aR.old = ctx->S[1][sw]; aR.out = ctx->S[1][1 - sw]; aR.smooth = ctx->smooth[1];
         aR.viewin = ctx->list[0]; aR.viewsrc = ctx->S[0][1 - sw]; aR.winners = ctx->win[1];
-        CK(pm_launch_propagate(aR, exact, st), "propagate right");
-        CK(pm_launch_view_list(ctx->S[1][1 - sw], W, H, ctx->list[1], st), "view list");
+        {
+            PhaseTimer tm(ctx, st, ctx->ev_prop);
+            LK(pm_launch_propagate(aR, exact, st), "propagate right");
+            tm.stop();
+        }
+        ctx->stats.propagate_launches += 2;
+        LK(pm_launch_view_list(ctx->S[1][1 - sw], W, H, ctx->list[1], st), "view list");
         const float lambda = theta * p.thetascale + 5.0f;
         for (int v = 0; v < 2; ++v) {                              /* :228-261 */
-            CK(pm_launch_consistency(ctx->S[v][1 - sw], ctx->S[1 - v][1 - sw], W, H, p.maxdispdiff, p.maxanglediff,
+            LK(pm_launch_consistency(ctx->S[v][1 - sw], ctx->S[1 - v][1 - sw], W, H, p.maxdispdiff, p.maxanglediff,
                                      v == 0 ? 1 : 0, ctx->tmp, nullptr, st), "consistency");
-            CK(pm_launch_fill_state(ctx->tmp, W, H, dmax, v == 0 ? 1 : 0, ctx->tmp2, st), "fill");
+            LK(pm_launch_fill_state(ctx->tmp, W, H, dmax, v == 0 ? 1 : 0, ctx->tmp2, st), "fill");
             if ((s = pd_apply(ctx, ctx->smooth[v], ctx->tmp2, ctx->wgt[v], lambda, p.pd_iterations, W, H, st)) != CVTPM_OK)
                 return s;
         }
         if (iter >= 5) theta = smoothstep01(((float)iter - 5.0f) / ((float)N - 5.0f)) * 1.0f;
     }
     const int fin = 1 - ((N - 1) & 1);                              /* :268-290 */
-    CK(pm_launch_consistency(ctx->S[0][fin], ctx->S[1][fin], W, H, p.maxdispdiff, p.maxanglediff, 1, ctx->tmp,
+    LK(pm_launch_consistency(ctx->S[0][fin], ctx->S[1][fin], W, H, p.maxdispdiff, p.maxanglediff, 1, ctx->tmp,
                              ctx->valid, st), "consistency");
-    CK(pm_launch_fill_output(ctx->tmp, W, H, dscale, dmap, dpitch / 4, (float4*)nmap, npitch / 16, st), "fill output");
+    LK(pm_launch_fill_output(ctx->tmp, W, H, dscale, dmap, dpitch / 4, (float4*)nmap, npitch / 16, st), "fill output");
     if (trace) {
         if (trace->winners) {
             CK(cudaMemcpyAsync(trace->winners, ctx->win[0], n, cudaMemcpyDeviceToDevice, st), "trace");
@@ -353,6 +413,10 @@ cvtpm_status cvtpm_destroy(cvtpm_ctx* ctx) {
     cudaSetDevice(ctx->device);
     if (ctx->pool) cudaFree(ctx->pool);
     if (ctx->stage) cudaFree(ctx->stage);
+    if (ctx->dcount) cudaFree(ctx->dcount);
+    for (auto& pr : ctx->ev_prop) { cudaEventDestroy(pr.first); cudaEventDestroy(pr.second); }
+    for (auto& pr : ctx->ev_pd) { cudaEventDestroy(pr.first); cudaEventDestroy(pr.second); }
+    for (auto e : ctx->ev_free) cudaEventDestroy(e);
     delete ctx;
     return CVTPM_OK;
 }
@@ -446,7 +510,56 @@ cvtpm_status cvtpm_cost_eval(cvtpm_ctx* ctx, const float* img1, const float* img
     if ((s = ensure_tables(ctx, p, st)) != CVTPM_OK) return s;
     if ((s = prep_views(ctx, p, img1, img2, width, height, pitch, st)) != CVTPM_OK) return s;
     PmPassArgs a = base_args(ctx, p, width, height, 0);
-    CK(pm_launch_cost_field(a, p.arith == CVTPM_ARITH_EXACT, (const float4*)states, cost, st), "cost field");
+    LK(pm_launch_cost_field(a, p.arith == CVTPM_ARITH_EXACT, (const float4*)states, cost, st), "cost field");
+    return CVTPM_OK;
+}
+
+cvtpm_status cvtpm_set_timing(cvtpm_ctx* ctx, int enable) {
+    if (!ctx) return CVTPM_ERR_INVALID_ARGUMENT;
+    ctx->timing = enable != 0;
+    return CVTPM_OK;
+}
+
+static cvtpm_status drain_events(cvtpm_ctx* ctx, std::vector<std::pair<cudaEvent_t, cudaEvent_t>>& list, float* acc) {
+    for (auto& pr : list) {
+        CK(cudaEventSynchronize(pr.second), "event");
+        float ms = 0.0f;
+        CK(cudaEventElapsedTime(&ms, pr.first, pr.second), "event");
+        *acc += ms;
+        ctx->ev_free.push_back(pr.first);
+        ctx->ev_free.push_back(pr.second);
+    }
+    list.clear();
+    return CVTPM_OK;
+}
+
+cvtpm_status cvtpm_reset_stats(cvtpm_ctx* ctx) {
+    if (!ctx) return CVTPM_ERR_INVALID_ARGUMENT;
+    CK(cudaSetDevice(ctx->device), "cudaSetDevice");
+    CK(cudaDeviceSynchronize(), "synchronize");
+    float dummy = 0.0f;
+    cvtpm_status s;
+    if ((s = drain_events(ctx, ctx->ev_prop, &dummy)) != CVTPM_OK) return s;
+    if ((s = drain_events(ctx, ctx->ev_pd, &dummy)) != CVTPM_OK) return s;
+    if (ctx->dcount) CK(cudaMemset(ctx->dcount, 0, 2 * sizeof(unsigned long long)), "counters");
+    memset(&ctx->stats, 0, sizeof(ctx->stats));
+    return CVTPM_OK;
+}
+
+cvtpm_status cvtpm_get_stats(cvtpm_ctx* ctx, cvtpm_stats* out) {
+    if (!ctx || !out) return CVTPM_ERR_INVALID_ARGUMENT;
+    CK(cudaSetDevice(ctx->device), "cudaSetDevice");
+    CK(cudaDeviceSynchronize(), "synchronize");
+    cvtpm_status s;
+    if ((s = drain_events(ctx, ctx->ev_prop, &ctx->stats.propagate_ms)) != CVTPM_OK) return s;
+    if ((s = drain_events(ctx, ctx->ev_pd, &ctx->stats.pd_ms)) != CVTPM_OK) return s;
+    if (ctx->dcount) {
+        unsigned long long c[2];
+        CK(cudaMemcpy(c, ctx->dcount, sizeof(c), cudaMemcpyDeviceToHost), "counters");
+        ctx->stats.cost_evals = c[0];
+        ctx->stats.cost_taps = c[1];
+    }
+    *out = ctx->stats;
     return CVTPM_OK;
 }
 
@@ -457,6 +570,38 @@ cvtpm_status cvtpm_cost_adjoint(cvtpm_ctx* ctx, const float*, const float*, int,
 
 cvtpm_status cvtpm_depthmap_batched(cvtpm_ctx* ctx, const cvtpm_pair*, int, void*) {
     return fail(ctx, CVTPM_ERR_NOT_SUPPORTED, "batched path not built yet");
+}
+
+cvtpm_status cvtpm_tool_fp32_peak(int device, void* stream, float* tflops) {
+    if (!tflops) return CVTPM_ERR_INVALID_ARGUMENT;
+    cudaStream_t st = (cudaStream_t)stream;
+    if (cudaSetDevice(device) != cudaSuccess) return CVTPM_ERR_CUDA;
+    int sms = 0;
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess) return CVTPM_ERR_CUDA;
+    const int blocks = sms * 8, iters = 1 << 16;
+    float* out = nullptr;
+    if (cudaMalloc(&out, sizeof(float) * blocks * 256) != cudaSuccess) return CVTPM_ERR_ALLOC;
+    cudaEvent_t a, b;
+    cudaEventCreate(&a);
+    cudaEventCreate(&b);
+    float best = 1e30f;
+    cvtpm_status s = CVTPM_OK;
+    for (int rep = 0; rep < 4 && s == CVTPM_OK; ++rep) {
+        cudaEventRecord(a, st);
+        if (pm_launch_ffma_peak(out, blocks, iters, st) != cudaSuccess) s = CVTPM_ERR_CUDA;
+        cudaEventRecord(b, st);
+        if (cudaEventSynchronize(b) != cudaSuccess) s = CVTPM_ERR_CUDA;
+        float ms = 0.0f;
+        cudaEventElapsedTime(&ms, a, b);
+        if (rep > 0 && ms < best) best = ms;    /* the first launch warms up */
+    }
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    cudaFree(out);
+    if (s != CVTPM_OK) return s;
+    const double flops = 2.0 * 8.0 * (double)iters * blocks * 256.0;
+    *tflops = (float)(flops / (best * 1e-3) / 1e12);
+    return CVTPM_OK;
 }
 
 }  // extern "C"

@@ -52,14 +52,14 @@ k_prep(const float4* __restrict__ img, size_t pitch4, int W, int H,
     wgt[o] = pm_exp(-3.0f * pm_pow(pm_sqrt(ex * ex + ey * ey), 0.8f)) + 0.0001f;
 }
 
-__global__ void k_records(const float4* __restrict__ col, const float4* __restrict__ grad, int W, int H,
+__global__ void k_records(const float4* __restrict__ col, const float4* __restrict__ grad, int W, int H, int rp,
                           float4* __restrict__ A, float4* __restrict__ Bq, float4* __restrict__ C,
                           float2* __restrict__ D) {
     const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y;
     if (x >= W || y >= H) return;
-    const size_t o = (size_t)y * W + x;
-    const size_t o1 = (size_t)y * W + min(x + 1, W - 1);
-    float4 c0 = col[o], c1 = col[o1], g0 = grad[o], g1 = grad[o1];
+    const size_t o = (size_t)y * rp + x;
+    const size_t i0 = (size_t)y * W + x, i1 = (size_t)y * W + min(x + 1, W - 1);
+    float4 c0 = col[i0], c1 = col[i1], g0 = grad[i0], g1 = grad[i1];
     A[o] = f4(c0.x, c0.y, c0.z, g0.x);
     Bq[o] = f4(g0.y, g0.z, g0.w, c1.x - c0.x);
     C[o] = f4(c1.y - c0.y, c1.z - c0.z, g1.x - g0.x, g1.y - g0.y);
@@ -81,16 +81,24 @@ PM_DEV void seed_rng(PmRng& rng, const PmPassArgs& a, int x, int y, bool init) {
 
 template <bool EXACT>
 __global__ void __launch_bounds__(256) k_init(PmPassArgs a) {
+    __shared__ float s_prof[EXACT ? 1 : PM_PROF_N * PM_PROF_N];
+    if (!EXACT) load_flat_profile(a.k, s_prof);
     const int x = blockIdx.x * 32 + threadIdx.x, y = blockIdx.y * 8 + threadIdx.y;
-    if (x >= a.k.W || y >= a.k.H) return;
+    const bool inside = x < a.k.W && y < a.k.H;
+    if (EXACT && !inside) return;
+    const int xc = min(x, a.k.W - 1), yc = min(y, a.k.H - 1);
     PmRng rng;
-    seed_rng(rng, a, x, y, true);
-    float4 s[1] = {state_init(rng, (float)x, (float)y, a.lr, 1.0f, a.depthmax)};
-    bool act[1] = {true};
-    float c[1];
-    eval_costs<1, EXACT>(a.k, a.v1, a.v2, x, y, s, act, c);
-    s[0].w = c[0];
-    a.out[(size_t)y * a.k.W + x] = s[0];
+    seed_rng(rng, a, xc, yc, true);
+    float4 s[1] = {state_init(rng, (float)xc, (float)yc, a.lr, 1.0f, a.depthmax)};
+    if (EXACT) {
+        bool act[1] = {true};
+        float c[1];
+        eval_costs<1, true>(a.k, a.v1, a.v2, x, y, s, act, c);
+        s[0].w = c[0];
+    } else {
+        s[0].w = coop_cost_warp(a.k, a.v1, a.v2, s_prof, xc, yc, s[0], inside);   /* random planes */
+    }
+    if (inside) a.out[(size_t)y * a.k.W + x] = s[0];
 }
 
 template <bool EXACT>
@@ -108,6 +116,8 @@ __global__ void __launch_bounds__(256) k_cost_field(PmPassArgs a, const float4* 
 /* --------------------------------------------------------- propagate -- */
 template <bool EXACT>
 __global__ void __launch_bounds__(256) k_propagate(PmPassArgs a) {
+    __shared__ float s_prof[EXACT ? 1 : PM_PROF_N * PM_PROF_N];
+    if (!EXACT) load_flat_profile(a.k, s_prof);
     const int W = a.k.W, H = a.k.H;
     const int x = blockIdx.x * 32 + threadIdx.x, y = blockIdx.y * 8 + threadIdx.y;
     const bool inside = x < W && y < H;
@@ -175,16 +185,29 @@ __global__ void __launch_bounds__(256) k_propagate(PmPassArgs a) {
             s[i] = a.old[(size_t)clampi(yc + oy, 0, H - 1) * W + clampi(xc + ox, 0, W - 1)];
         }
         s[3] = state_init(rng, cx, cy, lr, 2.0f, dmax);
-        eval_costs<4, EXACT>(a.k, a.v1, a.v2, xc, yc, s, act, c);
+        if (EXACT) {
+            eval_costs<4, true>(a.k, a.v1, a.v2, xc, yc, s, act, c);
+        } else {
+            /* random neighbours lane by lane; the random plane, whose disparity
+             * differs arbitrarily between lanes, cooperatively */
+            float4 s3[3] = {s[0], s[1], s[2]};
+            bool act3[3] = {true, true, true};
+            float c3[3];
+            eval_costs<3, false>(a.k, a.v1, a.v2, xc, yc, s3, act3, c3);
+            c[0] = c3[0]; c[1] = c3[1]; c[2] = c3[2];
+            c[3] = coop_cost_warp(a.k, a.v1, a.v2, s_prof, xc, yc, s[3], inside);
+        }
 #pragma unroll
         for (int i = 0; i < 4; ++i) accept(s[i], c[i], 13 + i);
     }
     /* 17-20: candidates from the other view (:372-379) */
+    int nview_total = 0;
     if (a.viewin) {
         short4 l = a.viewin[o];
         short li[4] = {l.x, l.y, l.z, l.w};
         int nview = (li[0] < 0) ? 0 : (li[1] < 0) ? 1 : (li[2] < 0) ? 2 : (li[3] < 0) ? 3 : 4;
         if (!inside) nview = 0;
+        nview_total = nview;
         if (__any_sync(0xffffffffu, nview > 0)) {
             float4 s[4]; bool act[4]; float c[4];
 #pragma unroll
@@ -210,6 +233,26 @@ __global__ void __launch_bounds__(256) k_propagate(PmPassArgs a) {
     if (inside) {
         a.out[o] = self;
         if (a.winners) a.winners[o] = (uint8_t)win;
+    }
+    if (a.counters) {
+        /* evaluations = 18 + view candidates; taps = in-image window taps */
+        unsigned long long ev = 0, taps = 0;
+        if (inside) {
+            const int P = a.k.P;
+            const int nx = min(xc + P, W - 1) - max(xc - P, 0) + 1;
+            const int ny = min(yc + P, H - 1) - max(yc - P, 0) + 1;
+            ev = 18ull + (unsigned long long)nview_total;
+            taps = ev * (unsigned long long)(nx * ny);
+        }
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) {
+            ev += __shfl_down_sync(0xffffffffu, ev, off);
+            taps += __shfl_down_sync(0xffffffffu, taps, off);
+        }
+        if ((threadIdx.x & 31) == 0) {
+            atomicAdd(&a.counters[0], ev);
+            atomicAdd(&a.counters[1], taps);
+        }
     }
 }
 
@@ -434,10 +477,10 @@ cudaError_t pm_launch_prep(const float4* img, size_t pitch4, int W, int H, float
     return cudaSuccess;
 }
 
-cudaError_t pm_launch_records(const float4* col, const float4* grad, int W, int H, float4* A, float4* B,
+cudaError_t pm_launch_records(const float4* col, const float4* grad, int W, int H, int rp, float4* A, float4* B,
                               float4* C, float2* D, cudaStream_t st) {
     dim3 b(128), g((W + 127) / 128, H);
-    k_records<<<g, b, 0, st>>>(col, grad, W, H, A, B, C, D);
+    k_records<<<g, b, 0, st>>>(col, grad, W, H, rp, A, B, C, D);
     PM_LAUNCH_CHECK();
     return cudaSuccess;
 }
@@ -497,6 +540,26 @@ cudaError_t pm_launch_pd_step(float4* uout, float4* pout, const float4* last, co
                               const float* wgt, float lambda, int W, int H, cudaStream_t st) {
     dim3 b(PD_TX, PD_TY), g((W + PD_TX - 1) / PD_TX, (H + PD_TY - 1) / PD_TY);
     k_pd_step<<<g, b, 0, st>>>(uout, pout, last, pin, f, wgt, lambda, W, H);
+    PM_LAUNCH_CHECK();
+    return cudaSuccess;
+}
+
+/* ------------------------------------------------- FP32 peak probe -- */
+/* 8 independent FFMA chains per thread; the result is stored so the chains
+ * cannot be removed. */
+__global__ void __launch_bounds__(256) k_ffma_peak(float* out, int iters, float b, float c) {
+    float a0 = threadIdx.x * 1e-3f, a1 = a0 + 1.0f, a2 = a0 + 2.0f, a3 = a0 + 3.0f;
+    float a4 = a0 + 4.0f, a5 = a0 + 5.0f, a6 = a0 + 6.0f, a7 = a0 + 7.0f;
+#pragma unroll 4
+    for (int i = 0; i < iters; ++i) {
+        a0 = fmaf(a0, b, c); a1 = fmaf(a1, b, c); a2 = fmaf(a2, b, c); a3 = fmaf(a3, b, c);
+        a4 = fmaf(a4, b, c); a5 = fmaf(a5, b, c); a6 = fmaf(a6, b, c); a7 = fmaf(a7, b, c);
+    }
+    out[blockIdx.x * blockDim.x + threadIdx.x] = ((a0 + a1) + (a2 + a3)) + ((a4 + a5) + (a6 + a7));
+}
+
+cudaError_t pm_launch_ffma_peak(float* out, int blocks, int iters, cudaStream_t st) {
+    k_ffma_peak<<<blocks, 256, 0, st>>>(out, iters, 0.999999f, 1e-6f);
     PM_LAUNCH_CHECK();
     return cudaSuccess;
 }

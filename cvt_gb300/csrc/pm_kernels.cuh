@@ -23,12 +23,13 @@ struct PmPassArgs {
     const float4* viewsrc;     /* states the view list refers to    */
     float4* out;
     uint8_t* winners;
+    unsigned long long* counters;   /* [0] cost evaluations, [1] in-image taps; may be NULL */
 };
 
 cudaError_t pm_upload_tables(const unsigned long long* pow2, const float* prof, cudaStream_t st);
 cudaError_t pm_launch_prep(const float4* img, size_t pitch4, int W, int H, float4* col, float4* grad,
                            float* wgt, cudaStream_t st);
-cudaError_t pm_launch_records(const float4* col, const float4* grad, int W, int H, float4* A, float4* B,
+cudaError_t pm_launch_records(const float4* col, const float4* grad, int W, int H, int rp, float4* A, float4* B,
                               float4* C, float2* D, cudaStream_t st);
 cudaError_t pm_launch_init(const PmPassArgs& a, bool exact, cudaStream_t st);
 cudaError_t pm_launch_cost_field(const PmPassArgs& a, bool exact, const float4* states, float* cost,
@@ -44,5 +45,7 @@ cudaError_t pm_launch_fill_output(const float4* in, int W, int H, float scale, f
 cudaError_t pm_launch_pd_step(float4* uout, float4* pout, const float4* last, const float4* pin,
                               const float4* f, const float* wgt, float lambda, int W, int H,
                               cudaStream_t st);
+
+cudaError_t pm_launch_ffma_peak(float* out, int blocks, int iters, cudaStream_t st);
 
 #endif

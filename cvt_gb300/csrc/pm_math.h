@@ -91,7 +91,8 @@ PM_HD float pm_exp(float x) {
     const float SHIFT = 12582912.0f;              /* 1.5 * 2^23: round to integer */
     float xc = fminf(fmaxf(x, -104.0f), 89.0f);
     float t = xc * L2E;
-    float kf = (t + SHIFT) - SHIFT;               /* round to nearest even */
+    float big = t + SHIFT;                        /* SHIFT + round(t): the integer sits in the low bits */
+    float kf = big - SHIFT;                       /* round to nearest even */
     float r = fmaf(-kf, LN2_HI, xc);
     r = fmaf(-kf, LN2_LO, r);
     float p = 1.98412698e-04f;                    /* 1/7! */
@@ -102,7 +103,7 @@ PM_HD float pm_exp(float x) {
     p = fmaf(p, r, 0.5f);
     p = fmaf(p, r, 1.0f);
     p = fmaf(p, r, 1.0f);
-    int k = (int)kf;
+    int k = pm_f2i(big) - 0x4B400000;             /* == (int)kf, without a float-to-int conversion */
     int ka = k >> 1;                              /* floor(k/2) */
     int kb = k - ka;
     float res = (p * pm_pow2i(ka)) * pm_pow2i(kb);

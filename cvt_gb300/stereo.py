@@ -72,6 +72,17 @@ class PMHuberStereo:
         self._check(_lib.lib().cvtpm_set_params(self._h, ctypes.byref(params)))
         self.params = params
 
+    def set_timing(self, enable: bool):
+        self._check(_lib.lib().cvtpm_set_timing(self._h, int(bool(enable))))
+
+    def reset_stats(self):
+        self._check(_lib.lib().cvtpm_reset_stats(self._h))
+
+    def stats(self) -> dict:
+        st = _lib.CvtpmStats()
+        self._check(_lib.lib().cvtpm_get_stats(self._h, ctypes.byref(st)))
+        return st.as_dict()
+
     def get_params(self) -> CvtpmParams:
         p = CvtpmParams()
         self._check(_lib.lib().cvtpm_get_params(self._h, ctypes.byref(p)))

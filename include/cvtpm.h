@@ -94,6 +94,20 @@ typedef struct cvtpm_trace {
 
 typedef struct cvtpm_ctx cvtpm_ctx;
 
+/* Counters of the calls since the last cvtpm_reset_stats (no reference
+ * counterpart: observability for benchmarks and tests). */
+typedef struct cvtpm_stats {
+    uint64_t calls;              /* depthmap calls                              */
+    uint64_t launches;           /* kernels this library launched               */
+    uint64_t propagate_launches;
+    uint64_t cost_evals;         /* (pixel, candidate) cost evaluations of the
+                                    propagation passes, counted on the device   */
+    uint64_t cost_taps;          /* in-image window taps of those evaluations   */
+    uint64_t pd_launches;
+    float    propagate_ms;       /* CUDA-event time of the propagation launches */
+    float    pd_ms;              /* CUDA-event time of the PD smoother loops    */
+} cvtpm_stats;
+
 /* One stereo pair of a batch. */
 typedef struct cvtpm_pair {
     const float* left;      /* device RGBA f32 */
@@ -165,6 +179,12 @@ cvtpm_status cvtpm_cost_adjoint(cvtpm_ctx* ctx,
                                 const float* dcost,
                                 float* cost, float* dplanes,
                                 float* dimg1, float* dimg2, void* stream);
+
+/* Enable CUDA-event timing of the propagation and PD phases (on the call's
+ * stream); cvtpm_get_stats waits for the recorded events. */
+cvtpm_status cvtpm_set_timing(cvtpm_ctx* ctx, int enable);
+cvtpm_status cvtpm_reset_stats(cvtpm_ctx* ctx);
+cvtpm_status cvtpm_get_stats(cvtpm_ctx* ctx, cvtpm_stats* out);
 
 /* Many pairs of uneven size in one graph-captured launch sequence. */
 cvtpm_status cvtpm_depthmap_batched(cvtpm_ctx* ctx, const cvtpm_pair* pairs,

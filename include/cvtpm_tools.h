@@ -1,0 +1,22 @@
+/*
+ * cvtpm_tools.h — measurement helpers exported by libcvtpm.so beside the
+ * drop-in ABI of cvtpm.h.  They have no counterpart in the reference: they
+ * supply denominators for roofline reporting.
+ */
+#ifndef CVTPM_TOOLS_H
+#define CVTPM_TOOLS_H
+
+#include "cvtpm.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* FP32 CUDA-core peak of `device`: a grid of independent FFMA chains
+ * (2 flops each), timed with CUDA events on `stream`.  Writes TFLOP/s. */
+cvtpm_status cvtpm_tool_fp32_peak(int device, void* stream, float* tflops);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,50 @@
+/* Drop-in check for C++ callers: reads two RGBA float32 images (raw, W*H*4),
+ * runs cvt::PMHuberStereo::depthMap through include/cvt/PMHuberStereo.hpp and
+ * writes the disparity map (raw, W*H floats).
+ * usage: facade_main W H patchsize depthmax iterations left.raw right.raw out.raw */
+#include <cstdio>
+#include <cstdlib>
+#include <vector>
+
+#include "cvt/PMHuberStereo.hpp"
+
+static bool read_all(const char* path, std::vector<float>& v) {
+    FILE* f = fopen(path, "rb");
+    if (!f) return false;
+    size_t n = fread(v.data(), sizeof(float), v.size(), f);
+    fclose(f);
+    return n == v.size();
+}
+
+int main(int argc, char** argv) {
+    if (argc != 9) { fprintf(stderr, "usage\n"); return 2; }
+    size_t W = (size_t)atoi(argv[1]), H = (size_t)atoi(argv[2]);
+    size_t patch = (size_t)atoi(argv[3]);
+    float dmax = (float)atof(argv[4]);
+    size_t iters = (size_t)atoi(argv[5]);
+    std::vector<float> l(W * H * 4), r(W * H * 4), d(W * H);
+    if (!read_all(argv[6], l) || !read_all(argv[7], r)) { fprintf(stderr, "read failed\n"); return 3; }
+    try {
+        cvt::Image left(W, H), right(W, H), dmap;
+        left.upload(l.data());
+        right.upload(r.data());
+        cvt::PMHuberStereo stereo;                         /* REFERENCE preset */
+        stereo.depthMap(dmap, left, right, patch, dmax, iters, 4);
+        dmap.download(d.data());
+        try {
+            cvt::Image other(W + 1, H);
+            stereo.depthMap(dmap, left, other, patch, dmax, iters, 4);
+            fprintf(stderr, "expected CVTException\n");
+            return 5;
+        } catch (const cvt::CVTException&) {
+        }
+    } catch (const std::exception& e) {
+        fprintf(stderr, "error: %s\n", e.what());
+        return 4;
+    }
+    FILE* f = fopen(argv[8], "wb");
+    if (!f) return 6;
+    fwrite(d.data(), sizeof(float), d.size(), f);
+    fclose(f);
+    return 0;
+}

@@ -1,0 +1,53 @@
+"""The C++ facade include/cvt/PMHuberStereo.hpp: it compiles against the C
+ABI here, and on a GPU a C++ program using it gives the same disparity map
+as the oracle."""
+import os
+import shutil
+import subprocess
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+CUDA_INC = "/usr/local/cuda/include"
+CUDA_LIB = "/usr/local/cuda/lib64"
+
+
+def _gxx():
+    g = shutil.which("g++")
+    if not g or not os.path.isdir(CUDA_INC):
+        pytest.skip("g++ or CUDA headers missing")
+    return g
+
+
+def test_facade_compiles(tmp_path):
+    g = _gxx()
+    src = os.path.join(ROOT, "tests", "cpp", "facade_main.cpp")
+    r = subprocess.run([g, "-std=c++17", "-fsyntax-only", "-Wall", "-I", os.path.join(ROOT, "include"),
+                        "-I", CUDA_INC, src], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+
+
+@pytest.mark.gpu
+def test_facade_matches_oracle(tmp_path, cuda, oracle):
+    g = _gxx()
+    from cvt_gb300 import scenes
+    from cvt_gb300.params import default_params, PRESET_REFERENCE
+    from cvt_gb300._lib import LIB_PATH
+    exe = str(tmp_path / "facade")
+    r = subprocess.run([g, "-std=c++17", "-O1", "-I", os.path.join(ROOT, "include"), "-I", CUDA_INC,
+                        os.path.join(ROOT, "tests", "cpp", "facade_main.cpp"), "-o", exe,
+                        LIB_PATH, f"-Wl,-rpath,{os.path.dirname(LIB_PATH)}", "-L", CUDA_LIB, "-lcudart",
+                        f"-Wl,-rpath,{CUDA_LIB}"], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    sc = scenes.make_scene(45, 33, 3, 10.0, seed=12)
+    sc.left.tofile(tmp_path / "l.raw")
+    sc.right.tofile(tmp_path / "r.raw")
+    out = tmp_path / "d.raw"
+    r = subprocess.run([exe, "45", "33", "5", "10", "2", str(tmp_path / "l.raw"), str(tmp_path / "r.raw"), str(out)],
+                       capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr
+    got = np.fromfile(out, np.float32).reshape(33, 45)
+    want, _ = oracle.depthmap(default_params(PRESET_REFERENCE, patchsize=5, depthmax=10.0, iterations=2),
+                              sc.left, sc.right)
+    assert np.array_equal(got.view(np.uint32), want.view(np.uint32))
