@@ -35,7 +35,7 @@ class CvtpmPair(ctypes.Structure):
 
 class CvtpmStats(ctypes.Structure):
     _fields_ = [("calls", ctypes.c_uint64), ("launches", ctypes.c_uint64), ("propagate_launches", ctypes.c_uint64),
-                ("cost_evals", ctypes.c_uint64), ("cost_taps", ctypes.c_uint64), ("pd_launches", ctypes.c_uint64),
+                ("cost_evals", ctypes.c_uint64), ("cost_taps", ctypes.c_uint64), ("pd_launches", ctypes.c_uint64), ("pd_steps", ctypes.c_uint64),
                 ("propagate_ms", ctypes.c_float), ("pd_ms", ctypes.c_float)]
 
     def as_dict(self) -> dict:

@@ -195,11 +195,6 @@ PmPassArgs base_args(cvtpm_ctx* ctx, const cvtpm_params& p, int W, int H, int v1
     a.k.alpha = p.color_alpha; a.k.oma = 1.0f - p.color_alpha;
     a.k.cmax = p.color_maxdiff; a.k.gmax = p.grad_maxdiff;
     a.k.rp = rec_pitch(W);
-    a.k.n = 2 * p.patchsize + 1;
-    a.k.ntaps = a.k.n * a.k.n;
-    a.k.ni = (a.k.ntaps + 31) / 32;
-    a.k.kstep = 32 / a.k.n;
-    a.k.rstep = 32 % a.k.n;
     const int v2 = 1 - v1;
     a.v1 = {ctx->col[v1], ctx->grad[v1], ctx->recA[v1], ctx->recB[v1], ctx->recC[v1], ctx->recD[v1]};
     a.v2 = {ctx->col[v2], ctx->grad[v2], ctx->recA[v2], ctx->recB[v2], ctx->recC[v2], ctx->recD[v2]};
@@ -221,26 +216,37 @@ cvtpm_status prep_views(cvtpm_ctx* ctx, const cvtpm_params& p, const float* img0
     return CVTPM_OK;
 }
 
-/* PDROF::apply, cvt/gfx/PDROF.h:50-96: u warm-starts from `output`, p from 0. */
+/* PDROF::apply, cvt/gfx/PDROF.h:50-96: u warm-starts from `output`, p from 0;
+ * `iters` steps, plus one when `iters` is odd so the result lands in
+ * `output` (:83-95).  The steps run PDB_K at a time in the temporally blocked
+ * kernel (identical arithmetic); iters == 0 keeps the reference's single
+ * extra step from a copy of the input. */
 cvtpm_status pd_apply(cvtpm_ctx* ctx, float4* output, const float4* input, const float* wgt, float lambda, int iters,
                       int W, int H, cudaStream_t st) {
     const size_t n = (size_t)W * H;
-    CK(cudaMemcpyAsync(ctx->pdT, input, n * 16, cudaMemcpyDeviceToDevice, st), "pd copy");
-    CK(cudaMemsetAsync(ctx->pdP[0], 0, n * 32, st), "pd clear");
-    CK(cudaMemsetAsync(ctx->pdP[1], 0, n * 32, st), "pd clear");
-    float4* img[2] = {ctx->pdT, output};
-    float4* pp[2] = {ctx->pdP[0], ctx->pdP[1]};
     PhaseTimer tm(ctx, st, ctx->ev_pd);
-    int swap = 0;
-    for (int i = 0; i < iters; ++i) {
-        swap = i & 1;
-        LK(pm_launch_pd_step(img[swap], pp[swap], img[1 - swap], pp[1 - swap], input, wgt, lambda, W, H, st), "pd step");
+    if (iters == 0) {
+        CK(cudaMemcpyAsync(ctx->pdT, input, n * 16, cudaMemcpyDeviceToDevice, st), "pd copy");
+        CK(cudaMemsetAsync(ctx->pdP[0], 0, n * 32, st), "pd clear");
+        LK(pm_launch_pd_step(output, ctx->pdP[1], ctx->pdT, ctx->pdP[0], input, wgt, lambda, W, H, st), "pd step");
         ++ctx->stats.pd_launches;
+        ++ctx->stats.pd_steps;
+        tm.stop();
+        return CVTPM_OK;
     }
-    if (!swap) {
-        LK(pm_launch_pd_step(img[1], pp[1], img[0], pp[0], input, wgt, lambda, W, H, st), "pd step");
+    const int total = iters + (iters & 1);
+    const int K = pm_pd_block_steps();
+    float4* U[2] = {output, ctx->pdT};
+    float4* Pp[2] = {ctx->pdP[0], ctx->pdP[1]};
+    int l = 0;
+    for (int done = 0; done < total; done += K, ++l) {
+        const int steps = total - done < K ? total - done : K;
+        LK(pm_launch_pd_block(U[(l + 1) & 1], Pp[(l + 1) & 1], U[l & 1], Pp[l & 1], l == 0 ? 1 : 0, input, wgt, lambda,
+                              steps, W, H, st), "pd block");
         ++ctx->stats.pd_launches;
+        ctx->stats.pd_steps += (uint64_t)steps;
     }
+    if (U[l & 1] != output) CK(cudaMemcpyAsync(output, U[l & 1], n * 16, cudaMemcpyDeviceToDevice, st), "pd copy");
     tm.stop();
     return CVTPM_OK;
 }

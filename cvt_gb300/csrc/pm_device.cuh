@@ -216,9 +216,6 @@ struct PmCostConsts {
     float Wf, Hf;
     float alpha, oma, cmax, gmax;
     int rp;          /* row pitch (elements) of the record planes */
-    /* the window as a flat tap list t = (dy+P)*n + (dx+P); a warp-cooperative
-     * evaluation gives lane l the taps t = l, l+32, ...; 32 = kstep*n + rstep */
-    int n, ntaps, ni, kstep, rstep;
 };
 
 #ifdef PM_KERNELS_TU
@@ -318,82 +315,5 @@ PM_DEV void eval_costs(const PmCostConsts& k, const PmView& v1, const PmView& v2
 }
 #endif
 
-#ifdef PM_KERNELS_TU
-/* Flat-order copy of the spatial profile in shared memory (block-wide). */
-PM_DEV void load_flat_profile(const PmCostConsts& k, float* s_prof) {
-    const int tid = threadIdx.y * blockDim.x + threadIdx.x, nt = blockDim.x * blockDim.y;
-    for (int t = tid; t < k.ntaps; t += nt) {
-        const int dy = t / k.n - k.P, dx = t % k.n - k.P;
-        s_prof[t] = c_prof[(dy + PM_PMAX) * PM_PROF_N + (dx + PM_PMAX)];
-    }
-    __syncthreads();
-}
-
-/* Warp-cooperative FAST cost: every active lane brings one plane for its own
- * pixel; the warp evaluates them one pixel at a time with the 32 lanes
- * splitting the window (lane l sums taps t = l, l+32, ... in order; a
- * butterfly over lane distances 16..1 adds the partial sums).  All lanes then
- * sample the other view with the same plane, so the record loads of a
- * request are contiguous — the shape for candidates whose planes differ
- * arbitrarily from lane to lane (random planes).  Returns the lane's cost. */
-PM_DEV float coop_cost_warp(const PmCostConsts& k, const PmView& v1, const PmView& v2, const float* s_prof,
-                            int x, int y, float4 s, bool active) {
-    const int lane = threadIdx.x & 31;
-    const unsigned todo = __ballot_sync(0xffffffffu, active);
-    float mine = 1e5f;
-    for (int p = 0; p < 32; ++p) {
-        if (!((todo >> p) & 1u)) continue;
-        const int px = __shfl_sync(0xffffffffu, x, p), py = __shfl_sync(0xffffffffu, y, p);
-        const float sx = __shfl_sync(0xffffffffu, s.x, p);
-        const float sy = __shfl_sync(0xffffffffu, s.y, p);
-        const float sz = __shfl_sync(0xffffffffu, s.z, p);
-        float cost = 1e5f;
-        if (isfinite(sx) && isfinite(sy) && isfinite(sz)) {
-            const float4 vc = __ldg(&v1.col[(size_t)py * k.W + px]);
-            float ws = 0.0f, r1 = 0.0f, r2 = 0.0f;
-            int col = lane % k.n, row = lane / k.n;
-            for (int i = 0; i < k.ni; ++i) {
-                const int t = lane + 32 * i;
-                const int qx = px + col - k.P, qy = py + row - k.P;
-                if (t < k.ntaps && qx >= 0 && qy >= 0 && qx < k.W && qy < k.H) {
-                    const size_t qo = (size_t)qy * k.W + qx;
-                    const float4 a1 = __ldg(&v1.col[qo]);
-                    const float4 g1 = __ldg(&v1.grad[qo]);
-                    const float d = (fabsf(vc.x - a1.x) + fabsf(vc.y - a1.y)) + fabsf(vc.z - a1.z);
-                    const float w1 = pm_exp(-d * s_prof[t]);
-                    const float xp = fmaf(sx, (float)qx, fmaf(sy, (float)qy, sz));
-                    if (xp >= 0.0f && xp < k.Wf) {
-                        const float fi = floorf(xp);
-                        const float a = xp - fi;
-                        const size_t j = (size_t)qy * k.rp + (int)fi;
-                        const float4 A = __ldg(&v2.recA[j]);
-                        const float4 B = __ldg(&v2.recB[j]);
-                        const float4 Cc = __ldg(&v2.recC[j]);
-                        const float2 D = __ldg(&v2.recD[j]);
-                        const float v0 = fmaf(a, B.w, A.x), v1c = fmaf(a, Cc.x, A.y), v2c = fmaf(a, Cc.y, A.z);
-                        const float u0 = fmaf(a, Cc.z, A.w), u1 = fmaf(a, Cc.w, B.x), u2 = fmaf(a, D.x, B.y), u3 = fmaf(a, D.y, B.z);
-                        const float cc = (fminf(fabsf(a1.x - v0), k.cmax) + fminf(fabsf(a1.y - v1c), k.cmax)) + fminf(fabsf(a1.z - v2c), k.cmax);
-                        const float gc = ((fminf(fabsf(g1.x - u0), k.gmax) + fminf(fabsf(g1.y - u1), k.gmax)) + fminf(fabsf(g1.z - u2), k.gmax)) + fminf(fabsf(g1.w - u3), k.gmax);
-                        r1 = fmaf(w1, cc, r1);
-                        r2 = fmaf(w1, gc, r2);
-                        ws = ws + w1;
-                    }
-                }
-                col += k.rstep; row += k.kstep;
-                if (col >= k.n) { col -= k.n; row += 1; }
-            }
-#pragma unroll
-            for (int off = 16; off > 0; off >>= 1) {
-                ws = ws + __shfl_xor_sync(0xffffffffu, ws, off);
-                r1 = r1 + __shfl_xor_sync(0xffffffffu, r1, off);
-                r2 = r2 + __shfl_xor_sync(0xffffffffu, r2, off);
-            }
-            if (!(ws <= 1.1f)) cost = fmaf(k.alpha, r1, k.oma * r2) / ws;
-        }
-        if (lane == p) mine = cost;
-    }
-    return mine;
-}
-#endif
 
 #endif

@@ -81,24 +81,16 @@ PM_DEV void seed_rng(PmRng& rng, const PmPassArgs& a, int x, int y, bool init) {
 
 template <bool EXACT>
 __global__ void __launch_bounds__(256) k_init(PmPassArgs a) {
-    __shared__ float s_prof[EXACT ? 1 : PM_PROF_N * PM_PROF_N];
-    if (!EXACT) load_flat_profile(a.k, s_prof);
     const int x = blockIdx.x * 32 + threadIdx.x, y = blockIdx.y * 8 + threadIdx.y;
-    const bool inside = x < a.k.W && y < a.k.H;
-    if (EXACT && !inside) return;
-    const int xc = min(x, a.k.W - 1), yc = min(y, a.k.H - 1);
+    if (x >= a.k.W || y >= a.k.H) return;
     PmRng rng;
-    seed_rng(rng, a, xc, yc, true);
-    float4 s[1] = {state_init(rng, (float)xc, (float)yc, a.lr, 1.0f, a.depthmax)};
-    if (EXACT) {
-        bool act[1] = {true};
-        float c[1];
-        eval_costs<1, true>(a.k, a.v1, a.v2, x, y, s, act, c);
-        s[0].w = c[0];
-    } else {
-        s[0].w = coop_cost_warp(a.k, a.v1, a.v2, s_prof, xc, yc, s[0], inside);   /* random planes */
-    }
-    if (inside) a.out[(size_t)y * a.k.W + x] = s[0];
+    seed_rng(rng, a, x, y, true);
+    float4 s[1] = {state_init(rng, (float)x, (float)y, a.lr, 1.0f, a.depthmax)};
+    bool act[1] = {true};
+    float c[1];
+    eval_costs<1, EXACT>(a.k, a.v1, a.v2, x, y, s, act, c);
+    s[0].w = c[0];
+    a.out[(size_t)y * a.k.W + x] = s[0];
 }
 
 template <bool EXACT>
@@ -116,8 +108,6 @@ __global__ void __launch_bounds__(256) k_cost_field(PmPassArgs a, const float4* 
 /* --------------------------------------------------------- propagate -- */
 template <bool EXACT>
 __global__ void __launch_bounds__(256) k_propagate(PmPassArgs a) {
-    __shared__ float s_prof[EXACT ? 1 : PM_PROF_N * PM_PROF_N];
-    if (!EXACT) load_flat_profile(a.k, s_prof);
     const int W = a.k.W, H = a.k.H;
     const int x = blockIdx.x * 32 + threadIdx.x, y = blockIdx.y * 8 + threadIdx.y;
     const bool inside = x < W && y < H;
@@ -185,18 +175,7 @@ __global__ void __launch_bounds__(256) k_propagate(PmPassArgs a) {
             s[i] = a.old[(size_t)clampi(yc + oy, 0, H - 1) * W + clampi(xc + ox, 0, W - 1)];
         }
         s[3] = state_init(rng, cx, cy, lr, 2.0f, dmax);
-        if (EXACT) {
-            eval_costs<4, true>(a.k, a.v1, a.v2, xc, yc, s, act, c);
-        } else {
-            /* random neighbours lane by lane; the random plane, whose disparity
-             * differs arbitrarily between lanes, cooperatively */
-            float4 s3[3] = {s[0], s[1], s[2]};
-            bool act3[3] = {true, true, true};
-            float c3[3];
-            eval_costs<3, false>(a.k, a.v1, a.v2, xc, yc, s3, act3, c3);
-            c[0] = c3[0]; c[1] = c3[1]; c[2] = c3[2];
-            c[3] = coop_cost_warp(a.k, a.v1, a.v2, s_prof, xc, yc, s[3], inside);
-        }
+        eval_costs<4, EXACT>(a.k, a.v1, a.v2, xc, yc, s, act, c);
 #pragma unroll
         for (int i = 0; i < 4; ++i) accept(s[i], c[i], 13 + i);
     }
@@ -399,31 +378,65 @@ __global__ void __launch_bounds__(32) k_fill_output(const float4* __restrict__ i
 }
 
 /* ------------------------------------------------------------ PD step -- */
-/* One weighted Huber-ROF primal-dual step (PDHuberWeighted.cl:34-104):
- * dual ascent with Huber smoothing and projection, primal descent, over-
- * relaxation.  The dual of the pixel to the left and above is recomputed by
- * the block edge threads, as the reference's work-group halo does. */
-PM_DEV void pd_dual(const float4* __restrict__ last, const float4* __restrict__ pin, const float* __restrict__ wgt,
-                    int W, int H, int qx, int qy, float4& lo, float4& hi) {
+/* One weighted Huber-ROF primal-dual step (PDHuberWeighted.cl:34-104): dual
+ * ascent with Huber smoothing and projection, primal descent, over-
+ * relaxation.  The arithmetic lives in pd_dual / pd_primal, shared by the
+ * one-step kernel and the temporally blocked kernel. */
+
+/* 1 + SIGMA*ALPHA/w, the dual's denominator (PDHuberWeighted.cl:62,64);
+ * constant per pixel over the smoother's steps.  Infinite where w == 0. */
+PM_DEV float pd_den(float w) {
     const float SIGMA = 1.0f / pm_sqrt(8.0f), ALPHA = 0.001f;
+    return 1.0f + SIGMA * ALPHA / w;
+}
+
+/* x / d with d >= 1: x/1 is x exactly, so the division is skipped there. */
+PM_DEV float div_ge1(float x, float d) { return d == 1.0f ? x : x / d; }
+/* x / d with d > 0 (possibly infinite): a zero numerator gives that zero
+ * back exactly, so the division is skipped there. */
+PM_DEV float div_pos(float x, float d) { return x == 0.0f ? x : x / d; }
+
+/* The dual at q from u(q), u(q+x), u(q+y), the old dual and w(q) (:49-68). */
+PM_DEV void pd_dual(float w, float den, float4 uq, float4 ux, float4 uy, float4 plo, float4 phi,
+                    float4& lo, float4& hi) {
+    const float SIGMA = 1.0f / pm_sqrt(8.0f);
+    const float4 dx = w * (uq - ux);
+    const float4 dy = w * (uq - uy);
+    const float4 nl = plo + SIGMA * dx, nh = phi + SIGMA * dy;
+    const float4 l = f4(div_pos(nl.x, den), div_pos(nl.y, den), div_pos(nl.z, den), div_pos(nl.w, den));
+    const float4 h = f4(div_pos(nh.x, den), div_pos(nh.y, den), div_pos(nh.z, den), div_pos(nh.w, den));
+    const float4 pt = l * l + h * h;
+    const float sxy = fmaxf(1.0f, pm_sqrt(pt.x + pt.y));
+    const float sz = fmaxf(1.0f, pm_sqrt(pt.z));
+    const float sw = fmaxf(1.0f, pm_sqrt(0.0f));
+    lo = f4(div_ge1(l.x, sxy), div_ge1(l.y, sxy), div_ge1(l.z, sz), div_ge1(l.w, sw));
+    hi = f4(div_ge1(h.x, sxy), div_ge1(h.y, sxy), div_ge1(h.z, sz), div_ge1(h.w, sw));
+}
+
+/* The primal update at c (:70-78); den_u = 1 + TAU*lambda. */
+PM_DEV float4 pd_primal(float4 uc, float4 img, float wc, float4 lo_c, float4 lo_l, float4 hi_c, float4 hi_u,
+                        float lambda, float den_u) {
+    const float TAU = 1.0f / pm_sqrt(8.0f), THETA = 0.5f;
+    const float4 div = lo_c - lo_l + hi_c - hi_u;
+    const float4 lam = f4s(lambda);
+    const float4 num = uc + TAU * (lam * img - wc * div);
+    float4 un = f4(num.x / den_u, num.y / den_u, num.z / den_u, 0.0f);   /* .w is overwritten below */
+    un = un + THETA * (un - uc);
+    un.w = 1.0f;
+    return un;
+}
+
+PM_DEV void pd_dual_at(const float4* __restrict__ last, const float4* __restrict__ pin, const float* __restrict__ wgt,
+                       int W, int H, int qx, int qy, float4& lo, float4& hi) {
     const bool in = qx >= 0 && qy >= 0 && qx < W && qy < H;
     const float w = in ? wgt[(size_t)qy * W + qx] : 0.0f;
     const int cx0 = clampi(qx, 0, W - 1), cy0 = clampi(qy, 0, H - 1);
     const float4 uq = last[(size_t)cy0 * W + cx0];
     const float4 ux = last[(size_t)cy0 * W + clampi(qx + 1, 0, W - 1)];
     const float4 uy = last[(size_t)clampi(qy + 1, 0, H - 1) * W + cx0];
-    const float4 dx = w * (uq - ux);
-    const float4 dy = w * (uq - uy);
     const float4 plo = in ? pin[((size_t)qy * W + qx) * 2] : f4s(0.0f);
     const float4 phi = in ? pin[((size_t)qy * W + qx) * 2 + 1] : f4s(0.0f);
-    const float den = 1.0f + SIGMA * ALPHA / w;
-    const float4 l = (plo + SIGMA * dx) / f4s(den);
-    const float4 h = (phi + SIGMA * dy) / f4s(den);
-    const float4 pt = l * l + h * h;
-    const float sxy = pm_sqrt(pt.x + pt.y);
-    const float4 pproj = f4(fmaxf(1.0f, sxy), fmaxf(1.0f, sxy), fmaxf(1.0f, pm_sqrt(pt.z)), fmaxf(1.0f, pm_sqrt(0.0f)));
-    lo = l / pproj;
-    hi = h / pproj;
+    pd_dual(w, pd_den(w), uq, ux, uy, plo, phi, lo, hi);
 }
 
 #define PD_TX 32
@@ -437,25 +450,104 @@ k_pd_step(float4* __restrict__ uout, float4* __restrict__ pout, const float4* __
     const int tx = threadIdx.x, ty = threadIdx.y;
     const int x = blockIdx.x * PD_TX + tx, y = blockIdx.y * PD_TY + ty;
     float4 lo, hi;
-    pd_dual(last, pin, wgt, W, H, x, y, lo, hi);
+    pd_dual_at(last, pin, wgt, W, H, x, y, lo, hi);
     slo[ty + 1][tx + 1] = lo; shi[ty + 1][tx + 1] = hi;
-    if (tx == 0) { float4 l2, h2; pd_dual(last, pin, wgt, W, H, x - 1, y, l2, h2); slo[ty + 1][0] = l2; shi[ty + 1][0] = h2; }
-    if (ty == 0) { float4 l2, h2; pd_dual(last, pin, wgt, W, H, x, y - 1, l2, h2); slo[0][tx + 1] = l2; shi[0][tx + 1] = h2; }
+    if (tx == 0) { float4 l2, h2; pd_dual_at(last, pin, wgt, W, H, x - 1, y, l2, h2); slo[ty + 1][0] = l2; shi[ty + 1][0] = h2; }
+    if (ty == 0) { float4 l2, h2; pd_dual_at(last, pin, wgt, W, H, x, y - 1, l2, h2); slo[0][tx + 1] = l2; shi[0][tx + 1] = h2; }
     __syncthreads();
     if (x >= W || y >= H) return;
-    const float TAU = 1.0f / pm_sqrt(8.0f), THETA = 0.5f;
-    const float4 div = slo[ty + 1][tx + 1] - slo[ty + 1][tx] + shi[ty + 1][tx + 1] - shi[ty][tx + 1];
+    const float TAU = 1.0f / pm_sqrt(8.0f);
     const size_t o = (size_t)y * W + x;
-    const float4 img = f[o];
-    const float4 uc = last[o];
-    const float wc = wgt[o];
-    const float4 lam = f4s(lambda);
-    float4 un = (uc + TAU * (lam * img - wc * div)) / (f4s(1.0f) + TAU * lam);
-    un = un + THETA * (un - uc);
-    un.w = 1.0f;
+    const float4 un = pd_primal(last[o], f[o], wgt[o], slo[ty + 1][tx + 1], slo[ty + 1][tx], shi[ty + 1][tx + 1],
+                                shi[ty][tx + 1], lambda, 1.0f + TAU * lambda);
     uout[o] = un;
     pout[o * 2] = lo;
     pout[o * 2 + 1] = hi;
+}
+
+/* PDB_K steps per launch on a PDB_TX x PDB_TY tile with a PDB_K-pixel halo
+ * held in shared memory.  Every step recomputes the dual over the whole
+ * region (phase 1) and then the primal (phase 2), in place; errors from the
+ * region's open edges advance one pixel per step, so after PDB_K steps the
+ * tile is exact.  Image borders keep the reference's semantics: u is read
+ * clamped to the edge, the dual and the weight are zero outside. */
+#define PDB_TX 32
+#define PDB_TY 16
+#define PDB_K 4
+#define PDB_RX (PDB_TX + 2 * PDB_K)
+#define PDB_RY (PDB_TY + 2 * PDB_K)
+#define PDB_N (PDB_RX * PDB_RY)
+
+__global__ void __launch_bounds__(PDB_TX * PDB_TY)
+k_pd_block(float4* __restrict__ uout, float4* __restrict__ pout, const float4* __restrict__ uin,
+           const float4* __restrict__ pin, int pzero, const float4* __restrict__ f, const float* __restrict__ wgt,
+           float lambda, int nsteps, int W, int H) {
+    extern __shared__ __align__(16) float4 sm4[];
+    float4* su = sm4;
+    float4* slo = su + PDB_N;
+    float4* shi = slo + PDB_N;
+    float4* sf = shi + PDB_N;
+    float* sw = (float*)(sf + PDB_N);
+    float* sden = sw + PDB_N;
+    const int tid = threadIdx.y * PDB_TX + threadIdx.x, nt = PDB_TX * PDB_TY;
+    const int rx0 = blockIdx.x * PDB_TX - PDB_K, ry0 = blockIdx.y * PDB_TY - PDB_K;
+    for (int i = tid; i < PDB_N; i += nt) {
+        const int gx = rx0 + i % PDB_RX, gy = ry0 + i / PDB_RX;
+        const bool in = gx >= 0 && gy >= 0 && gx < W && gy < H;
+        const size_t o = (size_t)clampi(gy, 0, H - 1) * W + clampi(gx, 0, W - 1);
+        su[i] = uin[o];
+        const float w = in ? wgt[o] : 0.0f;
+        sw[i] = w;
+        sden[i] = pd_den(w);
+        sf[i] = in ? f[o] : f4s(0.0f);
+        slo[i] = (in && !pzero) ? pin[o * 2] : f4s(0.0f);
+        shi[i] = (in && !pzero) ? pin[o * 2 + 1] : f4s(0.0f);
+    }
+    __syncthreads();
+    const float TAU = 1.0f / pm_sqrt(8.0f);
+    const float den_u = 1.0f + TAU * lambda;
+    /* region index of image position (gx, gy) clamped to the image, then to the region */
+    auto at = [&](int gx, int gy) {
+        const int lx = clampi(clampi(gx, 0, W - 1) - rx0, 0, PDB_RX - 1);
+        const int ly = clampi(clampi(gy, 0, H - 1) - ry0, 0, PDB_RY - 1);
+        return ly * PDB_RX + lx;
+    };
+    /* Step st updates the duals at ring distance >= st from the region edge and
+     * the primal at distance >= st+1: by induction u is exact at distance
+     * >= st+1 afterwards (its left/upper duals at distance >= st are exact), so
+     * after the last step the tile (distance PDB_K) is. */
+    for (int st = 0; st < nsteps; ++st) {
+        const int dw = PDB_RX - 2 * st, dh = PDB_RY - 2 * st;
+        for (int k = tid; k < dw * dh; k += nt) {                     /* duals */
+            const int lx = st + k % dw, ly = st + k / dw;
+            const int i = ly * PDB_RX + lx;
+            const int gx = rx0 + lx, gy = ry0 + ly;
+            float4 lo, hi;
+            pd_dual(sw[i], sden[i], su[at(gx, gy)], su[at(gx + 1, gy)], su[at(gx, gy + 1)], slo[i], shi[i], lo, hi);
+            slo[i] = lo;
+            shi[i] = hi;
+        }
+        __syncthreads();
+        const int pw = dw - 2, ph = dh - 2;
+        for (int k = tid; k < pw * ph; k += nt) {                     /* primal */
+            const int lx = st + 1 + k % pw, ly = st + 1 + k / pw;
+            const int gx = rx0 + lx, gy = ry0 + ly;
+            if (gx < 0 || gy < 0 || gx >= W || gy >= H) continue;
+            const int i = ly * PDB_RX + lx;
+            su[i] = pd_primal(su[i], sf[i], sw[i], slo[i], slo[i - 1], shi[i], shi[i - PDB_RX], lambda, den_u);
+        }
+        __syncthreads();
+    }
+    for (int i = tid; i < PDB_TX * PDB_TY; i += nt) {
+        const int lx = PDB_K + i % PDB_TX, ly = PDB_K + i / PDB_TX;
+        const int gx = rx0 + lx, gy = ry0 + ly;
+        if (gx >= W || gy >= H) continue;
+        const int r = ly * PDB_RX + lx;
+        const size_t o = (size_t)gy * W + gx;
+        uout[o] = su[r];
+        pout[o * 2] = slo[r];
+        pout[o * 2 + 1] = shi[r];
+    }
 }
 
 /* ---------------------------------------------------------- launchers -- */
@@ -532,6 +624,20 @@ cudaError_t pm_launch_fill_state(const float4* in, int W, int H, float depthmax,
 cudaError_t pm_launch_fill_output(const float4* in, int W, int H, float scale, float* dmap, size_t dpitch,
                                   float4* nmap, size_t npitch, cudaStream_t st) {
     k_fill_output<<<H, 32, sizeof(int) * W, st>>>(in, W, H, scale, dmap, dpitch, nmap, npitch);
+    PM_LAUNCH_CHECK();
+    return cudaSuccess;
+}
+
+int pm_pd_block_steps() { return PDB_K; }
+
+cudaError_t pm_launch_pd_block(float4* uout, float4* pout, const float4* uin, const float4* pin, int pzero,
+                               const float4* f, const float* wgt, float lambda, int nsteps, int W, int H,
+                               cudaStream_t st) {
+    const size_t smem = (size_t)PDB_N * (4 * sizeof(float4) + 2 * sizeof(float));
+    cudaError_t e = cudaFuncSetAttribute(k_pd_block, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    dim3 b(PDB_TX, PDB_TY), g((W + PDB_TX - 1) / PDB_TX, (H + PDB_TY - 1) / PDB_TY);
+    k_pd_block<<<g, b, smem, st>>>(uout, pout, uin, pin, pzero, f, wgt, lambda, nsteps, W, H);
     PM_LAUNCH_CHECK();
     return cudaSuccess;
 }

@@ -104,6 +104,7 @@ typedef struct cvtpm_stats {
                                     propagation passes, counted on the device   */
     uint64_t cost_taps;          /* in-image window taps of those evaluations   */
     uint64_t pd_launches;
+    uint64_t pd_steps;           /* PD smoother steps (several per launch)      */
     float    propagate_ms;       /* CUDA-event time of the propagation launches */
     float    pd_ms;              /* CUDA-event time of the PD smoother loops    */
 } cvtpm_stats;

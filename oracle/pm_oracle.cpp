@@ -353,62 +353,6 @@ static float cost_eval(const CostCfg& k, const View& v1, const View& v2, int cx,
     return fmaf(k.alpha, rc, k.one_m_alpha * rg) / wsum;
 }
 
-/* ARITH_FAST, warp-cooperative form (the CUDA kernels use it for random
- * planes: init and the random-plane candidate): the window is the flat tap
- * list t = (dy+P)*n + (dx+P); "lane" l sums the taps t = l, l+32, ... in
- * order, then a butterfly over lane distances 16, 8, 4, 2, 1 adds the 32
- * partial sums. */
-static float cost_eval_coop(const CostCfg& k, const View& v1, const View& v2, int cx, int cy, F4 s) {
-    if (!finite3(s)) return 1e5f;
-    const int W = v1.W, H = v1.H, P = k.P, n = 2 * P + 1;
-    const float Wf = (float)W;
-    const F4 vc = v1.col[(size_t)cy * W + cx];
-    const int ntaps = n * n, ni = (ntaps + 31) / 32;
-    float lws[32], lr1[32], lr2[32];
-    for (int l = 0; l < 32; ++l) {
-        float ws = 0.0f, rc = 0.0f, rg = 0.0f;
-        for (int i = 0; i < ni; ++i) {
-            const int t = l + 32 * i;
-            if (t >= ntaps) break;
-            const int qx = cx + t % n - P, qy = cy + t / n - P;
-            if (qx < 0 || qy < 0 || qx >= W || qy >= H) continue;
-            const F4 a1 = v1.col[(size_t)qy * W + qx];
-            const F4 g1 = v1.grad[(size_t)qy * W + qx];
-            float d = (fabsf(vc.x - a1.x) + fabsf(vc.y - a1.y)) + fabsf(vc.z - a1.z);
-            float w1 = pm_exp(-d * k.prof[t]);
-            float xp = fmaf(s.x, (float)qx, fmaf(s.y, (float)qy, s.z));
-            if (!(xp >= 0.0f && xp < Wf)) continue;
-            float fi = floorf(xp);
-            float a = xp - fi;
-            const float* r = &v2.rec[((size_t)qy * W + (size_t)(int)fi) * 14];
-            float v[7];
-            for (int c = 0; c < 7; ++c) v[c] = fmaf(a, r[7 + c], r[c]);
-            float cc = (fminf(fabsf(a1.x - v[0]), k.cmax) + fminf(fabsf(a1.y - v[1]), k.cmax)) + fminf(fabsf(a1.z - v[2]), k.cmax);
-            float gc = ((fminf(fabsf(g1.x - v[3]), k.gmax) + fminf(fabsf(g1.y - v[4]), k.gmax)) + fminf(fabsf(g1.z - v[5]), k.gmax)) + fminf(fabsf(g1.w - v[6]), k.gmax);
-            rc = fmaf(w1, cc, rc);
-            rg = fmaf(w1, gc, rg);
-            ws = ws + w1;
-        }
-        lws[l] = ws; lr1[l] = rc; lr2[l] = rg;
-    }
-    for (int off = 16; off > 0; off >>= 1) {
-        float tws[32], tr1[32], tr2[32];
-        for (int l = 0; l < 32; ++l) {
-            tws[l] = lws[l] + lws[l ^ off];
-            tr1[l] = lr1[l] + lr1[l ^ off];
-            tr2[l] = lr2[l] + lr2[l ^ off];
-        }
-        memcpy(lws, tws, sizeof(tws)); memcpy(lr1, tr1, sizeof(tr1)); memcpy(lr2, tr2, sizeof(tr2));
-    }
-    if (lws[0] <= 1.1f) return 1e5f;
-    return fmaf(k.alpha, lr1[0], k.one_m_alpha * lr2[0]) / lws[0];
-}
-
-/* The evaluation a random plane gets: EXACT raster order, or FAST cooperative. */
-static float cost_eval_random(const CostCfg& k, const View& v1, const View& v2, int cx, int cy, F4 s) {
-    return k.arith == CVTPM_ARITH_FAST ? cost_eval_coop(k, v1, v2, cx, cy, s) : cost_eval(k, v1, v2, cx, cy, s);
-}
-
 /* ------------------------------------------------------ preprocessing -- */
 static inline float gray_at(const F4* img, int W, int H, int x, int y) {
     if (x < 0 || y < 0 || x >= W || y >= H) return 0.0f;             /* CLK_ADDRESS_CLAMP */
@@ -479,7 +423,7 @@ static void init_pass(const Pass& ps, F4* out) {                      /* :230-24
             if (ps.rngkind == CVTPM_RNG_PHILOX) philox_init(rng, ps.seed, p, PHILOX_TAG_INIT, view_id(ps.lr));
             else mwc_init(rng, (uint64_t)p * 3u);
             F4 s = state_init(rng, (float)x, (float)y, ps.lr, 1.0f, ps.depthmax);
-            s.w = cost_eval_random(*ps.k, *ps.v1, *ps.v2, x, y, s);
+            s.w = cost_eval(*ps.k, *ps.v1, *ps.v2, x, y, s);
             out[(size_t)y * W + x] = s;
         }
 }
@@ -510,8 +454,7 @@ static void propagate_pass(const Pass& ps, const F4* old, const F4* smoothimg,
              * (RNG.cl:151-154, pmhstereo.cl:327). */
             else mwc_init(rng, ((uint64_t)p + (uint64_t)ps.iter) * 33u + 12u);
             auto consider = [&](F4 cand, int idx) {
-                cand.w = (idx == 16) ? cost_eval_random(*ps.k, *ps.v1, *ps.v2, x, y, cand)
-                                     : cost_eval(*ps.k, *ps.v1, *ps.v2, x, y, cand);
+                cand.w = cost_eval(*ps.k, *ps.v1, *ps.v2, x, y, cand);
                 float da, db;
                 smooth_distance(cand, self, smooth, cx, cy, dmax, lr, &da, &db);
                 if (cand.w + theta * da <= self.w + theta * db) { self = cand; win = idx; }

@@ -143,3 +143,14 @@ def test_errors(stereo):
         stereo.depthMap(None, a, a, 40, 8.0, 1, 4)
     with pytest.raises(CvtpmError):
         stereo.depthMap(None, a, a, 3, -1.0, 1, 4)
+
+
+@pytest.mark.parametrize("pd_iters", [0, 1, 3, 9])
+def test_pd_step_counts(stereo, oracle, pd_iters):
+    """PDROF::apply with 0, odd and even step counts (PDROF.h:67-95), through
+    the blocked smoother (4 steps per launch) and the one-step path."""
+    sc = scenes.make_scene(70, 41, 3, 10.0, seed=30 + pd_iters)
+    p = default_params(PRESET_BASELINE, patchsize=4, depthmax=10.0, iterations=2, pd_iterations=pd_iters)
+    dm, _, tr, want, ex = run_both(stereo, oracle, sc, p, normalmap=False)
+    assert_bitexact(tr["states"], ex["states"], "states")
+    assert_bitexact(dm, want, "dmap")
