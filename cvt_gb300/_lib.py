@@ -20,6 +20,7 @@ EXPORTS = (
     "cvtpm_set_params", "cvtpm_get_params", "cvtpm_last_error", "cvtpm_synchronize", "cvtpm_depthmap",
     "cvtpm_depthmap_host", "cvtpm_cost_eval", "cvtpm_cost_adjoint", "cvtpm_depthmap_batched",
     "cvtpm_set_timing", "cvtpm_reset_stats", "cvtpm_get_stats", "cvtpm_tool_fp32_peak",
+    "cvtpm_cost_eval_noalloc",
 )
 
 
@@ -80,6 +81,7 @@ def lib() -> ctypes.CDLL:
     L.cvtpm_reset_stats.argtypes = [vp]
     L.cvtpm_get_stats.argtypes = [vp, ctypes.POINTER(CvtpmStats)]
     L.cvtpm_tool_fp32_peak.argtypes = [i, vp, ctypes.POINTER(ctypes.c_float)]
+    L.cvtpm_cost_eval_noalloc.argtypes = [P, vp, vp, i, i, sz, vp, vp, vp]
     for name in EXPORTS:
         if name not in ("cvtpm_version", "cvtpm_status_string", "cvtpm_last_error"):
             getattr(L, name).restype = ctypes.c_int

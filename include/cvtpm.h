@@ -187,6 +187,24 @@ cvtpm_status cvtpm_set_timing(cvtpm_ctx* ctx, int enable);
 cvtpm_status cvtpm_reset_stats(cvtpm_ctx* ctx);
 cvtpm_status cvtpm_get_stats(cvtpm_ctx* ctx, cvtpm_stats* out);
 
+/* cvtpm_cost_eval without any device allocation and without a context.  No
+ * counterpart in the reference: it serves callers that may not allocate
+ * device memory (hosts that own every allocation through their own pool or
+ * budget, real-time code that reserves memory up front) and can only pass
+ * their own input and output buffers.  Its intermediate images live in a
+ * fixed 16 MiB device array inside the library (present on every GPU that
+ * loads it, until exit): width*height is limited to about 135 000 pixels
+ * (e.g. 360 x 360); larger images return CVTPM_ERR_SIZE.  The first call on
+ * a device looks the array up (make it before any stream capture).  Calls
+ * share the array, so calls that overlap on the GPU race; serialise them.
+ * Same arguments and results as cvtpm_cost_eval, with the parameters passed
+ * explicitly. */
+cvtpm_status cvtpm_cost_eval_noalloc(const cvtpm_params* params,
+                                     const float* img1, const float* img2,
+                                     int width, int height, size_t pitch,
+                                     const float* states, float* cost,
+                                     void* stream);
+
 /* Many pairs of uneven size in one graph-captured launch sequence. */
 cvtpm_status cvtpm_depthmap_batched(cvtpm_ctx* ctx, const cvtpm_pair* pairs,
                                     int npairs, void* stream);
