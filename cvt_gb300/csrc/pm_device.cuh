@@ -228,19 +228,25 @@ template <int K, bool EXACT>
 PM_DEV void eval_costs(const PmCostConsts& k, const PmView& v1, const PmView& v2, int x, int y,
                        const float4 (&s)[K], const bool (&act)[K], float (&cost)[K]) {
     float sx[K], sy[K], sz[K];
+    long long S0[K], S1[K], XC[K];
     bool live[K];
 #pragma unroll
     for (int c = 0; c < K; ++c) {
         live[c] = act[c] && finite3(s[c]);
-        sx[c] = live[c] ? s[c].x : 0.0f;
-        sy[c] = live[c] ? s[c].y : 0.0f;
-        sz[c] = live[c] ? s[c].z : -1.0e30f;    /* never inside [0, W) */
+        if (EXACT) {
+            sx[c] = live[c] ? s[c].x : 0.0f;
+            sy[c] = live[c] ? s[c].y : 0.0f;
+            sz[c] = live[c] ? s[c].z : -1.0e30f;    /* never inside [0, W) */
+        } else {
+            pm_fix_plane(live[c], s[c].x, s[c].y, s[c].z, x, y, &S0[c], &S1[c], &XC[c]);
+        }
     }
     float ws[K], r1[K], r2[K];
 #pragma unroll
     for (int c = 0; c < K; ++c) { ws[c] = 0.0f; r1[c] = 0.0f; r2[c] = 0.0f; }
     const float4 vc = __ldg(&v1.col[(size_t)y * k.W + x]);
     const int P = k.P;
+    const int dxlo = max(-P, -x), dxhi = min(P, k.W - 1 - x);
     for (int dy = -P; dy <= P; ++dy) {
         const int qy = y + dy;
         if (qy < 0 || qy >= k.H) continue;
@@ -248,14 +254,13 @@ PM_DEV void eval_costs(const PmCostConsts& k, const PmView& v1, const PmView& v2
         const float4* c1row = v1.col + (size_t)qy * k.W;
         const float4* g1row = v1.grad + (size_t)qy * k.W;
         const float* prow = c_prof + (dy + PM_PMAX) * PM_PROF_N + PM_PMAX;
-        float rowb[K];
+        long long X[K];
         if (!EXACT) {
 #pragma unroll
-            for (int c = 0; c < K; ++c) rowb[c] = fmaf(sy[c], qyf, sz[c]);
+            for (int c = 0; c < K; ++c) X[c] = XC[c] + (long long)dy * S1[c] + (long long)dxlo * S0[c];
         }
-        for (int dx = -P; dx <= P; ++dx) {
+        for (int dx = dxlo; dx <= dxhi; ++dx) {
             const int qx = x + dx;
-            if (qx < 0 || qx >= k.W) continue;
             const float qxf = (float)qx;
             const float4 a1 = __ldg(&c1row[qx]);
             const float4 g1 = __ldg(&g1row[qx]);
@@ -285,11 +290,12 @@ PM_DEV void eval_costs(const PmCostConsts& k, const PmView& v1, const PmView& v2
                     const float C = k.alpha * cc + k.oma * gc;
                     r1[c] += w1 * C;
                 } else {
-                    const float xp = fmaf(sx[c], qxf, rowb[c]);
-                    if (!(xp >= 0.0f && xp < k.Wf)) continue;
-                    const float fi = floorf(xp);
-                    const float a = xp - fi;
-                    const size_t j = (size_t)qy * k.rp + (int)fi;
+                    const long long Xt = X[c];
+                    X[c] += S0[c];
+                    const int xi = (int)(Xt >> 32);
+                    if ((unsigned)xi >= (unsigned)k.W) continue;
+                    const float a = pm_fix_frac(Xt);
+                    const size_t j = (size_t)qy * k.rp + xi;
                     const float4 A = __ldg(&v2.recA[j]);
                     const float4 B = __ldg(&v2.recB[j]);
                     const float4 Cc = __ldg(&v2.recC[j]);

@@ -81,6 +81,64 @@ PM_HD float pm_div(float a, float b) {
 #endif
 }
 
+/* Round-to-nearest-even conversions and the double FMA, one definition per
+ * side; IEEE fixes each result, so CPU and GPU agree bit for bit. */
+PM_HD long long pm_f2ll_rn(float x) {
+#if defined(__CUDA_ARCH__)
+    return __float2ll_rn(x);
+#else
+    return llrintf(x);
+#endif
+}
+PM_HD long long pm_d2ll_rn(double x) {
+#if defined(__CUDA_ARCH__)
+    return __double2ll_rn(x);
+#else
+    return llrint(x);
+#endif
+}
+PM_HD float pm_u2f_rn(unsigned x) {
+#if defined(__CUDA_ARCH__)
+    return __uint2float_rn(x);
+#else
+    return (float)x;
+#endif
+}
+PM_HD double pm_fma_d(double a, double b, double c) {
+#if defined(__CUDA_ARCH__)
+    return __fma_rn(a, b, c);
+#else
+    return fma(a, b, c);
+#endif
+}
+
+/* Tap positions of the FAST arithmetic in fixed point.  The sample column
+ * x' = s0*qx + s1*qy + s2 of tap (qx, qy) = (x + dx, y + dy) is written as
+ * x'(x, y) + s0*dx + s1*dy and carried in Q31.32 (int64 with 32 fraction
+ * bits): the centre value is formed in double and rounded once, the slopes
+ * are rounded once, and every tap adds integers, so a tap position is within
+ * 18 * 2^-33 px of the exact value whatever the image width (an FP32
+ * evaluation is off by up to half an ulp of x', 6e-5 px at x' ~ 1000).  The
+ * integer part is the record index, the fraction the interpolation weight.
+ * Planes with |s0| or |s1| >= 2^24 (at most one tap per window row or column
+ * can fall inside any image) or |x'(x, y)| >= 2^30 (no tap inside) are not
+ * representable: they get XC = PM_FIX_NONE, which no tap reaches. */
+#define PM_FIX_NONE (-(1LL << 62))
+PM_HD bool pm_fix_plane(bool live, float s0, float s1, float s2, int x, int y,
+                        long long* S0, long long* S1, long long* XC) {
+    const float one = 4294967296.0f;                               /* 2^32 */
+    const bool ok0 = live && isfinite(s0) && isfinite(s1) && isfinite(s2) &&
+                     fabsf(s0) < 16777216.0f && fabsf(s1) < 16777216.0f;
+    const double xc = ok0 ? pm_fma_d((double)s0, (double)x, pm_fma_d((double)s1, (double)y, (double)s2)) : 0.0;
+    const bool ok = ok0 && fabs(xc) < 1073741824.0;               /* 2^30 */
+    *S0 = ok ? pm_f2ll_rn(s0 * one) : 0;
+    *S1 = ok ? pm_f2ll_rn(s1 * one) : 0;
+    *XC = ok ? pm_d2ll_rn(xc * 4294967296.0) : PM_FIX_NONE;
+    return ok;
+}
+/* The interpolation weight: the 32 fraction bits, rounded to float. */
+PM_HD float pm_fix_frac(long long X) { return pm_u2f_rn((unsigned)X) * 2.3283064365386963e-10f; }
+
 /* 2^n as a float for -126 <= n <= 127. */
 PM_HD float pm_pow2i(int n) { return pm_i2f((n + 127) << 23); }
 

@@ -69,6 +69,9 @@ def lib():
         L.orc_depthmap.argtypes = [P, f32p, f32p, c_int, c_int, f32p, ctypes.c_void_p, ctypes.c_void_p,
                                    ctypes.c_void_p, ctypes.c_void_p]
         L.orc_depthmap.restype = c_int
+        f64p = np.ctypeslib.ndpointer(np.float64, flags="C_CONTIGUOUS")
+        L.orc_cost_field_f64.argtypes = [P, f32p, f32p, c_int, c_int, f32p, ctypes.c_double, f64p, u8p]
+        L.orc_cost_field_f64.restype = c_int
         _lib = L
     return _lib
 
@@ -112,6 +115,18 @@ def cost_field(params: CvtpmParams, img1, img2, states):
     rc = lib().orc_cost_field(ctypes.byref(params), img1, img2, w, h, states, out)
     assert rc == 0, rc
     return out
+
+
+def cost_field_f64(params: CvtpmParams, img1, img2, states, eps: float = 1e-3):
+    """FP64 cost of a fixed state field and the mask of pixels with a tap
+    within eps of the sample-validity bounds."""
+    img1, img2, states = _f32(img1), _f32(img2), _f32(states)
+    h, w = img1.shape[:2]
+    out = np.empty((h, w), np.float64)
+    edge = np.empty((h, w), np.uint8)
+    rc = lib().orc_cost_field_f64(ctypes.byref(params), img1, img2, w, h, states, float(eps), out, edge)
+    assert rc == 0, rc
+    return out, edge.astype(bool)
 
 
 def init(params: CvtpmParams, img1, img2, lr: int):

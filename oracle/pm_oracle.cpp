@@ -320,13 +320,15 @@ static float cost_eval(const CostCfg& k, const View& v1, const View& v2, int cx,
         return ret / wsum;
     }
     /* ARITH_FAST: mirror of the CUDA fast kernels: taps in raster order,
-     * x' = fma(s0, qx, fma(s1, qy, s2)), (value, forward difference) records
-     * of the other view, colour and gradient sums kept apart. */
+     * tap positions in Q31.32 fixed point (pm_fix_plane), (value, forward
+     * difference) records of the other view, colour and gradient sums kept
+     * apart. */
     float wsum = 0.0f, rc = 0.0f, rg = 0.0f;
+    long long S0, S1, XC;
+    pm_fix_plane(true, s.x, s.y, s.z, cx, cy, &S0, &S1, &XC);
     for (int dy = -P; dy <= P; ++dy) {
         int qy = cy + dy;
         if (qy < 0 || qy >= H) continue;
-        float rowb = fmaf(s.y, (float)qy, s.z);
         const float* rrow = &v2.rec[(size_t)qy * W * 14];
         for (int dx = -P; dx <= P; ++dx) {
             int qx = cx + dx;
@@ -335,11 +337,11 @@ static float cost_eval(const CostCfg& k, const View& v1, const View& v2, int cx,
             const F4 g1 = v1.grad[(size_t)qy * W + qx];
             float d = (fabsf(vc.x - a1.x) + fabsf(vc.y - a1.y)) + fabsf(vc.z - a1.z);
             float w1 = pm_exp(-d * k.prof[(size_t)(dy + P) * n + (dx + P)]);
-            float xp = fmaf(s.x, (float)qx, rowb);
-            if (!(xp >= 0.0f && xp < Wf)) continue;
-            float fi = floorf(xp);
-            float a = xp - fi;
-            const float* r = rrow + (size_t)(int)fi * 14;
+            const long long X = XC + (long long)dy * S1 + (long long)dx * S0;
+            const int xi = (int)(X >> 32);
+            if ((unsigned)xi >= (unsigned)W) continue;
+            float a = pm_fix_frac(X);
+            const float* r = rrow + (size_t)xi * 14;
             float v[7];
             for (int c = 0; c < 7; ++c) v[c] = fmaf(a, r[7 + c], r[c]);
             float cc = (fminf(fabsf(a1.x - v[0]), k.cmax) + fminf(fabsf(a1.y - v[1]), k.cmax)) + fminf(fabsf(a1.z - v[2]), k.cmax);
@@ -684,6 +686,73 @@ static void make_views(const float* left, const float* right, int W, int H, int 
 
 }  // namespace
 
+/* ----------------------------------------------------------- FP64 -- */
+/* The aggregated cost of pmhstereo.cl:170-228 evaluated in double precision:
+ * gradients (:785-831), bilateral weights (exp), the spatial profile
+ * (smoothstep), the sample position x' = s0*qx + s1*qy + s2 and the linear
+ * interpolation along the row all in double.  `edge` flags pixels with a tap
+ * whose x' lies within `eps` of the validity bounds 0 and W (where an FP32
+ * evaluation may count the tap differently). */
+struct D4 { double x, y, z, w; };
+static void gradxy_f64(const F4* img, int W, int H, std::vector<D4>& out) {
+    auto g = [&](int x, int y) -> double {
+        if (x < 0 || y < 0 || x >= W || y >= H) return 0.0;
+        F4 c = img[(size_t)y * W + x];
+        return (double)c.x * 0.2126 + (double)c.y * 0.7152 + (double)c.z * 0.0722;
+    };
+    out.resize((size_t)W * H);
+    for (int y = 0; y < H; ++y)
+        for (int x = 0; x < W; ++x) {
+            D4 d;
+            d.x = (g(x + 1, y) - g(x - 1, y)) * 0.5 + (g(x + 1, y - 1) - g(x - 1, y - 1)) * 0.25 + (g(x + 1, y + 1) - g(x - 1, y + 1)) * 0.25;
+            d.y = (g(x, y + 1) - g(x, y - 1)) * 0.5 + (g(x - 1, y + 1) - g(x - 1, y - 1)) * 0.25 + (g(x + 1, y + 1) - g(x + 1, y - 1)) * 0.25;
+            d.z = g(x + 1, y + 1) - g(x - 1, y - 1);
+            d.w = g(x - 1, y + 1) - g(x + 1, y - 1);
+            out[(size_t)y * W + x] = d;
+        }
+}
+static double profile_f64(int dx, int dy, double cw, int profile) {
+    if (profile == CVTPM_PROFILE_CONSTANT) return cw;
+    double len = std::sqrt((double)dx * dx + (double)dy * dy);
+    double t = std::min(std::max(len / 26.0, 0.0), 1.0);
+    return t * t * (3.0 - 2.0 * t) * 1.5 * cw + 5.0;
+}
+static double cost_f64(const cvtpm_params* prm, const F4* c1, const std::vector<D4>& g1, const F4* c2,
+                       const std::vector<D4>& g2, int W, int H, int cx, int cy, const float* st, double eps, bool* edge) {
+    *edge = false;
+    const double s0 = st[0], s1 = st[1], s2 = st[2];
+    if (!std::isfinite(s0) || !std::isfinite(s1) || !std::isfinite(s2)) return 1e5;
+    const int P = prm->patchsize;
+    const double alpha = prm->color_alpha, cmax = prm->color_maxdiff, gmax = prm->grad_maxdiff;
+    const F4 vc = c1[(size_t)cy * W + cx];
+    double ws = 0.0, ret = 0.0;
+    for (int dy = -P; dy <= P; ++dy)
+        for (int dx = -P; dx <= P; ++dx) {
+            const int qx = cx + dx, qy = cy + dy;
+            if (qx < 0 || qy < 0 || qx >= W || qy >= H) continue;
+            const F4 a1 = c1[(size_t)qy * W + qx];
+            const D4 b1 = g1[(size_t)qy * W + qx];
+            const double d = std::fabs((double)vc.x - a1.x) + std::fabs((double)vc.y - a1.y) + std::fabs((double)vc.z - a1.z);
+            const double w = std::exp(-d * profile_f64(dx, dy, prm->color_weight, prm->weight_profile));
+            const double xp = s0 * qx + s1 * qy + s2;
+            if (std::fabs(xp) < eps || std::fabs(xp - W) < eps) *edge = true;
+            if (!(xp >= 0.0 && xp < (double)W)) continue;
+            ws += w;
+            const double fi = std::floor(xp), a = xp - fi;
+            const int i0 = clampi((int)fi, 0, W - 1), i1 = clampi((int)fi + 1, 0, W - 1);
+            const F4 p0 = c2[(size_t)qy * W + i0], p1 = c2[(size_t)qy * W + i1];
+            const D4 h0 = g2[(size_t)qy * W + i0], h1 = g2[(size_t)qy * W + i1];
+            const double v[3] = {(1 - a) * p0.x + a * p1.x, (1 - a) * p0.y + a * p1.y, (1 - a) * p0.z + a * p1.z};
+            const double u[4] = {(1 - a) * h0.x + a * h1.x, (1 - a) * h0.y + a * h1.y, (1 - a) * h0.z + a * h1.z, (1 - a) * h0.w + a * h1.w};
+            const double cc = std::min(std::fabs(a1.x - v[0]), cmax) + std::min(std::fabs(a1.y - v[1]), cmax) + std::min(std::fabs(a1.z - v[2]), cmax);
+            const double gc = std::min(std::fabs(b1.x - u[0]), gmax) + std::min(std::fabs(b1.y - u[1]), gmax) + std::min(std::fabs(b1.z - u[2]), gmax) + std::min(std::fabs(b1.w - u[3]), gmax);
+            ret += w * (alpha * cc + (1.0 - alpha) * gc);
+        }
+    if (std::fabs(ws - 1.1) < 1e-6) *edge = true;
+    if (ws <= 1.1) return 1e5;
+    return ret / ws;
+}
+
 /* ===================================================== extern "C" API == */
 extern "C" {
 
@@ -844,6 +913,25 @@ int orc_depthmap(const cvtpm_params* prm, const float* left, const float* right,
         memcpy(states_out + 4 * n, SR[fin].data(), n * sizeof(F4));
     }
     if (winners) { memcpy(winners, winL.data(), n); memcpy(winners + n, winR.data(), n); }
+    return CVTPM_OK;
+}
+
+/* FP64 cost of a fixed state field; edge[p] = 1 where a tap sits within eps
+ * of the validity bounds. */
+int orc_cost_field_f64(const cvtpm_params* prm, const float* img1, const float* img2, int W, int H,
+                       const float* states, double eps, double* cost, uint8_t* edge) {
+    if (!check_params(prm)) return CVTPM_ERR_INVALID_ARGUMENT;
+    std::vector<D4> g1, g2;
+    gradxy_f64((const F4*)img1, W, H, g1);
+    gradxy_f64((const F4*)img2, W, H, g2);
+#pragma omp parallel for schedule(dynamic, 1)
+    for (int y = 0; y < H; ++y)
+        for (int x = 0; x < W; ++x) {
+            bool e = false;
+            cost[(size_t)y * W + x] = cost_f64(prm, (const F4*)img1, g1, (const F4*)img2, g2, W, H, x, y,
+                                               states + ((size_t)y * W + x) * 4, eps, &e);
+            if (edge) edge[(size_t)y * W + x] = e ? 1 : 0;
+        }
     return CVTPM_OK;
 }
 
