@@ -206,11 +206,11 @@ PmPassArgs base_args(cvtpm_ctx* ctx, const cvtpm_params& p, int W, int H, int v1
 }
 
 cvtpm_status prep_views(cvtpm_ctx* ctx, const cvtpm_params& p, const float* img0, const float* img1, int W, int H,
-                        size_t pitch, cudaStream_t st) {
+                        size_t pitch, cudaStream_t st, bool records = false) {
     const float* im[2] = {img0, img1};
     for (int v = 0; v < 2; ++v) {
         LK(pm_launch_prep((const float4*)im[v], pitch / 16, W, H, ctx->col[v], ctx->grad[v], ctx->wgt[v], st), "prep");
-        if (p.arith == CVTPM_ARITH_FAST)
+        if (p.arith == CVTPM_ARITH_FAST || records)
             LK(pm_launch_records(ctx->col[v], ctx->grad[v], W, H, rec_pitch(W), ctx->recA[v], ctx->recB[v], ctx->recC[v], ctx->recD[v], st), "records");
     }
     return CVTPM_OK;
@@ -569,9 +569,38 @@ cvtpm_status cvtpm_get_stats(cvtpm_ctx* ctx, cvtpm_stats* out) {
     return CVTPM_OK;
 }
 
-cvtpm_status cvtpm_cost_adjoint(cvtpm_ctx* ctx, const float*, const float*, int, int, size_t, const float*, int,
-                                const float*, float*, float*, float*, float*, void*) {
-    return fail(ctx, CVTPM_ERR_NOT_SUPPORTED, "cost adjoint not built yet");
+cvtpm_status cvtpm_cost_adjoint(cvtpm_ctx* ctx, const float* img1, const float* img2, int width, int height,
+                                size_t pitch, const float* planes, int lr, const float* dcost, float* cost,
+                                float* dplanes, float* dimg1, float* dimg2, void* stream) {
+    if (!ctx) return CVTPM_ERR_INVALID_ARGUMENT;
+    cvtpm_status s;
+    const cvtpm_params& p = ctx->prm;
+    if ((s = check_params(ctx, p)) != CVTPM_OK) return s;
+    if ((s = check_image(ctx, img1, width, height, pitch, "img1")) != CVTPM_OK) return s;
+    if ((s = check_image(ctx, img2, width, height, pitch, "img2")) != CVTPM_OK) return s;
+    if (!planes) return fail(ctx, CVTPM_ERR_INVALID_ARGUMENT, "null planes");
+    if (((uintptr_t)planes & 15) || ((uintptr_t)dplanes & 15))
+        return fail(ctx, CVTPM_ERR_INVALID_ARGUMENT, "planes/dplanes must be 16-byte aligned");
+    if (!dcost && (dplanes || dimg1 || dimg2))
+        return fail(ctx, CVTPM_ERR_INVALID_ARGUMENT, "gradients requested without dcost");
+    cudaStream_t st = (cudaStream_t)stream;
+    CK(cudaSetDevice(ctx->device), "cudaSetDevice");
+    if ((s = ensure_buffers(ctx, width, height)) != CVTPM_OK) return s;
+    if ((s = ensure_tables(ctx, p, st)) != CVTPM_OK) return s;
+    if ((s = prep_views(ctx, p, img1, img2, width, height, pitch, st, true)) != CVTPM_OK) return s;
+    const PmPassArgs a = base_args(ctx, p, width, height, 0);
+    /* the four image-adjoint accumulators reuse the propagation state buffers */
+    const bool img = dimg1 || dimg2;
+    const size_t n = (size_t)width * height;
+    float4 *dI1 = ctx->S[0][0], *dG1 = ctx->S[0][1], *dI2 = ctx->S[1][0], *dG2 = ctx->S[1][1];
+    if (img) {
+        for (float4* b : {dI1, dG1, dI2, dG2}) CK(cudaMemsetAsync(b, 0, n * 16, st), "adjoint clear");
+    }
+    LK(pm_launch_cost_adjoint(a.k, a.v1, a.v2, (const float4*)planes, lr, dcost, cost, (float4*)dplanes,
+                              img ? dI1 : nullptr, dG1, dI2, dG2, st), "cost adjoint");
+    if (dimg1) LK(pm_launch_adjoint_finish(dI1, dG1, width, height, dimg1, st), "adjoint image 1");
+    if (dimg2) LK(pm_launch_adjoint_finish(dI2, dG2, width, height, dimg2, st), "adjoint image 2");
+    return CVTPM_OK;
 }
 
 cvtpm_status cvtpm_depthmap_batched(cvtpm_ctx* ctx, const cvtpm_pair*, int, void*) {

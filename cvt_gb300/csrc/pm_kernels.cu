@@ -557,8 +557,9 @@ cudaError_t pm_upload_tables(const unsigned long long* pow2, const float* prof, 
     cudaError_t e = cudaMemcpyToSymbolAsync(c_mwc_pow2, pow2, sizeof(unsigned long long) * 64, 0,
                                             cudaMemcpyHostToDevice, st);
     if (e != cudaSuccess) return e;
-    return cudaMemcpyToSymbolAsync(c_prof, prof, sizeof(float) * PM_PROF_N * PM_PROF_N, 0,
-                                   cudaMemcpyHostToDevice, st);
+    e = cudaMemcpyToSymbolAsync(c_prof, prof, sizeof(float) * PM_PROF_N * PM_PROF_N, 0, cudaMemcpyHostToDevice, st);
+    if (e != cudaSuccess) return e;
+    return pm_adjoint_upload_profile(prof, st);      /* the adjoint unit keeps its own copy */
 }
 
 cudaError_t pm_launch_prep(const float4* img, size_t pitch4, int W, int H, float4* col, float4* grad,

@@ -52,4 +52,11 @@ cudaError_t pm_launch_pd_block(float4* uout, float4* pout, const float4* uin, co
                                cudaStream_t st);
 cudaError_t pm_launch_ffma_peak(float* out, int blocks, int iters, cudaStream_t st);
 
+/* pm_adjoint.cu */
+cudaError_t pm_adjoint_upload_profile(const float* prof, cudaStream_t st);
+cudaError_t pm_launch_cost_adjoint(const PmCostConsts& k, const PmView& v1, const PmView& v2, const float4* planes,
+                                   int lr, const float* dcost, float* cost, float4* dplanes, float4* dI1, float4* dG1,
+                                   float4* dI2, float4* dG2, cudaStream_t st);
+cudaError_t pm_launch_adjoint_finish(const float4* dI, const float4* dG, int W, int H, float* out, cudaStream_t st);
+
 #endif

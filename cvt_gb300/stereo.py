@@ -163,3 +163,34 @@ class PMHuberStereo:
                                         states.data_ptr(), int(lr), out.data_ptr(), _stream_ptr(img1))
         self._check(rc)
         return out
+
+    def cost_adjoint(self, img1: torch.Tensor, img2: torch.Tensor, planes: torch.Tensor, lr: int = 1,
+                     dcost: torch.Tensor | None = None, want_planes: bool = True, want_images: bool = True):
+        """cvtpm_cost_adjoint.  planes (H, W, 4) = (a, b, c, -) with
+        d = a*x + b*y + c (x_other = x - d for lr = 1, x + d for lr = 0).
+        Returns (cost, dplanes, dimg1, dimg2); the gradients are None when
+        dcost is None or not wanted."""
+        _check_img(img1, "img1")
+        _check_img(img2, "img2")
+        if img1.shape != img2.shape or planes.shape != img1.shape:
+            raise CVTException("img1/img2/planes shapes differ")
+        planes = planes.contiguous()
+        H, W = img1.shape[:2]
+        dev = img1.device
+        cost = torch.empty((H, W), dtype=torch.float32, device=dev)
+        dpl = d1 = d2 = None
+        if dcost is not None:
+            dcost = dcost.to(torch.float32).contiguous()
+            if dcost.shape != (H, W):
+                raise CVTException("dcost must be (H, W)")
+            if want_planes:
+                dpl = torch.empty((H, W, 4), dtype=torch.float32, device=dev)
+            if want_images:
+                d1 = torch.empty((H, W, 4), dtype=torch.float32, device=dev)
+                d2 = torch.empty((H, W, 4), dtype=torch.float32, device=dev)
+        ptr = lambda t: None if t is None else t.data_ptr()
+        rc = _lib.lib().cvtpm_cost_adjoint(self._h, img1.data_ptr(), img2.data_ptr(), W, H, img1.stride(0) * 4,
+                                           planes.data_ptr(), int(lr), ptr(dcost), cost.data_ptr(), ptr(dpl),
+                                           ptr(d1), ptr(d2), _stream_ptr(img1))
+        self._check(rc)
+        return cost, dpl, d1, d2

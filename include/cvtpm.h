@@ -168,11 +168,18 @@ cvtpm_status cvtpm_cost_eval(cvtpm_ctx* ctx,
                              const float* states, int lr, float* cost,
                              void* stream);
 
-/* Adjoint of cvtpm_cost_eval with respect to the planes and both images.
- * planes are per-pixel (a, b, c, unused) in the disparity convention
- * d = a*x + b*y + c of view 1 (x_other = x - d for lr = 1, x + d for lr = 0).
- * dcost is W*H; dplanes W*H*4 (a, b, c, 0); dimg1/dimg2 W*H*4 RGBA (alpha 0).
- * Any output may be NULL.  Window weights are recomputed, not stored. */
+/* Adjoint of the aggregated cost (pmhstereo.cl:170-228) with respect to the
+ * planes and both images; no counterpart in the reference, which never
+ * differentiates its cost.  planes are per-pixel (a, b, c, unused), 16-byte
+ * aligned, in the disparity convention d = a*x + b*y + c of view 1
+ * (x_other = x - d for lr = 1, x + d for lr = 0).  cost (W*H, may be NULL)
+ * receives the cost, evaluated in the FAST arithmetic (fixed-point tap
+ * positions) whatever params.arith says.  With dcost (W*H, dL/dcost) given,
+ * dplanes (W*H*4: dL/da, dL/db, dL/dc, 0), dimg1 and dimg2 (W*H*4 RGBA,
+ * alpha 0) receive the gradients; each may be NULL.  Without dcost no
+ * gradient may be requested.  Window weights are recomputed, not stored.
+ * The image gradients are summed with float atomics, so their last bits vary
+ * from run to run. */
 cvtpm_status cvtpm_cost_adjoint(cvtpm_ctx* ctx,
                                 const float* img1, const float* img2,
                                 int width, int height, size_t pitch,

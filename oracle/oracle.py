@@ -72,6 +72,12 @@ def lib():
         f64p = np.ctypeslib.ndpointer(np.float64, flags="C_CONTIGUOUS")
         L.orc_cost_field_f64.argtypes = [P, f32p, f32p, c_int, c_int, f32p, ctypes.c_double, f64p, u8p]
         L.orc_cost_field_f64.restype = c_int
+        u64p = np.ctypeslib.ndpointer(np.uint64, flags="C_CONTIGUOUS")
+        L.orc_cost_planes_f64.argtypes = [P, f64p, f64p, c_int, c_int, f64p, c_int, ctypes.c_double, f64p, u8p, u64p]
+        L.orc_cost_planes_f64.restype = c_int
+        L.orc_cost_adjoint_f64.argtypes = [P, f64p, f64p, c_int, c_int, f64p, c_int, f64p, f64p, f64p, f64p, f64p,
+                                           ctypes.c_double, u8p, u8p, u8p]
+        L.orc_cost_adjoint_f64.restype = c_int
         _lib = L
     return _lib
 
@@ -127,6 +133,42 @@ def cost_field_f64(params: CvtpmParams, img1, img2, states, eps: float = 1e-3):
     rc = lib().orc_cost_field_f64(ctypes.byref(params), img1, img2, w, h, states, float(eps), out, edge)
     assert rc == 0, rc
     return out, edge.astype(bool)
+
+
+def _f64(a):
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
+def cost_planes_f64(params: CvtpmParams, img1, img2, planes, lr: int = 1, eps: float = 1e-3):
+    """FP64 cost of per-pixel planes (a, b, c, _) of view lr on double images;
+    returns (cost, edge mask, branch signature per pixel)."""
+    img1, img2, planes = _f64(img1), _f64(img2), _f64(planes)
+    h, w = img1.shape[:2]
+    out = np.empty((h, w), np.float64)
+    edge = np.empty((h, w), np.uint8)
+    sig = np.empty((h, w), np.uint64)
+    rc = lib().orc_cost_planes_f64(ctypes.byref(params), img1, img2, w, h, planes, int(lr), float(eps), out, edge, sig)
+    assert rc == 0, rc
+    return out, edge.astype(bool), sig
+
+
+def cost_adjoint_f64(params: CvtpmParams, img1, img2, planes, dcost, lr: int = 1, kink_eps: float = 0.0):
+    """FP64 adjoint: returns (cost, dplanes (H,W,4), dimg1 (H,W,4), dimg2 (H,W,4));
+    with kink_eps > 0 also the (H,W) masks of plane / image-1 / image-2
+    entries reached by a tap within kink_eps of a kink."""
+    img1, img2, planes, dcost = _f64(img1), _f64(img2), _f64(planes), _f64(dcost)
+    h, w = img1.shape[:2]
+    cost = np.empty((h, w), np.float64)
+    dpl = np.empty((h, w, 4), np.float64)
+    d1 = np.empty((h, w, 4), np.float64)
+    d2 = np.empty((h, w, 4), np.float64)
+    am = [np.zeros((h, w), np.uint8) for _ in range(3)]
+    rc = lib().orc_cost_adjoint_f64(ctypes.byref(params), img1, img2, w, h, planes, int(lr), dcost, cost, dpl, d1, d2,
+                                    float(kink_eps), *am)
+    assert rc == 0, rc
+    if kink_eps > 0:
+        return cost, dpl, d1, d2, tuple(m.astype(bool) for m in am)
+    return cost, dpl, d1, d2
 
 
 def init(params: CvtpmParams, img1, img2, lr: int):

@@ -687,28 +687,58 @@ static void make_views(const float* left, const float* right, int W, int H, int 
 }  // namespace
 
 /* ----------------------------------------------------------- FP64 -- */
-/* The aggregated cost of pmhstereo.cl:170-228 evaluated in double precision:
- * gradients (:785-831), bilateral weights (exp), the spatial profile
- * (smoothstep), the sample position x' = s0*qx + s1*qy + s2 and the linear
- * interpolation along the row all in double.  `edge` flags pixels with a tap
- * whose x' lies within `eps` of the validity bounds 0 and W (where an FP32
- * evaluation may count the tap differently). */
+/* The aggregated cost of pmhstereo.cl:170-228 and its adjoint, in double
+ * precision on double images: gradients (:785-831), bilateral weights (exp),
+ * the spatial profile (smoothstep), the sample position x' = s0*qx + s1*qy +
+ * s2 and the linear interpolation along the row.  `edge` flags pixels with a
+ * tap whose x' lies within `eps` of the validity bounds 0 and W, or whose
+ * weight sum lies within 1e-6 of the 1.1 threshold (there the cost jumps). */
 struct D4 { double x, y, z, w; };
-static void gradxy_f64(const F4* img, int W, int H, std::vector<D4>& out) {
-    auto g = [&](int x, int y) -> double {
+struct ImgD {
+    int W, H;
+    const double* c;            /* RGBA, W*H*4 */
+    std::vector<D4> g;          /* gradients */
+    D4 col(int x, int y) const { const double* q = c + ((size_t)y * W + x) * 4; return {q[0], q[1], q[2], q[3]}; }
+};
+/* The gradient stencil of pmhstereo_gradxy as (dx, dy, component, weight)
+ * terms on the grey image B (zero outside): G.comp(x, y) += weight * B(x+dx, y+dy). */
+struct GradTerm { int dx, dy, comp; double w; };
+static const GradTerm kGradTerms[] = {
+    {1, 0, 0, 0.5}, {-1, 0, 0, -0.5}, {1, -1, 0, 0.25}, {-1, -1, 0, -0.25}, {1, 1, 0, 0.25}, {-1, 1, 0, -0.25},
+    {0, 1, 1, 0.5}, {0, -1, 1, -0.5}, {-1, 1, 1, 0.25}, {-1, -1, 1, -0.25}, {1, 1, 1, 0.25}, {1, -1, 1, -0.25},
+    {1, 1, 2, 1.0}, {-1, -1, 2, -1.0},
+    {-1, 1, 3, 1.0}, {1, -1, 3, -1.0},
+};
+static const double kGrey[3] = {0.2126, 0.7152, 0.0722};
+static void grad_f64(ImgD& im) {
+    const int W = im.W, H = im.H;
+    im.g.assign((size_t)W * H, D4{0, 0, 0, 0});
+    auto B = [&](int x, int y) -> double {
         if (x < 0 || y < 0 || x >= W || y >= H) return 0.0;
-        F4 c = img[(size_t)y * W + x];
-        return (double)c.x * 0.2126 + (double)c.y * 0.7152 + (double)c.z * 0.0722;
+        const double* q = im.c + ((size_t)y * W + x) * 4;
+        return q[0] * kGrey[0] + q[1] * kGrey[1] + q[2] * kGrey[2];
     };
-    out.resize((size_t)W * H);
     for (int y = 0; y < H; ++y)
         for (int x = 0; x < W; ++x) {
-            D4 d;
-            d.x = (g(x + 1, y) - g(x - 1, y)) * 0.5 + (g(x + 1, y - 1) - g(x - 1, y - 1)) * 0.25 + (g(x + 1, y + 1) - g(x - 1, y + 1)) * 0.25;
-            d.y = (g(x, y + 1) - g(x, y - 1)) * 0.5 + (g(x - 1, y + 1) - g(x - 1, y - 1)) * 0.25 + (g(x + 1, y + 1) - g(x + 1, y - 1)) * 0.25;
-            d.z = g(x + 1, y + 1) - g(x - 1, y - 1);
-            d.w = g(x - 1, y + 1) - g(x + 1, y - 1);
-            out[(size_t)y * W + x] = d;
+            double v[4] = {0, 0, 0, 0};
+            for (const GradTerm& t : kGradTerms) v[t.comp] += t.w * B(x + t.dx, y + t.dy);
+            im.g[(size_t)y * W + x] = D4{v[0], v[1], v[2], v[3]};
+        }
+}
+/* Adjoint of grad_f64: dimg += d(grey)/d(RGB) * sum of the transposed stencil of dg. */
+static void grad_f64_adjoint(const std::vector<D4>& dg, int W, int H, double* dimg) {
+    for (int v = 0; v < H; ++v)
+        for (int u = 0; u < W; ++u) {
+            double dB = 0.0;
+            for (const GradTerm& t : kGradTerms) {
+                const int x = u - t.dx, y = v - t.dy;
+                if (x < 0 || y < 0 || x >= W || y >= H) continue;
+                const D4& q = dg[(size_t)y * W + x];
+                const double comp = t.comp == 0 ? q.x : t.comp == 1 ? q.y : t.comp == 2 ? q.z : q.w;
+                dB += t.w * comp;
+            }
+            double* o = dimg + ((size_t)v * W + u) * 4;
+            for (int ch = 0; ch < 3; ++ch) o[ch] += kGrey[ch] * dB;
         }
 }
 static double profile_f64(int dx, int dy, double cw, int profile) {
@@ -717,40 +747,205 @@ static double profile_f64(int dx, int dy, double cw, int profile) {
     double t = std::min(std::max(len / 26.0, 0.0), 1.0);
     return t * t * (3.0 - 2.0 * t) * 1.5 * cw + 5.0;
 }
-static double cost_f64(const cvtpm_params* prm, const F4* c1, const std::vector<D4>& g1, const F4* c2,
-                       const std::vector<D4>& g2, int W, int H, int cx, int cy, const float* st, double eps, bool* edge) {
+static inline double sgn(double v) { return (v > 0) - (v < 0); }
+
+/* One tap of the window of (cx, cy): everything the cost and its adjoint need. */
+struct TapF64 {
+    bool valid;
+    double w, prof, c, a, xp;
+    int i0, i1, qx, qy;
+    double e[3], eg[4];          /* image-1 minus interpolated image-2 (colour, gradient) */
+    double D[3], Dg[4];          /* d(interpolated)/dx' */
+    double dsign[3];             /* sign(I1(c) - I1(q)) per channel */
+};
+static void tap_f64(const cvtpm_params* prm, const ImgD& i1, const ImgD& i2, int cx, int cy, int dx, int dy,
+                    const double s[3], TapF64& t) {
+    const int W = i1.W;
+    t.qx = cx + dx; t.qy = cy + dy;
+    const D4 vc = i1.col(cx, cy), a1 = i1.col(t.qx, t.qy);
+    const D4& b1 = i1.g[(size_t)t.qy * W + t.qx];
+    const double dc[3] = {vc.x - a1.x, vc.y - a1.y, vc.z - a1.z};
+    double d = 0.0;
+    for (int ch = 0; ch < 3; ++ch) { d += std::fabs(dc[ch]); t.dsign[ch] = sgn(dc[ch]); }
+    t.prof = profile_f64(dx, dy, prm->color_weight, prm->weight_profile);
+    t.w = std::exp(-d * t.prof);
+    t.xp = s[0] * t.qx + s[1] * t.qy + s[2];
+    t.valid = t.xp >= 0.0 && t.xp < (double)W;
+    if (!t.valid) return;
+    const double fi = std::floor(t.xp);
+    t.a = t.xp - fi;
+    t.i0 = clampi((int)fi, 0, W - 1);
+    t.i1 = clampi((int)fi + 1, 0, W - 1);
+    const D4 p0 = i2.col(t.i0, t.qy), p1 = i2.col(t.i1, t.qy);
+    const D4& h0 = i2.g[(size_t)t.qy * W + t.i0];
+    const D4& h1 = i2.g[(size_t)t.qy * W + t.i1];
+    const double T0[7] = {p0.x, p0.y, p0.z, h0.x, h0.y, h0.z, h0.w};
+    const double T1[7] = {p1.x, p1.y, p1.z, h1.x, h1.y, h1.z, h1.w};
+    const double A[7] = {a1.x, a1.y, a1.z, b1.x, b1.y, b1.z, b1.w};
+    double cc = 0.0, gc = 0.0;
+    for (int k = 0; k < 7; ++k) {
+        const double v = (1.0 - t.a) * T0[k] + t.a * T1[k];
+        const double e = A[k] - v;
+        if (k < 3) { t.e[k] = e; t.D[k] = T1[k] - T0[k]; cc += std::min(std::fabs(e), (double)prm->color_maxdiff); }
+        else { t.eg[k - 3] = e; t.Dg[k - 3] = T1[k] - T0[k]; gc += std::min(std::fabs(e), (double)prm->grad_maxdiff); }
+    }
+    t.c = prm->color_alpha * cc + (1.0 - prm->color_alpha) * gc;
+}
+
+/* States (s0, s1, s2) of plane (a, b, c) of view lr: x' = x - d (lr = 1) or
+ * x + d (lr = 0), d = a*x + b*y + c; ds/d(a, b, c) = -1 (lr = 1) or +1. */
+static inline void plane_state(const double* pl, int lr, double s[3]) {
+    if (lr) { s[0] = 1.0 - pl[0]; s[1] = -pl[1]; s[2] = -pl[2]; }
+    else { s[0] = 1.0 + pl[0]; s[1] = pl[1]; s[2] = pl[2]; }
+}
+
+/* Branch signature of one tap: validity, interpolation cell, and the sign
+ * and truncation of every |.| term.  Two evaluations with equal signatures
+ * over all taps lie on one smooth piece of the cost. */
+static inline uint64_t sig_mix(uint64_t h, uint64_t v) { return (h ^ v) * 0x100000001B3ull; }
+static uint64_t tap_signature(const cvtpm_params* prm, const TapF64& t, uint64_t h) {
+    h = sig_mix(h, t.valid ? 1 : 2);
+    for (int ch = 0; ch < 3; ++ch) h = sig_mix(h, (uint64_t)(sgn(t.dsign[ch]) + 1));
+    if (!t.valid) return h;
+    h = sig_mix(h, (uint64_t)(int64_t)t.i0 + 7);
+    for (int ch = 0; ch < 3; ++ch)
+        h = sig_mix(h, (uint64_t)(sgn(t.e[ch]) + 1) * 2 + (std::fabs(t.e[ch]) < prm->color_maxdiff));
+    for (int k = 0; k < 4; ++k)
+        h = sig_mix(h, (uint64_t)(sgn(t.eg[k]) + 1) * 2 + (std::fabs(t.eg[k]) < prm->grad_maxdiff));
+    return h;
+}
+
+static double cost_f64(const cvtpm_params* prm, const ImgD& i1, const ImgD& i2, int cx, int cy,
+                       const double s[3], double eps, bool* edge, double* wsum, uint64_t* sig = nullptr) {
     *edge = false;
-    const double s0 = st[0], s1 = st[1], s2 = st[2];
-    if (!std::isfinite(s0) || !std::isfinite(s1) || !std::isfinite(s2)) return 1e5;
-    const int P = prm->patchsize;
-    const double alpha = prm->color_alpha, cmax = prm->color_maxdiff, gmax = prm->grad_maxdiff;
-    const F4 vc = c1[(size_t)cy * W + cx];
+    uint64_t h = 0xCBF29CE484222325ull;
+    if (!std::isfinite(s[0]) || !std::isfinite(s[1]) || !std::isfinite(s[2])) {
+        *wsum = 0;
+        if (sig) *sig = h;
+        return 1e5;
+    }
+    const int P = prm->patchsize, W = i1.W, H = i1.H;
     double ws = 0.0, ret = 0.0;
+    TapF64 t;
     for (int dy = -P; dy <= P; ++dy)
         for (int dx = -P; dx <= P; ++dx) {
-            const int qx = cx + dx, qy = cy + dy;
-            if (qx < 0 || qy < 0 || qx >= W || qy >= H) continue;
-            const F4 a1 = c1[(size_t)qy * W + qx];
-            const D4 b1 = g1[(size_t)qy * W + qx];
-            const double d = std::fabs((double)vc.x - a1.x) + std::fabs((double)vc.y - a1.y) + std::fabs((double)vc.z - a1.z);
-            const double w = std::exp(-d * profile_f64(dx, dy, prm->color_weight, prm->weight_profile));
-            const double xp = s0 * qx + s1 * qy + s2;
-            if (std::fabs(xp) < eps || std::fabs(xp - W) < eps) *edge = true;
-            if (!(xp >= 0.0 && xp < (double)W)) continue;
-            ws += w;
-            const double fi = std::floor(xp), a = xp - fi;
-            const int i0 = clampi((int)fi, 0, W - 1), i1 = clampi((int)fi + 1, 0, W - 1);
-            const F4 p0 = c2[(size_t)qy * W + i0], p1 = c2[(size_t)qy * W + i1];
-            const D4 h0 = g2[(size_t)qy * W + i0], h1 = g2[(size_t)qy * W + i1];
-            const double v[3] = {(1 - a) * p0.x + a * p1.x, (1 - a) * p0.y + a * p1.y, (1 - a) * p0.z + a * p1.z};
-            const double u[4] = {(1 - a) * h0.x + a * h1.x, (1 - a) * h0.y + a * h1.y, (1 - a) * h0.z + a * h1.z, (1 - a) * h0.w + a * h1.w};
-            const double cc = std::min(std::fabs(a1.x - v[0]), cmax) + std::min(std::fabs(a1.y - v[1]), cmax) + std::min(std::fabs(a1.z - v[2]), cmax);
-            const double gc = std::min(std::fabs(b1.x - u[0]), gmax) + std::min(std::fabs(b1.y - u[1]), gmax) + std::min(std::fabs(b1.z - u[2]), gmax) + std::min(std::fabs(b1.w - u[3]), gmax);
-            ret += w * (alpha * cc + (1.0 - alpha) * gc);
+            if (cx + dx < 0 || cy + dy < 0 || cx + dx >= W || cy + dy >= H) continue;
+            tap_f64(prm, i1, i2, cx, cy, dx, dy, s, t);
+            if (sig) h = tap_signature(prm, t, h);
+            if (std::fabs(t.xp) < eps || std::fabs(t.xp - W) < eps) *edge = true;
+            if (!t.valid) continue;
+            ws += t.w;
+            ret += t.w * t.c;
         }
+    *wsum = ws;
+    if (sig) *sig = sig_mix(h, ws > 1.1 ? 3 : 4);
     if (std::fabs(ws - 1.1) < 1e-6) *edge = true;
     if (ws <= 1.1) return 1e5;
     return ret / ws;
+}
+
+/* Cost and adjoint of one pixel.  L = sum_p dcost_p * C_p; C = R / S with
+ * S = sum w_t, R = sum w_t c_t over valid taps:
+ *   dL/dc_t = g w_t / S,  dL/dw_t = g (c_t - C) / S,  dw_t/dd_t = -prof_t w_t,
+ *   dc_t/dx' = -(alpha sum_ch s_ch D_ch + (1 - alpha) sum_k s_k Dg_k),
+ * s = sign(e) where |e| is below its truncation (0 above), D = T1 - T0.
+ * Validity changes and the 1.1 threshold are measure-zero and not
+ * differentiated; a pixel with cost 1e5 has zero gradient. */
+/* Entries an evaluation in another precision may differentiate on the other
+ * side of a kink: taps within `keps` of a kink mark what their slope reaches
+ * (the pixel's plane; the image-1 pixel q and the image-2 columns i0, i1,
+ * with the 3x3 stencil of the gradient images where a gradient term is
+ * involved); a tap near the validity bounds or a weight sum near 1.1 marks
+ * everything the pixel's window reaches. */
+struct Ambiguity {
+    double keps;
+    int W, H;
+    uint8_t *pl, *im1, *im2;
+    void mark(uint8_t* m, int x, int y, int r) const {
+        if (!m) return;
+        for (int yy = y - r; yy <= y + r; ++yy)
+            for (int xx = x - r; xx <= x + r; ++xx)
+                if (xx >= 0 && yy >= 0 && xx < W && yy < H) m[(size_t)yy * W + xx] = 1;
+    }
+};
+
+static double adjoint_f64(const cvtpm_params* prm, const ImgD& i1, const ImgD& i2, int cx, int cy, const double s[3],
+                          double g, double gs[3], double* dimg1, double* dimg2, std::vector<D4>& dg1,
+                          std::vector<D4>& dg2, const Ambiguity* amb) {
+    bool edge;
+    double S;
+    const double keps = amb ? amb->keps : 0.0;
+    const double C = cost_f64(prm, i1, i2, cx, cy, s, keps, &edge, &S);
+    gs[0] = gs[1] = gs[2] = 0.0;
+    const int P = prm->patchsize, W = i1.W, H = i1.H;
+    TapF64 t;
+    if (amb && edge && g != 0.0) {             /* S may change: everything the window reaches */
+        amb->mark(amb->pl, cx, cy, 0);
+        for (int dy = -P; dy <= P; ++dy)
+            for (int dx = -P; dx <= P; ++dx) {
+                if (cx + dx < 0 || cy + dy < 0 || cx + dx >= W || cy + dy >= H) continue;
+                tap_f64(prm, i1, i2, cx, cy, dx, dy, s, t);
+                amb->mark(amb->im1, t.qx, t.qy, 1);
+                if (t.valid) { amb->mark(amb->im2, t.i0, t.qy, 1); amb->mark(amb->im2, t.i1, t.qy, 1); }
+            }
+    }
+    if (!(S > 1.1) || g == 0.0) return C;
+    const double al = prm->color_alpha, cm = prm->color_maxdiff, gm = prm->grad_maxdiff;
+    const double u = g / S;
+    for (int dy = -P; dy <= P; ++dy)
+        for (int dx = -P; dx <= P; ++dx) {
+            if (cx + dx < 0 || cy + dy < 0 || cx + dx >= W || cy + dy >= H) continue;
+            tap_f64(prm, i1, i2, cx, cy, dx, dy, s, t);
+            if (!t.valid) continue;
+            if (amb) {
+                bool kc = false, kg = false;
+                for (int ch = 0; ch < 3; ++ch)
+                    kc |= std::fabs(t.e[ch]) < keps || std::fabs(std::fabs(t.e[ch]) - cm) < keps;
+                for (int k = 0; k < 4; ++k)
+                    kg |= std::fabs(t.eg[k]) < keps || std::fabs(std::fabs(t.eg[k]) - gm) < keps;
+                const bool kx = std::fabs(t.xp - std::nearbyint(t.xp)) < keps;
+                if (kc || kg || kx) amb->mark(amb->pl, cx, cy, 0);
+                if (kc) { amb->mark(amb->im1, t.qx, t.qy, 0); amb->mark(amb->im2, t.i0, t.qy, 0); amb->mark(amb->im2, t.i1, t.qy, 0); }
+                if (kg) { amb->mark(amb->im1, t.qx, t.qy, 1); amb->mark(amb->im2, t.i0, t.qy, 1); amb->mark(amb->im2, t.i1, t.qy, 1); }
+                if (kx) for (int c = t.i0 - 1; c <= t.i0 + 2; ++c) amb->mark(amb->im2, c, t.qy, 1);
+            }
+            const double gc = u * t.w;                       /* dL/dc_t */
+            const double gd = u * (t.c - C) * (-t.prof * t.w); /* dL/dd_t */
+            double sc[3], sg[4], gx = 0.0;
+            for (int ch = 0; ch < 3; ++ch) {
+                sc[ch] = std::fabs(t.e[ch]) < cm ? sgn(t.e[ch]) : 0.0;
+                gx -= al * sc[ch] * t.D[ch];
+            }
+            for (int k = 0; k < 4; ++k) {
+                sg[k] = std::fabs(t.eg[k]) < gm ? sgn(t.eg[k]) : 0.0;
+                gx -= (1.0 - al) * sg[k] * t.Dg[k];
+            }
+            gx *= gc;
+            gs[0] += gx * t.qx; gs[1] += gx * t.qy; gs[2] += gx;
+            double* dc = dimg1 + ((size_t)cy * W + cx) * 4;
+            double* dq = dimg1 + ((size_t)t.qy * W + t.qx) * 4;
+            double* d0 = dimg2 + ((size_t)t.qy * W + t.i0) * 4;
+            double* d1 = dimg2 + ((size_t)t.qy * W + t.i1) * 4;
+            for (int ch = 0; ch < 3; ++ch) {
+                dc[ch] += gd * t.dsign[ch];
+                dq[ch] += -gd * t.dsign[ch] + gc * al * sc[ch];
+                d0[ch] -= gc * al * sc[ch] * (1.0 - t.a);
+                d1[ch] -= gc * al * sc[ch] * t.a;
+            }
+            D4& q1 = dg1[(size_t)t.qy * W + t.qx];
+            D4& r0 = dg2[(size_t)t.qy * W + t.i0];
+            D4& r1 = dg2[(size_t)t.qy * W + t.i1];
+            double* q1v[4] = {&q1.x, &q1.y, &q1.z, &q1.w};
+            double* r0v[4] = {&r0.x, &r0.y, &r0.z, &r0.w};
+            double* r1v[4] = {&r1.x, &r1.y, &r1.z, &r1.w};
+            for (int k = 0; k < 4; ++k) {
+                const double v = gc * (1.0 - al) * sg[k];
+                *q1v[k] += v;
+                *r0v[k] -= v * (1.0 - t.a);
+                *r1v[k] -= v * t.a;
+            }
+        }
+    return C;
 }
 
 /* ===================================================== extern "C" API == */
@@ -916,22 +1111,86 @@ int orc_depthmap(const cvtpm_params* prm, const float* left, const float* right,
     return CVTPM_OK;
 }
 
-/* FP64 cost of a fixed state field; edge[p] = 1 where a tap sits within eps
- * of the validity bounds. */
+/* FP64 cost of a fixed state field (FP32 images and states, widened);
+ * edge[p] = 1 where a tap sits within eps of the validity bounds or the
+ * weight sum within 1e-6 of 1.1. */
 int orc_cost_field_f64(const cvtpm_params* prm, const float* img1, const float* img2, int W, int H,
                        const float* states, double eps, double* cost, uint8_t* edge) {
     if (!check_params(prm)) return CVTPM_ERR_INVALID_ARGUMENT;
-    std::vector<D4> g1, g2;
-    gradxy_f64((const F4*)img1, W, H, g1);
-    gradxy_f64((const F4*)img2, W, H, g2);
+    const size_t n = (size_t)W * H;
+    std::vector<double> c1(img1, img1 + n * 4), c2(img2, img2 + n * 4);
+    ImgD i1{W, H, c1.data(), {}}, i2{W, H, c2.data(), {}};
+    grad_f64(i1);
+    grad_f64(i2);
 #pragma omp parallel for schedule(dynamic, 1)
     for (int y = 0; y < H; ++y)
         for (int x = 0; x < W; ++x) {
+            const float* st = states + ((size_t)y * W + x) * 4;
+            const double s[3] = {st[0], st[1], st[2]};
             bool e = false;
-            cost[(size_t)y * W + x] = cost_f64(prm, (const F4*)img1, g1, (const F4*)img2, g2, W, H, x, y,
-                                               states + ((size_t)y * W + x) * 4, eps, &e);
+            double ws;
+            cost[(size_t)y * W + x] = cost_f64(prm, i1, i2, x, y, s, eps, &e, &ws);
             if (edge) edge[(size_t)y * W + x] = e ? 1 : 0;
         }
+    return CVTPM_OK;
+}
+
+/* FP64 cost of per-pixel planes (a, b, c, unused) of view lr on double
+ * images (RGBA, W*H*4); sig (optional) receives each pixel's branch
+ * signature. */
+int orc_cost_planes_f64(const cvtpm_params* prm, const double* img1, const double* img2, int W, int H,
+                        const double* planes, int lr, double eps, double* cost, uint8_t* edge, uint64_t* sig) {
+    if (!check_params(prm)) return CVTPM_ERR_INVALID_ARGUMENT;
+    ImgD i1{W, H, img1, {}}, i2{W, H, img2, {}};
+    grad_f64(i1);
+    grad_f64(i2);
+#pragma omp parallel for schedule(dynamic, 1)
+    for (int y = 0; y < H; ++y)
+        for (int x = 0; x < W; ++x) {
+            double s[3];
+            plane_state(planes + ((size_t)y * W + x) * 4, lr, s);
+            bool e = false;
+            double ws;
+            cost[(size_t)y * W + x] = cost_f64(prm, i1, i2, x, y, s, eps, &e, &ws, sig ? sig + (size_t)y * W + x : nullptr);
+            if (edge) edge[(size_t)y * W + x] = e ? 1 : 0;
+        }
+    return CVTPM_OK;
+}
+
+/* FP64 adjoint: given dcost = dL/dC per pixel, the cost and dL/d(planes),
+ * dL/d(img1), dL/d(img2) (alpha channel 0).  Sequential (the image
+ * gradients are scattered).  With kink_eps > 0 the amb_* masks (optional,
+ * W*H) flag the entries a tap within kink_eps of a kink reaches. */
+int orc_cost_adjoint_f64(const cvtpm_params* prm, const double* img1, const double* img2, int W, int H,
+                         const double* planes, int lr, const double* dcost, double* cost, double* dplanes,
+                         double* dimg1, double* dimg2, double kink_eps, uint8_t* amb_planes, uint8_t* amb_img1,
+                         uint8_t* amb_img2) {
+    if (!check_params(prm)) return CVTPM_ERR_INVALID_ARGUMENT;
+    ImgD i1{W, H, img1, {}}, i2{W, H, img2, {}};
+    grad_f64(i1);
+    grad_f64(i2);
+    const size_t n = (size_t)W * H;
+    std::fill(dimg1, dimg1 + n * 4, 0.0);
+    std::fill(dimg2, dimg2 + n * 4, 0.0);
+    std::vector<D4> dg1(n, D4{0, 0, 0, 0}), dg2(n, D4{0, 0, 0, 0});
+    const double ds = lr ? -1.0 : 1.0;
+    Ambiguity amb{kink_eps, W, H, amb_planes, amb_img1, amb_img2};
+    for (uint8_t* m : {amb_planes, amb_img1, amb_img2})
+        if (m) std::fill(m, m + n, (uint8_t)0);
+    const bool track = kink_eps > 0.0 && (amb_planes || amb_img1 || amb_img2);
+    for (int y = 0; y < H; ++y)
+        for (int x = 0; x < W; ++x) {
+            const size_t o = (size_t)y * W + x;
+            double s[3], gs[3];
+            plane_state(planes + o * 4, lr, s);
+            cost[o] = adjoint_f64(prm, i1, i2, x, y, s, dcost[o], gs, dimg1, dimg2, dg1, dg2, track ? &amb : nullptr);
+            dplanes[o * 4 + 0] = ds * gs[0];
+            dplanes[o * 4 + 1] = ds * gs[1];
+            dplanes[o * 4 + 2] = ds * gs[2];
+            dplanes[o * 4 + 3] = 0.0;
+        }
+    grad_f64_adjoint(dg1, W, H, dimg1);
+    grad_f64_adjoint(dg2, W, H, dimg2);
     return CVTPM_OK;
 }
 
