@@ -44,6 +44,14 @@ struct cvtpm_ctx {
     short4* list[2];
     uint8_t* win[2];
     uint8_t* valid;
+    /* FAST shared-window neighbour costs: weight volumes of both views and
+     * the per-pixel costs of candidates 1-8, when the budget allows */
+    float* vol = nullptr;
+    size_t vol_bytes = 0;
+    size_t vol_budget = SIZE_MAX;
+    bool vol_on = false;
+    float* wvol[2] = {nullptr, nullptr};
+    float* nbcost = nullptr;
     /* staging for the *_host entry points */
     void* stage = nullptr;
     size_t stage_bytes = 0;
@@ -205,6 +213,34 @@ PmPassArgs base_args(cvtpm_ctx* ctx, const cvtpm_params& p, int W, int H, int v1
     return a;
 }
 
+/* The weight volumes ((2P+1)^2 floats per pixel and view) and the
+ * neighbour-cost buffer of the FAST shared-window path.  Used when they fit
+ * the context's budget and 60 % of the free device memory; otherwise the
+ * propagation evaluates every neighbour per pixel (same results). */
+cvtpm_status ensure_volumes(cvtpm_ctx* ctx, int W, int H, int P) {
+    const size_t n = (size_t)W * H, N2 = (size_t)(2 * P + 1) * (2 * P + 1);
+    const size_t need = (2 * N2 + 8) * n * sizeof(float);
+    ctx->vol_on = false;
+    if (need > ctx->vol_budget) return CVTPM_OK;
+    if (ctx->vol_bytes < need) {
+        if (ctx->vol) { CK(cudaFree(ctx->vol), "free volumes"); ctx->vol = nullptr; ctx->vol_bytes = 0; }
+        size_t fr = 0, tot = 0;
+        CK(cudaMemGetInfo(&fr, &tot), "memory info");
+        if ((double)need > 0.6 * (double)fr) return CVTPM_OK;
+        if (cudaMalloc(&ctx->vol, need) != cudaSuccess) {
+            cudaGetLastError();                      /* clear the failed allocation; use the per-pixel path */
+            ctx->vol = nullptr;
+            return CVTPM_OK;
+        }
+        ctx->vol_bytes = need;
+    }
+    ctx->wvol[0] = ctx->vol;
+    ctx->wvol[1] = ctx->vol + N2 * n;
+    ctx->nbcost = ctx->vol + 2 * N2 * n;
+    ctx->vol_on = true;
+    return CVTPM_OK;
+}
+
 cvtpm_status prep_views(cvtpm_ctx* ctx, const cvtpm_params& p, const float* img0, const float* img1, int W, int H,
                         size_t pitch, cudaStream_t st, bool records = false) {
     const float* im[2] = {img0, img1};
@@ -277,6 +313,15 @@ cvtpm_status run_depthmap(cvtpm_ctx* ctx, const cvtpm_params& p, float* dmap, si
     const float dscale = p.dscale <= 0.0f ? 1.0f / dmax : p.dscale;
     const int N = p.iterations;
     PmPassArgs aL = base_args(ctx, p, W, H, 0), aR = base_args(ctx, p, W, H, 1);
+    if (!exact) {
+        if ((s = ensure_volumes(ctx, W, H, p.patchsize)) != CVTPM_OK) return s;
+        if (ctx->vol_on) {
+            LK(pm_launch_weights(ctx->col[0], W, H, p.patchsize, ctx->wvol[0], st), "weights left");
+            LK(pm_launch_weights(ctx->col[1], W, H, p.patchsize, ctx->wvol[1], st), "weights right");
+            aL.wvol = ctx->wvol[0]; aR.wvol = ctx->wvol[1];
+            aL.nbcost = aR.nbcost = ctx->nbcost;
+        }
+    }
     if (!ctx->dcount) {
         CK(cudaMalloc(&ctx->dcount, 2 * sizeof(unsigned long long)), "counters");
         CK(cudaMemset(ctx->dcount, 0, 2 * sizeof(unsigned long long)), "counters");
@@ -419,6 +464,7 @@ cvtpm_status cvtpm_destroy(cvtpm_ctx* ctx) {
     cudaSetDevice(ctx->device);
     if (ctx->pool) cudaFree(ctx->pool);
     if (ctx->stage) cudaFree(ctx->stage);
+    if (ctx->vol) cudaFree(ctx->vol);
     if (ctx->dcount) cudaFree(ctx->dcount);
     for (auto& pr : ctx->ev_prop) { cudaEventDestroy(pr.first); cudaEventDestroy(pr.second); }
     for (auto& pr : ctx->ev_pd) { cudaEventDestroy(pr.first); cudaEventDestroy(pr.second); }
@@ -517,6 +563,18 @@ cvtpm_status cvtpm_cost_eval(cvtpm_ctx* ctx, const float* img1, const float* img
     if ((s = prep_views(ctx, p, img1, img2, width, height, pitch, st)) != CVTPM_OK) return s;
     PmPassArgs a = base_args(ctx, p, width, height, 0);
     LK(pm_launch_cost_field(a, p.arith == CVTPM_ARITH_EXACT, (const float4*)states, cost, st), "cost field");
+    return CVTPM_OK;
+}
+
+cvtpm_status cvtpm_set_memory_budget(cvtpm_ctx* ctx, size_t bytes) {
+    if (!ctx) return CVTPM_ERR_INVALID_ARGUMENT;
+    ctx->vol_budget = bytes;
+    if (ctx->vol && ctx->vol_bytes > bytes) {
+        CK(cudaSetDevice(ctx->device), "cudaSetDevice");
+        CK(cudaFree(ctx->vol), "free volumes");
+        ctx->vol = nullptr;
+        ctx->vol_bytes = 0;
+    }
     return CVTPM_OK;
 }
 

@@ -218,6 +218,30 @@ struct PmCostConsts {
     int rp;          /* row pitch (elements) of the record planes */
 };
 
+/* The matching terms of one tap in the FAST arithmetic: colour and gradient
+ * truncated-L1 distances between image 1 at the tap (a1, g1) and the other
+ * view interpolated from record j with weight a.  They depend on the tap
+ * and the plane only, not on the pixel whose window holds the tap. */
+PM_DEV void fast_tap_terms(const PmCostConsts& k, const PmView& v2, size_t j, float a, float4 a1, float4 g1,
+                           float& cc, float& gc) {
+    const float4 A = __ldg(&v2.recA[j]);
+    const float4 B = __ldg(&v2.recB[j]);
+    const float4 Cc = __ldg(&v2.recC[j]);
+    const float2 D = __ldg(&v2.recD[j]);
+    const float v0 = fmaf(a, B.w, A.x), v1c = fmaf(a, Cc.x, A.y), v2c = fmaf(a, Cc.y, A.z);
+    const float u0 = fmaf(a, Cc.z, A.w), u1 = fmaf(a, Cc.w, B.x), u2 = fmaf(a, D.x, B.y), u3 = fmaf(a, D.y, B.z);
+    cc = (fminf(fabsf(a1.x - v0), k.cmax) + fminf(fabsf(a1.y - v1c), k.cmax)) + fminf(fabsf(a1.z - v2c), k.cmax);
+    gc = ((fminf(fabsf(g1.x - u0), k.gmax) + fminf(fabsf(g1.y - u1), k.gmax)) + fminf(fabsf(g1.z - u2), k.gmax)) +
+         fminf(fabsf(g1.w - u3), k.gmax);
+}
+
+/* The bilateral weight of tap (centre colour vc, tap colour a1, profile
+ * value prof): the FAST and EXACT paths and the weight volume share it. */
+PM_DEV float tap_weight(float4 vc, float4 a1, float prof) {
+    const float d = (fabsf(vc.x - a1.x) + fabsf(vc.y - a1.y)) + fabsf(vc.z - a1.z);
+    return pm_exp(-d * prof);
+}
+
 #ifdef PM_KERNELS_TU
 /* Aggregated ASW cost (patch_eval_color_grad_weighted, pmhstereo.cl:170-228)
  * of K candidate planes at pixel (x, y), sharing the image-1 reads and the
@@ -238,7 +262,7 @@ PM_DEV void eval_costs(const PmCostConsts& k, const PmView& v1, const PmView& v2
             sy[c] = live[c] ? s[c].y : 0.0f;
             sz[c] = live[c] ? s[c].z : -1.0e30f;    /* never inside [0, W) */
         } else {
-            pm_fix_plane(live[c], s[c].x, s[c].y, s[c].z, x, y, &S0[c], &S1[c], &XC[c]);
+            pm_fix_plane(live[c], s[c].x, s[c].y, s[c].z, k.W / 2, k.H / 2, &S0[c], &S1[c], &XC[c]);
         }
     }
     float ws[K], r1[K], r2[K];
@@ -257,15 +281,15 @@ PM_DEV void eval_costs(const PmCostConsts& k, const PmView& v1, const PmView& v2
         long long X[K];
         if (!EXACT) {
 #pragma unroll
-            for (int c = 0; c < K; ++c) X[c] = XC[c] + (long long)dy * S1[c] + (long long)dxlo * S0[c];
+            for (int c = 0; c < K; ++c)
+                X[c] = XC[c] + (long long)(qy - k.H / 2) * S1[c] + (long long)(x + dxlo - k.W / 2) * S0[c];
         }
         for (int dx = dxlo; dx <= dxhi; ++dx) {
             const int qx = x + dx;
             const float qxf = (float)qx;
             const float4 a1 = __ldg(&c1row[qx]);
             const float4 g1 = __ldg(&g1row[qx]);
-            const float d = (fabsf(vc.x - a1.x) + fabsf(vc.y - a1.y)) + fabsf(vc.z - a1.z);
-            const float w1 = pm_exp(-d * prow[dx]);
+            const float w1 = tap_weight(vc, a1, prow[dx]);
 #pragma unroll
             for (int c = 0; c < K; ++c) {
                 if (EXACT) {
@@ -294,16 +318,8 @@ PM_DEV void eval_costs(const PmCostConsts& k, const PmView& v1, const PmView& v2
                     X[c] += S0[c];
                     const int xi = (int)(Xt >> 32);
                     if ((unsigned)xi >= (unsigned)k.W) continue;
-                    const float a = pm_fix_frac(Xt);
-                    const size_t j = (size_t)qy * k.rp + xi;
-                    const float4 A = __ldg(&v2.recA[j]);
-                    const float4 B = __ldg(&v2.recB[j]);
-                    const float4 Cc = __ldg(&v2.recC[j]);
-                    const float2 D = __ldg(&v2.recD[j]);
-                    const float v0 = fmaf(a, B.w, A.x), v1c = fmaf(a, Cc.x, A.y), v2c = fmaf(a, Cc.y, A.z);
-                    const float u0 = fmaf(a, Cc.z, A.w), u1 = fmaf(a, Cc.w, B.x), u2 = fmaf(a, D.x, B.y), u3 = fmaf(a, D.y, B.z);
-                    const float cc = (fminf(fabsf(a1.x - v0), k.cmax) + fminf(fabsf(a1.y - v1c), k.cmax)) + fminf(fabsf(a1.z - v2c), k.cmax);
-                    const float gc = ((fminf(fabsf(g1.x - u0), k.gmax) + fminf(fabsf(g1.y - u1), k.gmax)) + fminf(fabsf(g1.z - u2), k.gmax)) + fminf(fabsf(g1.w - u3), k.gmax);
+                    float cc, gc;
+                    fast_tap_terms(k, v2, (size_t)qy * k.rp + xi, pm_fix_frac(Xt), a1, g1, cc, gc);
                     r1[c] = fmaf(w1, cc, r1[c]);
                     r2[c] = fmaf(w1, gc, r2[c]);
                     ws[c] = ws[c] + w1;

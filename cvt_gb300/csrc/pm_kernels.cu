@@ -133,7 +133,11 @@ __global__ void __launch_bounds__(256) k_propagate(PmPassArgs a) {
         if (cand.w + theta * da <= self.w + theta * db) { self = cand; win = idx; }
     };
 
-    /* candidates 1-8: the 3x3 neighbourhood of `old`, clamped to the edge (:330-342) */
+    /* candidates 1-8: the 3x3 neighbourhood of `old`, clamped to the edge
+     * (:330-342).  With the shared-window costs of k_nbcost (FAST), only
+     * neighbours the clamp moves (pixels on the image border) are evaluated
+     * here; the others are read. */
+    const bool shared = !EXACT && a.nbcost != nullptr;
 #pragma unroll 1
     for (int b = 0; b < 2; ++b) {
         float4 s[4]; bool act[4]; float c[4];
@@ -143,9 +147,18 @@ __global__ void __launch_bounds__(256) k_propagate(PmPassArgs a) {
             int nn = n < 4 ? n : n + 1;        /* skip the centre */
             int px = nn % 3 - 1, py = nn / 3 - 1;
             s[i] = a.old[(size_t)clampi(yc + py, 0, H - 1) * W + clampi(xc + px, 0, W - 1)];
-            act[i] = true;
+            const bool edge = xc + px < 0 || xc + px >= W || yc + py < 0 || yc + py >= H;
+            act[i] = !shared || edge;
+            c[i] = act[i] ? 0.0f : a.nbcost[(size_t)n * W * H + o];
         }
-        eval_costs<4, EXACT>(a.k, a.v1, a.v2, xc, yc, s, act, c);
+        bool any = act[0] || act[1] || act[2] || act[3];
+        if (!shared || __any_sync(0xffffffffu, any)) {
+            float ce[4];
+            eval_costs<4, EXACT>(a.k, a.v1, a.v2, xc, yc, s, act, ce);
+#pragma unroll
+            for (int i = 0; i < 4; ++i)
+                if (act[i]) c[i] = ce[i];
+        }
 #pragma unroll
         for (int i = 0; i < 4; ++i) accept(s[i], c[i], 1 + b * 4 + i);
     }
@@ -232,6 +245,115 @@ __global__ void __launch_bounds__(256) k_propagate(PmPassArgs a) {
             atomicAdd(&a.counters[0], ev);
             atomicAdd(&a.counters[1], taps);
         }
+    }
+}
+
+/* ---------------------------------------- shared neighbour windows -- */
+/* Bilateral weights of every pixel p and window offset o = (dy+P)(2P+1) +
+ * (dx+P), stored at wvol[o * W*H + p] (0 outside the image); the same
+ * arithmetic as the weight of eval_costs. */
+__global__ void __launch_bounds__(256) k_weights(const float4* __restrict__ col, int W, int H, int P,
+                                                 float* __restrict__ wvol) {
+    const int x = blockIdx.x * 32 + threadIdx.x, y = blockIdx.y * 8 + threadIdx.y;
+    if (x >= W || y >= H) return;
+    const size_t n = (size_t)W * H, p = (size_t)y * W + x;
+    const float4 vc = col[p];
+    const int N = 2 * P + 1;
+    for (int dy = -P; dy <= P; ++dy) {
+        const int qy = y + dy;
+        const float* prow = c_prof + (dy + PM_PMAX) * PM_PROF_N + PM_PMAX;
+        float* orow = wvol + (size_t)((dy + P) * N + P) * n + p;
+        for (int dx = -P; dx <= P; ++dx) {
+            const int qx = x + dx;
+            float w = 0.0f;
+            if (qy >= 0 && qy < H && qx >= 0 && qx < W) w = tap_weight(vc, __ldg(&col[(size_t)qy * W + qx]), prow[dx]);
+            orow[(ptrdiff_t)dx * (ptrdiff_t)n] = w;
+        }
+    }
+}
+
+/* Candidates 1-8 (pmhstereo.cl:330-342) evaluated plane by plane.  Thread m
+ * owns the plane old[m]; it is candidate k of the pixel u_k = m - o_k for
+ * the 8 offsets o_k of the 3x3 neighbourhood (u_k inside the image makes the
+ * clamp of :335-336 the identity; border pixels evaluate their clamped
+ * neighbours themselves).  A tap's matching terms depend on the tap and the
+ * plane only, so they are computed once over the union of the 8 windows
+ * (37 x 37) and folded into every user's sums with that user's weight from
+ * the weight volume.  Each user receives its taps in raster order with the
+ * operations of eval_costs, so its cost has the bits of a separate
+ * evaluation.  Costs go to nb[k * W*H + u_k]. */
+__global__ void __launch_bounds__(256, 2) k_nbcost(PmPassArgs a) {
+    const int W = a.k.W, H = a.k.H, P = a.k.P, N = 2 * P + 1;
+    const int mx = blockIdx.x * 32 + threadIdx.x, my = blockIdx.y * 8 + threadIdx.y;
+    if (mx >= W || my >= H) return;
+    const size_t n = (size_t)W * H, m = (size_t)my * W + mx;
+    const float4 s = a.old[m];
+    long long S0, S1, XA;
+    const bool fin = finite3(s);
+    pm_fix_plane(fin, s.x, s.y, s.z, W / 2, H / 2, &S0, &S1, &XA);
+    unsigned uok = 0;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+        const int nn = k < 4 ? k : k + 1, ox = nn % 3 - 1, oy = nn / 3 - 1;
+        const int ux = mx - ox, uy = my - oy;
+        if (ux >= 0 && ux < W && uy >= 0 && uy < H) uok |= 1u << k;
+    }
+    float r1[8], r2[8], ws[8];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) { r1[k] = 0.0f; r2[k] = 0.0f; ws[k] = 0.0f; }
+    const int qx0 = max(mx - P - 1, 0), qx1 = min(mx + P + 1, W - 1);
+    const int qy0 = max(my - P - 1, 0), qy1 = min(my + P + 1, H - 1);
+    for (int qy = qy0; qy <= qy1; ++qy) {
+        const int ry = qy - my;
+        unsigned rmask = 0;
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+            const int oy = (k < 4 ? k : k + 1) / 3 - 1;
+            if (abs(ry + oy) <= P) rmask |= 1u << k;
+        }
+        rmask &= uok;
+        if (!rmask) continue;
+        const float4* c1row = a.v1.col + (size_t)qy * W;
+        const float4* g1row = a.v1.grad + (size_t)qy * W;
+        const size_t jrow = (size_t)qy * a.k.rp;
+        long long X = XA + (long long)(qy - H / 2) * S1 + (long long)(qx0 - W / 2) * S0;
+        for (int qx = qx0; qx <= qx1; ++qx) {
+            const long long Xt = X;
+            X += S0;
+            const int xi = (int)(Xt >> 32);
+            if ((unsigned)xi >= (unsigned)W) continue;
+            const int rx = qx - mx;
+            unsigned mask = rmask;
+            if (rx <= -P || rx >= P) {
+#pragma unroll
+                for (int k = 0; k < 8; ++k) {
+                    const int ox = (k < 4 ? k : k + 1) % 3 - 1;
+                    if (abs(rx + ox) > P) mask &= ~(1u << k);
+                }
+            }
+            const float4 a1 = __ldg(&c1row[qx]);
+            const float4 g1 = __ldg(&g1row[qx]);
+            float cc, gc;
+            fast_tap_terms(a.k, a.v2, jrow + xi, pm_fix_frac(Xt), a1, g1, cc, gc);
+            /* user k's weight: offset (ry + oy_k, rx + ox_k), pixel m - (oy_k W + ox_k) */
+            const ptrdiff_t wb = ((ptrdiff_t)(ry + P) * N + (rx + P)) * (ptrdiff_t)n + (ptrdiff_t)m;
+#pragma unroll
+            for (int k = 0; k < 8; ++k) {
+                if (!((mask >> k) & 1u)) continue;
+                const int nn = k < 4 ? k : k + 1, ox = nn % 3 - 1, oy = nn / 3 - 1;
+                const float w = __ldg(&a.wvol[wb + (ptrdiff_t)(oy * N + ox) * (ptrdiff_t)n - (ptrdiff_t)(oy * W + ox)]);
+                r1[k] = fmaf(w, cc, r1[k]);
+                r2[k] = fmaf(w, gc, r2[k]);
+                ws[k] = ws[k] + w;
+            }
+        }
+    }
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+        if (!((uok >> k) & 1u)) continue;
+        const int nn = k < 4 ? k : k + 1, ox = nn % 3 - 1, oy = nn / 3 - 1;
+        const float v = fmaf(a.k.alpha, r1[k], a.k.oma * r2[k]) / ws[k];
+        a.nbcost[(size_t)k * n + m - (size_t)(oy * W + ox)] = (!fin || ws[k] <= 1.1f) ? 1e5f : v;
     }
 }
 
@@ -595,8 +717,23 @@ cudaError_t pm_launch_cost_field(const PmPassArgs& a, bool exact, const float4* 
 }
 
 cudaError_t pm_launch_propagate(const PmPassArgs& a, bool exact, cudaStream_t st) {
-    if (exact) k_propagate<true><<<pix_grid(a.k.W, a.k.H), dim3(32, 8), 0, st>>>(a);
-    else k_propagate<false><<<pix_grid(a.k.W, a.k.H), dim3(32, 8), 0, st>>>(a);
+    if (exact) {
+        k_propagate<true><<<pix_grid(a.k.W, a.k.H), dim3(32, 8), 0, st>>>(a);
+    } else {
+        PmPassArgs b = a;
+        if (!b.wvol) b.nbcost = nullptr;
+        if (b.nbcost) {
+            k_nbcost<<<pix_grid(a.k.W, a.k.H), dim3(32, 8), 0, st>>>(b);
+            PM_LAUNCH_CHECK();
+        }
+        k_propagate<false><<<pix_grid(a.k.W, a.k.H), dim3(32, 8), 0, st>>>(b);
+    }
+    PM_LAUNCH_CHECK();
+    return cudaSuccess;
+}
+
+cudaError_t pm_launch_weights(const float4* col, int W, int H, int P, float* wvol, cudaStream_t st) {
+    k_weights<<<pix_grid(W, H), dim3(32, 8), 0, st>>>(col, W, H, P, wvol);
     PM_LAUNCH_CHECK();
     return cudaSuccess;
 }

@@ -113,27 +113,31 @@ PM_HD double pm_fma_d(double a, double b, double c) {
 }
 
 /* Tap positions of the FAST arithmetic in fixed point.  The sample column
- * x' = s0*qx + s1*qy + s2 of tap (qx, qy) = (x + dx, y + dy) is written as
- * x'(x, y) + s0*dx + s1*dy and carried in Q31.32 (int64 with 32 fraction
- * bits): the centre value is formed in double and rounded once, the slopes
- * are rounded once, and every tap adds integers, so a tap position is within
- * 18 * 2^-33 px of the exact value whatever the image width (an FP32
- * evaluation is off by up to half an ulp of x', 6e-5 px at x' ~ 1000).  The
+ * x' = s0*qx + s1*qy + s2 of tap (qx, qy) is carried in Q31.32 (int64 with
+ * 32 fraction bits), anchored at the image centre (ax, ay) = (W/2, H/2):
+ *   X(q) = XA + (qx - ax)*S0 + (qy - ay)*S1,
+ *   S = round(s * 2^32), XA = round(x'(ax, ay) * 2^32) formed in double.
+ * The anchor depends on the image only, so a plane's tap positions are the
+ * same integers whichever pixel evaluates it (a window can be shared by all
+ * pixels testing one plane).  Slopes with |s| >= 2^-9 are exact in Q32, so a
+ * position is within half a unit of 2^-32 px of x' (plus 2^-33 px per
+ * coordinate of distance for smaller slopes) at any image width; an FP32
+ * evaluation is off by up to half an ulp of x', 6e-5 px at x' ~ 1000.  The
  * integer part is the record index, the fraction the interpolation weight.
- * Planes with |s0| or |s1| >= 2^24 (at most one tap per window row or column
- * can fall inside any image) or |x'(x, y)| >= 2^30 (no tap inside) are not
- * representable: they get XC = PM_FIX_NONE, which no tap reaches. */
+ * Planes with |s0| or |s1| >= 2^14 or |x'(ax, ay)| >= 2^30 are not
+ * representable (with W <= 2^14 and H <= 2^16, |X| < 2^31 * 2^32 then):
+ * they get XA = PM_FIX_NONE and S = 0, which no tap reaches. */
 #define PM_FIX_NONE (-(1LL << 62))
-PM_HD bool pm_fix_plane(bool live, float s0, float s1, float s2, int x, int y,
-                        long long* S0, long long* S1, long long* XC) {
+PM_HD bool pm_fix_plane(bool live, float s0, float s1, float s2, int ax, int ay,
+                        long long* S0, long long* S1, long long* XA) {
     const float one = 4294967296.0f;                               /* 2^32 */
     const bool ok0 = live && isfinite(s0) && isfinite(s1) && isfinite(s2) &&
-                     fabsf(s0) < 16777216.0f && fabsf(s1) < 16777216.0f;
-    const double xc = ok0 ? pm_fma_d((double)s0, (double)x, pm_fma_d((double)s1, (double)y, (double)s2)) : 0.0;
-    const bool ok = ok0 && fabs(xc) < 1073741824.0;               /* 2^30 */
+                     fabsf(s0) < 16384.0f && fabsf(s1) < 16384.0f;
+    const double xa = ok0 ? pm_fma_d((double)s0, (double)ax, pm_fma_d((double)s1, (double)ay, (double)s2)) : 0.0;
+    const bool ok = ok0 && fabs(xa) < 1073741824.0;               /* 2^30 */
     *S0 = ok ? pm_f2ll_rn(s0 * one) : 0;
     *S1 = ok ? pm_f2ll_rn(s1 * one) : 0;
-    *XC = ok ? pm_d2ll_rn(xc * 4294967296.0) : PM_FIX_NONE;
+    *XA = ok ? pm_d2ll_rn(xa * 4294967296.0) : PM_FIX_NONE;
     return ok;
 }
 /* The interpolation weight: the 32 fraction bits, rounded to float. */

@@ -164,6 +164,11 @@ class PMHuberStereo:
         self._check(rc)
         return out
 
+    def set_memory_budget(self, nbytes: int) -> None:
+        """Device bytes the FAST path may use for its shared-window weight
+        volumes (0: evaluate neighbours per pixel; results are the same)."""
+        self._check(_lib.lib().cvtpm_set_memory_budget(self._h, int(nbytes)))
+
     def cost_adjoint(self, img1: torch.Tensor, img2: torch.Tensor, planes: torch.Tensor, lr: int = 1,
                      dcost: torch.Tensor | None = None, want_planes: bool = True, want_images: bool = True):
         """cvtpm_cost_adjoint.  planes (H, W, 4) = (a, b, c, -) with

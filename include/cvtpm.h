@@ -188,6 +188,15 @@ cvtpm_status cvtpm_cost_adjoint(cvtpm_ctx* ctx,
                                 float* cost, float* dplanes,
                                 float* dimg1, float* dimg2, void* stream);
 
+/* Device memory the context may use for the FAST path's shared-window
+ * neighbour costs: two weight volumes of (2*patchsize+1)^2 floats per pixel
+ * (4.9 KB per pixel at patchsize 17) plus 32 bytes per pixel.  Within the
+ * budget (and 60 % of the free memory) the 8 neighbour candidates of a pass
+ * are evaluated once per plane over the union of their windows; otherwise
+ * per pixel.  Results are identical either way.  Default: no limit;
+ * 0 turns the volumes off.  No counterpart in the reference. */
+cvtpm_status cvtpm_set_memory_budget(cvtpm_ctx* ctx, size_t bytes);
+
 /* Enable CUDA-event timing of the propagation and PD phases (on the call's
  * stream); cvtpm_get_stats waits for the recorded events. */
 cvtpm_status cvtpm_set_timing(cvtpm_ctx* ctx, int enable);

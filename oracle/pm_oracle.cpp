@@ -325,7 +325,7 @@ static float cost_eval(const CostCfg& k, const View& v1, const View& v2, int cx,
      * apart. */
     float wsum = 0.0f, rc = 0.0f, rg = 0.0f;
     long long S0, S1, XC;
-    pm_fix_plane(true, s.x, s.y, s.z, cx, cy, &S0, &S1, &XC);
+    pm_fix_plane(true, s.x, s.y, s.z, W / 2, H / 2, &S0, &S1, &XC);
     for (int dy = -P; dy <= P; ++dy) {
         int qy = cy + dy;
         if (qy < 0 || qy >= H) continue;
@@ -337,7 +337,7 @@ static float cost_eval(const CostCfg& k, const View& v1, const View& v2, int cx,
             const F4 g1 = v1.grad[(size_t)qy * W + qx];
             float d = (fabsf(vc.x - a1.x) + fabsf(vc.y - a1.y)) + fabsf(vc.z - a1.z);
             float w1 = pm_exp(-d * k.prof[(size_t)(dy + P) * n + (dx + P)]);
-            const long long X = XC + (long long)dy * S1 + (long long)dx * S0;
+            const long long X = XC + (long long)(qy - H / 2) * S1 + (long long)(qx - W / 2) * S0;
             const int xi = (int)(X >> 32);
             if ((unsigned)xi >= (unsigned)W) continue;
             float a = pm_fix_frac(X);

@@ -9,6 +9,8 @@ import torch
 
 from cvt_gb300.params import default_params, PRESET_REFERENCE
 
+from bitcmp import bit_diff
+
 pytestmark = pytest.mark.gpu
 GOLDEN = os.path.join(os.path.dirname(__file__), "golden", "pm_reference_golden.npz")
 
@@ -16,7 +18,7 @@ GOLDEN = os.path.join(os.path.dirname(__file__), "golden", "pm_reference_golden.
 def assert_bits(got, want, what):
     got, want = np.ascontiguousarray(got), np.ascontiguousarray(want)
     assert got.shape == want.shape, what
-    d = got.view(np.uint32) != want.view(np.uint32)
+    d = bit_diff(got, want)
     assert not d.any(), f"{what}: {int(d.sum())} of {d.size} values differ"
 
 

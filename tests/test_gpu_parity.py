@@ -11,21 +11,18 @@ from cvt_gb300 import scenes
 from cvt_gb300.params import (default_params, PRESET_REFERENCE, PRESET_BASELINE, ARITH_EXACT, ARITH_FAST,
                               RNG_MWC64X, RNG_PHILOX)
 
+from bitcmp import bit_diff
+
 pytestmark = pytest.mark.gpu
 
 MODES = [(ARITH_EXACT, RNG_MWC64X), (ARITH_FAST, RNG_PHILOX), (ARITH_EXACT, RNG_PHILOX), (ARITH_FAST, RNG_MWC64X)]
 MODE_IDS = ["exact-mwc64x", "fast-philox", "exact-philox", "fast-mwc64x"]
 
 
-def bits(a):
-    a = np.ascontiguousarray(a)
-    return a.view(np.uint32) if a.dtype == np.float32 else a
-
-
 def assert_bitexact(got, want, what):
     got, want = np.asarray(got), np.asarray(want)
     assert got.shape == want.shape, what
-    diff = bits(got) != bits(want)
+    diff = bit_diff(got, want)
     assert not diff.any(), f"{what}: {int(diff.sum())} of {diff.size} differ, first at {np.argwhere(diff)[0]}"
 
 
@@ -94,6 +91,27 @@ def test_depthmap_bitexact(stereo, oracle, mode):
     assert_bitexact(tr["states"], ex["states"], "states")
     assert_bitexact(dm, want, "dmap")
     assert_bitexact(nm, ex["normalmap"], "normalmap")
+
+
+def test_shared_windows_match_per_pixel_neighbours(oracle):
+    """FAST: the 8 neighbour candidates evaluated plane by plane over shared
+    windows (weight volumes) give the same bits as the per-pixel evaluation
+    (memory budget 0), and both match the oracle."""
+    from cvt_gb300.stereo import PMHuberStereo
+    sc = scenes.make_scene(150, 70, 5, 20.0, seed=12)
+    p = default_params(PRESET_BASELINE, patchsize=11, depthmax=20.0, iterations=3, pd_iterations=10)
+    outs = []
+    for budget in (None, 0):
+        st = PMHuberStereo(0)
+        if budget is not None:
+            st.set_memory_budget(budget)
+        outs.append(run_both(st, oracle, sc, p))
+    (dm1, nm1, tr1, want, ex), (dm0, nm0, tr0, _, _) = outs
+    for k in ("winners", "valid", "states"):
+        assert_bitexact(tr1[k], tr0[k], k + " (shared vs per pixel)")
+        assert_bitexact(tr1[k], ex[k], k + " (vs oracle)")
+    assert_bitexact(dm1, dm0, "dmap")
+    assert_bitexact(dm1, want, "dmap vs oracle")
 
 
 def test_depthmap_theta_ramp(stereo, oracle):

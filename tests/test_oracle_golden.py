@@ -9,6 +9,8 @@ import pytest
 
 from cvt_gb300.params import default_params, PRESET_REFERENCE
 
+from bitcmp import bit_diff
+
 GOLDEN = os.path.join(os.path.dirname(__file__), "golden", "pm_reference_golden.npz")
 
 
@@ -20,7 +22,7 @@ def G():
 def assert_bits(got, want, what):
     got, want = np.ascontiguousarray(got), np.ascontiguousarray(want)
     assert got.shape == want.shape, what
-    d = got.view(np.uint32) != want.view(np.uint32)
+    d = bit_diff(got, want)
     assert not d.any(), f"{what}: {int(d.sum())} of {d.size} values differ"
 
 
