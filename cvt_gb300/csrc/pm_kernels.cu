@@ -281,7 +281,10 @@ __global__ void __launch_bounds__(256) k_weights(const float4* __restrict__ col,
  * (37 x 37) and folded into every user's sums with that user's weight from
  * the weight volume.  Each user receives its taps in raster order with the
  * operations of eval_costs, so its cost has the bits of a separate
- * evaluation.  Costs go to nb[k * W*H + u_k]. */
+ * evaluation.  Costs go to nb[k * W*H + u_k].  (Staging the weight slices in
+ * a shared-memory ring with cp.async, the block walking the offsets in
+ * lockstep, measured slower: the per-batch barriers expose the latency of
+ * the record loads that the free-running warps overlap.) */
 __global__ void __launch_bounds__(256, 2) k_nbcost(PmPassArgs a) {
     const int W = a.k.W, H = a.k.H, P = a.k.P, N = 2 * P + 1;
     const int mx = blockIdx.x * 32 + threadIdx.x, my = blockIdx.y * 8 + threadIdx.y;
@@ -303,8 +306,20 @@ __global__ void __launch_bounds__(256, 2) k_nbcost(PmPassArgs a) {
     for (int k = 0; k < 8; ++k) { r1[k] = 0.0f; r2[k] = 0.0f; ws[k] = 0.0f; }
     const int qx0 = max(mx - P - 1, 0), qx1 = min(mx + P + 1, W - 1);
     const int qy0 = max(my - P - 1, 0), qy1 = min(my + P + 1, H - 1);
+    const int lane = threadIdx.x & 31;
+    const ptrdiff_t wrow0 = (ptrdiff_t)my * W + (mx - lane) - 1;     /* the warp's pixel row, one left */
     for (int qy = qy0; qy <= qy1; ++qy) {
         const int ry = qy - my;
+        /* L2 prefetch of the weight-volume slice row the next iteration row
+         * starts to use (offset row ry + P + 2), for this warp's pixel row:
+         * 2 lines of 128 B per slice, N slices */
+        if (ry + P + 2 < N) {
+            for (int i = lane; i < 2 * N; i += 32) {
+                const ptrdiff_t pix = min(max(wrow0 + (ptrdiff_t)(i & 1) * 32, (ptrdiff_t)0), (ptrdiff_t)n - 1);
+                const float* pf = a.wvol + (ptrdiff_t)((ry + P + 2) * N + (i >> 1)) * (ptrdiff_t)n + pix;
+                asm volatile("prefetch.global.L2 [%0];" :: "l"(pf));
+            }
+        }
         unsigned rmask = 0;
 #pragma unroll
         for (int k = 0; k < 8; ++k) {
