@@ -19,6 +19,7 @@ EXPORTS = (
     "cvtpm_version", "cvtpm_status_string", "cvtpm_params_default", "cvtpm_create", "cvtpm_destroy",
     "cvtpm_set_params", "cvtpm_get_params", "cvtpm_last_error", "cvtpm_synchronize", "cvtpm_depthmap",
     "cvtpm_depthmap_host", "cvtpm_cost_eval", "cvtpm_cost_adjoint", "cvtpm_depthmap_batched", "cvtpm_set_memory_budget",
+    "cvtpm_set_batch_lanes", "cvtpm_get_batch_info",
     "cvtpm_set_timing", "cvtpm_reset_stats", "cvtpm_get_stats", "cvtpm_tool_fp32_peak",
     "cvtpm_cost_eval_noalloc",
 )
@@ -32,6 +33,23 @@ class CvtpmPair(ctypes.Structure):
     _fields_ = [("left", ctypes.c_void_p), ("right", ctypes.c_void_p), ("width", ctypes.c_int),
                 ("height", ctypes.c_int), ("pitch", ctypes.c_size_t), ("depthmax", ctypes.c_float),
                 ("dmap", ctypes.c_void_p), ("dmap_pitch", ctypes.c_size_t)]
+
+
+BATCH_MAX_CAND = 8
+
+
+class CvtpmBatchInfo(ctypes.Structure):
+    _fields_ = [("lanes", ctypes.c_int), ("volumes", ctypes.c_int), ("tuned", ctypes.c_int), ("ncand", ctypes.c_int),
+                ("cand_lanes", ctypes.c_int * BATCH_MAX_CAND), ("cand_volumes", ctypes.c_int * BATCH_MAX_CAND),
+                ("cand_ms", ctypes.c_float * BATCH_MAX_CAND), ("graph_nodes", ctypes.c_longlong),
+                ("replays", ctypes.c_longlong)]
+
+    def as_dict(self) -> dict:
+        n = self.ncand
+        return {"lanes": self.lanes, "volumes": self.volumes, "tuned": self.tuned,
+                "candidates": [{"lanes": self.cand_lanes[i], "volumes": self.cand_volumes[i], "proxy_ms": self.cand_ms[i]}
+                               for i in range(n)],
+                "graph_nodes": self.graph_nodes, "replays": self.replays}
 
 
 class CvtpmStats(ctypes.Structure):
@@ -79,6 +97,8 @@ def lib() -> ctypes.CDLL:
     L.cvtpm_depthmap_batched.argtypes = [vp, ctypes.POINTER(CvtpmPair), i, vp]
     L.cvtpm_set_timing.argtypes = [vp, i]
     L.cvtpm_set_memory_budget.argtypes = [vp, sz]
+    L.cvtpm_set_batch_lanes.argtypes = [vp, i]
+    L.cvtpm_get_batch_info.argtypes = [vp, ctypes.POINTER(CvtpmBatchInfo)]
     L.cvtpm_reset_stats.argtypes = [vp]
     L.cvtpm_get_stats.argtypes = [vp, ctypes.POINTER(CvtpmStats)]
     L.cvtpm_tool_fp32_peak.argtypes = [i, vp, ctypes.POINTER(ctypes.c_float)]

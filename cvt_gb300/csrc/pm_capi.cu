@@ -13,6 +13,7 @@
  *  - the view-candidate buffers hold source positions instead of copies of
  *    the candidate planes (k_view_list).
  */
+#include <algorithm>
 #include <cstdio>
 #include <cstring>
 #include <mutex>
@@ -52,6 +53,22 @@ struct cvtpm_ctx {
     bool vol_on = false;
     float* wvol[2] = {nullptr, nullptr};
     float* nbcost = nullptr;
+    /* set while a launch sequence is being captured into a graph: scratch
+     * must already be sized, nothing may be allocated */
+    bool no_alloc = false;
+    /* cvtpm_depthmap_batched: lanes (own scratch and stream each), the
+     * captured graph of the last batch and the tuning record */
+    struct Lane { cvtpm_ctx* c = nullptr; cudaStream_t s = nullptr; cudaEvent_t done = nullptr; };
+    std::vector<Lane> lanes;
+    cudaStream_t bstream = nullptr;
+    cudaEvent_t bfork = nullptr, bjoin = nullptr;
+    cudaGraphExec_t bexec = nullptr;
+    std::vector<unsigned char> bkey;
+    std::vector<unsigned char> tkey;   /* shapes of the last tuned batch (no pointers) */
+    int tuned_lanes = 0;
+    bool tuned_vol = false;
+    int batch_lanes = 0;              /* 0: autotune */
+    cvtpm_batch_info binfo{};
     /* staging for the *_host entry points */
     void* stage = nullptr;
     size_t stage_bytes = 0;
@@ -163,6 +180,7 @@ cvtpm_status ensure_buffers(cvtpm_ctx* ctx, int W, int H) {
     add((void**)&ctx->valid, n);
     const size_t need = align_up(off, 256);
     if (need > ctx->pool_bytes) {
+        if (ctx->no_alloc) return fail(ctx, CVTPM_ERR_ALLOC, "scratch not sized before capture");
         if (ctx->pool) { cudaFree(ctx->pool); ctx->pool = nullptr; ctx->pool_bytes = 0; }
         cudaError_t e = cudaMalloc(&ctx->pool, need);
         if (e != cudaSuccess) { ctx->pool = nullptr; return fail(ctx, CVTPM_ERR_ALLOC, std::string("scratch allocation: ") + cudaGetErrorString(e)); }
@@ -223,6 +241,7 @@ cvtpm_status ensure_volumes(cvtpm_ctx* ctx, int W, int H, int P) {
     ctx->vol_on = false;
     if (need > ctx->vol_budget) return CVTPM_OK;
     if (ctx->vol_bytes < need) {
+        if (ctx->no_alloc) return CVTPM_OK;          /* capturing: per-pixel neighbours */
         if (ctx->vol) { CK(cudaFree(ctx->vol), "free volumes"); ctx->vol = nullptr; ctx->vol_bytes = 0; }
         size_t fr = 0, tot = 0;
         CK(cudaMemGetInfo(&fr, &tot), "memory info");
@@ -323,6 +342,7 @@ cvtpm_status run_depthmap(cvtpm_ctx* ctx, const cvtpm_params& p, float* dmap, si
         }
     }
     if (!ctx->dcount) {
+        if (ctx->no_alloc) return fail(ctx, CVTPM_ERR_ALLOC, "counters not allocated before capture");
         CK(cudaMalloc(&ctx->dcount, 2 * sizeof(unsigned long long)), "counters");
         CK(cudaMemset(ctx->dcount, 0, 2 * sizeof(unsigned long long)), "counters");
     }
@@ -455,6 +475,20 @@ cvtpm_status cvtpm_create(cvtpm_ctx** out, int device) {
     if (!c) return CVTPM_ERR_ALLOC;
     c->device = device;
     cvtpm_params_default(&c->prm, CVTPM_PRESET_REFERENCE);
+    {
+        static std::mutex mu;
+        static std::vector<int> prepared;
+        std::lock_guard<std::mutex> lk(mu);
+        bool done = false;
+        for (int d : prepared) done |= d == device;
+        if (!done) {
+            if (cudaSetDevice(device) != cudaSuccess || pm_prepare_kernels() != cudaSuccess) {
+                delete c;
+                return CVTPM_ERR_CUDA;
+            }
+            prepared.push_back(device);
+        }
+    }
     *out = c;
     return CVTPM_OK;
 }
@@ -463,6 +497,15 @@ cvtpm_status cvtpm_destroy(cvtpm_ctx* ctx) {
     if (!ctx) return CVTPM_ERR_INVALID_ARGUMENT;
     cudaSetDevice(ctx->device);
     if (ctx->pool) cudaFree(ctx->pool);
+    if (ctx->bexec) cudaGraphExecDestroy(ctx->bexec);
+    for (auto& l : ctx->lanes) {
+        if (l.c) cvtpm_destroy(l.c);
+        if (l.s) cudaStreamDestroy(l.s);
+        if (l.done) cudaEventDestroy(l.done);
+    }
+    if (ctx->bstream) cudaStreamDestroy(ctx->bstream);
+    if (ctx->bfork) cudaEventDestroy(ctx->bfork);
+    if (ctx->bjoin) cudaEventDestroy(ctx->bjoin);
     if (ctx->stage) cudaFree(ctx->stage);
     if (ctx->vol) cudaFree(ctx->vol);
     if (ctx->dcount) cudaFree(ctx->dcount);
@@ -661,8 +704,251 @@ cvtpm_status cvtpm_cost_adjoint(cvtpm_ctx* ctx, const float* img1, const float* 
     return CVTPM_OK;
 }
 
-cvtpm_status cvtpm_depthmap_batched(cvtpm_ctx* ctx, const cvtpm_pair*, int, void*) {
-    return fail(ctx, CVTPM_ERR_NOT_SUPPORTED, "batched path not built yet");
+/* ---------------------------------------------------------- batched -- */
+namespace {
+
+cvtpm_status check_pair(cvtpm_ctx* ctx, const cvtpm_pair& q, int i) {
+    const std::string w = "pair " + std::to_string(i);
+    cvtpm_status s;
+    if ((s = check_image(ctx, q.left, q.width, q.height, q.pitch, (w + " left").c_str())) != CVTPM_OK) return s;
+    if ((s = check_image(ctx, q.right, q.width, q.height, q.pitch, (w + " right").c_str())) != CVTPM_OK) return s;
+    if (!(q.depthmax > 0.0f)) return fail(ctx, CVTPM_ERR_INVALID_ARGUMENT, w + ": depthmax must be > 0");
+    if (!q.dmap || q.dmap_pitch % 4 != 0 || q.dmap_pitch < (size_t)q.width * 4)
+        return fail(ctx, CVTPM_ERR_INVALID_ARGUMENT, w + ": dmap is NULL or its pitch is too small");
+    return CVTPM_OK;
+}
+
+/* Lanes: each has its own context (scratch, weight volumes, counters) and
+ * stream, so the pairs of different lanes run concurrently. */
+cvtpm_status ensure_lanes(cvtpm_ctx* ctx, int k) {
+    while ((int)ctx->lanes.size() < k) {
+        cvtpm_ctx::Lane l;
+        cvtpm_status s = cvtpm_create(&l.c, ctx->device);
+        if (s != CVTPM_OK) return fail(ctx, s, "lane context");
+        CK(cudaStreamCreateWithFlags(&l.s, cudaStreamNonBlocking), "lane stream");
+        CK(cudaEventCreateWithFlags(&l.done, cudaEventDisableTiming), "lane event");
+        CK(cudaMalloc(&l.c->dcount, 2 * sizeof(unsigned long long)), "lane counters");
+        CK(cudaMemset(l.c->dcount, 0, 2 * sizeof(unsigned long long)), "lane counters");
+        ctx->lanes.push_back(l);
+    }
+    if (!ctx->bstream) {
+        CK(cudaStreamCreateWithFlags(&ctx->bstream, cudaStreamNonBlocking), "batch stream");
+        CK(cudaEventCreateWithFlags(&ctx->bfork, cudaEventDisableTiming), "batch event");
+        CK(cudaEventCreateWithFlags(&ctx->bjoin, cudaEventDisableTiming), "batch event");
+    }
+    return CVTPM_OK;
+}
+
+/* Longest-processing-time assignment of pairs to k lanes (work ~ W*H). */
+std::vector<std::vector<int>> assign_lanes(const cvtpm_pair* pairs, int npairs, int k) {
+    std::vector<int> order(npairs);
+    for (int i = 0; i < npairs; ++i) order[i] = i;
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
+        return (size_t)pairs[a].width * pairs[a].height > (size_t)pairs[b].width * pairs[b].height;
+    });
+    std::vector<std::vector<int>> out(k);
+    std::vector<size_t> load(k, 0);
+    for (int i : order) {
+        int best = 0;
+        for (int j = 1; j < k; ++j)
+            if (load[j] < load[best]) best = j;
+        out[best].push_back(i);
+        load[best] += (size_t)pairs[i].width * pairs[i].height;
+    }
+    return out;
+}
+
+/* Captures the whole batch (every pair's depthMap schedule, lanes as
+ * parallel branches) into one graph and instantiates it. */
+cvtpm_status capture_batch(cvtpm_ctx* ctx, const cvtpm_pair* pairs, int npairs, int k, bool volumes, int iterations,
+                           cudaGraphExec_t* exec, size_t* nodes) {
+    cvtpm_status s;
+    if ((s = ensure_lanes(ctx, k)) != CVTPM_OK) return s;
+    const auto plan = assign_lanes(pairs, npairs, k);
+    cvtpm_params p = ctx->prm;
+    p.iterations = iterations;
+    /* size every lane for its pairs and load the tables, outside the capture */
+    for (int j = 0; j < k; ++j) {
+        cvtpm_ctx* c = ctx->lanes[j].c;
+        c->prm = p;
+        if ((s = cvtpm_set_memory_budget(c, volumes ? ctx->vol_budget : 0)) != CVTPM_OK) return fail(ctx, s, c->err);
+        c->timing = false;
+        for (int i : plan[j]) {
+            if ((s = ensure_buffers(c, pairs[i].width, pairs[i].height)) != CVTPM_OK) return fail(ctx, s, c->err);
+            if (p.arith == CVTPM_ARITH_FAST &&
+                (s = ensure_volumes(c, pairs[i].width, pairs[i].height, p.patchsize)) != CVTPM_OK)
+                return fail(ctx, s, c->err);
+        }
+    }
+    if (k > 0 && (s = ensure_tables(ctx->lanes[0].c, p, ctx->bstream)) != CVTPM_OK) return fail(ctx, s, ctx->lanes[0].c->err);
+    CK(cudaStreamSynchronize(ctx->bstream), "batch prepare");
+    CK(cudaStreamBeginCapture(ctx->bstream, cudaStreamCaptureModeThreadLocal), "begin capture");
+    cvtpm_status err = CVTPM_OK;
+    std::string msg;
+    auto note = [&](cvtpm_status st, const std::string& m) { if (err == CVTPM_OK && st != CVTPM_OK) { err = st; msg = m; } };
+    note(cudaEventRecord(ctx->bfork, ctx->bstream) == cudaSuccess ? CVTPM_OK : CVTPM_ERR_CUDA, "fork");
+    for (int j = 0; j < k && err == CVTPM_OK; ++j) {
+        cvtpm_ctx::Lane& l = ctx->lanes[j];
+        note(cudaStreamWaitEvent(l.s, ctx->bfork, 0) == cudaSuccess ? CVTPM_OK : CVTPM_ERR_CUDA, "fork wait");
+        l.c->no_alloc = true;
+        for (int i : plan[j]) {
+            if (err != CVTPM_OK) break;
+            const cvtpm_pair& q = pairs[i];
+            cvtpm_params pq = p;
+            pq.depthmax = q.depthmax;
+            cvtpm_status st = run_depthmap(l.c, pq, q.dmap, q.dmap_pitch, q.left, q.right, q.width, q.height, q.pitch,
+                                           nullptr, 0, nullptr, l.s);
+            note(st, "pair " + std::to_string(i) + ": " + l.c->err);
+        }
+        l.c->no_alloc = false;
+        note(cudaEventRecord(l.done, l.s) == cudaSuccess ? CVTPM_OK : CVTPM_ERR_CUDA, "join record");
+        note(cudaStreamWaitEvent(ctx->bstream, l.done, 0) == cudaSuccess ? CVTPM_OK : CVTPM_ERR_CUDA, "join wait");
+    }
+    cudaGraph_t graph = nullptr;
+    cudaError_t e = cudaStreamEndCapture(ctx->bstream, &graph);
+    if (err != CVTPM_OK) { if (graph) cudaGraphDestroy(graph); return fail(ctx, err, msg); }
+    if (e != cudaSuccess) { if (graph) cudaGraphDestroy(graph); return cuda_fail(ctx, e, "end capture"); }
+    *nodes = 0;
+    cudaGraphGetNodes(graph, nullptr, nodes);
+    e = cudaGraphInstantiate(exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "graph instantiate");
+    return CVTPM_OK;
+}
+
+/* Runs a graph on the caller's stream order (the graph lives on the batch
+ * stream, which waits for `st` before and is waited on after). */
+cvtpm_status launch_batch(cvtpm_ctx* ctx, cudaGraphExec_t exec, cudaStream_t st) {
+    CK(cudaEventRecord(ctx->bjoin, st), "batch order");
+    CK(cudaStreamWaitEvent(ctx->bstream, ctx->bjoin, 0), "batch order");
+    CK(cudaGraphLaunch(exec, ctx->bstream), "graph launch");
+    CK(cudaEventRecord(ctx->bjoin, ctx->bstream), "batch order");
+    CK(cudaStreamWaitEvent(st, ctx->bjoin, 0), "batch order");
+    return CVTPM_OK;
+}
+
+/* The autotuner: times a one-iteration proxy of the batch (one graph launch
+ * each) for 1, 2, 4 and 8 lanes with the shared-window weight volumes
+ * allowed (FAST), then the best lane count without them, and keeps the
+ * fastest. */
+cvtpm_status tune_batch(cvtpm_ctx* ctx, const cvtpm_pair* pairs, int npairs, int* lanes_out, bool* vol_out) {
+    const bool fast = ctx->prm.arith == CVTPM_ARITH_FAST;
+    std::vector<std::pair<int, bool>> cand;
+    for (int k : {1, 2, 4, 8})
+        if (k == 1 || k <= npairs) cand.push_back({k, fast && ctx->vol_budget > 0});
+    cvtpm_batch_info& bi = ctx->binfo;
+    bi.ncand = 0;
+    float best = 0.0f;
+    cudaEvent_t t0, t1;
+    CK(cudaEventCreate(&t0), "tune event");
+    CK(cudaEventCreate(&t1), "tune event");
+    for (size_t ci = 0; ci < cand.size(); ++ci) {
+        {
+            const int k = cand[ci].first;
+            const bool vol = cand[ci].second;
+            cudaGraphExec_t ex = nullptr;
+            size_t nodes = 0;
+            cvtpm_status s = capture_batch(ctx, pairs, npairs, k, vol, 1, &ex, &nodes);
+            if (s != CVTPM_OK) { cudaEventDestroy(t0); cudaEventDestroy(t1); return s; }
+            float ms = 0.0f;
+            bool ok = cudaEventRecord(t0, ctx->bstream) == cudaSuccess &&
+                      cudaGraphLaunch(ex, ctx->bstream) == cudaSuccess &&
+                      cudaEventRecord(t1, ctx->bstream) == cudaSuccess &&
+                      cudaEventSynchronize(t1) == cudaSuccess &&
+                      cudaEventElapsedTime(&ms, t0, t1) == cudaSuccess;
+            cudaGraphExecDestroy(ex);
+            if (!ok) { cudaEventDestroy(t0); cudaEventDestroy(t1); return cuda_fail(ctx, cudaGetLastError(), "tuning run"); }
+            if (bi.ncand < CVTPM_BATCH_MAX_CAND) {
+                bi.cand_lanes[bi.ncand] = k;
+                bi.cand_volumes[bi.ncand] = vol ? 1 : 0;
+                bi.cand_ms[bi.ncand] = ms;
+                ++bi.ncand;
+            }
+            if (best == 0.0f || ms < best) { best = ms; *lanes_out = k; *vol_out = vol; }
+        }
+        if (ci + 1 == cand.size() && cand.back().second)     /* then the best lane count without volumes */
+            cand.push_back({*lanes_out, false});
+    }
+    cudaEventDestroy(t0);
+    cudaEventDestroy(t1);
+    return CVTPM_OK;
+}
+
+}  // namespace
+
+cvtpm_status cvtpm_depthmap_batched(cvtpm_ctx* ctx, const cvtpm_pair* pairs, int npairs, void* stream) {
+    if (!ctx) return CVTPM_ERR_INVALID_ARGUMENT;
+    if (!pairs || npairs < 1) return fail(ctx, CVTPM_ERR_INVALID_ARGUMENT, "no pairs");
+    cvtpm_status s;
+    if ((s = check_params(ctx, ctx->prm)) != CVTPM_OK) return s;
+    for (int i = 0; i < npairs; ++i)
+        if ((s = check_pair(ctx, pairs[i], i)) != CVTPM_OK) return s;
+    CK(cudaSetDevice(ctx->device), "cudaSetDevice");
+    cudaStream_t st = (cudaStream_t)stream;
+    /* the graph of the previous call is replayed when nothing changed */
+    std::vector<unsigned char> key;
+    auto put = [&](const void* v, size_t nb) { key.insert(key.end(), (const unsigned char*)v, (const unsigned char*)v + nb); };
+    const cvtpm_params& pr = ctx->prm;          /* field by field: no padding bytes in the key */
+    put(&pr.patchsize, sizeof(int)); put(&pr.depthmax, sizeof(float)); put(&pr.iterations, sizeof(int));
+    put(&pr.viewsamples, sizeof(int)); put(&pr.dscale, sizeof(float)); put(&pr.maxdispdiff, sizeof(float));
+    put(&pr.maxanglediff, sizeof(float)); put(&pr.thetascale, sizeof(float)); put(&pr.pd_iterations, sizeof(int));
+    put(&pr.color_weight, sizeof(float)); put(&pr.color_alpha, sizeof(float)); put(&pr.color_maxdiff, sizeof(float));
+    put(&pr.grad_maxdiff, sizeof(float)); put(&pr.weight_profile, sizeof(int)); put(&pr.rng, sizeof(int));
+    put(&pr.seed, sizeof(uint64_t)); put(&pr.arith, sizeof(int)); put(&pr.schedule, sizeof(int));
+    put(&ctx->batch_lanes, sizeof(int));
+    put(&ctx->vol_budget, sizeof(size_t));
+    for (int i = 0; i < npairs; ++i) {
+        const cvtpm_pair& q = pairs[i];
+        put(&q.width, sizeof(int)); put(&q.height, sizeof(int)); put(&q.depthmax, sizeof(float));
+    }
+    const std::vector<unsigned char> tkey = key;       /* parameters and shapes */
+    for (int i = 0; i < npairs; ++i) {
+        const cvtpm_pair& q = pairs[i];
+        put(&q.left, sizeof(void*)); put(&q.right, sizeof(void*)); put(&q.pitch, sizeof(size_t));
+        put(&q.dmap, sizeof(void*)); put(&q.dmap_pitch, sizeof(size_t));
+    }
+    if (ctx->bexec && key == ctx->bkey) {
+        ++ctx->binfo.replays;
+        return launch_batch(ctx, ctx->bexec, st);
+    }
+    if (ctx->bexec) { cudaGraphExecDestroy(ctx->bexec); ctx->bexec = nullptr; ctx->bkey.clear(); }
+    if ((s = ensure_lanes(ctx, 1)) != CVTPM_OK) return s;
+    CK(cudaStreamSynchronize(st), "batch order");      /* inputs written on `st` before tuning reads them */
+    int k = ctx->batch_lanes;
+    bool vol = ctx->prm.arith == CVTPM_ARITH_FAST && ctx->vol_budget > 0;
+    ctx->binfo.tuned = 0;
+    if (k <= 0) {
+        if (tkey == ctx->tkey) {                         /* same shapes: keep the tuned choice */
+            k = ctx->tuned_lanes;
+            vol = ctx->tuned_vol;
+        } else {
+            if ((s = tune_batch(ctx, pairs, npairs, &k, &vol)) != CVTPM_OK) return s;
+            ctx->tkey = tkey;
+            ctx->tuned_lanes = k;
+            ctx->tuned_vol = vol;
+        }
+        ctx->binfo.tuned = 1;
+    }
+    size_t nodes = 0;
+    if ((s = capture_batch(ctx, pairs, npairs, k, vol, ctx->prm.iterations, &ctx->bexec, &nodes)) != CVTPM_OK) return s;
+    ctx->bkey = key;
+    ctx->binfo.lanes = k;
+    ctx->binfo.volumes = vol ? 1 : 0;
+    ctx->binfo.graph_nodes = (long long)nodes;
+    ctx->binfo.replays = 0;
+    return launch_batch(ctx, ctx->bexec, st);
+}
+
+cvtpm_status cvtpm_set_batch_lanes(cvtpm_ctx* ctx, int lanes) {
+    if (!ctx || lanes < 0 || lanes > 64) return CVTPM_ERR_INVALID_ARGUMENT;
+    ctx->batch_lanes = lanes;
+    return CVTPM_OK;
+}
+
+cvtpm_status cvtpm_get_batch_info(const cvtpm_ctx* ctx, cvtpm_batch_info* out) {
+    if (!ctx || !out) return CVTPM_ERR_INVALID_ARGUMENT;
+    *out = ctx->binfo;
+    return CVTPM_OK;
 }
 
 cvtpm_status cvtpm_tool_fp32_peak(int device, void* stream, float* tflops) {

@@ -783,12 +783,16 @@ cudaError_t pm_launch_fill_output(const float4* in, int W, int H, float scale, f
 
 int pm_pd_block_steps() { return PDB_K; }
 
+static const size_t kPdBlockSmem = (size_t)PDB_N * (4 * sizeof(float4) + 2 * sizeof(float));
+
+cudaError_t pm_prepare_kernels() {
+    return cudaFuncSetAttribute(k_pd_block, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kPdBlockSmem);
+}
+
 cudaError_t pm_launch_pd_block(float4* uout, float4* pout, const float4* uin, const float4* pin, int pzero,
                                const float4* f, const float* wgt, float lambda, int nsteps, int W, int H,
                                cudaStream_t st) {
-    const size_t smem = (size_t)PDB_N * (4 * sizeof(float4) + 2 * sizeof(float));
-    cudaError_t e = cudaFuncSetAttribute(k_pd_block, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return e;
+    const size_t smem = kPdBlockSmem;
     dim3 b(PDB_TX, PDB_TY), g((W + PDB_TX - 1) / PDB_TX, (H + PDB_TY - 1) / PDB_TY);
     k_pd_block<<<g, b, smem, st>>>(uout, pout, uin, pin, pzero, f, wgt, lambda, nsteps, W, H);
     PM_LAUNCH_CHECK();

@@ -49,6 +49,10 @@ cudaError_t pm_launch_pd_step(float4* uout, float4* pout, const float4* last, co
                               const float4* f, const float* wgt, float lambda, int W, int H,
                               cudaStream_t st);
 
+/* Kernel attributes (dynamic shared memory limits) for the current device;
+ * call once per device before the first launch or stream capture. */
+cudaError_t pm_prepare_kernels();
+
 int pm_pd_block_steps();
 cudaError_t pm_launch_pd_block(float4* uout, float4* pout, const float4* uin, const float4* pin, int pzero,
                                const float4* f, const float* wgt, float lambda, int nsteps, int W, int H,

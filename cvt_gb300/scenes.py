@@ -168,6 +168,26 @@ def make_scene(width: int, height: int, nplanes: int, dmax: float, seed: int,
                        occluded=occ, planes=planes, labels=labels, dmax=float(dmax))
 
 
+def batch_shapes(npairs: int = 64, seed: int = 3000):
+    """Pair shapes of the batched workload: widths uniform in 320-1920,
+    heights in 240-1080, disparity ranges 32-256 px, 4-24 planes; returns
+    (width, height, dmax, nplanes, scene seed) per pair."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for i in range(npairs):
+        w = int(rng.integers(320, 1921))
+        h = int(rng.integers(240, 1081))
+        dmax = float(rng.integers(32, 257))
+        nplanes = int(rng.integers(4, 25))
+        out.append((w, h, dmax, nplanes, seed + 1 + i))
+    return out
+
+
+def batch_scene(shape) -> StereoScene:
+    w, h, dmax, nplanes, seed = shape
+    return make_scene(w, h, nplanes, dmax, seed)
+
+
 def config_scene(index: int, pair: int = 0) -> StereoScene:
     """The scene of a named workload, seeded 1000*config + pair.
 

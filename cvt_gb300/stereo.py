@@ -164,6 +164,42 @@ class PMHuberStereo:
         self._check(rc)
         return out
 
+    def depthMapBatched(self, pairs, outs=None, stream=None):
+        """cvtpm_depthmap_batched.  pairs: list of (left, right, depthmax) with
+        left/right (H, W, 4) float32 CUDA tensors; returns the (H, W) disparity
+        maps (scaled like depthMap: dscale, or 1/depthmax per pair).  Passing
+        the returned maps back as `outs` (same inputs) replays the captured
+        graph instead of capturing a new one."""
+        arr = (_lib.CvtpmPair * len(pairs))()
+        if outs is None:
+            outs = [None] * len(pairs)
+        outs = list(outs)
+        for i, (left, right, dmax) in enumerate(pairs):
+            _check_img(left, "left")
+            _check_img(right, "right")
+            if left.shape != right.shape or left.stride(0) != right.stride(0):
+                raise CVTException(f"pair {i}: left/right shapes or pitches differ")
+            H, W = left.shape[:2]
+            d = outs[i]
+            if d is None or tuple(d.shape) != (H, W) or not d.is_contiguous() or d.dtype != torch.float32:
+                d = torch.empty((H, W), dtype=torch.float32, device=left.device)
+            outs[i] = d
+            arr[i] = _lib.CvtpmPair(left.data_ptr(), right.data_ptr(), W, H, left.stride(0) * 4, float(dmax),
+                                    d.data_ptr(), W * 4)
+        self._batch_keep = (arr, outs, list(pairs))
+        st = _stream_ptr(pairs[0][0]) if stream is None else stream
+        self._check(_lib.lib().cvtpm_depthmap_batched(self._h, arr, len(pairs), st))
+        return outs
+
+    def set_batch_lanes(self, lanes: int) -> None:
+        """Fix the lane count of depthMapBatched (0: autotune)."""
+        self._check(_lib.lib().cvtpm_set_batch_lanes(self._h, int(lanes)))
+
+    def batch_info(self) -> dict:
+        info = _lib.CvtpmBatchInfo()
+        self._check(_lib.lib().cvtpm_get_batch_info(self._h, ctypes.byref(info)))
+        return info.as_dict()
+
     def set_memory_budget(self, nbytes: int) -> None:
         """Device bytes the FAST path may use for its shared-window weight
         volumes (0: evaluate neighbours per pixel; results are the same)."""

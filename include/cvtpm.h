@@ -221,9 +221,38 @@ cvtpm_status cvtpm_cost_eval_noalloc(const cvtpm_params* params,
                                      const float* states, float* cost,
                                      void* stream);
 
-/* Many pairs of uneven size in one graph-captured launch sequence. */
+/* PMHuberStereo::depthMap for many pairs of uneven size and disparity range
+ * (pair.depthmax) in one CUDA-graph launch; no counterpart in the reference,
+ * which handles one pair per call.  Each pair's result is bit-identical to
+ * cvtpm_depthmap on that pair with the context's parameters (normal map and
+ * trace are not produced).  The pairs are spread over lanes, each with its
+ * own scratch and stream; the whole launch sequence of every lane is captured
+ * into one graph, which is replayed while the context's parameters and the
+ * pair descriptors (pointers, sizes, depthmax) stay the same.  Capture and
+ * tuning synchronise `stream` once; replays do not.  With the lane count 0
+ * (default) the first call of a new batch runs the autotuner: it times
+ * one-iteration proxies of the batch for 1, 2, 4 and 8 lanes, with and
+ * without the FAST path's shared-window weight volumes, and keeps the
+ * fastest (cvtpm_get_batch_info reports the candidates). */
 cvtpm_status cvtpm_depthmap_batched(cvtpm_ctx* ctx, const cvtpm_pair* pairs,
                                     int npairs, void* stream);
+
+#define CVTPM_BATCH_MAX_CAND 8
+typedef struct cvtpm_batch_info {
+    int lanes;                 /* lanes of the current graph */
+    int volumes;               /* shared-window weight volumes allowed */
+    int tuned;                 /* 1 if the autotuner chose the configuration */
+    int ncand;
+    int cand_lanes[CVTPM_BATCH_MAX_CAND];
+    int cand_volumes[CVTPM_BATCH_MAX_CAND];
+    float cand_ms[CVTPM_BATCH_MAX_CAND];   /* one-iteration proxy time */
+    long long graph_nodes;
+    long long replays;
+} cvtpm_batch_info;
+
+/* Fix the lane count of cvtpm_depthmap_batched (0: autotune). */
+cvtpm_status cvtpm_set_batch_lanes(cvtpm_ctx* ctx, int lanes);
+cvtpm_status cvtpm_get_batch_info(const cvtpm_ctx* ctx, cvtpm_batch_info* out);
 
 #ifdef __cplusplus
 }
