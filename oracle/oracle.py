@@ -69,6 +69,12 @@ def lib():
         L.orc_depthmap.argtypes = [P, f32p, f32p, c_int, c_int, f32p, ctypes.c_void_p, ctypes.c_void_p,
                                    ctypes.c_void_p, ctypes.c_void_p]
         L.orc_depthmap.restype = c_int
+        L.orc_depthmap_inpaint.argtypes = [P, f32p, f32p, c_int, c_int, f32p, ctypes.c_void_p, ctypes.c_void_p,
+                                           ctypes.c_void_p]
+        L.orc_depthmap_inpaint.restype = c_int
+        L.orc_occmap.argtypes = [f32p, f32p, c_int, c_int, c_float, c_int, f32p]
+        L.orc_normal_depth.argtypes = [f32p, c_int, c_int, c_float, c_int, f32p]
+        L.orc_pd_apply_inpaint.argtypes = [f32p, f32p, f32p, f32p, c_float, c_int, c_int, c_int]
         f64p = np.ctypeslib.ndpointer(np.float64, flags="C_CONTIGUOUS")
         L.orc_cost_field_f64.argtypes = [P, f32p, f32p, c_int, c_int, f32p, ctypes.c_double, f64p, u8p]
         L.orc_cost_field_f64.restype = c_int
@@ -264,3 +270,41 @@ def depthmap(params: CvtpmParams, left, right, normalmap: bool = False, trace: b
     rc = lib().orc_depthmap(ctypes.byref(params), left, right, w, h, dmap, _ptr(nm), _ptr(st), _ptr(win), _ptr(val))
     assert rc == 0, rc
     return dmap, {"normalmap": nm, "states": st, "winners": win, "valid": val}
+
+
+def depthmap_inpaint(params: CvtpmParams, left, right, trace: bool = False):
+    """PMHuberStereo::depthMapInpaint on the CPU.  Returns (dmap in pixels,
+    extras) with extras 'states' (2,H,W,4), 'winners' (2,H,W), 'valid' (H,W)."""
+    left, right = _f32(left), _f32(right)
+    h, w = left.shape[:2]
+    dmap = np.empty((h, w), np.float32)
+    st = np.empty((2, h, w, 4), np.float32) if trace else None
+    win = np.empty((2, h, w), np.uint8) if trace else None
+    val = np.empty((h, w), np.uint8) if trace else None
+    rc = lib().orc_depthmap_inpaint(ctypes.byref(params), left, right, w, h, dmap, _ptr(st), _ptr(win), _ptr(val))
+    assert rc == 0, rc
+    return dmap, {"states": st, "winners": win, "valid": val}
+
+
+def occmap(L, R, maxdiff, lr):
+    L, R = _f32(L), _f32(R)
+    h, w = L.shape[:2]
+    out = np.empty((h, w), np.float32)
+    lib().orc_occmap(L, R, w, h, float(maxdiff), int(lr), out)
+    return out
+
+
+def normal_depth(states, depthmax, lr):
+    states = _f32(states)
+    h, w = states.shape[:2]
+    out = np.empty((h, w, 4), np.float32)
+    lib().orc_normal_depth(states, w, h, float(depthmax), int(lr), out)
+    return out
+
+
+def pd_apply_inpaint(output, inp, wgt, mask, lam, iters):
+    out = _f32(output).copy()
+    inp, wgt, mask = _f32(inp), _f32(wgt), _f32(mask)
+    h, w = inp.shape[:2]
+    lib().orc_pd_apply_inpaint(out, inp, wgt, mask, float(lam), int(iters), w, h)
+    return out

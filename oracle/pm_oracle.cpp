@@ -516,6 +516,38 @@ static void consistency(const F4* L, const F4* R, int W, int H, float maxdisp, f
         }
 }
 
+/* pmhstereo_occmap, pmhstereo.cl:682-712: the test of the consistency check
+ * with the angle bound fixed at 5 degrees; 1 where both views agree. */
+static void occmap(const F4* L, const F4* R, int W, int H, float maxdiff, int lr, float* mask) {
+    const float athr = 5.0f / 180.0f;
+#pragma omp parallel for schedule(static)
+    for (int y = 0; y < H; ++y)
+        for (int x = 0; x < W; ++x) {
+            F4 sl = L[(size_t)y * W + x];
+            float x2 = transform_x(sl, (float)x, (float)y);
+            F4 sr;
+            if (x2 < 0 || x2 >= (float)W) sr = f4s(1e5f);
+            else sr = R[(size_t)y * W + clampi(f2i_nan0(roundf(x2)), 0, W - 1)];
+            float na[3], nb[3];
+            if (lr) { to_normal(sl, na); to_normal(viewprop(sr), nb); }
+            else { to_normal(sr, na); to_normal(viewprop(sl), nb); }
+            float ndiff = (na[0] * nb[0] + na[1] * nb[1]) + na[2] * nb[2];
+            float dm = fabsf((float)x - transform_x(sr, x2, (float)y));
+            bool bad = (dm >= maxdiff) || (pm_acospi(ndiff) >= athr);
+            mask[(size_t)y * W + x] = bad ? 0.0f : 1.0f;
+        }
+}
+
+/* pmhstereo_normal_depth, pmhstereo.cl:663-680: (n.x, n.y, d/dmax, 1). */
+static void normal_depth(const F4* in, int W, int H, float depthmax, int lr, F4* out) {
+#pragma omp parallel for schedule(static)
+    for (int y = 0; y < H; ++y)
+        for (int x = 0; x < W; ++x) {
+            F4 val = to_ref_normal_depth(in[(size_t)y * W + x], (float)x, (float)y, lr);
+            out[(size_t)y * W + x] = f4(val.x, val.y, val.w / depthmax, 1.0f);
+        }
+}
+
 /* nearest index to the left/right of each x whose value passes `ok` */
 template <class OK>
 static void row_neighbours(const F4* row, int W, OK ok, std::vector<int>& lft, std::vector<int>& rgt) {
@@ -600,8 +632,11 @@ static void fill_normalmap(const F4* in, int W, int H, F4* out) {      /* :557-6
 
 /* ------------------------------------------------------------ PD ROF -- */
 /* One PDHuberWeighted launch, PDHuberWeighted.cl:34-104. */
+/* mask != NULL: one PDHuberWeightedInpaint launch, PDHuberWeightedInpaint.cl:
+ * 34-102 — the dual projected per channel (:67) and the fidelity weight
+ * lambda * mask(x, y) (:82). */
 static void pd_step(F4* uout, F4* pout, const F4* last, const F4* pin, const F4* f,
-                    const float* wgt, float lambda, int W, int H) {
+                    const float* wgt, float lambda, int W, int H, const float* mask = nullptr) {
     const float SIGMA = 1.0f / sqrtf(8.0f), TAU = 1.0f / sqrtf(8.0f);
     const float THETA = 0.5f, ALPHA = 0.001f;
     auto U = [&](int x, int y) { return last[(size_t)clampi(y, 0, H - 1) * W + clampi(x, 0, W - 1)]; };
@@ -617,8 +652,13 @@ static void pd_step(F4* uout, F4* pout, const F4* last, const F4* pin, const F4*
         F4 l = (plo + SIGMA * dx) / f4s(den);
         F4 h = (phi + SIGMA * dy) / f4s(den);
         F4 pt = l * l + h * h;
-        float sxy = sqrtf(pt.x + pt.y);
-        F4 pproj = f4(fmaxf(1.0f, sxy), fmaxf(1.0f, sxy), fmaxf(1.0f, sqrtf(pt.z)), fmaxf(1.0f, sqrtf(0.0f)));
+        F4 pproj;
+        if (mask) {
+            pproj = f4(fmaxf(1.0f, sqrtf(pt.x)), fmaxf(1.0f, sqrtf(pt.y)), fmaxf(1.0f, sqrtf(pt.z)), fmaxf(1.0f, sqrtf(pt.w)));
+        } else {
+            float sxy = sqrtf(pt.x + pt.y);
+            pproj = f4(fmaxf(1.0f, sxy), fmaxf(1.0f, sxy), fmaxf(1.0f, sqrtf(pt.z)), fmaxf(1.0f, sqrtf(0.0f)));
+        }
         *lo = l / pproj; *hi = h / pproj;
     };
 #pragma omp parallel for schedule(static)
@@ -632,7 +672,7 @@ static void pd_step(F4* uout, F4* pout, const F4* last, const F4* pin, const F4*
             F4 img = f[(size_t)y * W + x];
             F4 uc = last[(size_t)y * W + x];
             float wc = wgt[(size_t)y * W + x];
-            F4 lam = f4s(lambda);
+            F4 lam = f4s(mask ? lambda * mask[(size_t)y * W + x] : lambda);
             F4 un = (uc + TAU * (lam * img - wc * div)) / (f4s(1.0f) + TAU * lam);  /* :76 */
             un = un + THETA * (un - uc);
             un.w = 1.0f;
@@ -642,8 +682,11 @@ static void pd_step(F4* uout, F4* pout, const F4* last, const F4* pin, const F4*
         }
 }
 
-/* PDROF::apply, cvt/gfx/PDROF.h:50-96.  `output` is read as the warm start. */
-static void pd_apply(F4* output, const F4* input, const float* wgt, float lambda, int iters, int W, int H) {
+/* PDROF::apply, cvt/gfx/PDROF.h:50-96 (mask == NULL), and
+ * PDROFInpaint::apply, cvt/gfx/PDROFInpaint.h:50-98 (mask: the occlusion
+ * map's x channel).  `output` is read as the warm start. */
+static void pd_apply(F4* output, const F4* input, const float* wgt, float lambda, int iters, int W, int H,
+                     const float* mask = nullptr) {
     size_t n = (size_t)W * H;
     std::vector<F4> tmp(input, input + n);
     std::vector<F4> p1(2 * n, f4s(0.0f)), p2(2 * n, f4s(0.0f));
@@ -652,9 +695,9 @@ static void pd_apply(F4* output, const F4* input, const float* wgt, float lambda
     int swap = 0;
     for (int i = 0; i < iters; ++i) {
         swap = i & 1;
-        pd_step(img[swap], pp[swap], img[1 - swap], pp[1 - swap], input, wgt, lambda, W, H);
+        pd_step(img[swap], pp[swap], img[1 - swap], pp[1 - swap], input, wgt, lambda, W, H, mask);
     }
-    if (!swap) pd_step(img[1], pp[1], img[0], pp[0], input, wgt, lambda, W, H);
+    if (!swap) pd_step(img[1], pp[1], img[0], pp[0], input, wgt, lambda, W, H, mask);
 }
 
 static float smoothstep01(float x) {                                   /* cvt/math/Math.h:88-92 */
@@ -1109,6 +1152,74 @@ int orc_depthmap(const cvtpm_params* prm, const float* left, const float* right,
     }
     if (winners) { memcpy(winners, winL.data(), n); memcpy(winners + n, winR.data(), n); }
     return CVTPM_OK;
+}
+
+/* PMHuberStereo::depthMapInpaint, PMHuberStereo.cpp:293-506: the depthMap
+ * schedule with the occlusion-masked smoother (PDROFInpaint, 100 steps,
+ * lambda = 20*theta + 5), theta ramped from iteration 4, the final check on
+ * state buffer 1 (the reference reads clmatches[1] whatever the iteration
+ * count, :491-496) with 1 px / 5 degrees, and the disparity in pixels
+ * (scale 1, :503).  states_out: the last propagation outputs. */
+int orc_depthmap_inpaint(const cvtpm_params* prm, const float* left, const float* right, int W, int H,
+                         float* dmap, float* states_out, uint8_t* winners, uint8_t* valid) {
+    if (!check_params(prm) || !left || !right || !dmap || W < 1 || H < 1) return CVTPM_ERR_INVALID_ARGUMENT;
+    const size_t n = (size_t)W * H;
+    const int N = prm->iterations;
+    const float dmax = prm->depthmax;
+    Views v;
+    make_views(left, right, W, H, prm->arith, v);
+    CostCfg k = make_cost_cfg(prm);
+    std::vector<float> wl(n), wr(n), mask(n);
+    edge_weight((const F4*)left, W, H, wl.data());
+    edge_weight((const F4*)right, W, H, wr.data());
+    std::vector<F4> smL(n, f4s(0.0f)), smR(n, f4s(0.0f));
+    std::vector<F4> SL[2] = {std::vector<F4>(n), std::vector<F4>(n)};
+    std::vector<F4> SR[2] = {std::vector<F4>(n), std::vector<F4>(n)};
+    std::vector<F4> tmp(n), tmp2(n);
+    std::vector<int16_t> list1(n * 4, -1), list2(n * 4, -1);
+    std::vector<uint8_t> winL(n, 0), winR(n, 0);
+    Pass pl = {&v.L, &v.R, &k, 1, 0, prm->rng, prm->seed, dmax, 0.0f};
+    Pass pr = {&v.R, &v.L, &k, 0, 0, prm->rng, prm->seed, dmax, 0.0f};
+    init_pass(pl, SL[0].data());                                       /* :345-363 */
+    init_pass(pr, SR[0].data());
+    float theta = 0.0f;
+    for (int iter = 0; iter < N; ++iter) {                             /* :371-482 */
+        int swap = iter & 1;
+        pl.iter = pr.iter = iter;
+        pl.theta = pr.theta = theta;
+        propagate_pass(pl, SL[swap].data(), smL.data(), list2.data(), SR[swap].data(), SL[1 - swap].data(), winL.data());
+        build_view_list(SL[1 - swap].data(), W, H, list1.data());
+        propagate_pass(pr, SR[swap].data(), smR.data(), list1.data(), SL[1 - swap].data(), SR[1 - swap].data(), winR.data());
+        build_view_list(SR[1 - swap].data(), W, H, list2.data());
+        const float lambda = theta * 20.0f + 5.0f;
+        occmap(SL[1 - swap].data(), SR[1 - swap].data(), W, H, 0.5f, 1, mask.data());
+        normal_depth(SL[1 - swap].data(), W, H, dmax, 1, tmp2.data());
+        pd_apply(smL.data(), tmp2.data(), wl.data(), lambda, 100, W, H, mask.data());
+        occmap(SR[1 - swap].data(), SL[1 - swap].data(), W, H, 0.5f, 0, mask.data());
+        normal_depth(SR[1 - swap].data(), W, H, dmax, 0, tmp2.data());
+        pd_apply(smR.data(), tmp2.data(), wr.data(), lambda, 100, W, H, mask.data());
+        if (iter >= 4) theta = smoothstep01(((float)iter - 4.0f) / ((float)N - 4.0f)) * 1.0f;
+    }
+    consistency(SL[1].data(), SR[1].data(), W, H, 1.0f, 5.0f, 1, tmp.data(), valid);
+    fill_depthmap(tmp.data(), W, H, 1.0f, dmap);
+    const int fin = 1 - ((N - 1) & 1);
+    if (states_out) {
+        memcpy(states_out, SL[fin].data(), n * sizeof(F4));
+        memcpy(states_out + 4 * n, SR[fin].data(), n * sizeof(F4));
+    }
+    if (winners) { memcpy(winners, winL.data(), n); memcpy(winners + n, winR.data(), n); }
+    return CVTPM_OK;
+}
+
+void orc_occmap(const float* L, const float* R, int W, int H, float maxdiff, int lr, float* mask) {
+    occmap((const F4*)L, (const F4*)R, W, H, maxdiff, lr, mask);
+}
+void orc_normal_depth(const float* in, int W, int H, float depthmax, int lr, float* out) {
+    normal_depth((const F4*)in, W, H, depthmax, lr, (F4*)out);
+}
+void orc_pd_apply_inpaint(float* output, const float* input, const float* wgt, const float* mask, float lambda,
+                          int iters, int W, int H) {
+    pd_apply((F4*)output, (const F4*)input, wgt, lambda, iters, W, H, mask);
 }
 
 /* FP64 cost of a fixed state field (FP32 images and states, widened);

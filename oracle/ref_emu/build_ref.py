@@ -3,7 +3,8 @@
 they lie, under /root/reference, and copies none into the repository), so it
 runs only where they are present.
 
-  1. translate.py rewrites cvt/cl/kernel/{pmhstereo,RNG,PDHuberWeighted,fill}.cl
+  1. translate.py rewrites cvt/cl/kernel/{pmhstereo,RNG,PDHuberWeighted,
+     PDHuberWeightedInpaint,fill}.cl
      into _build/ref_gen/*.inc (generated, never committed);
   2. one C++ unit per kernel file wraps its .inc in a namespace and registers
      the kernels with clemu;
@@ -25,7 +26,7 @@ REF = "/root/reference"
 GEN = os.path.join(ROOT, "_build", "ref_gen")
 OUT = os.path.join(ORACLE, "_ref")
 LIB = os.path.join(OUT, "libpmref.so")
-KERNEL_FILES = ["RNG", "pmhstereo", "PDHuberWeighted", "fill"]
+KERNEL_FILES = ["RNG", "pmhstereo", "PDHuberWeighted", "PDHuberWeightedInpaint", "fill"]
 
 sys.path.insert(0, HERE)
 import translate  # noqa: E402
@@ -112,7 +113,10 @@ def build(force: bool = False, verbose: bool = False) -> str | None:
             bad.append(src)
     if bad:
         raise RuntimeError(f"emulated reference: compile failed for {bad}")
-    subprocess.run(["g++", "-shared", "-fopenmp", "-o", LIB + ".tmp", *objs], check=True)
+    # -z now: every symbol bound at load.  Lazy binding would resolve symbols
+    # from inside the work-item fibers, on several threads at once, which
+    # crashed Python processes intermittently.
+    subprocess.run(["g++", "-shared", "-fopenmp", "-Wl,-z,now", "-o", LIB + ".tmp", *objs], check=True)
     os.replace(LIB + ".tmp", LIB)
     return LIB
 

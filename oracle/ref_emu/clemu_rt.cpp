@@ -4,11 +4,11 @@
  * row-major order (rows of groups spread over OpenMP threads), and work-items
  * of a group run as fibers in raster order so that barrier() suspends each
  * item until all items of the group reach it.  Fibers start on their own
- * stacks through makecontext and switch with _setjmp/_longjmp afterwards.
+ * stacks through makecontext and switch with swapcontext.
  */
-#include <setjmp.h>
 #include <ucontext.h>
 
+#include <cstdint>
 #include <cstdio>
 #include <cstdlib>
 #include <map>
@@ -31,7 +31,6 @@ const size_t STACK = 256 * 1024;
 
 struct Fiber {
     ucontext_t uc;
-    jmp_buf jb;
     char* stack = nullptr;
     int state = 0;            /* 0 fresh, 1 at a barrier, 2 done, 3 running */
     WorkItem wi;
@@ -40,7 +39,6 @@ struct Fiber {
 struct Sched {
     std::vector<Fiber> fibers;
     std::vector<char> stacks;
-    jmp_buf jb;
     ucontext_t uc;
     Fiber* cur = nullptr;
     const ItemFn* fn = nullptr;
@@ -50,30 +48,28 @@ struct Sched {
 thread_local Sched* t_sched = nullptr;
 thread_local std::vector<std::vector<char>> t_arena;
 
+/* Every switch between the scheduler and a work-item goes through
+ * swapcontext/setcontext, which also switch the shadow stack of processes
+ * that run with one (a longjmp onto another stack does not). */
 void trampoline() {
     Sched* s = t_sched;
     (*s->fn)(*s->args);
     s->cur->state = 2;
-    _longjmp(s->jb, 1);
+    setcontext(&s->uc);
 }
 
 void resume(Sched* s, Fiber* f) {
     s->cur = f;
     t_item = &f->wi;
-    if (_setjmp(s->jb) == 0) {
-        if (f->state == 0) {
-            getcontext(&f->uc);
-            f->uc.uc_stack.ss_sp = f->stack;
-            f->uc.uc_stack.ss_size = STACK;
-            f->uc.uc_link = nullptr;
-            makecontext(&f->uc, trampoline, 0);
-            f->state = 3;
-            swapcontext(&s->uc, &f->uc);
-        } else {
-            f->state = 3;
-            _longjmp(f->jb, 1);
-        }
+    if (f->state == 0) {
+        getcontext(&f->uc);
+        f->uc.uc_stack.ss_sp = f->stack;
+        f->uc.uc_stack.ss_size = STACK;
+        f->uc.uc_link = nullptr;
+        makecontext(&f->uc, trampoline, 0);
     }
+    f->state = 3;
+    swapcontext(&s->uc, &f->uc);
 }
 
 }  // namespace
@@ -83,13 +79,17 @@ void barrier(int) {
     if (!s) { fprintf(stderr, "clemu: barrier() in a kernel registered without barriers\n"); abort(); }
     Fiber* f = s->cur;
     f->state = 1;
-    if (_setjmp(f->jb) == 0) _longjmp(s->jb, 1);
+    swapcontext(&f->uc, &s->uc);
 }
 
+/* Local memory of argument `index`, 64-byte aligned: the kernels' local
+ * float8 buffers are 32-byte aligned types, and vector code may use aligned
+ * loads on them (std::vector storage alone guarantees only 16 bytes). */
 void* local_arena(int index, size_t bytes) {
     if ((int)t_arena.size() <= index) t_arena.resize(index + 1);
-    if (t_arena[index].size() < bytes) t_arena[index].assign(bytes, 0);
-    return t_arena[index].data();
+    std::vector<char>& a = t_arena[index];
+    if (a.size() < bytes + 64) a.assign(bytes + 64, 0);
+    return (void*)(((uintptr_t)a.data() + 63) & ~(uintptr_t)63);
 }
 
 void reg(const std::string& name, bool uses_barrier, ItemFn fn) { registry()[name] = Entry{uses_barrier, fn}; }

@@ -1,8 +1,9 @@
 /*
  * ref_harness.cpp — TEST INFRASTRUCTURE.  C entry points around the
  * reference's own code compiled for the OpenCL-C emulation:
- * cvt::PMHuberStereo::depthMap (cvt/vision/PMHuberStereo.cpp:64-291),
- * cvt::PDROF::apply (cvt/gfx/PDROF.h:50-96) and single kernels of
+ * cvt::PMHuberStereo::depthMap (cvt/vision/PMHuberStereo.cpp:64-291) and
+ * depthMapInpaint (:293-506), cvt::PDROF::apply (cvt/gfx/PDROF.h:50-96),
+ * cvt::PDROFInpaint::apply (cvt/gfx/PDROFInpaint.h:50-98) and single kernels of
  * cvt/cl/kernel/pmhstereo.cl.  It produces the golden fixtures under
  * tests/golden/ (tests/golden/make_golden.py) and never ships.
  */
@@ -144,6 +145,67 @@ int ref_propagate(const float* img1, const float* img2, int W, int H, const floa
                                           int_arg(lr), int_arg(iter), bi, bo}, W, H);
     memcpy(out, res.data(), sizeof(float) * 4 * (size_t)W * H);
     if (viewout) memcpy(viewout, vout.ptr(), 80 * (size_t)W * H);
+    return 0;
+}
+
+/* PMHuberStereo::depthMapInpaint (PMHuberStereo.cpp:293-506).  states
+ * (optional, 2*W*H*4): the outputs of the last left and right
+ * pmhstereo_propagate_view launches. */
+int ref_depthmap_inpaint(const float* left, const float* right, int W, int H, int patchsize, float depthmax,
+                         int iterations, float* dmap, float* states) {
+    Image L = rgba(left, W, H), R = rgba(right, W, H);
+    std::vector<float> last[2];
+    clemu::on_launch = [&](const std::string& name, const std::vector<clemu::Arg>& args) {
+        if (name == "pmhstereo_propagate_view") {
+            const clemu::Img* out = args[0].img;
+            int lr = args[10].i;
+            last[lr ? 0 : 1].assign(out->data, out->data + (size_t)out->w * out->h * 4);
+        }
+    };
+    Image dm;
+    try {
+        cvt::PMHuberStereo st;
+        st.depthMapInpaint(dm, L, R, (size_t)patchsize, depthmax, (size_t)iterations, 4);
+    } catch (...) {
+        clemu::on_launch = nullptr;
+        return 1;
+    }
+    clemu::on_launch = nullptr;
+    memcpy(dmap, dm.data(), sizeof(float) * (size_t)W * H);
+    if (states) {
+        size_t n = (size_t)W * H * 4;
+        if (last[0].size() != n || last[1].size() != n) return 2;
+        memcpy(states, last[0].data(), n * sizeof(float));
+        memcpy(states + n, last[1].data(), n * sizeof(float));
+    }
+    return 0;
+}
+
+/* pmhstereo_occmap (pmhstereo.cl:682-712) of state images a (view lr) and b. */
+int ref_occmap(const float* a, const float* b, int W, int H, float maxdiff, int lr, float* out) {
+    Image ia = rgba(a, W, H), ib = rgba(b, W, H), o((size_t)W, (size_t)H, IFormat::RGBA_FLOAT, IALLOCATOR_CL);
+    launch2d("pmhstereo_occmap", {img_arg(o), img_arg(ia), img_arg(ib), float_arg(maxdiff), int_arg(lr)}, W, H);
+    memcpy(out, o.data(), sizeof(float) * 4 * (size_t)W * H);
+    return 0;
+}
+
+/* pmhstereo_normal_depth (pmhstereo.cl:663-680). */
+int ref_normal_depth(const float* states, int W, int H, float depthmax, int lr, float* out) {
+    Image in = rgba(states, W, H), o((size_t)W, (size_t)H, IFormat::RGBA_FLOAT, IALLOCATOR_CL);
+    launch2d("pmhstereo_normal_depth", {img_arg(o), img_arg(in), float_arg(depthmax), int_arg(lr)}, W, H);
+    memcpy(out, o.data(), sizeof(float) * 4 * (size_t)W * H);
+    return 0;
+}
+
+/* cvt::PDROFInpaint::apply (PDROFInpaint.h:50-98); mask RGBA (x used). */
+int ref_pdrof_inpaint(float* output, const float* input, const float* weight, const float* mask, int W, int H,
+                      float lambda, int iters) {
+    Image out = rgba(output, W, H), in = rgba(input, W, H), m = rgba(mask, W, H);
+    Image w((size_t)W, (size_t)H, IFormat::GRAY_FLOAT, IALLOCATOR_CL);
+    memcpy(w.data(), weight, sizeof(float) * (size_t)W * H);
+    cvt::PDROFInpaint pd;
+    pd.apply(out, in, w, m, lambda, iters);
+    memcpy(output, out.data(), sizeof(float) * 4 * (size_t)W * H);
     return 0;
 }
 

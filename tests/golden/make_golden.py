@@ -11,6 +11,10 @@ reference's outputs:
            PDROF::apply (PDROF.h:50-96) for 250 and 7 steps
   runs     PMHuberStereo::depthMap (PMHuberStereo.cpp:64-291): final states of
            both views, disparity map and normal map
+  inpaint  pmhstereo_occmap / pmhstereo_normal_depth (pmhstereo.cl:663-712),
+           PDROFInpaint::apply (PDROFInpaint.h:50-98) for 100 and 7 steps, and
+           PMHuberStereo::depthMapInpaint (PMHuberStereo.cpp:293-506) runs with
+           odd and even iteration counts
 
 Run in the container that holds the reference:
     python tests/golden/make_golden.py
@@ -40,6 +44,13 @@ RUNS = [
 ]
 
 
+# (name, W, H, planes, dmax, seed, patchsize, iterations)
+INPAINT_RUNS = [
+    ("inp_a", 56, 40, 3, 12.0, 201, 9, 3),
+    ("inp_b", 44, 32, 3, 10.0, 202, 7, 6),
+]
+
+
 def load():
     lib = build_ref.build()
     if lib is None:
@@ -53,6 +64,10 @@ def load():
     R.ref_init.argtypes = [f32, f32, i, i, i, f, i, f32]
     R.ref_pdrof.argtypes = [f32, f32, f32, i, i, f, i]
     R.ref_depthmap.argtypes = [f32, f32, i, i, i, f, i, f, f32, vp, vp]
+    R.ref_depthmap_inpaint.argtypes = [f32, f32, i, i, i, f, i, f32, vp]
+    R.ref_occmap.argtypes = [f32, f32, i, i, f, i, f32]
+    R.ref_normal_depth.argtypes = [f32, i, i, f, i, f32]
+    R.ref_pdrof_inpaint.argtypes = [f32, f32, f32, f32, i, i, f, i]
     return R
 
 
@@ -95,6 +110,33 @@ def main():
         u = u0.copy()
         R.ref_pdrof(u, fin, wl, W, H, lam, it)
         out[f"k_pd_{it}"] = u
+    # ---- inpaint kernels: the init states of both views, a random mask
+    sl, sr = out["k_init_lr1"], out["k_init_lr0"]
+    for lr, (a, b) in ((1, (sl, sr)), (0, (sr, sl))):
+        o = np.empty((H, W, 4), np.float32)
+        R.ref_occmap(a, b, W, H, 0.5, lr, o)
+        out[f"k_occmap_lr{lr}"] = o
+        nd = np.empty((H, W, 4), np.float32)
+        R.ref_normal_depth(a, W, H, 14.0, lr, nd)
+        out[f"k_normal_depth_lr{lr}"] = nd
+    mask = np.zeros((H, W, 4), np.float32)
+    mask[..., :3] = (rng.random((H, W)) < 0.7)[..., None]
+    mask[..., 3] = 1.0
+    out["k_pdi_mask"] = mask
+    for it, lam in ((100, 5.0), (7, 17.5)):
+        u = u0.copy()
+        R.ref_pdrof_inpaint(u, fin, wl, mask, W, H, lam, it)
+        out[f"k_pdi_{it}"] = u
+    for name, W2, H2, planes, dmax, seed, P, iters in INPAINT_RUNS:
+        sc2 = scenes.make_scene(W2, H2, planes, dmax, seed=seed)
+        d = np.empty((H2, W2), np.float32)
+        s2 = np.empty((2, H2, W2, 4), np.float32)
+        rc = R.ref_depthmap_inpaint(sc2.left, sc2.right, W2, H2, P, dmax, iters, d, s2.ctypes.data)
+        assert rc == 0, rc
+        out[f"{name}_left"], out[f"{name}_right"] = sc2.left, sc2.right
+        out[f"{name}_cfg"] = np.array([W2, H2, P, iters, dmax], np.float64)
+        out[f"{name}_dmap"], out[f"{name}_states"] = d, s2
+        print(f"{name}: {W2}x{H2} P={P} iterations={iters} done", file=sys.stderr)
     # ---- full runs
     for name, W, H, planes, dmax, seed, P, iters in RUNS:
         sc = scenes.make_scene(W, H, planes, dmax, seed=seed)

@@ -57,3 +57,26 @@ def test_depthmap_runs(oracle, G, name):
     assert_bits(ex["states"], G[f"{name}_states"], "states")
     assert_bits(dmap, G[f"{name}_dmap"], "dmap")
     assert_bits(ex["normalmap"], G[f"{name}_normalmap"], "normalmap")
+
+
+@pytest.mark.parametrize("lr", [1, 0])
+def test_occmap_normal_depth(oracle, G, lr):
+    a, b = (G["k_init_lr1"], G["k_init_lr0"]) if lr else (G["k_init_lr0"], G["k_init_lr1"])
+    assert_bits(oracle.occmap(a, b, 0.5, lr), np.ascontiguousarray(G[f"k_occmap_lr{lr}"][..., 0]), "occmap")
+    assert_bits(oracle.normal_depth(a, 14.0, lr), G[f"k_normal_depth_lr{lr}"], "normal_depth")
+
+
+@pytest.mark.parametrize("it,lam", [(100, 5.0), (7, 17.5)])
+def test_pdrof_inpaint(oracle, G, it, lam):
+    mask = np.ascontiguousarray(G["k_pdi_mask"][..., 0])
+    u = oracle.pd_apply_inpaint(G["k_pd_warm"], G["k_pd_input"], G["k_weight_left"], mask, lam, it)
+    assert_bits(u, G[f"k_pdi_{it}"], f"PDROFInpaint {it}")
+
+
+@pytest.mark.parametrize("name", ["inp_a", "inp_b"])
+def test_depthmap_inpaint_runs(oracle, G, name):
+    W, H, P, iters, dmax = G[f"{name}_cfg"]
+    p = default_params(PRESET_REFERENCE, patchsize=int(P), depthmax=float(dmax), iterations=int(iters))
+    dmap, ex = oracle.depthmap_inpaint(p, G[f"{name}_left"], G[f"{name}_right"], trace=True)
+    assert_bits(ex["states"], G[f"{name}_states"], "states")
+    assert_bits(dmap, G[f"{name}_dmap"], "dmap")
