@@ -18,7 +18,7 @@ LIB_PATH = os.path.join(_HERE, "libcvtpm.so")
 EXPORTS = (
     "cvtpm_version", "cvtpm_status_string", "cvtpm_params_default", "cvtpm_create", "cvtpm_destroy",
     "cvtpm_set_params", "cvtpm_get_params", "cvtpm_last_error", "cvtpm_synchronize", "cvtpm_depthmap",
-    "cvtpm_depthmap_host", "cvtpm_cost_eval", "cvtpm_cost_adjoint", "cvtpm_depthmap_batched", "cvtpm_set_memory_budget",
+    "cvtpm_depthmap_host", "cvtpm_depthmap_inpaint", "cvtpm_cost_eval", "cvtpm_cost_adjoint", "cvtpm_depthmap_batched", "cvtpm_set_memory_budget",
     "cvtpm_set_batch_lanes", "cvtpm_get_batch_info",
     "cvtpm_set_timing", "cvtpm_reset_stats", "cvtpm_get_stats", "cvtpm_tool_fp32_peak",
     "cvtpm_cost_eval_noalloc",
@@ -92,6 +92,7 @@ def lib() -> ctypes.CDLL:
     L.cvtpm_synchronize.argtypes = [vp, vp]
     L.cvtpm_depthmap.argtypes = [vp, vp, sz, vp, vp, i, i, sz, i, f, i, i, f, vp, sz, ctypes.POINTER(CvtpmTrace), vp]
     L.cvtpm_depthmap_host.argtypes = [vp, vp, sz, vp, vp, i, i, sz, i, f, i, i, f, vp, sz, vp]
+    L.cvtpm_depthmap_inpaint.argtypes = [vp, vp, sz, vp, vp, i, i, sz, i, f, i, i, ctypes.POINTER(CvtpmTrace), vp]
     L.cvtpm_cost_eval.argtypes = [vp, vp, vp, i, i, sz, vp, i, vp, vp]
     L.cvtpm_cost_adjoint.argtypes = [vp, vp, vp, i, i, sz, vp, i, vp, vp, vp, vp, vp, vp]
     L.cvtpm_depthmap_batched.argtypes = [vp, ctypes.POINTER(CvtpmPair), i, vp]

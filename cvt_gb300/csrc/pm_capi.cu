@@ -45,6 +45,7 @@ struct cvtpm_ctx {
     short4* list[2];
     uint8_t* win[2];
     uint8_t* valid;
+    float* occ;                       /* occlusion mask of depthMapInpaint */
     /* FAST shared-window neighbour costs: weight volumes of both views and
      * the per-pixel costs of candidates 1-8, when the budget allows */
     float* vol = nullptr;
@@ -178,6 +179,7 @@ cvtpm_status ensure_buffers(cvtpm_ctx* ctx, int W, int H) {
     add((void**)&ctx->tmp2, n * 16);
     add((void**)&ctx->pdT, n * 16);
     add((void**)&ctx->valid, n);
+    add((void**)&ctx->occ, n * 4);
     const size_t need = align_up(off, 256);
     if (need > ctx->pool_bytes) {
         if (ctx->no_alloc) return fail(ctx, CVTPM_ERR_ALLOC, "scratch not sized before capture");
@@ -271,19 +273,21 @@ cvtpm_status prep_views(cvtpm_ctx* ctx, const cvtpm_params& p, const float* img0
     return CVTPM_OK;
 }
 
-/* PDROF::apply, cvt/gfx/PDROF.h:50-96: u warm-starts from `output`, p from 0;
+/* PDROF::apply, cvt/gfx/PDROF.h:50-96 (mask == NULL), or
+ * PDROFInpaint::apply, cvt/gfx/PDROFInpaint.h:50-98 (mask: the occlusion
+ * map): u warm-starts from `output`, p from 0;
  * `iters` steps, plus one when `iters` is odd so the result lands in
  * `output` (:83-95).  The steps run PDB_K at a time in the temporally blocked
  * kernel (identical arithmetic); iters == 0 keeps the reference's single
  * extra step from a copy of the input. */
 cvtpm_status pd_apply(cvtpm_ctx* ctx, float4* output, const float4* input, const float* wgt, float lambda, int iters,
-                      int W, int H, cudaStream_t st) {
+                      int W, int H, cudaStream_t st, const float* mask = nullptr) {
     const size_t n = (size_t)W * H;
     PhaseTimer tm(ctx, st, ctx->ev_pd);
     if (iters == 0) {
         CK(cudaMemcpyAsync(ctx->pdT, input, n * 16, cudaMemcpyDeviceToDevice, st), "pd copy");
         CK(cudaMemsetAsync(ctx->pdP[0], 0, n * 32, st), "pd clear");
-        LK(pm_launch_pd_step(output, ctx->pdP[1], ctx->pdT, ctx->pdP[0], input, wgt, lambda, W, H, st), "pd step");
+        LK(pm_launch_pd_step(output, ctx->pdP[1], ctx->pdT, ctx->pdP[0], input, wgt, mask, lambda, W, H, st), "pd step");
         ++ctx->stats.pd_launches;
         ++ctx->stats.pd_steps;
         tm.stop();
@@ -296,8 +300,8 @@ cvtpm_status pd_apply(cvtpm_ctx* ctx, float4* output, const float4* input, const
     int l = 0;
     for (int done = 0; done < total; done += K, ++l) {
         const int steps = total - done < K ? total - done : K;
-        LK(pm_launch_pd_block(U[(l + 1) & 1], Pp[(l + 1) & 1], U[l & 1], Pp[l & 1], l == 0 ? 1 : 0, input, wgt, lambda,
-                              steps, W, H, st), "pd block");
+        LK(pm_launch_pd_block(U[(l + 1) & 1], Pp[(l + 1) & 1], U[l & 1], Pp[l & 1], l == 0 ? 1 : 0, input, wgt, mask,
+                              lambda, steps, W, H, st), "pd block");
         ++ctx->stats.pd_launches;
         ctx->stats.pd_steps += (uint64_t)steps;
     }
@@ -407,7 +411,105 @@ cvtpm_status run_depthmap(cvtpm_ctx* ctx, const cvtpm_params& p, float* dmap, si
     return CVTPM_OK;
 }
 
+/* PMHuberStereo::depthMapInpaint, PMHuberStereo.cpp:293-506: the depthMap
+ * schedule with the occlusion-masked smoother (PDROFInpaint, 100 steps,
+ * lambda = 20*theta + 5, :442-480), theta ramped from iteration 4 (:481-482),
+ * the final check on state buffer 1 whatever the iteration count
+ * (clmatches[1], :491-496) with 1 px / 5 degrees, and the disparity in
+ * pixels (scale 1, :503).  trace->states: the last propagation outputs. */
+cvtpm_status run_depthmap_inpaint(cvtpm_ctx* ctx, const cvtpm_params& p, float* dmap, size_t dpitch,
+                                  const float* left, const float* right, int W, int H, size_t pitch,
+                                  const cvtpm_trace* trace, cudaStream_t st) {
+    cvtpm_status s;
+    if ((s = check_params(ctx, p)) != CVTPM_OK) return s;
+    if ((s = check_image(ctx, left, W, H, pitch, "left")) != CVTPM_OK) return s;
+    if ((s = check_image(ctx, right, W, H, pitch, "right")) != CVTPM_OK) return s;
+    if (!dmap) return fail(ctx, CVTPM_ERR_INVALID_ARGUMENT, "dmap is NULL");
+    if (dpitch % 4 != 0 || dpitch < (size_t)W * 4) return fail(ctx, CVTPM_ERR_INVALID_ARGUMENT, "dmap pitch");
+    CK(cudaSetDevice(ctx->device), "cudaSetDevice");
+    if ((s = ensure_buffers(ctx, W, H)) != CVTPM_OK) return s;
+    if ((s = ensure_tables(ctx, p, st)) != CVTPM_OK) return s;
+    if ((s = prep_views(ctx, p, left, right, W, H, pitch, st)) != CVTPM_OK) return s;
+    const size_t n = (size_t)W * H;
+    const bool exact = p.arith == CVTPM_ARITH_EXACT;
+    const float dmax = p.depthmax;
+    const int N = p.iterations;
+    PmPassArgs aL = base_args(ctx, p, W, H, 0), aR = base_args(ctx, p, W, H, 1);
+    if (!exact) {
+        if ((s = ensure_volumes(ctx, W, H, p.patchsize)) != CVTPM_OK) return s;
+        if (ctx->vol_on) {
+            LK(pm_launch_weights(ctx->col[0], W, H, p.patchsize, ctx->wvol[0], st), "weights left");
+            LK(pm_launch_weights(ctx->col[1], W, H, p.patchsize, ctx->wvol[1], st), "weights right");
+            aL.wvol = ctx->wvol[0]; aR.wvol = ctx->wvol[1];
+            aL.nbcost = aR.nbcost = ctx->nbcost;
+        }
+    }
+    if (!ctx->dcount) {
+        if (ctx->no_alloc) return fail(ctx, CVTPM_ERR_ALLOC, "counters not allocated before capture");
+        CK(cudaMalloc(&ctx->dcount, 2 * sizeof(unsigned long long)), "counters");
+        CK(cudaMemset(ctx->dcount, 0, 2 * sizeof(unsigned long long)), "counters");
+    }
+    ++ctx->stats.calls;
+    aL.out = ctx->S[0][0];                                         /* :345-363 */
+    LK(pm_launch_init(aL, exact, st), "init");
+    aR.out = ctx->S[1][0];
+    LK(pm_launch_init(aR, exact, st), "init");
+    CK(cudaMemsetAsync(ctx->smooth[0], 0, n * 16, st), "clear");   /* :330-336 */
+    CK(cudaMemsetAsync(ctx->smooth[1], 0, n * 16, st), "clear");
+    CK(cudaMemsetAsync(ctx->list[1], 0xFF, n * 8, st), "clear");   /* :365-369 */
+    float theta = 0.0f;
+    for (int iter = 0; iter < N; ++iter) {                         /* :371-483 */
+        const int sw = iter & 1;
+        aL.iter = aR.iter = iter;
+        aL.theta = aR.theta = theta;
+        aL.old = ctx->S[0][sw]; aL.out = ctx->S[0][1 - sw]; aL.smooth = ctx->smooth[0];
+        aL.viewin = ctx->list[1]; aL.viewsrc = ctx->S[1][sw]; aL.winners = ctx->win[0];
+        aL.counters = aR.counters = ctx->dcount;
+        {
+            PhaseTimer tm(ctx, st, ctx->ev_prop);
+            LK(pm_launch_propagate(aL, exact, st), "propagate left");
+            tm.stop();
+        }
+        LK(pm_launch_view_list(ctx->S[0][1 - sw], W, H, ctx->list[0], st), "view list");
+        aR.old = ctx->S[1][sw]; aR.out = ctx->S[1][1 - sw]; aR.smooth = ctx->smooth[1];
+        aR.viewin = ctx->list[0]; aR.viewsrc = ctx->S[0][1 - sw]; aR.winners = ctx->win[1];
+        {
+            PhaseTimer tm(ctx, st, ctx->ev_prop);
+            LK(pm_launch_propagate(aR, exact, st), "propagate right");
+            tm.stop();
+        }
+        ctx->stats.propagate_launches += 2;
+        LK(pm_launch_view_list(ctx->S[1][1 - sw], W, H, ctx->list[1], st), "view list");
+        const float lambda = theta * 20.0f + 5.0f;
+        for (int v = 0; v < 2; ++v) {                              /* :442-480 */
+            const int lr = v == 0 ? 1 : 0;
+            LK(pm_launch_occmap(ctx->S[v][1 - sw], ctx->S[1 - v][1 - sw], W, H, 0.5f, lr, ctx->occ, st), "occmap");
+            LK(pm_launch_normal_depth(ctx->S[v][1 - sw], W, H, dmax, lr, ctx->tmp2, st), "normal depth");
+            if ((s = pd_apply(ctx, ctx->smooth[v], ctx->tmp2, ctx->wgt[v], lambda, 100, W, H, st, ctx->occ)) != CVTPM_OK)
+                return s;
+        }
+        if (iter >= 4) theta = smoothstep01(((float)iter - 4.0f) / ((float)N - 4.0f)) * 1.0f;
+    }
+    LK(pm_launch_consistency(ctx->S[0][1], ctx->S[1][1], W, H, 1.0f, 5.0f, 1, ctx->tmp, ctx->valid, st),
+       "consistency");
+    LK(pm_launch_fill_output(ctx->tmp, W, H, 1.0f, dmap, dpitch / 4, nullptr, 0, st), "fill output");
+    if (trace) {
+        const int fin = 1 - ((N - 1) & 1);
+        if (trace->winners) {
+            CK(cudaMemcpyAsync(trace->winners, ctx->win[0], n, cudaMemcpyDeviceToDevice, st), "trace");
+            CK(cudaMemcpyAsync(trace->winners + n, ctx->win[1], n, cudaMemcpyDeviceToDevice, st), "trace");
+        }
+        if (trace->valid) CK(cudaMemcpyAsync(trace->valid, ctx->valid, n, cudaMemcpyDeviceToDevice, st), "trace");
+        if (trace->states) {
+            CK(cudaMemcpyAsync(trace->states, ctx->S[0][fin], n * 16, cudaMemcpyDeviceToDevice, st), "trace");
+            CK(cudaMemcpyAsync(trace->states + 4 * n, ctx->S[1][fin], n * 16, cudaMemcpyDeviceToDevice, st), "trace");
+        }
+    }
+    return CVTPM_OK;
+}
+
 }  // namespace
+
 
 /* ====================================================== public API === */
 extern "C" {
@@ -551,6 +653,20 @@ cvtpm_status cvtpm_depthmap(cvtpm_ctx* ctx, float* dmap, size_t dmap_pitch, cons
     p.dscale = dscale;
     return run_depthmap(ctx, p, dmap, dmap_pitch, left, right, width, height, pitch, normalmap, normalmap_pitch,
                         trace, (cudaStream_t)stream);
+}
+
+cvtpm_status cvtpm_depthmap_inpaint(cvtpm_ctx* ctx, float* dmap, size_t dmap_pitch, const float* left,
+                                    const float* right, int width, int height, size_t pitch, int patchsize,
+                                    float depthmax, int iterations, int viewsamples, const cvtpm_trace* trace,
+                                    void* stream) {
+    if (!ctx) return CVTPM_ERR_INVALID_ARGUMENT;
+    (void)viewsamples;
+    cvtpm_params p = ctx->prm;
+    p.patchsize = patchsize;
+    p.depthmax = depthmax;
+    p.iterations = iterations;
+    return run_depthmap_inpaint(ctx, p, dmap, dmap_pitch, left, right, width, height, pitch, trace,
+                                (cudaStream_t)stream);
 }
 
 cvtpm_status cvtpm_depthmap_host(cvtpm_ctx* ctx, float* dmap, size_t dmap_pitch, const float* left,

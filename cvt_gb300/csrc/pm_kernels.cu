@@ -429,6 +429,37 @@ __global__ void k_consistency(const float4* __restrict__ L, const float4* __rest
     if (valid) valid[o] = bad ? 0 : 1;
 }
 
+/* pmhstereo_occmap (pmhstereo.cl:682-712): the test of k_consistency with
+ * the angle bound fixed at 5 degrees; mask 1 where both views agree. */
+__global__ void k_occmap(const float4* __restrict__ L, const float4* __restrict__ R, int W, int H, float maxdiff,
+                         int lr, float* __restrict__ mask) {
+    const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
+    if (x >= W || y >= H) return;
+    const size_t o = (size_t)y * W + x;
+    float4 sl = L[o];
+    float x2 = transform_x(sl, (float)x, (float)y);
+    float4 sr;
+    if (x2 < 0 || x2 >= (float)W) sr = f4s(1e5f);
+    else sr = R[(size_t)y * W + clampi(f2i_nan0(roundf(x2)), 0, W - 1)];
+    float ax, ay, az, bx, by, bz;
+    if (lr) { to_normal(sl, ax, ay, az); to_normal(viewprop(sr), bx, by, bz); }
+    else { to_normal(sr, ax, ay, az); to_normal(viewprop(sl), bx, by, bz); }
+    float ndiff = (ax * bx + ay * by) + az * bz;
+    float dm = fabsf((float)x - transform_x(sr, x2, (float)y));
+    bool bad = (dm >= maxdiff) || (pm_acospi(ndiff) >= 5.0f / 180.0f);
+    mask[o] = bad ? 0.0f : 1.0f;
+}
+
+/* pmhstereo_normal_depth (pmhstereo.cl:663-680): (n.x, n.y, d/dmax, 1). */
+__global__ void k_normal_depth(const float4* __restrict__ in, int W, int H, float depthmax, int lr,
+                               float4* __restrict__ out) {
+    const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
+    if (x >= W || y >= H) return;
+    const size_t o = (size_t)y * W + x;
+    const float4 val = to_ref_normal_depth(in[o], (float)x, (float)y, lr);
+    out[o] = f4(val.x, val.y, val.w / depthmax, 1.0f);
+}
+
 /* ------------------------------------------------- row scans / fills -- */
 /* For every x of the row: the nearest index to the left (lft, in shared
  * memory) whose value passes ok(); then, right to left, the nearest to the
@@ -533,7 +564,10 @@ PM_DEV float div_ge1(float x, float d) { return d == 1.0f ? x : x / d; }
  * back exactly, so the division is skipped there. */
 PM_DEV float div_pos(float x, float d) { return x == 0.0f ? x : x / d; }
 
-/* The dual at q from u(q), u(q+x), u(q+y), the old dual and w(q) (:49-68). */
+/* The dual at q from u(q), u(q+x), u(q+y), the old dual and w(q) (:49-68).
+ * INPAINT: PDHuberWeightedInpaint.cl projects every channel on its own
+ * (:67) instead of (x, y) jointly and z apart. */
+template <bool INPAINT>
 PM_DEV void pd_dual(float w, float den, float4 uq, float4 ux, float4 uy, float4 plo, float4 phi,
                     float4& lo, float4& hi) {
     const float SIGMA = 1.0f / pm_sqrt(8.0f);
@@ -543,14 +577,23 @@ PM_DEV void pd_dual(float w, float den, float4 uq, float4 ux, float4 uy, float4 
     const float4 l = f4(div_pos(nl.x, den), div_pos(nl.y, den), div_pos(nl.z, den), div_pos(nl.w, den));
     const float4 h = f4(div_pos(nh.x, den), div_pos(nh.y, den), div_pos(nh.z, den), div_pos(nh.w, den));
     const float4 pt = l * l + h * h;
-    const float sxy = fmaxf(1.0f, pm_sqrt(pt.x + pt.y));
-    const float sz = fmaxf(1.0f, pm_sqrt(pt.z));
-    const float sw = fmaxf(1.0f, pm_sqrt(0.0f));
-    lo = f4(div_ge1(l.x, sxy), div_ge1(l.y, sxy), div_ge1(l.z, sz), div_ge1(l.w, sw));
-    hi = f4(div_ge1(h.x, sxy), div_ge1(h.y, sxy), div_ge1(h.z, sz), div_ge1(h.w, sw));
+    float sx, sy, sz, sw;
+    if (INPAINT) {
+        sx = fmaxf(1.0f, pm_sqrt(pt.x));
+        sy = fmaxf(1.0f, pm_sqrt(pt.y));
+        sz = fmaxf(1.0f, pm_sqrt(pt.z));
+        sw = fmaxf(1.0f, pm_sqrt(pt.w));
+    } else {
+        sx = sy = fmaxf(1.0f, pm_sqrt(pt.x + pt.y));
+        sz = fmaxf(1.0f, pm_sqrt(pt.z));
+        sw = fmaxf(1.0f, pm_sqrt(0.0f));
+    }
+    lo = f4(div_ge1(l.x, sx), div_ge1(l.y, sy), div_ge1(l.z, sz), div_ge1(l.w, sw));
+    hi = f4(div_ge1(h.x, sx), div_ge1(h.y, sy), div_ge1(h.z, sz), div_ge1(h.w, sw));
 }
 
-/* The primal update at c (:70-78); den_u = 1 + TAU*lambda. */
+/* The primal update at c (:70-78); den_u = 1 + TAU*lambda.  The inpainting
+ * smoother passes lambda * mask(c) (PDHuberWeightedInpaint.cl:82-83). */
 PM_DEV float4 pd_primal(float4 uc, float4 img, float wc, float4 lo_c, float4 lo_l, float4 hi_c, float4 hi_u,
                         float lambda, float den_u) {
     const float TAU = 1.0f / pm_sqrt(8.0f), THETA = 0.5f;
@@ -563,6 +606,7 @@ PM_DEV float4 pd_primal(float4 uc, float4 img, float wc, float4 lo_c, float4 lo_
     return un;
 }
 
+template <bool INPAINT>
 PM_DEV void pd_dual_at(const float4* __restrict__ last, const float4* __restrict__ pin, const float* __restrict__ wgt,
                        int W, int H, int qx, int qy, float4& lo, float4& hi) {
     const bool in = qx >= 0 && qy >= 0 && qx < W && qy < H;
@@ -573,30 +617,32 @@ PM_DEV void pd_dual_at(const float4* __restrict__ last, const float4* __restrict
     const float4 uy = last[(size_t)clampi(qy + 1, 0, H - 1) * W + cx0];
     const float4 plo = in ? pin[((size_t)qy * W + qx) * 2] : f4s(0.0f);
     const float4 phi = in ? pin[((size_t)qy * W + qx) * 2 + 1] : f4s(0.0f);
-    pd_dual(w, pd_den(w), uq, ux, uy, plo, phi, lo, hi);
+    pd_dual<INPAINT>(w, pd_den(w), uq, ux, uy, plo, phi, lo, hi);
 }
 
 #define PD_TX 32
 #define PD_TY 8
+template <bool INPAINT>
 __global__ void __launch_bounds__(PD_TX * PD_TY)
 k_pd_step(float4* __restrict__ uout, float4* __restrict__ pout, const float4* __restrict__ last,
           const float4* __restrict__ pin, const float4* __restrict__ f, const float* __restrict__ wgt,
-          float lambda, int W, int H) {
+          const float* __restrict__ mask, float lambda, int W, int H) {
     __shared__ float4 slo[PD_TY + 1][PD_TX + 1];
     __shared__ float4 shi[PD_TY + 1][PD_TX + 1];
     const int tx = threadIdx.x, ty = threadIdx.y;
     const int x = blockIdx.x * PD_TX + tx, y = blockIdx.y * PD_TY + ty;
     float4 lo, hi;
-    pd_dual_at(last, pin, wgt, W, H, x, y, lo, hi);
+    pd_dual_at<INPAINT>(last, pin, wgt, W, H, x, y, lo, hi);
     slo[ty + 1][tx + 1] = lo; shi[ty + 1][tx + 1] = hi;
-    if (tx == 0) { float4 l2, h2; pd_dual_at(last, pin, wgt, W, H, x - 1, y, l2, h2); slo[ty + 1][0] = l2; shi[ty + 1][0] = h2; }
-    if (ty == 0) { float4 l2, h2; pd_dual_at(last, pin, wgt, W, H, x, y - 1, l2, h2); slo[0][tx + 1] = l2; shi[0][tx + 1] = h2; }
+    if (tx == 0) { float4 l2, h2; pd_dual_at<INPAINT>(last, pin, wgt, W, H, x - 1, y, l2, h2); slo[ty + 1][0] = l2; shi[ty + 1][0] = h2; }
+    if (ty == 0) { float4 l2, h2; pd_dual_at<INPAINT>(last, pin, wgt, W, H, x, y - 1, l2, h2); slo[0][tx + 1] = l2; shi[0][tx + 1] = h2; }
     __syncthreads();
     if (x >= W || y >= H) return;
     const float TAU = 1.0f / pm_sqrt(8.0f);
     const size_t o = (size_t)y * W + x;
+    const float lam = INPAINT ? lambda * mask[o] : lambda;
     const float4 un = pd_primal(last[o], f[o], wgt[o], slo[ty + 1][tx + 1], slo[ty + 1][tx], shi[ty + 1][tx + 1],
-                                shi[ty][tx + 1], lambda, 1.0f + TAU * lambda);
+                                shi[ty][tx + 1], lam, 1.0f + TAU * lam);
     uout[o] = un;
     pout[o * 2] = lo;
     pout[o * 2 + 1] = hi;
@@ -615,10 +661,11 @@ k_pd_step(float4* __restrict__ uout, float4* __restrict__ pout, const float4* __
 #define PDB_RY (PDB_TY + 2 * PDB_K)
 #define PDB_N (PDB_RX * PDB_RY)
 
+template <bool INPAINT>
 __global__ void __launch_bounds__(PDB_TX * PDB_TY)
 k_pd_block(float4* __restrict__ uout, float4* __restrict__ pout, const float4* __restrict__ uin,
            const float4* __restrict__ pin, int pzero, const float4* __restrict__ f, const float* __restrict__ wgt,
-           float lambda, int nsteps, int W, int H) {
+           const float* __restrict__ mask, float lambda, int nsteps, int W, int H) {
     extern __shared__ __align__(16) float4 sm4[];
     float4* su = sm4;
     float4* slo = su + PDB_N;
@@ -660,7 +707,7 @@ k_pd_block(float4* __restrict__ uout, float4* __restrict__ pout, const float4* _
             const int i = ly * PDB_RX + lx;
             const int gx = rx0 + lx, gy = ry0 + ly;
             float4 lo, hi;
-            pd_dual(sw[i], sden[i], su[at(gx, gy)], su[at(gx + 1, gy)], su[at(gx, gy + 1)], slo[i], shi[i], lo, hi);
+            pd_dual<INPAINT>(sw[i], sden[i], su[at(gx, gy)], su[at(gx + 1, gy)], su[at(gx, gy + 1)], slo[i], shi[i], lo, hi);
             slo[i] = lo;
             shi[i] = hi;
         }
@@ -671,7 +718,12 @@ k_pd_block(float4* __restrict__ uout, float4* __restrict__ pout, const float4* _
             const int gx = rx0 + lx, gy = ry0 + ly;
             if (gx < 0 || gy < 0 || gx >= W || gy >= H) continue;
             const int i = ly * PDB_RX + lx;
-            su[i] = pd_primal(su[i], sf[i], sw[i], slo[i], slo[i - 1], shi[i], shi[i - PDB_RX], lambda, den_u);
+            if (INPAINT) {
+                const float lam = lambda * __ldg(&mask[(size_t)gy * W + gx]);
+                su[i] = pd_primal(su[i], sf[i], sw[i], slo[i], slo[i - 1], shi[i], shi[i - PDB_RX], lam, 1.0f + TAU * lam);
+            } else {
+                su[i] = pd_primal(su[i], sf[i], sw[i], slo[i], slo[i - 1], shi[i], shi[i - PDB_RX], lambda, den_u);
+            }
         }
         __syncthreads();
     }
@@ -786,23 +838,41 @@ int pm_pd_block_steps() { return PDB_K; }
 static const size_t kPdBlockSmem = (size_t)PDB_N * (4 * sizeof(float4) + 2 * sizeof(float));
 
 cudaError_t pm_prepare_kernels() {
-    return cudaFuncSetAttribute(k_pd_block, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kPdBlockSmem);
+    cudaError_t e = cudaFuncSetAttribute(k_pd_block<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kPdBlockSmem);
+    if (e != cudaSuccess) return e;
+    return cudaFuncSetAttribute(k_pd_block<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kPdBlockSmem);
 }
 
 cudaError_t pm_launch_pd_block(float4* uout, float4* pout, const float4* uin, const float4* pin, int pzero,
-                               const float4* f, const float* wgt, float lambda, int nsteps, int W, int H,
-                               cudaStream_t st) {
+                               const float4* f, const float* wgt, const float* mask, float lambda, int nsteps, int W,
+                               int H, cudaStream_t st) {
     const size_t smem = kPdBlockSmem;
     dim3 b(PDB_TX, PDB_TY), g((W + PDB_TX - 1) / PDB_TX, (H + PDB_TY - 1) / PDB_TY);
-    k_pd_block<<<g, b, smem, st>>>(uout, pout, uin, pin, pzero, f, wgt, lambda, nsteps, W, H);
+    if (mask) k_pd_block<true><<<g, b, smem, st>>>(uout, pout, uin, pin, pzero, f, wgt, mask, lambda, nsteps, W, H);
+    else k_pd_block<false><<<g, b, smem, st>>>(uout, pout, uin, pin, pzero, f, wgt, nullptr, lambda, nsteps, W, H);
     PM_LAUNCH_CHECK();
     return cudaSuccess;
 }
 
 cudaError_t pm_launch_pd_step(float4* uout, float4* pout, const float4* last, const float4* pin, const float4* f,
-                              const float* wgt, float lambda, int W, int H, cudaStream_t st) {
+                              const float* wgt, const float* mask, float lambda, int W, int H, cudaStream_t st) {
     dim3 b(PD_TX, PD_TY), g((W + PD_TX - 1) / PD_TX, (H + PD_TY - 1) / PD_TY);
-    k_pd_step<<<g, b, 0, st>>>(uout, pout, last, pin, f, wgt, lambda, W, H);
+    if (mask) k_pd_step<true><<<g, b, 0, st>>>(uout, pout, last, pin, f, wgt, mask, lambda, W, H);
+    else k_pd_step<false><<<g, b, 0, st>>>(uout, pout, last, pin, f, wgt, nullptr, lambda, W, H);
+    PM_LAUNCH_CHECK();
+    return cudaSuccess;
+}
+
+cudaError_t pm_launch_occmap(const float4* L, const float4* R, int W, int H, float maxdiff, int lr, float* mask,
+                             cudaStream_t st) {
+    k_occmap<<<pix_grid(W, H), dim3(32, 8), 0, st>>>(L, R, W, H, maxdiff, lr, mask);
+    PM_LAUNCH_CHECK();
+    return cudaSuccess;
+}
+
+cudaError_t pm_launch_normal_depth(const float4* in, int W, int H, float depthmax, int lr, float4* out,
+                                   cudaStream_t st) {
+    k_normal_depth<<<pix_grid(W, H), dim3(32, 8), 0, st>>>(in, W, H, depthmax, lr, out);
     PM_LAUNCH_CHECK();
     return cudaSuccess;
 }

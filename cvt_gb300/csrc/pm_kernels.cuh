@@ -45,9 +45,14 @@ cudaError_t pm_launch_fill_state(const float4* in, int W, int H, float depthmax,
                                  cudaStream_t st);
 cudaError_t pm_launch_fill_output(const float4* in, int W, int H, float scale, float* dmap, size_t dpitch,
                                   float4* nmap, size_t npitch, cudaStream_t st);
+/* mask == NULL: PDHuberWeighted; else PDHuberWeightedInpaint with lambda * mask. */
 cudaError_t pm_launch_pd_step(float4* uout, float4* pout, const float4* last, const float4* pin,
-                              const float4* f, const float* wgt, float lambda, int W, int H,
+                              const float4* f, const float* wgt, const float* mask, float lambda, int W, int H,
                               cudaStream_t st);
+cudaError_t pm_launch_occmap(const float4* L, const float4* R, int W, int H, float maxdiff, int lr, float* mask,
+                             cudaStream_t st);
+cudaError_t pm_launch_normal_depth(const float4* in, int W, int H, float depthmax, int lr, float4* out,
+                                   cudaStream_t st);
 
 /* Kernel attributes (dynamic shared memory limits) for the current device;
  * call once per device before the first launch or stream capture. */
@@ -55,8 +60,8 @@ cudaError_t pm_prepare_kernels();
 
 int pm_pd_block_steps();
 cudaError_t pm_launch_pd_block(float4* uout, float4* pout, const float4* uin, const float4* pin, int pzero,
-                               const float4* f, const float* wgt, float lambda, int nsteps, int W, int H,
-                               cudaStream_t st);
+                               const float4* f, const float* wgt, const float* mask, float lambda, int nsteps, int W,
+                               int H, cudaStream_t st);
 cudaError_t pm_launch_ffma_peak(float* out, int blocks, int iters, cudaStream_t st);
 
 /* pm_adjoint.cu */

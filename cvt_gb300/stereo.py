@@ -164,6 +164,37 @@ class PMHuberStereo:
         self._check(rc)
         return out
 
+    def depthMapInpaint(self, dmap: torch.Tensor, left: torch.Tensor, right: torch.Tensor, patchsize: int,
+                        depthmax: float, iterations: int, viewsamples: int, trace: dict | None = None) -> torch.Tensor:
+        """PMHuberStereo::depthMapInpaint: disparity in pixels; ``trace`` as
+        for depthMap."""
+        _check_img(left, "left")
+        _check_img(right, "right")
+        if left.shape != right.shape or left.device != right.device or left.device.index != self.device:
+            raise CVTException("Left/Right stereo images inconsistent or incompatible memory type")
+        if left.stride(0) != right.stride(0):
+            right = right.contiguous()
+            left = left.contiguous()
+        H, W = left.shape[:2]
+        if dmap is None:
+            dmap = torch.empty((H, W), dtype=torch.float32, device=left.device)
+        if dmap.device != left.device or dmap.dtype != torch.float32:
+            raise CVTException("dmap must be a float32 tensor on the images' device")
+        if dmap.shape != (H, W) or not dmap.is_contiguous():
+            dmap.resize_(H, W)
+        tr = None
+        if trace is not None:
+            trace["winners"] = torch.empty((2, H, W), dtype=torch.uint8, device=left.device)
+            trace["valid"] = torch.empty((H, W), dtype=torch.uint8, device=left.device)
+            trace["states"] = torch.empty((2, H, W, 4), dtype=torch.float32, device=left.device)
+            tr = _lib.CvtpmTrace(trace["winners"].data_ptr(), trace["valid"].data_ptr(), trace["states"].data_ptr())
+        rc = _lib.lib().cvtpm_depthmap_inpaint(
+            self._h, dmap.data_ptr(), W * 4, left.data_ptr(), right.data_ptr(), W, H, left.stride(0) * 4,
+            int(patchsize), float(depthmax), int(iterations), int(viewsamples),
+            ctypes.byref(tr) if tr is not None else None, _stream_ptr(left))
+        self._check(rc)
+        return dmap
+
     def depthMapBatched(self, pairs, outs=None, stream=None):
         """cvtpm_depthmap_batched.  pairs: list of (left, right, depthmax) with
         left/right (H, W, 4) float32 CUDA tensors; returns the (H, W) disparity

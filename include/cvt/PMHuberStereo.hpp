@@ -119,6 +119,20 @@ class PMHuberStereo {
         check(cvtpm_synchronize(_ctx, stream));
     }
 
+    /* PMHuberStereo::depthMapInpaint (PMHuberStereo.h:41): disparity in pixels. */
+    void depthMapInpaint(Image& dmap, const Image& left, const Image& right, size_t patchsize, float depthmax,
+                         size_t iterations, size_t viewsamples, cudaStream_t stream = 0) {
+        if (left.width() != right.width() || left.height() != right.height() ||
+            left.format() != IFormat::RGBA_FLOAT || right.format() != IFormat::RGBA_FLOAT ||
+            left.pitch() != right.pitch())
+            throw CVTException("Left/Right stereo images inconsistent or incompatible memory type");
+        dmap.reallocate(left.width(), left.height(), IFormat::GRAY_FLOAT);
+        check(cvtpm_depthmap_inpaint(_ctx, dmap.data(), dmap.pitch(), left.data(), right.data(), (int)left.width(),
+                                     (int)left.height(), left.pitch(), (int)patchsize, depthmax, (int)iterations,
+                                     (int)viewsamples, NULL, stream));
+        check(cvtpm_synchronize(_ctx, stream));
+    }
+
   private:
     void check(cvtpm_status s) {
         if (s != CVTPM_OK) throw CVTException(std::string(cvtpm_status_string(s)) + ": " + cvtpm_last_error(_ctx));

@@ -156,6 +156,24 @@ cvtpm_status cvtpm_depthmap_host(cvtpm_ctx* ctx,
                                  float* normalmap, size_t normalmap_pitch,
                                  void* stream);
 
+/* PMHuberStereo::depthMapInpaint (PMHuberStereo.h:41, PMHuberStereo.cpp:
+ * 293-506) on device images: the depthMap schedule with the occlusion-masked
+ * Huber-ROF smoother (100 steps, lambda = 20*theta + 5), theta ramped from
+ * iteration 4, the final consistency check with 1 px / 5 degrees on state
+ * buffer 1 (as the reference, whatever the iteration count) and the
+ * disparity in pixels (scale 1).  dmap is W*H floats (pitch in bytes).
+ * Parameters other than patchsize/depthmax/iterations come from the
+ * context (cvtpm_set_params); maxdispdiff, maxanglediff, thetascale,
+ * pd_iterations and dscale are not used.  trace (optional) as for
+ * cvtpm_depthmap. */
+cvtpm_status cvtpm_depthmap_inpaint(cvtpm_ctx* ctx,
+                                    float* dmap, size_t dmap_pitch,
+                                    const float* left, const float* right,
+                                    int width, int height, size_t pitch,
+                                    int patchsize, float depthmax, int iterations,
+                                    int viewsamples, const cvtpm_trace* trace,
+                                    void* stream);
+
 /* Fixed-plane cost evaluator: the aggregated ASW cost
  * patch_eval_color_grad_weighted (pmhstereo.cl:170-228) of every pixel of
  * view `lr` (1 = left is image 1, 0 = right is image 1) for the given state

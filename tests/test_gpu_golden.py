@@ -51,3 +51,17 @@ def test_depthmap_runs(setup, name):
     assert_bits(tr["states"].cpu().numpy(), G[f"{name}_states"], "states")
     assert_bits(dm.cpu().numpy(), G[f"{name}_dmap"], "dmap")
     assert_bits(nm.cpu().numpy(), G[f"{name}_normalmap"], "normalmap")
+
+
+@pytest.mark.parametrize("name", ["inp_a", "inp_b"])
+def test_depthmap_inpaint_golden(setup, name):
+    st, G = setup
+    W, H, P, iters, dmax = G[f"{name}_cfg"]
+    p = default_params(PRESET_REFERENCE, patchsize=int(P), depthmax=float(dmax), iterations=int(iters))
+    st.set_params(p)
+    tr = {}
+    dm = st.depthMapInpaint(None, torch.from_numpy(G[f"{name}_left"]).cuda(), torch.from_numpy(G[f"{name}_right"]).cuda(),
+                            int(P), float(dmax), int(iters), 4, trace=tr)
+    torch.cuda.synchronize()
+    assert_bits(tr["states"].cpu().numpy(), G[f"{name}_states"], "states")
+    assert_bits(dm.cpu().numpy(), G[f"{name}_dmap"], "dmap")

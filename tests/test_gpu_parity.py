@@ -172,3 +172,22 @@ def test_pd_step_counts(stereo, oracle, pd_iters):
     dm, _, tr, want, ex = run_both(stereo, oracle, sc, p, normalmap=False)
     assert_bitexact(tr["states"], ex["states"], "states")
     assert_bitexact(dm, want, "dmap")
+
+
+@pytest.mark.parametrize("mode", MODES, ids=MODE_IDS)
+@pytest.mark.parametrize("iters", [3, 6])
+def test_depthmap_inpaint_bitexact(stereo, oracle, mode, iters):
+    """PMHuberStereo::depthMapInpaint: odd and even iteration counts (the final
+    check reads state buffer 1 either way), theta > 0 from iteration 5."""
+    arith, rng = mode
+    sc = scenes.make_scene(90, 52, 4, 14.0, seed=31 + iters)
+    p = default_params(PRESET_REFERENCE, arith=arith, rng=rng, seed=7, patchsize=7, depthmax=14.0, iterations=iters)
+    stereo.set_params(p)
+    tr = {}
+    dm = stereo.depthMapInpaint(None, to_dev(sc.left), to_dev(sc.right), 7, 14.0, iters, 4, trace=tr)
+    torch.cuda.synchronize()
+    want, ex = oracle.depthmap_inpaint(p, sc.left, sc.right, trace=True)
+    assert_bitexact(tr["winners"].cpu().numpy(), ex["winners"], "winners")
+    assert_bitexact(tr["valid"].cpu().numpy(), ex["valid"], "valid")
+    assert_bitexact(tr["states"].cpu().numpy(), ex["states"], "states")
+    assert_bitexact(dm.cpu().numpy(), want, "dmap")
