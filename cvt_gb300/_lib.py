@@ -18,7 +18,7 @@ LIB_PATH = os.path.join(_HERE, "libcvtpm.so")
 EXPORTS = (
     "cvtpm_version", "cvtpm_status_string", "cvtpm_params_default", "cvtpm_create", "cvtpm_destroy",
     "cvtpm_set_params", "cvtpm_get_params", "cvtpm_last_error", "cvtpm_synchronize", "cvtpm_depthmap",
-    "cvtpm_depthmap_host", "cvtpm_depthmap_inpaint", "cvtpm_cost_eval", "cvtpm_cost_adjoint", "cvtpm_depthmap_batched", "cvtpm_set_memory_budget",
+    "cvtpm_depthmap_host", "cvtpm_depthmap_inpaint", "cvtpm_cost_eval", "cvtpm_cost_adjoint", "cvtpm_polish_planes", "cvtpm_depthmap_batched", "cvtpm_set_memory_budget",
     "cvtpm_set_batch_lanes", "cvtpm_get_batch_info",
     "cvtpm_set_timing", "cvtpm_reset_stats", "cvtpm_get_stats", "cvtpm_tool_fp32_peak",
     "cvtpm_cost_eval_noalloc",
@@ -98,6 +98,7 @@ def lib() -> ctypes.CDLL:
     L.cvtpm_depthmap_batched.argtypes = [vp, ctypes.POINTER(CvtpmPair), i, vp]
     L.cvtpm_set_timing.argtypes = [vp, i]
     L.cvtpm_set_memory_budget.argtypes = [vp, sz]
+    L.cvtpm_polish_planes.argtypes = [vp, vp, vp, i, i, sz, vp, i, i, vp, vp]
     L.cvtpm_set_batch_lanes.argtypes = [vp, i]
     L.cvtpm_get_batch_info.argtypes = [vp, ctypes.POINTER(CvtpmBatchInfo)]
     L.cvtpm_reset_stats.argtypes = [vp]

@@ -249,3 +249,132 @@ cudaError_t pm_launch_adjoint_finish(const float4* dI, const float4* dG, int W, 
     k_adjoint_finish<<<grid, block, 0, st>>>(dI, dG, W, H, out);
     return cudaGetLastError();
 }
+
+/* ------------------------------------------------- plane polishing -- */
+/* Levenberg-Marquardt ("adjoint-driven Gauss-Newton") polishing of a plane
+ * field: per pixel, `steps` trial steps on the plane that minimise its
+ * aggregated cost C (the FAST evaluation above).  One window sweep at a
+ * plane gives C, the gradient g = dC/ds of the adjoint (ds = state), and a
+ * Gauss-Newton matrix from the truncated-L1 terms read as reweighted least
+ * squares (|e| ~ e^2 / (2 |e0|) near the current residual e0):
+ *   H = (1/S) sum_t w_t sum_k beta_k [|e_k| < cap_k] D_k^2 / max(|e_k|, eps_k) g_t g_t^T,
+ * g_t = (qx, qy, 1), D_k the slope of the interpolated channel along x'.
+ * A step solves (H + mu diag(H) + tiny I) delta = -g in double and is kept
+ * only if C decreases (then mu /= 10, else mu *= 10), so C never grows.
+ * Costs of 1e5 (no support) are left alone. */
+struct PmGnArgs {
+    PmCostConsts k;
+    PmView v1, v2;
+    float4* planes;            /* (a, b, c, -) in/out */
+    int lr, steps;
+    float* cost;               /* may be NULL */
+};
+
+/* One sweep: cost, gradient and GN matrix (upper triangle) at state s. */
+__device__ float gn_sweep(const PmGnArgs& a, int x, int y, double s0, double s1, double s2, float* g, float* Hm) {
+    const int W = a.k.W, H = a.k.H, P = a.k.P;
+    long long S0, S1, XC;
+    const bool live = fix_plane_d(s0, s1, s2, x, y, S0, S1, XC);
+    const float4 vc = __ldg(&a.v1.col[(size_t)y * W + x]);
+    const int dxlo = max(-P, -x), dxhi = min(P, W - 1 - x);
+    const float al = a.k.alpha, oma = a.k.oma;
+    const float epsc = 0.05f * a.k.cmax, epsg = 0.05f * a.k.gmax;
+    float ws = 0.0f, r1 = 0.0f, r2 = 0.0f;
+    float gs[3] = {0.0f, 0.0f, 0.0f}, hs[6] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
+    for (int dy = -P; dy <= P; ++dy) {
+        const int qy = y + dy;
+        if (qy < 0 || qy >= H) continue;
+        const float* prow = c_prof + (dy + PM_PMAX) * PM_PROF_N + PM_PMAX;
+        long long X = XC + (long long)dy * S1 + (long long)dxlo * S0;
+        const float qyf = (float)qy;
+        for (int dx = dxlo; dx <= dxhi; ++dx) {
+            const long long Xt = X;
+            X += S0;
+            const int xi = (int)(Xt >> 32);
+            if ((unsigned)xi >= (unsigned)W) continue;
+            const int qx = x + dx;
+            const size_t q = (size_t)qy * W + qx;
+            const float4 a1 = __ldg(&a.v1.col[q]);
+            const float4 g1 = __ldg(&a.v1.grad[q]);
+            const float w1 = tap_weight(vc, a1, prow[dx]);
+            TapVals t;
+            load_tap(a.v2, (size_t)qy * a.k.rp + xi, pm_fix_frac(Xt), t);
+            const float e[7] = {a1.x - t.v[0], a1.y - t.v[1], a1.z - t.v[2],
+                                g1.x - t.v[3], g1.y - t.v[4], g1.z - t.v[5], g1.w - t.v[6]};
+            const float cc = (fminf(fabsf(e[0]), a.k.cmax) + fminf(fabsf(e[1]), a.k.cmax)) + fminf(fabsf(e[2]), a.k.cmax);
+            const float gc = ((fminf(fabsf(e[3]), a.k.gmax) + fminf(fabsf(e[4]), a.k.gmax)) +
+                              fminf(fabsf(e[5]), a.k.gmax)) + fminf(fabsf(e[6]), a.k.gmax);
+            r1 = fmaf(w1, cc, r1);
+            r2 = fmaf(w1, gc, r2);
+            ws = ws + w1;
+            float slope = 0.0f, curv = 0.0f;
+#pragma unroll
+            for (int k = 0; k < 7; ++k) {
+                const bool colour = k < 3;
+                const float cap = colour ? a.k.cmax : a.k.gmax;
+                if (!(fabsf(e[k]) < cap)) continue;
+                const float beta = colour ? al : oma;
+                slope = fmaf(beta * tsgn(e[k], cap), t.D[k], slope);
+                curv = fmaf(beta * t.D[k], t.D[k] / fmaxf(fabsf(e[k]), colour ? epsc : epsg), curv);
+            }
+            const float gx = -w1 * slope, hx = w1 * curv;
+            const float qxf = (float)qx;
+            gs[0] = fmaf(gx, qxf, gs[0]); gs[1] = fmaf(gx, qyf, gs[1]); gs[2] += gx;
+            hs[0] = fmaf(hx, qxf * qxf, hs[0]); hs[1] = fmaf(hx, qxf * qyf, hs[1]); hs[2] = fmaf(hx, qxf, hs[2]);
+            hs[3] = fmaf(hx, qyf * qyf, hs[3]); hs[4] = fmaf(hx, qyf, hs[4]); hs[5] += hx;
+        }
+    }
+    if (!live || !(ws > 1.1f)) return 1e5f;
+    const float inv = 1.0f / ws;
+    for (int i = 0; i < 3; ++i) g[i] = gs[i] * inv;
+    for (int i = 0; i < 6; ++i) Hm[i] = hs[i] * inv;
+    return fmaf(a.k.alpha, r1, a.k.oma * r2) / ws;
+}
+
+__global__ void __launch_bounds__(256) k_gn_polish(PmGnArgs a) {
+    const int x = blockIdx.x * 32 + threadIdx.x, y = blockIdx.y * 8 + threadIdx.y;
+    if (x >= a.k.W || y >= a.k.H) return;
+    const size_t o = (size_t)y * a.k.W + x;
+    const float4 pl = a.planes[o];
+    const double ds = a.lr ? -1.0 : 1.0;
+    double s[3] = {1.0 + ds * pl.x, ds * pl.y, ds * pl.z};
+    float g[3], Hm[6];
+    float C = gn_sweep(a, x, y, s[0], s[1], s[2], g, Hm);
+    double mu = 1e-3;
+    for (int it = 0; it < a.steps && C < 1e4f; ++it) {
+        /* (H + mu diag(H) + tiny) delta = -g, symmetric 3x3 by Cramer's rule in double */
+        const double tiny = 1e-9 * (fabs((double)Hm[0]) + fabs((double)Hm[3]) + fabs((double)Hm[5]) + 1e-12);
+        const double m00 = Hm[0] * (1.0 + mu) + tiny, m11 = Hm[3] * (1.0 + mu) + tiny, m22 = Hm[5] * (1.0 + mu) + tiny;
+        const double m01 = Hm[1], m02 = Hm[2], m12 = Hm[4];
+        const double c00 = m11 * m22 - m12 * m12, c01 = m02 * m12 - m01 * m22, c02 = m01 * m12 - m02 * m11;
+        const double det = m00 * c00 + m01 * c01 + m02 * c02;
+        if (!(fabs(det) > 0.0) || !isfinite(det)) break;
+        const double c11 = m00 * m22 - m02 * m02, c12 = m01 * m02 - m00 * m12, c22 = m00 * m11 - m01 * m01;
+        const double b0 = -g[0], b1 = -g[1], b2 = -g[2];
+        const double d0 = (c00 * b0 + c01 * b1 + c02 * b2) / det;
+        const double d1 = (c01 * b0 + c11 * b1 + c12 * b2) / det;
+        const double d2 = (c02 * b0 + c12 * b1 + c22 * b2) / det;
+        float g2[3], H2[6];
+        const float C2 = gn_sweep(a, x, y, s[0] + d0, s[1] + d1, s[2] + d2, g2, H2);
+        if (C2 < C) {
+            s[0] += d0; s[1] += d1; s[2] += d2;
+            C = C2;
+            for (int i = 0; i < 3; ++i) g[i] = g2[i];
+            for (int i = 0; i < 6; ++i) Hm[i] = H2[i];
+            mu = fmax(mu * 0.1, 1e-9);
+        } else {
+            mu *= 10.0;
+        }
+    }
+    a.planes[o] = make_float4((float)(ds * (s[0] - 1.0)), (float)(ds * s[1]), (float)(ds * s[2]), pl.w);
+    if (a.cost) a.cost[o] = C;
+}
+
+cudaError_t pm_launch_gn_polish(const PmCostConsts& k, const PmView& v1, const PmView& v2, float4* planes, int lr,
+                                int steps, float* cost, cudaStream_t st) {
+    PmGnArgs a;
+    a.k = k; a.v1 = v1; a.v2 = v2; a.planes = planes; a.lr = lr; a.steps = steps; a.cost = cost;
+    dim3 grid((k.W + 31) / 32, (k.H + 7) / 8), block(32, 8);
+    k_gn_polish<<<grid, block, 0, st>>>(a);
+    return cudaGetLastError();
+}

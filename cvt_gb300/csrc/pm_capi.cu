@@ -737,6 +737,26 @@ cvtpm_status cvtpm_set_memory_budget(cvtpm_ctx* ctx, size_t bytes) {
     return CVTPM_OK;
 }
 
+cvtpm_status cvtpm_polish_planes(cvtpm_ctx* ctx, const float* img1, const float* img2, int width, int height,
+                                 size_t pitch, float* planes, int lr, int steps, float* cost, void* stream) {
+    if (!ctx) return CVTPM_ERR_INVALID_ARGUMENT;
+    cvtpm_status s;
+    const cvtpm_params& p = ctx->prm;
+    if ((s = check_params(ctx, p)) != CVTPM_OK) return s;
+    if ((s = check_image(ctx, img1, width, height, pitch, "img1")) != CVTPM_OK) return s;
+    if ((s = check_image(ctx, img2, width, height, pitch, "img2")) != CVTPM_OK) return s;
+    if (!planes || ((uintptr_t)planes & 15)) return fail(ctx, CVTPM_ERR_INVALID_ARGUMENT, "planes NULL or not 16-byte aligned");
+    if (steps < 0) return fail(ctx, CVTPM_ERR_INVALID_ARGUMENT, "steps must be >= 0");
+    cudaStream_t st = (cudaStream_t)stream;
+    CK(cudaSetDevice(ctx->device), "cudaSetDevice");
+    if ((s = ensure_buffers(ctx, width, height)) != CVTPM_OK) return s;
+    if ((s = ensure_tables(ctx, p, st)) != CVTPM_OK) return s;
+    if ((s = prep_views(ctx, p, img1, img2, width, height, pitch, st, true)) != CVTPM_OK) return s;
+    const PmPassArgs a = base_args(ctx, p, width, height, 0);
+    LK(pm_launch_gn_polish(a.k, a.v1, a.v2, (float4*)planes, lr, steps, cost, st), "plane polishing");
+    return CVTPM_OK;
+}
+
 cvtpm_status cvtpm_set_timing(cvtpm_ctx* ctx, int enable) {
     if (!ctx) return CVTPM_ERR_INVALID_ARGUMENT;
     ctx->timing = enable != 0;

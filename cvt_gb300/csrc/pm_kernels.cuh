@@ -70,5 +70,7 @@ cudaError_t pm_launch_cost_adjoint(const PmCostConsts& k, const PmView& v1, cons
                                    int lr, const float* dcost, float* cost, float4* dplanes, float4* dI1, float4* dG1,
                                    float4* dI2, float4* dG2, cudaStream_t st);
 cudaError_t pm_launch_adjoint_finish(const float4* dI, const float4* dG, int W, int H, float* out, cudaStream_t st);
+cudaError_t pm_launch_gn_polish(const PmCostConsts& k, const PmView& v1, const PmView& v2, float4* planes, int lr,
+                                int steps, float* cost, cudaStream_t st);
 
 #endif

@@ -231,6 +231,21 @@ class PMHuberStereo:
         self._check(_lib.lib().cvtpm_get_batch_info(self._h, ctypes.byref(info)))
         return info.as_dict()
 
+    def polish_planes(self, img1: torch.Tensor, img2: torch.Tensor, planes: torch.Tensor, lr: int = 1,
+                      steps: int = 4) -> torch.Tensor:
+        """cvtpm_polish_planes on (H, W, 4) planes (a, b, c, -), in place;
+        returns the final per-pixel cost."""
+        _check_img(img1, "img1")
+        _check_img(img2, "img2")
+        if planes.shape != img1.shape or not planes.is_contiguous() or planes.dtype != torch.float32:
+            raise CVTException("planes must be a contiguous float32 (H, W, 4) tensor")
+        H, W = img1.shape[:2]
+        cost = torch.empty((H, W), dtype=torch.float32, device=img1.device)
+        self._check(_lib.lib().cvtpm_polish_planes(self._h, img1.data_ptr(), img2.data_ptr(), W, H,
+                                                   img1.stride(0) * 4, planes.data_ptr(), int(lr), int(steps),
+                                                   cost.data_ptr(), _stream_ptr(img1)))
+        return cost
+
     def set_memory_budget(self, nbytes: int) -> None:
         """Device bytes the FAST path may use for its shared-window weight
         volumes (0: evaluate neighbours per pixel; results are the same)."""

@@ -206,6 +206,20 @@ cvtpm_status cvtpm_cost_adjoint(cvtpm_ctx* ctx,
                                 float* cost, float* dplanes,
                                 float* dimg1, float* dimg2, void* stream);
 
+/* Plane polishing, no counterpart in the reference: `steps` Levenberg-
+ * Marquardt trial steps per pixel on the plane (a, b, c, unused) of view lr
+ * (convention of cvtpm_cost_adjoint), minimising its aggregated cost
+ * (FAST evaluation, fixed-point taps).  The gradient is the adjoint's; the
+ * curvature is the Gauss-Newton matrix of the truncated-L1 terms read as
+ * reweighted least squares.  A step is kept only if the cost decreases, so
+ * no pixel's cost grows; pixels without support (cost 1e5) are unchanged.
+ * planes is updated in place (16-byte aligned); cost (W*H, may be NULL)
+ * receives the final costs. */
+cvtpm_status cvtpm_polish_planes(cvtpm_ctx* ctx, const float* img1, const float* img2,
+                                 int width, int height, size_t pitch,
+                                 float* planes, int lr, int steps, float* cost,
+                                 void* stream);
+
 /* Device memory the context may use for the FAST path's shared-window
  * neighbour costs: two weight volumes of (2*patchsize+1)^2 floats per pixel
  * (4.9 KB per pixel at patchsize 17) plus 32 bytes per pixel.  Within the
