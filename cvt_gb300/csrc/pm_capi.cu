@@ -201,7 +201,8 @@ cvtpm_status check_params(cvtpm_ctx* ctx, const cvtpm_params& p) {
     if (p.pd_iterations < 0) return fail(ctx, CVTPM_ERR_INVALID_ARGUMENT, "pd_iterations must be >= 0");
     if (p.rng != CVTPM_RNG_MWC64X && p.rng != CVTPM_RNG_PHILOX) return fail(ctx, CVTPM_ERR_INVALID_ARGUMENT, "bad rng");
     if (p.arith != CVTPM_ARITH_EXACT && p.arith != CVTPM_ARITH_FAST) return fail(ctx, CVTPM_ERR_INVALID_ARGUMENT, "bad arith");
-    if (p.schedule != CVTPM_SCHEDULE_JACOBI) return fail(ctx, CVTPM_ERR_NOT_SUPPORTED, "only the Jacobi schedule is built");
+    if (p.schedule != CVTPM_SCHEDULE_JACOBI && p.schedule != CVTPM_SCHEDULE_REDBLACK)
+        return fail(ctx, CVTPM_ERR_INVALID_ARGUMENT, "schedule must be CVTPM_SCHEDULE_JACOBI or _REDBLACK");
     if (p.weight_profile != CVTPM_PROFILE_SMOOTHSTEP && p.weight_profile != CVTPM_PROFILE_CONSTANT)
         return fail(ctx, CVTPM_ERR_INVALID_ARGUMENT, "bad weight_profile");
     return CVTPM_OK;
@@ -230,7 +231,29 @@ PmPassArgs base_args(cvtpm_ctx* ctx, const cvtpm_params& p, int W, int H, int v1
     a.rng = p.rng;
     a.key0 = (uint32_t)p.seed; a.key1 = (uint32_t)(p.seed >> 32);
     a.depthmax = p.depthmax;
+    a.color = -1;
     return a;
+}
+
+/* One propagation pass of a view: old states a.old -> a.out.  Jacobi (the
+ * reference, pmhstereo.cl:286-404): every pixel from the old field.
+ * Red/black (optional): the pixels with (x + y) even from the old field,
+ * then the odd ones from the field with the even ones updated; the old
+ * buffer is overwritten with that intermediate field. */
+cvtpm_status propagate_view(cvtpm_ctx* ctx, PmPassArgs a, bool exact, bool redblack, size_t n, cudaStream_t st) {
+    if (!redblack) {
+        a.color = -1;
+        LK(pm_launch_propagate(a, exact, st), "propagate");
+        return CVTPM_OK;
+    }
+    float4* A = const_cast<float4*>(a.old);
+    CK(cudaMemcpyAsync(a.out, A, n * 16, cudaMemcpyDeviceToDevice, st), "red/black copy");
+    a.color = 0;
+    LK(pm_launch_propagate(a, exact, st), "propagate red");
+    CK(cudaMemcpyAsync(A, a.out, n * 16, cudaMemcpyDeviceToDevice, st), "red/black copy");
+    a.color = 1;
+    LK(pm_launch_propagate(a, exact, st), "propagate black");
+    return CVTPM_OK;
 }
 
 /* The weight volumes ((2P+1)^2 floats per pixel and view) and the
@@ -370,7 +393,7 @@ cvtpm_status run_depthmap(cvtpm_ctx* ctx, const cvtpm_params& p, float* dmap, si
         aL.counters = aR.counters = ctx->dcount;
         {
             PhaseTimer tm(ctx, st, ctx->ev_prop);
-            LK(pm_launch_propagate(aL, exact, st), "propagate left");
+            if ((s = propagate_view(ctx, aL, exact, p.schedule == CVTPM_SCHEDULE_REDBLACK, n, st)) != CVTPM_OK) return s;
             tm.stop();
         }
         LK(pm_launch_view_list(ctx->S[0][1 - sw], W, H, ctx->list[0], st), "view list");
@@ -378,7 +401,7 @@ cvtpm_status run_depthmap(cvtpm_ctx* ctx, const cvtpm_params& p, float* dmap, si
         aR.viewin = ctx->list[0]; aR.viewsrc = ctx->S[0][1 - sw]; aR.winners = ctx->win[1];
         {
             PhaseTimer tm(ctx, st, ctx->ev_prop);
-            LK(pm_launch_propagate(aR, exact, st), "propagate right");
+            if ((s = propagate_view(ctx, aR, exact, p.schedule == CVTPM_SCHEDULE_REDBLACK, n, st)) != CVTPM_OK) return s;
             tm.stop();
         }
         ctx->stats.propagate_launches += 2;
@@ -467,7 +490,7 @@ cvtpm_status run_depthmap_inpaint(cvtpm_ctx* ctx, const cvtpm_params& p, float* 
         aL.counters = aR.counters = ctx->dcount;
         {
             PhaseTimer tm(ctx, st, ctx->ev_prop);
-            LK(pm_launch_propagate(aL, exact, st), "propagate left");
+            if ((s = propagate_view(ctx, aL, exact, p.schedule == CVTPM_SCHEDULE_REDBLACK, n, st)) != CVTPM_OK) return s;
             tm.stop();
         }
         LK(pm_launch_view_list(ctx->S[0][1 - sw], W, H, ctx->list[0], st), "view list");
@@ -475,7 +498,7 @@ cvtpm_status run_depthmap_inpaint(cvtpm_ctx* ctx, const cvtpm_params& p, float* 
         aR.viewin = ctx->list[0]; aR.viewsrc = ctx->S[0][1 - sw]; aR.winners = ctx->win[1];
         {
             PhaseTimer tm(ctx, st, ctx->ev_prop);
-            LK(pm_launch_propagate(aR, exact, st), "propagate right");
+            if ((s = propagate_view(ctx, aR, exact, p.schedule == CVTPM_SCHEDULE_REDBLACK, n, st)) != CVTPM_OK) return s;
             tm.stop();
         }
         ctx->stats.propagate_launches += 2;

@@ -109,7 +109,10 @@ __global__ void __launch_bounds__(256) k_cost_field(PmPassArgs a, const float4* 
 template <bool EXACT>
 __global__ void __launch_bounds__(256) k_propagate(PmPassArgs a) {
     const int W = a.k.W, H = a.k.H;
-    const int x = blockIdx.x * 32 + threadIdx.x, y = blockIdx.y * 8 + threadIdx.y;
+    const int y = blockIdx.y * 8 + threadIdx.y;
+    /* red/black passes: thread t of a row owns the t-th pixel of that colour */
+    const int x = a.color < 0 ? blockIdx.x * 32 + threadIdx.x
+                              : 2 * (blockIdx.x * 32 + threadIdx.x) + ((y + a.color) & 1);
     const bool inside = x < W && y < H;
     const int xc = min(x, W - 1), yc = min(y, H - 1);   /* lanes outside still follow the warp */
     const float cx = (float)xc, cy = (float)yc;
@@ -784,16 +787,17 @@ cudaError_t pm_launch_cost_field(const PmPassArgs& a, bool exact, const float4* 
 }
 
 cudaError_t pm_launch_propagate(const PmPassArgs& a, bool exact, cudaStream_t st) {
+    const dim3 grid = a.color < 0 ? pix_grid(a.k.W, a.k.H) : pix_grid((a.k.W + 1) / 2, a.k.H);
     if (exact) {
-        k_propagate<true><<<pix_grid(a.k.W, a.k.H), dim3(32, 8), 0, st>>>(a);
+        k_propagate<true><<<grid, dim3(32, 8), 0, st>>>(a);
     } else {
         PmPassArgs b = a;
-        if (!b.wvol) b.nbcost = nullptr;
+        if (!b.wvol || b.color >= 0) b.nbcost = nullptr;   /* red/black: neighbours per pixel */
         if (b.nbcost) {
             k_nbcost<<<pix_grid(a.k.W, a.k.H), dim3(32, 8), 0, st>>>(b);
             PM_LAUNCH_CHECK();
         }
-        k_propagate<false><<<pix_grid(a.k.W, a.k.H), dim3(32, 8), 0, st>>>(b);
+        k_propagate<false><<<grid, dim3(32, 8), 0, st>>>(b);
     }
     PM_LAUNCH_CHECK();
     return cudaSuccess;

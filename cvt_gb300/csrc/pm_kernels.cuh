@@ -26,6 +26,7 @@ struct PmPassArgs {
     unsigned long long* counters;   /* [0] cost evaluations, [1] in-image taps; may be NULL */
     const float* wvol;         /* FAST: bilateral weights of v1, [(2P+1)^2][W*H], or NULL */
     float* nbcost;             /* FAST with wvol: costs of candidates 1-8, [8][W*H] */
+    int color;                 /* -1: every pixel (Jacobi); 0 / 1: pixels with (x + y) & 1 == color */
 };
 
 cudaError_t pm_upload_tables(const unsigned long long* pow2, const float* prof, cudaStream_t st);

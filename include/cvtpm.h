@@ -77,7 +77,10 @@ typedef struct cvtpm_params {
     int   rng;              /* CVTPM_RNG_*                                  */
     uint64_t seed;          /* Philox key (ignored by MWC64X)               */
     int   arith;            /* CVTPM_ARITH_*                                */
-    int   schedule;         /* CVTPM_SCHEDULE_*                             */
+    int   schedule;         /* CVTPM_SCHEDULE_*: JACOBI is the reference's;
+                               REDBLACK (added) updates the pixels with
+                               (x+y) even from the old field, then the odd
+                               ones from the updated field               */
 } cvtpm_params;
 
 /* Per-pixel integer outputs of a run, for bit-exact comparison. */

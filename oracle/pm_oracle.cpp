@@ -432,14 +432,17 @@ static void init_pass(const Pass& ps, F4* out) {                      /* :230-24
 
 /* pmhstereo_propagate_view, pmhstereo.cl:286-404, without the scatter
  * (build_view_list runs after the pass). */
+/* color >= 0: only the pixels with (x + y) & 1 == color are updated, the
+ * others take their old state (one half of a red/black pass). */
 static void propagate_pass(const Pass& ps, const F4* old, const F4* smoothimg,
-                           const int16_t* viewin, const F4* viewsrc, F4* out, uint8_t* winners) {
+                           const int16_t* viewin, const F4* viewsrc, F4* out, uint8_t* winners, int color = -1) {
     const int W = ps.v1->W, H = ps.v1->H;
     const float dmax = ps.depthmax, theta = ps.theta;
     const int lr = ps.lr;
 #pragma omp parallel for schedule(dynamic, 1)
     for (int y = 0; y < H; ++y)
         for (int x = 0; x < W; ++x) {
+            if (color >= 0 && ((x + y) & 1) != color) { out[(size_t)y * W + x] = old[(size_t)y * W + x]; continue; }
             const float cx = (float)x, cy = (float)y;
             F4 sm = smoothimg[(size_t)y * W + x];                       /* :320-323 */
             float nf = fmaxf(sqrtf(sm.x * sm.x + sm.y * sm.y) + 0.001f, 1.0f);
@@ -491,6 +494,20 @@ static void propagate_pass(const Pass& ps, const F4* old, const F4* smoothimg,
             out[(size_t)y * W + x] = self;
             if (winners) winners[(size_t)y * W + x] = (uint8_t)win;
         }
+}
+
+/* One view pass under the parameters' schedule: Jacobi (the reference), or
+ * red/black (pixels with (x + y) even from the old field, then the odd ones
+ * from the field with the even ones updated; `old` ends as that field). */
+static void propagate_view(const cvtpm_params* prm, const Pass& ps, std::vector<F4>& old, const F4* smoothimg,
+                           const int16_t* viewin, const F4* viewsrc, std::vector<F4>& out, uint8_t* winners) {
+    if (prm->schedule != CVTPM_SCHEDULE_REDBLACK) {
+        propagate_pass(ps, old.data(), smoothimg, viewin, viewsrc, out.data(), winners);
+        return;
+    }
+    propagate_pass(ps, old.data(), smoothimg, viewin, viewsrc, out.data(), winners, 0);
+    old = out;
+    propagate_pass(ps, old.data(), smoothimg, viewin, viewsrc, out.data(), winners, 1);
 }
 
 /* ------------------------------------------------- consistency / fill -- */
@@ -1129,9 +1146,9 @@ int orc_depthmap(const cvtpm_params* prm, const float* left, const float* right,
         int swap = iter & 1;
         pl.iter = pr.iter = iter;
         pl.theta = pr.theta = theta;
-        propagate_pass(pl, SL[swap].data(), smL.data(), list2.data(), SR[swap].data(), SL[1 - swap].data(), winL.data());
+        propagate_view(prm, pl, SL[swap], smL.data(), list2.data(), SR[swap].data(), SL[1 - swap], winL.data());
         build_view_list(SL[1 - swap].data(), W, H, list1.data());
-        propagate_pass(pr, SR[swap].data(), smR.data(), list1.data(), SL[1 - swap].data(), SR[1 - swap].data(), winR.data());
+        propagate_view(prm, pr, SR[swap], smR.data(), list1.data(), SL[1 - swap].data(), SR[1 - swap], winR.data());
         build_view_list(SR[1 - swap].data(), W, H, list2.data());
         float lambda = theta * prm->thetascale + 5.0f;
         consistency(SL[1 - swap].data(), SR[1 - swap].data(), W, H, prm->maxdispdiff, prm->maxanglediff, 1, tmp.data(), nullptr);
@@ -1187,9 +1204,9 @@ int orc_depthmap_inpaint(const cvtpm_params* prm, const float* left, const float
         int swap = iter & 1;
         pl.iter = pr.iter = iter;
         pl.theta = pr.theta = theta;
-        propagate_pass(pl, SL[swap].data(), smL.data(), list2.data(), SR[swap].data(), SL[1 - swap].data(), winL.data());
+        propagate_view(prm, pl, SL[swap], smL.data(), list2.data(), SR[swap].data(), SL[1 - swap], winL.data());
         build_view_list(SL[1 - swap].data(), W, H, list1.data());
-        propagate_pass(pr, SR[swap].data(), smR.data(), list1.data(), SL[1 - swap].data(), SR[1 - swap].data(), winR.data());
+        propagate_view(prm, pr, SR[swap], smR.data(), list1.data(), SL[1 - swap].data(), SR[1 - swap], winR.data());
         build_view_list(SR[1 - swap].data(), W, H, list2.data());
         const float lambda = theta * 20.0f + 5.0f;
         occmap(SL[1 - swap].data(), SR[1 - swap].data(), W, H, 0.5f, 1, mask.data());

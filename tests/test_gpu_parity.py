@@ -191,3 +191,37 @@ def test_depthmap_inpaint_bitexact(stereo, oracle, mode, iters):
     assert_bitexact(tr["valid"].cpu().numpy(), ex["valid"], "valid")
     assert_bitexact(tr["states"].cpu().numpy(), ex["states"], "states")
     assert_bitexact(dm.cpu().numpy(), want, "dmap")
+
+
+@pytest.mark.parametrize("mode", [MODES[0], MODES[1]], ids=MODE_IDS[:2])
+@pytest.mark.parametrize("W,H", [(96, 64), (75, 41)])
+def test_depthmap_redblack_bitexact(stereo, oracle, mode, W, H):
+    """The optional red/black schedule (pixels with x+y even first, then odd)
+    against the oracle's restatement of it; an odd width puts a different
+    number of red and black pixels in each row."""
+    from cvt_gb300.params import SCHEDULE_REDBLACK
+    arith, rng = mode
+    sc = scenes.make_scene(W, H, 4, 16.0, seed=W + H)
+    p = default_params(PRESET_REFERENCE, arith=arith, rng=rng, seed=5, patchsize=7, depthmax=16.0, iterations=3,
+                       pd_iterations=12, schedule=SCHEDULE_REDBLACK)
+    dm, nm, tr, want, ex = run_both(stereo, oracle, sc, p)
+    assert_bitexact(tr["winners"], ex["winners"], "winners")
+    assert_bitexact(tr["states"], ex["states"], "states")
+    assert_bitexact(dm, want, "dmap")
+    jac = default_params(PRESET_REFERENCE, arith=arith, rng=rng, seed=5, patchsize=7, depthmax=16.0, iterations=3,
+                         pd_iterations=12)
+    _, _, trj, _, _ = run_both(stereo, oracle, sc, jac, normalmap=False)
+    assert bit_diff(tr["states"], trj["states"]).any()      # a different schedule
+
+
+def test_depthmap_inpaint_redblack_bitexact(stereo, oracle):
+    from cvt_gb300.params import SCHEDULE_REDBLACK
+    sc = scenes.make_scene(80, 48, 3, 12.0, seed=77)
+    p = default_params(PRESET_BASELINE, patchsize=5, depthmax=12.0, iterations=3, schedule=SCHEDULE_REDBLACK)
+    stereo.set_params(p)
+    tr = {}
+    dm = stereo.depthMapInpaint(None, to_dev(sc.left), to_dev(sc.right), 5, 12.0, 3, 4, trace=tr)
+    torch.cuda.synchronize()
+    want, ex = oracle.depthmap_inpaint(p, sc.left, sc.right, trace=True)
+    assert_bitexact(tr["states"].cpu().numpy(), ex["states"], "states")
+    assert_bitexact(dm.cpu().numpy(), want, "dmap")
