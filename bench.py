@@ -168,6 +168,22 @@ def run_reference(args, rank, world):
     return 0
 
 
+def max_over_ranks(x: float, dist: bool, device) -> float:
+    """The largest value of x over all ranks (the slowest rank sets the time)."""
+    if not dist:
+        return x
+    import torch
+    import torch.distributed as tdist
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    tdist.all_reduce(t, op=tdist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_rate(world: int, W: int, H: int, iters: int, seconds: float) -> float:
+    """Whole-job Mpix-iter/s of `world` replicas, one W x H pair each."""
+    return world * W * H * iters / seconds / 1e6
+
+
 def run_ours(args, rank, world, local_rank):
     import torch
     from cvt_gb300 import scenes, _lib
@@ -216,12 +232,8 @@ def run_ours(args, rank, world, local_rank):
     st.set_timing(False)
     stats = st.stats()
     step_ms = [a.elapsed_time(b) for a, b in ev]
-    ms = float(np.mean(step_ms))
-    if dist:
-        t = torch.tensor([ms], device=dev)
-        tdist.all_reduce(t, op=tdist.ReduceOp.MAX)
-        ms = float(t.item())
-    value = world * W * H * ITERS / (ms * 1e-3) / 1e6
+    ms = max_over_ranks(float(np.mean(step_ms)), dist, dev)
+    value = replica_rate(world, W, H, ITERS, ms * 1e-3)
     bad1 = scenes.bad_pixel_rate(dmap.cpu().numpy() * DMAX, sc)
     epe = scenes.end_point_error(dmap.cpu().numpy() * DMAX, sc)
 
@@ -236,12 +248,8 @@ def run_ours(args, rank, world, local_rank):
     for _ in range(args.steps):
         st.depthMapHost(hl.numpy(), hr.numpy(), PATCH, DMAX, ITERS, 4, dmap=hd.numpy())
     barrier()
-    e2e_s = (time.perf_counter() - t0) / args.steps
-    if dist:
-        t = torch.tensor([e2e_s], device=dev)
-        tdist.all_reduce(t, op=tdist.ReduceOp.MAX)
-        e2e_s = float(t.item())
-    e2e = world * W * H * ITERS / e2e_s / 1e6
+    e2e_s = max_over_ranks((time.perf_counter() - t0) / args.steps, dist, dev)
+    e2e = replica_rate(world, W, H, ITERS, e2e_s)
 
     if rank != 0:
         return 0
