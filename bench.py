@@ -399,6 +399,122 @@ def run_batch(args):
     return 0
 
 
+def _disparity(planes, W, H):
+    import torch
+    yy, xx = torch.meshgrid(torch.arange(H, device=planes.device), torch.arange(W, device=planes.device), indexing="ij")
+    return planes[..., 0] * xx + planes[..., 1] * yy + planes[..., 2]
+
+
+def run_adjoint(args):
+    """The differentiation workload: forward + adjoint (planes and both
+    images) of the aggregated cost for 8 pairs at 640x480, plane fields =
+    ground truth + N(0, 0.01) on a, b and N(0, 1) on c."""
+    import torch
+    from cvt_gb300 import scenes
+    from cvt_gb300.stereo import PMHuberStereo
+    from cvt_gb300.params import default_params, PRESET_BASELINE
+    st = PMHuberStereo(0, default_params(PRESET_BASELINE, patchsize=PATCH))
+    rng = np.random.default_rng(4)
+    items = []
+    for i in range(8):
+        sc = scenes.make_scene(640, 480, 8, 64.0, seed=4000 + i)
+        pf = sc.plane_field().astype(np.float64)
+        pl = np.zeros((480, 640, 4), np.float32)
+        pl[..., 0] = np.clip(pf[..., 0] + rng.normal(0, 0.01, pf.shape[:2]), -0.3, 0.3)
+        pl[..., 1] = np.clip(pf[..., 1] + rng.normal(0, 0.01, pf.shape[:2]), -0.3, 0.3)
+        pl[..., 2] = np.clip(pf[..., 2] + rng.normal(0, 1.0, pf.shape[:2]), 0.0, 64.0)
+        items.append((torch.from_numpy(sc.left).cuda(), torch.from_numpy(sc.right).cuda(), torch.from_numpy(pl).cuda(),
+                      torch.randn(480, 640, device="cuda")))
+    stream = torch.cuda.current_stream()
+
+    def timed(fn, reps):
+        fn()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(reps):
+            fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / reps
+    fwd = timed(lambda: [st.cost_adjoint(a, b, p, 1) for a, b, p, g in items], args.steps)
+    full = timed(lambda: [st.cost_adjoint(a, b, p, 1, dcost=g) for a, b, p, g in items], args.steps)
+    mpx = 8 * 640 * 480 / 1e6
+    print(json.dumps({"workload": "adjoint", "config": {"workload": "8 pairs 640x480, 35x35 ASW, BASELINE preset, "
+                                                                     "forward + adjoint w.r.t. planes and both images"},
+                      "forward_ms": fwd, "forward_plus_adjoint_ms": full,
+                      "forward_mpix_per_s": mpx / (fwd * 1e-3), "forward_plus_adjoint_mpix_per_s": mpx / (full * 1e-3),
+                      "unit": "Mpix/s", "steps": args.steps}), flush=True)
+    return 0
+
+
+def run_combined(args):
+    """The combined workload: 16 uneven pairs (up to 1920x1080, disparity up
+    to 256) in one batched graph with 8 iterations, then 4 plane-polishing
+    steps per pixel of the left views; bad-1px and EPE against ground truth
+    and against the plain output."""
+    import multiprocessing as mp
+    import torch
+    from cvt_gb300 import scenes
+    from cvt_gb300.stereo import PMHuberStereo
+    shapes = scenes.batch_shapes(args.pairs, seed=5000)
+    with mp.get_context("spawn").Pool(min(16, os.cpu_count() or 4)) as pool:
+        scs = pool.map(scenes.batch_scene, shapes)
+    p = params_for("ours").replace(iterations=8)
+    pairs = [(torch.from_numpy(sc.left).cuda(), torch.from_numpy(sc.right).cuda(), sh[2]) for sc, sh in zip(scs, shapes)]
+    bat = PMHuberStereo(0, p)
+    outs = bat.depthMapBatched(pairs)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    bat.depthMapBatched(pairs, outs=outs)
+    e1.record()
+    torch.cuda.synchronize()
+    t_batch = e0.elapsed_time(e1) / 1e3
+    plain = PMHuberStereo(0, p)
+    t_polish = 0.0
+    rows = []
+    for (left, right, dmax), sc, d_b in zip(pairs, scs, outs):
+        H, W = left.shape[:2]
+        tr = {}
+        d_plain = plain.depthMap(None, left, right, PATCH, dmax, p.iterations, 4, trace=tr)
+        s = tr["states"][0]
+        planes = torch.zeros_like(s)
+        planes[..., 0], planes[..., 1], planes[..., 2] = 1 - s[..., 0], -s[..., 1], -s[..., 2]
+        planes = planes.contiguous()
+        a0 = _disparity(planes, W, H)
+        torch.cuda.synchronize()
+        q0, q1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        q0.record()
+        plain.polish_planes(left, right, planes, 1, 4)
+        q1.record()
+        torch.cuda.synchronize()
+        t_polish += q0.elapsed_time(q1) / 1e3
+        valid = tr["valid"].bool()
+        dp = d_plain * dmax
+        d_pol = torch.where(valid, _disparity(planes, W, H), dp)
+        gt = torch.from_numpy(sc.disp_left).cuda()
+        m = ~torch.from_numpy(sc.occluded).cuda()
+        same = bool((d_b == d_plain).all())
+        rows.append({"bad1_plain": float(((dp - gt).abs() > 1)[m].float().mean()) * 100,
+                     "bad1_polished": float(((d_pol - gt).abs() > 1)[m].float().mean()) * 100,
+                     "epe_plain": float((dp - gt).abs()[m].mean()), "epe_polished": float((d_pol - gt).abs()[m].mean()),
+                     "epe_vs_plain": float((d_pol - dp).abs()[m].mean()), "batched_equals_plain": same,
+                     "pixels": W * H})
+    npx = sum(r["pixels"] for r in rows)
+    wavg = lambda k: sum(r[k] * r["pixels"] for r in rows) / npx
+    print(json.dumps({"workload": "combined",
+                      "config": {"workload": f"{len(pairs)} pairs up to 1920x1080, dmax up to 256, 8 iterations batched, "
+                                             "then 4 plane-polishing steps, BASELINE preset, FAST + Philox",
+                                 "pixels": npx},
+                      "batched_seconds": t_batch, "batched_mpix_iter_per_s": npx * 8 / t_batch / 1e6,
+                      "polish_seconds": t_polish, "lanes": bat.batch_info()["lanes"],
+                      "quality": {k: wavg(k) for k in ("bad1_plain", "bad1_polished", "epe_plain", "epe_polished",
+                                                       "epe_vs_plain")},
+                      "batched_equals_plain": all(r["batched_equals_plain"] for r in rows)}), flush=True)
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -410,8 +526,9 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--profile", action="store_true", help="short run for ncu captures")
     ap.add_argument("--profile-iters", type=int, default=1)
-    ap.add_argument("--workload", choices=["pair", "batch"], default="pair",
-                    help="pair: the 1242x375 headline; batch: uneven pairs, plain loop vs batched graph")
+    ap.add_argument("--workload", choices=["pair", "batch", "adjoint", "combined"], default="pair",
+                    help="pair: the 1242x375 headline; batch: uneven pairs, plain loop vs batched graph; "
+                         "adjoint: forward + adjoint, 8 x 640x480; combined: 16 pairs batched + plane polishing")
     ap.add_argument("--pairs", type=int, default=64)
     ap.add_argument("--batch-iters", type=int, default=5)
     args = ap.parse_args()
@@ -419,6 +536,12 @@ def main():
         return run_profile(args)
     if args.workload == "batch":
         return run_batch(args)
+    if args.workload == "adjoint":
+        return run_adjoint(args)
+    if args.workload == "combined":
+        if args.pairs == 64:
+            args.pairs = 16
+        return run_combined(args)
     if args.warmup < 3 and args.impl == "ours":
         args.warmup = 3
     world = int(os.environ.get("WORLD_SIZE", "1"))
