@@ -391,7 +391,7 @@ def run_batch(args):
                        "pixels": npx},
             "plain_loop": {"value": mpix_iter / t_plain, "seconds": t_plain},
             "batched": {"value": mpix_iter / t_bat, "seconds": t_bat, "first_call_seconds": first,
-                        "lanes": info["lanes"], "volumes": info["volumes"], "graph_nodes": info["graph_nodes"],
+                        "lanes": info["lanes"], "shared_windows": info["shared_windows"], "graph_nodes": info["graph_nodes"],
                         "tuning": info["candidates"]},
             "speedup": t_plain / t_bat, "bit_identical_to_plain": same,
             "quality": {"bad1_nonocc_pct_mean": float(np.mean(bad))}}

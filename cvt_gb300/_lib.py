@@ -39,16 +39,15 @@ BATCH_MAX_CAND = 8
 
 
 class CvtpmBatchInfo(ctypes.Structure):
-    _fields_ = [("lanes", ctypes.c_int), ("volumes", ctypes.c_int), ("tuned", ctypes.c_int), ("ncand", ctypes.c_int),
-                ("cand_lanes", ctypes.c_int * BATCH_MAX_CAND), ("cand_volumes", ctypes.c_int * BATCH_MAX_CAND),
+    _fields_ = [("lanes", ctypes.c_int), ("shared_windows", ctypes.c_int), ("tuned", ctypes.c_int),
+                ("ncand", ctypes.c_int), ("cand_lanes", ctypes.c_int * BATCH_MAX_CAND),
                 ("cand_ms", ctypes.c_float * BATCH_MAX_CAND), ("graph_nodes", ctypes.c_longlong),
                 ("replays", ctypes.c_longlong)]
 
     def as_dict(self) -> dict:
         n = self.ncand
-        return {"lanes": self.lanes, "volumes": self.volumes, "tuned": self.tuned,
-                "candidates": [{"lanes": self.cand_lanes[i], "volumes": self.cand_volumes[i], "proxy_ms": self.cand_ms[i]}
-                               for i in range(n)],
+        return {"lanes": self.lanes, "shared_windows": self.shared_windows, "tuned": self.tuned,
+                "candidates": [{"lanes": self.cand_lanes[i], "proxy_ms": self.cand_ms[i]} for i in range(n)],
                 "graph_nodes": self.graph_nodes, "replays": self.replays}
 
 

@@ -46,14 +46,12 @@ struct cvtpm_ctx {
     uint8_t* win[2];
     uint8_t* valid;
     float* occ;                       /* occlusion mask of depthMapInpaint */
-    /* FAST shared-window neighbour costs: weight volumes of both views and
-     * the per-pixel costs of candidates 1-8, when the budget allows */
-    float* vol = nullptr;
-    size_t vol_bytes = 0;
-    size_t vol_budget = SIZE_MAX;
-    bool vol_on = false;
-    float* wvol[2] = {nullptr, nullptr};
+    /* FAST shared-window neighbour costs: the costs of candidates 1-8 per
+     * pixel ([8][W*H] floats), when the budget allows */
     float* nbcost = nullptr;
+    size_t nb_bytes = 0;
+    size_t nb_budget = SIZE_MAX;
+    bool nb_on = false;
     /* set while a launch sequence is being captured into a graph: scratch
      * must already be sized, nothing may be allocated */
     bool no_alloc = false;
@@ -67,7 +65,6 @@ struct cvtpm_ctx {
     std::vector<unsigned char> bkey;
     std::vector<unsigned char> tkey;   /* shapes of the last tuned batch (no pointers) */
     int tuned_lanes = 0;
-    bool tuned_vol = false;
     int batch_lanes = 0;              /* 0: autotune */
     cvtpm_batch_info binfo{};
     /* staging for the *_host entry points */
@@ -256,32 +253,28 @@ cvtpm_status propagate_view(cvtpm_ctx* ctx, PmPassArgs a, bool exact, bool redbl
     return CVTPM_OK;
 }
 
-/* The weight volumes ((2P+1)^2 floats per pixel and view) and the
- * neighbour-cost buffer of the FAST shared-window path.  Used when they fit
- * the context's budget and 60 % of the free device memory; otherwise the
- * propagation evaluates every neighbour per pixel (same results). */
-cvtpm_status ensure_volumes(cvtpm_ctx* ctx, int W, int H, int P) {
-    const size_t n = (size_t)W * H, N2 = (size_t)(2 * P + 1) * (2 * P + 1);
-    const size_t need = (2 * N2 + 8) * n * sizeof(float);
-    ctx->vol_on = false;
-    if (need > ctx->vol_budget) return CVTPM_OK;
-    if (ctx->vol_bytes < need) {
+/* The neighbour-cost buffer of the FAST shared-window path (8 floats per
+ * pixel).  Used when it fits the context's budget and 60 % of the free device
+ * memory; otherwise the propagation evaluates every neighbour per pixel (same
+ * results). */
+cvtpm_status ensure_nbcost(cvtpm_ctx* ctx, int W, int H) {
+    const size_t need = (size_t)8 * W * H * sizeof(float);
+    ctx->nb_on = false;
+    if (need > ctx->nb_budget) return CVTPM_OK;
+    if (ctx->nb_bytes < need) {
         if (ctx->no_alloc) return CVTPM_OK;          /* capturing: per-pixel neighbours */
-        if (ctx->vol) { CK(cudaFree(ctx->vol), "free volumes"); ctx->vol = nullptr; ctx->vol_bytes = 0; }
+        if (ctx->nbcost) { CK(cudaFree(ctx->nbcost), "free neighbour costs"); ctx->nbcost = nullptr; ctx->nb_bytes = 0; }
         size_t fr = 0, tot = 0;
         CK(cudaMemGetInfo(&fr, &tot), "memory info");
         if ((double)need > 0.6 * (double)fr) return CVTPM_OK;
-        if (cudaMalloc(&ctx->vol, need) != cudaSuccess) {
+        if (cudaMalloc(&ctx->nbcost, need) != cudaSuccess) {
             cudaGetLastError();                      /* clear the failed allocation; use the per-pixel path */
-            ctx->vol = nullptr;
+            ctx->nbcost = nullptr;
             return CVTPM_OK;
         }
-        ctx->vol_bytes = need;
+        ctx->nb_bytes = need;
     }
-    ctx->wvol[0] = ctx->vol;
-    ctx->wvol[1] = ctx->vol + N2 * n;
-    ctx->nbcost = ctx->vol + 2 * N2 * n;
-    ctx->vol_on = true;
+    ctx->nb_on = true;
     return CVTPM_OK;
 }
 
@@ -360,13 +353,8 @@ cvtpm_status run_depthmap(cvtpm_ctx* ctx, const cvtpm_params& p, float* dmap, si
     const int N = p.iterations;
     PmPassArgs aL = base_args(ctx, p, W, H, 0), aR = base_args(ctx, p, W, H, 1);
     if (!exact) {
-        if ((s = ensure_volumes(ctx, W, H, p.patchsize)) != CVTPM_OK) return s;
-        if (ctx->vol_on) {
-            LK(pm_launch_weights(ctx->col[0], W, H, p.patchsize, ctx->wvol[0], st), "weights left");
-            LK(pm_launch_weights(ctx->col[1], W, H, p.patchsize, ctx->wvol[1], st), "weights right");
-            aL.wvol = ctx->wvol[0]; aR.wvol = ctx->wvol[1];
-            aL.nbcost = aR.nbcost = ctx->nbcost;
-        }
+        if ((s = ensure_nbcost(ctx, W, H)) != CVTPM_OK) return s;
+        if (ctx->nb_on) aL.nbcost = aR.nbcost = ctx->nbcost;
     }
     if (!ctx->dcount) {
         if (ctx->no_alloc) return fail(ctx, CVTPM_ERR_ALLOC, "counters not allocated before capture");
@@ -459,13 +447,8 @@ cvtpm_status run_depthmap_inpaint(cvtpm_ctx* ctx, const cvtpm_params& p, float* 
     const int N = p.iterations;
     PmPassArgs aL = base_args(ctx, p, W, H, 0), aR = base_args(ctx, p, W, H, 1);
     if (!exact) {
-        if ((s = ensure_volumes(ctx, W, H, p.patchsize)) != CVTPM_OK) return s;
-        if (ctx->vol_on) {
-            LK(pm_launch_weights(ctx->col[0], W, H, p.patchsize, ctx->wvol[0], st), "weights left");
-            LK(pm_launch_weights(ctx->col[1], W, H, p.patchsize, ctx->wvol[1], st), "weights right");
-            aL.wvol = ctx->wvol[0]; aR.wvol = ctx->wvol[1];
-            aL.nbcost = aR.nbcost = ctx->nbcost;
-        }
+        if ((s = ensure_nbcost(ctx, W, H)) != CVTPM_OK) return s;
+        if (ctx->nb_on) aL.nbcost = aR.nbcost = ctx->nbcost;
     }
     if (!ctx->dcount) {
         if (ctx->no_alloc) return fail(ctx, CVTPM_ERR_ALLOC, "counters not allocated before capture");
@@ -632,7 +615,7 @@ cvtpm_status cvtpm_destroy(cvtpm_ctx* ctx) {
     if (ctx->bfork) cudaEventDestroy(ctx->bfork);
     if (ctx->bjoin) cudaEventDestroy(ctx->bjoin);
     if (ctx->stage) cudaFree(ctx->stage);
-    if (ctx->vol) cudaFree(ctx->vol);
+    if (ctx->nbcost) cudaFree(ctx->nbcost);
     if (ctx->dcount) cudaFree(ctx->dcount);
     for (auto& pr : ctx->ev_prop) { cudaEventDestroy(pr.first); cudaEventDestroy(pr.second); }
     for (auto& pr : ctx->ev_pd) { cudaEventDestroy(pr.first); cudaEventDestroy(pr.second); }
@@ -750,12 +733,12 @@ cvtpm_status cvtpm_cost_eval(cvtpm_ctx* ctx, const float* img1, const float* img
 
 cvtpm_status cvtpm_set_memory_budget(cvtpm_ctx* ctx, size_t bytes) {
     if (!ctx) return CVTPM_ERR_INVALID_ARGUMENT;
-    ctx->vol_budget = bytes;
-    if (ctx->vol && ctx->vol_bytes > bytes) {
+    ctx->nb_budget = bytes;
+    if (ctx->nbcost && ctx->nb_bytes > bytes) {
         CK(cudaSetDevice(ctx->device), "cudaSetDevice");
-        CK(cudaFree(ctx->vol), "free volumes");
-        ctx->vol = nullptr;
-        ctx->vol_bytes = 0;
+        CK(cudaFree(ctx->nbcost), "free neighbour costs");
+        ctx->nbcost = nullptr;
+        ctx->nb_bytes = 0;
     }
     return CVTPM_OK;
 }
@@ -877,7 +860,7 @@ cvtpm_status check_pair(cvtpm_ctx* ctx, const cvtpm_pair& q, int i) {
     return CVTPM_OK;
 }
 
-/* Lanes: each has its own context (scratch, weight volumes, counters) and
+/* Lanes: each has its own context (scratch, neighbour costs, counters) and
  * stream, so the pairs of different lanes run concurrently. */
 cvtpm_status ensure_lanes(cvtpm_ctx* ctx, int k) {
     while ((int)ctx->lanes.size() < k) {
@@ -919,7 +902,7 @@ std::vector<std::vector<int>> assign_lanes(const cvtpm_pair* pairs, int npairs, 
 
 /* Captures the whole batch (every pair's depthMap schedule, lanes as
  * parallel branches) into one graph and instantiates it. */
-cvtpm_status capture_batch(cvtpm_ctx* ctx, const cvtpm_pair* pairs, int npairs, int k, bool volumes, int iterations,
+cvtpm_status capture_batch(cvtpm_ctx* ctx, const cvtpm_pair* pairs, int npairs, int k, int iterations,
                            cudaGraphExec_t* exec, size_t* nodes) {
     cvtpm_status s;
     if ((s = ensure_lanes(ctx, k)) != CVTPM_OK) return s;
@@ -930,12 +913,12 @@ cvtpm_status capture_batch(cvtpm_ctx* ctx, const cvtpm_pair* pairs, int npairs, 
     for (int j = 0; j < k; ++j) {
         cvtpm_ctx* c = ctx->lanes[j].c;
         c->prm = p;
-        if ((s = cvtpm_set_memory_budget(c, volumes ? ctx->vol_budget : 0)) != CVTPM_OK) return fail(ctx, s, c->err);
+        if ((s = cvtpm_set_memory_budget(c, ctx->nb_budget)) != CVTPM_OK) return fail(ctx, s, c->err);
         c->timing = false;
         for (int i : plan[j]) {
             if ((s = ensure_buffers(c, pairs[i].width, pairs[i].height)) != CVTPM_OK) return fail(ctx, s, c->err);
             if (p.arith == CVTPM_ARITH_FAST &&
-                (s = ensure_volumes(c, pairs[i].width, pairs[i].height, p.patchsize)) != CVTPM_OK)
+                (s = ensure_nbcost(c, pairs[i].width, pairs[i].height)) != CVTPM_OK)
                 return fail(ctx, s, c->err);
         }
     }
@@ -987,14 +970,11 @@ cvtpm_status launch_batch(cvtpm_ctx* ctx, cudaGraphExec_t exec, cudaStream_t st)
 }
 
 /* The autotuner: times a one-iteration proxy of the batch (one graph launch
- * each) for 1, 2, 4 and 8 lanes with the shared-window weight volumes
- * allowed (FAST), then the best lane count without them, and keeps the
- * fastest. */
-cvtpm_status tune_batch(cvtpm_ctx* ctx, const cvtpm_pair* pairs, int npairs, int* lanes_out, bool* vol_out) {
-    const bool fast = ctx->prm.arith == CVTPM_ARITH_FAST;
-    std::vector<std::pair<int, bool>> cand;
+ * each) for 1, 2, 4 and 8 lanes and keeps the fastest. */
+cvtpm_status tune_batch(cvtpm_ctx* ctx, const cvtpm_pair* pairs, int npairs, int* lanes_out) {
+    std::vector<int> cand;
     for (int k : {1, 2, 4, 8})
-        if (k == 1 || k <= npairs) cand.push_back({k, fast && ctx->vol_budget > 0});
+        if (k == 1 || k <= npairs) cand.push_back(k);
     cvtpm_batch_info& bi = ctx->binfo;
     bi.ncand = 0;
     float best = 0.0f;
@@ -1003,11 +983,10 @@ cvtpm_status tune_batch(cvtpm_ctx* ctx, const cvtpm_pair* pairs, int npairs, int
     CK(cudaEventCreate(&t1), "tune event");
     for (size_t ci = 0; ci < cand.size(); ++ci) {
         {
-            const int k = cand[ci].first;
-            const bool vol = cand[ci].second;
+            const int k = cand[ci];
             cudaGraphExec_t ex = nullptr;
             size_t nodes = 0;
-            cvtpm_status s = capture_batch(ctx, pairs, npairs, k, vol, 1, &ex, &nodes);
+            cvtpm_status s = capture_batch(ctx, pairs, npairs, k, 1, &ex, &nodes);
             if (s != CVTPM_OK) { cudaEventDestroy(t0); cudaEventDestroy(t1); return s; }
             float ms = 0.0f;
             bool ok = cudaEventRecord(t0, ctx->bstream) == cudaSuccess &&
@@ -1019,14 +998,11 @@ cvtpm_status tune_batch(cvtpm_ctx* ctx, const cvtpm_pair* pairs, int npairs, int
             if (!ok) { cudaEventDestroy(t0); cudaEventDestroy(t1); return cuda_fail(ctx, cudaGetLastError(), "tuning run"); }
             if (bi.ncand < CVTPM_BATCH_MAX_CAND) {
                 bi.cand_lanes[bi.ncand] = k;
-                bi.cand_volumes[bi.ncand] = vol ? 1 : 0;
                 bi.cand_ms[bi.ncand] = ms;
                 ++bi.ncand;
             }
-            if (best == 0.0f || ms < best) { best = ms; *lanes_out = k; *vol_out = vol; }
+            if (best == 0.0f || ms < best) { best = ms; *lanes_out = k; }
         }
-        if (ci + 1 == cand.size() && cand.back().second)     /* then the best lane count without volumes */
-            cand.push_back({*lanes_out, false});
     }
     cudaEventDestroy(t0);
     cudaEventDestroy(t1);
@@ -1055,7 +1031,7 @@ cvtpm_status cvtpm_depthmap_batched(cvtpm_ctx* ctx, const cvtpm_pair* pairs, int
     put(&pr.grad_maxdiff, sizeof(float)); put(&pr.weight_profile, sizeof(int)); put(&pr.rng, sizeof(int));
     put(&pr.seed, sizeof(uint64_t)); put(&pr.arith, sizeof(int)); put(&pr.schedule, sizeof(int));
     put(&ctx->batch_lanes, sizeof(int));
-    put(&ctx->vol_budget, sizeof(size_t));
+    put(&ctx->nb_budget, sizeof(size_t));
     for (int i = 0; i < npairs; ++i) {
         const cvtpm_pair& q = pairs[i];
         put(&q.width, sizeof(int)); put(&q.height, sizeof(int)); put(&q.depthmax, sizeof(float));
@@ -1074,25 +1050,22 @@ cvtpm_status cvtpm_depthmap_batched(cvtpm_ctx* ctx, const cvtpm_pair* pairs, int
     if ((s = ensure_lanes(ctx, 1)) != CVTPM_OK) return s;
     CK(cudaStreamSynchronize(st), "batch order");      /* inputs written on `st` before tuning reads them */
     int k = ctx->batch_lanes;
-    bool vol = ctx->prm.arith == CVTPM_ARITH_FAST && ctx->vol_budget > 0;
     ctx->binfo.tuned = 0;
     if (k <= 0) {
         if (tkey == ctx->tkey) {                         /* same shapes: keep the tuned choice */
             k = ctx->tuned_lanes;
-            vol = ctx->tuned_vol;
         } else {
-            if ((s = tune_batch(ctx, pairs, npairs, &k, &vol)) != CVTPM_OK) return s;
+            if ((s = tune_batch(ctx, pairs, npairs, &k)) != CVTPM_OK) return s;
             ctx->tkey = tkey;
             ctx->tuned_lanes = k;
-            ctx->tuned_vol = vol;
         }
         ctx->binfo.tuned = 1;
     }
     size_t nodes = 0;
-    if ((s = capture_batch(ctx, pairs, npairs, k, vol, ctx->prm.iterations, &ctx->bexec, &nodes)) != CVTPM_OK) return s;
+    if ((s = capture_batch(ctx, pairs, npairs, k, ctx->prm.iterations, &ctx->bexec, &nodes)) != CVTPM_OK) return s;
     ctx->bkey = key;
     ctx->binfo.lanes = k;
-    ctx->binfo.volumes = vol ? 1 : 0;
+    ctx->binfo.shared_windows = ctx->prm.arith == CVTPM_ARITH_FAST && ctx->nb_budget > 0 ? 1 : 0;
     ctx->binfo.graph_nodes = (long long)nodes;
     ctx->binfo.replays = 0;
     return launch_batch(ctx, ctx->bexec, st);

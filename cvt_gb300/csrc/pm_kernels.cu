@@ -252,44 +252,26 @@ __global__ void __launch_bounds__(256) k_propagate(PmPassArgs a) {
 }
 
 /* ---------------------------------------- shared neighbour windows -- */
-/* Bilateral weights of every pixel p and window offset o = (dy+P)(2P+1) +
- * (dx+P), stored at wvol[o * W*H + p] (0 outside the image); the same
- * arithmetic as the weight of eval_costs. */
-__global__ void __launch_bounds__(256) k_weights(const float4* __restrict__ col, int W, int H, int P,
-                                                 float* __restrict__ wvol) {
-    const int x = blockIdx.x * 32 + threadIdx.x, y = blockIdx.y * 8 + threadIdx.y;
-    if (x >= W || y >= H) return;
-    const size_t n = (size_t)W * H, p = (size_t)y * W + x;
-    const float4 vc = col[p];
-    const int N = 2 * P + 1;
-    for (int dy = -P; dy <= P; ++dy) {
-        const int qy = y + dy;
-        const float* prow = c_prof + (dy + PM_PMAX) * PM_PROF_N + PM_PMAX;
-        float* orow = wvol + (size_t)((dy + P) * N + P) * n + p;
-        for (int dx = -P; dx <= P; ++dx) {
-            const int qx = x + dx;
-            float w = 0.0f;
-            if (qy >= 0 && qy < H && qx >= 0 && qx < W) w = tap_weight(vc, __ldg(&col[(size_t)qy * W + qx]), prow[dx]);
-            orow[(ptrdiff_t)dx * (ptrdiff_t)n] = w;
-        }
-    }
-}
-
 /* Candidates 1-8 (pmhstereo.cl:330-342) evaluated plane by plane.  Thread m
  * owns the plane old[m]; it is candidate k of the pixel u_k = m - o_k for
  * the 8 offsets o_k of the 3x3 neighbourhood (u_k inside the image makes the
  * clamp of :335-336 the identity; border pixels evaluate their clamped
  * neighbours themselves).  A tap's matching terms depend on the tap and the
  * plane only, so they are computed once over the union of the 8 windows
- * (37 x 37) and folded into every user's sums with that user's weight from
- * the weight volume.  Each user receives its taps in raster order with the
- * operations of eval_costs, so its cost has the bits of a separate
- * evaluation.  Costs go to nb[k * W*H + u_k].  (Staging the weight slices in
- * a shared-memory ring with cp.async, the block walking the offsets in
- * lockstep, measured slower: the per-batch barriers expose the latency of
- * the record loads that the free-running warps overlap.) */
+ * (37 x 37) and folded into every user's sums with that user's bilateral
+ * weight, formed by tap_weight from the user's centre colour as eval_costs
+ * forms it.  Each user receives its taps in raster order with the operations
+ * of eval_costs, so its cost has the bits of a separate evaluation.  Costs go
+ * to nb[k * W*H + u_k].  Within a warp the window offsets are the same in
+ * every lane, so the profile read is a constant-cache broadcast.
+ * (Measured alternatives: weights precomputed into a [(2P+1)^2][W*H] volume
+ * and loaded, 8 per tap, ran at the same speed for 4.9 KB per pixel; half
+ * loaded, half recomputed ran slower than either; staging the volume in a
+ * shared-memory ring exposed the latency of the record loads.)  The minimum
+ * of 2 blocks per SM makes the allocator use up to 128 registers: without
+ * it, it chose 97 and the kernel ran 8 % slower. */
 __global__ void __launch_bounds__(256, 2) k_nbcost(PmPassArgs a) {
-    const int W = a.k.W, H = a.k.H, P = a.k.P, N = 2 * P + 1;
+    const int W = a.k.W, H = a.k.H, P = a.k.P;
     const int mx = blockIdx.x * 32 + threadIdx.x, my = blockIdx.y * 8 + threadIdx.y;
     if (mx >= W || my >= H) return;
     const size_t n = (size_t)W * H, m = (size_t)my * W + mx;
@@ -304,25 +286,20 @@ __global__ void __launch_bounds__(256, 2) k_nbcost(PmPassArgs a) {
         const int ux = mx - ox, uy = my - oy;
         if (ux >= 0 && ux < W && uy >= 0 && uy < H) uok |= 1u << k;
     }
+    float4 uc[8];                                   /* the users' centre colours */
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+        const int nn = k < 4 ? k : k + 1, ox = nn % 3 - 1, oy = nn / 3 - 1;
+        const int ux = min(max(mx - ox, 0), W - 1), uy = min(max(my - oy, 0), H - 1);
+        uc[k] = __ldg(&a.v1.col[(size_t)uy * W + ux]);
+    }
     float r1[8], r2[8], ws[8];
 #pragma unroll
     for (int k = 0; k < 8; ++k) { r1[k] = 0.0f; r2[k] = 0.0f; ws[k] = 0.0f; }
     const int qx0 = max(mx - P - 1, 0), qx1 = min(mx + P + 1, W - 1);
     const int qy0 = max(my - P - 1, 0), qy1 = min(my + P + 1, H - 1);
-    const int lane = threadIdx.x & 31;
-    const ptrdiff_t wrow0 = (ptrdiff_t)my * W + (mx - lane) - 1;     /* the warp's pixel row, one left */
     for (int qy = qy0; qy <= qy1; ++qy) {
         const int ry = qy - my;
-        /* L2 prefetch of the weight-volume slice row the next iteration row
-         * starts to use (offset row ry + P + 2), for this warp's pixel row:
-         * 2 lines of 128 B per slice, N slices */
-        if (ry + P + 2 < N) {
-            for (int i = lane; i < 2 * N; i += 32) {
-                const ptrdiff_t pix = min(max(wrow0 + (ptrdiff_t)(i & 1) * 32, (ptrdiff_t)0), (ptrdiff_t)n - 1);
-                const float* pf = a.wvol + (ptrdiff_t)((ry + P + 2) * N + (i >> 1)) * (ptrdiff_t)n + pix;
-                asm volatile("prefetch.global.L2 [%0];" :: "l"(pf));
-            }
-        }
         unsigned rmask = 0;
 #pragma unroll
         for (int k = 0; k < 8; ++k) {
@@ -353,13 +330,12 @@ __global__ void __launch_bounds__(256, 2) k_nbcost(PmPassArgs a) {
             const float4 g1 = __ldg(&g1row[qx]);
             float cc, gc;
             fast_tap_terms(a.k, a.v2, jrow + xi, pm_fix_frac(Xt), a1, g1, cc, gc);
-            /* user k's weight: offset (ry + oy_k, rx + ox_k), pixel m - (oy_k W + ox_k) */
-            const ptrdiff_t wb = ((ptrdiff_t)(ry + P) * N + (rx + P)) * (ptrdiff_t)n + (ptrdiff_t)m;
 #pragma unroll
             for (int k = 0; k < 8; ++k) {
                 if (!((mask >> k) & 1u)) continue;
+                /* user k sees this tap at offset (ry + oy_k, rx + ox_k) */
                 const int nn = k < 4 ? k : k + 1, ox = nn % 3 - 1, oy = nn / 3 - 1;
-                const float w = __ldg(&a.wvol[wb + (ptrdiff_t)(oy * N + ox) * (ptrdiff_t)n - (ptrdiff_t)(oy * W + ox)]);
+                const float w = tap_weight(uc[k], a1, c_prof[(ry + oy + PM_PMAX) * PM_PROF_N + PM_PMAX + rx + ox]);
                 r1[k] = fmaf(w, cc, r1[k]);
                 r2[k] = fmaf(w, gc, r2[k]);
                 ws[k] = ws[k] + w;
@@ -792,19 +768,13 @@ cudaError_t pm_launch_propagate(const PmPassArgs& a, bool exact, cudaStream_t st
         k_propagate<true><<<grid, dim3(32, 8), 0, st>>>(a);
     } else {
         PmPassArgs b = a;
-        if (!b.wvol || b.color >= 0) b.nbcost = nullptr;   /* red/black: neighbours per pixel */
+        if (b.color >= 0) b.nbcost = nullptr;   /* red/black: neighbours per pixel */
         if (b.nbcost) {
             k_nbcost<<<pix_grid(a.k.W, a.k.H), dim3(32, 8), 0, st>>>(b);
             PM_LAUNCH_CHECK();
         }
         k_propagate<false><<<grid, dim3(32, 8), 0, st>>>(b);
     }
-    PM_LAUNCH_CHECK();
-    return cudaSuccess;
-}
-
-cudaError_t pm_launch_weights(const float4* col, int W, int H, int P, float* wvol, cudaStream_t st) {
-    k_weights<<<pix_grid(W, H), dim3(32, 8), 0, st>>>(col, W, H, P, wvol);
     PM_LAUNCH_CHECK();
     return cudaSuccess;
 }

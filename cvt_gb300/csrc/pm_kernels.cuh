@@ -24,8 +24,7 @@ struct PmPassArgs {
     float4* out;
     uint8_t* winners;
     unsigned long long* counters;   /* [0] cost evaluations, [1] in-image taps; may be NULL */
-    const float* wvol;         /* FAST: bilateral weights of v1, [(2P+1)^2][W*H], or NULL */
-    float* nbcost;             /* FAST with wvol: costs of candidates 1-8, [8][W*H] */
+    float* nbcost;             /* FAST: costs of candidates 1-8 by shared windows, [8][W*H], or NULL */
     int color;                 /* -1: every pixel (Jacobi); 0 / 1: pixels with (x + y) & 1 == color */
 };
 
@@ -38,7 +37,6 @@ cudaError_t pm_launch_init(const PmPassArgs& a, bool exact, cudaStream_t st);
 cudaError_t pm_launch_cost_field(const PmPassArgs& a, bool exact, const float4* states, float* cost,
                                  cudaStream_t st);
 cudaError_t pm_launch_propagate(const PmPassArgs& a, bool exact, cudaStream_t st);
-cudaError_t pm_launch_weights(const float4* col, int W, int H, int P, float* wvol, cudaStream_t st);
 cudaError_t pm_launch_view_list(const float4* src, int W, int H, short4* list, cudaStream_t st);
 cudaError_t pm_launch_consistency(const float4* L, const float4* R, int W, int H, float maxdisp,
                                   float maxangle, int lr, float4* out, uint8_t* valid, cudaStream_t st);

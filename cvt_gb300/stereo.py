@@ -247,8 +247,9 @@ class PMHuberStereo:
         return cost
 
     def set_memory_budget(self, nbytes: int) -> None:
-        """Device bytes the FAST path may use for its shared-window weight
-        volumes (0: evaluate neighbours per pixel; results are the same)."""
+        """Device bytes the FAST path may use for its shared-window neighbour
+        costs, 32 per pixel (0: evaluate neighbours per pixel; results are the
+        same)."""
         self._check(_lib.lib().cvtpm_set_memory_budget(self._h, int(nbytes)))
 
     def cost_adjoint(self, img1: torch.Tensor, img2: torch.Tensor, planes: torch.Tensor, lr: int = 1,

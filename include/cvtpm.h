@@ -224,12 +224,12 @@ cvtpm_status cvtpm_polish_planes(cvtpm_ctx* ctx, const float* img1, const float*
                                  void* stream);
 
 /* Device memory the context may use for the FAST path's shared-window
- * neighbour costs: two weight volumes of (2*patchsize+1)^2 floats per pixel
- * (4.9 KB per pixel at patchsize 17) plus 32 bytes per pixel.  Within the
- * budget (and 60 % of the free memory) the 8 neighbour candidates of a pass
- * are evaluated once per plane over the union of their windows; otherwise
- * per pixel.  Results are identical either way.  Default: no limit;
- * 0 turns the volumes off.  No counterpart in the reference. */
+ * neighbour costs: 32 bytes per pixel (the costs of the 8 neighbour
+ * candidates).  Within the budget (and 60 % of the free memory) the 8
+ * neighbour candidates of a pass are evaluated once per plane over the union
+ * of their windows; otherwise per pixel.  Results are identical either way.
+ * Default: no limit; 0 turns the shared windows off.  No counterpart in the
+ * reference. */
 cvtpm_status cvtpm_set_memory_budget(cvtpm_ctx* ctx, size_t bytes);
 
 /* Enable CUDA-event timing of the propagation and PD phases (on the call's
@@ -266,8 +266,7 @@ cvtpm_status cvtpm_cost_eval_noalloc(const cvtpm_params* params,
  * pair descriptors (pointers, sizes, depthmax) stay the same.  Capture and
  * tuning synchronise `stream` once; replays do not.  With the lane count 0
  * (default) the first call of a new batch runs the autotuner: it times
- * one-iteration proxies of the batch for 1, 2, 4 and 8 lanes, with and
- * without the FAST path's shared-window weight volumes, and keeps the
+ * one-iteration proxies of the batch for 1, 2, 4 and 8 lanes and keeps the
  * fastest (cvtpm_get_batch_info reports the candidates). */
 cvtpm_status cvtpm_depthmap_batched(cvtpm_ctx* ctx, const cvtpm_pair* pairs,
                                     int npairs, void* stream);
@@ -275,11 +274,10 @@ cvtpm_status cvtpm_depthmap_batched(cvtpm_ctx* ctx, const cvtpm_pair* pairs,
 #define CVTPM_BATCH_MAX_CAND 8
 typedef struct cvtpm_batch_info {
     int lanes;                 /* lanes of the current graph */
-    int volumes;               /* shared-window weight volumes allowed */
+    int shared_windows;        /* FAST shared-window neighbour costs in use (within the memory budget) */
     int tuned;                 /* 1 if the autotuner chose the configuration */
     int ncand;
     int cand_lanes[CVTPM_BATCH_MAX_CAND];
-    int cand_volumes[CVTPM_BATCH_MAX_CAND];
     float cand_ms[CVTPM_BATCH_MAX_CAND];   /* one-iteration proxy time */
     long long graph_nodes;
     long long replays;

@@ -51,6 +51,7 @@ def test_batched_matches_plain_per_pair(cuda, preset):
     info = bat.batch_info()
     assert info["tuned"] == 1 and info["replays"] == 1
     assert info["lanes"] in (1, 2, 4, 8) and len(info["candidates"]) >= 2
+    assert info["shared_windows"] == (1 if preset == PRESET_BASELINE else 0)
     assert all(c["proxy_ms"] > 0 for c in info["candidates"])
 
 

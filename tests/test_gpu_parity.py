@@ -95,7 +95,7 @@ def test_depthmap_bitexact(stereo, oracle, mode):
 
 def test_shared_windows_match_per_pixel_neighbours(oracle):
     """FAST: the 8 neighbour candidates evaluated plane by plane over shared
-    windows (weight volumes) give the same bits as the per-pixel evaluation
+    windows give the same bits as the per-pixel evaluation
     (memory budget 0), and both match the oracle."""
     from cvt_gb300.stereo import PMHuberStereo
     sc = scenes.make_scene(150, 70, 5, 20.0, seed=12)
