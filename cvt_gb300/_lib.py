@@ -22,6 +22,8 @@ EXPORTS = (
     "cvtpm_set_batch_lanes", "cvtpm_get_batch_info",
     "cvtpm_set_timing", "cvtpm_reset_stats", "cvtpm_get_stats", "cvtpm_tool_fp32_peak",
     "cvtpm_cost_eval_noalloc",
+    "cvtpm_iformat_bpp", "cvtpm_image_to_rgbaf", "cvtpm_depthmap_image", "cvtpm_raw_read", "cvtpm_raw_write",
+    "cvtpm_ppm_read", "cvtpm_pfm_write",
 )
 
 
@@ -33,6 +35,12 @@ class CvtpmPair(ctypes.Structure):
     _fields_ = [("left", ctypes.c_void_p), ("right", ctypes.c_void_p), ("width", ctypes.c_int),
                 ("height", ctypes.c_int), ("pitch", ctypes.c_size_t), ("depthmax", ctypes.c_float),
                 ("dmap", ctypes.c_void_p), ("dmap_pitch", ctypes.c_size_t)]
+
+
+class CvtpmImage(ctypes.Structure):
+    """cvtpm_image: a cvt::Image's storage (format, size, row stride in bytes, data)."""
+    _fields_ = [("format", ctypes.c_int), ("width", ctypes.c_int), ("height", ctypes.c_int),
+                ("stride", ctypes.c_size_t), ("data", ctypes.c_void_p)]
 
 
 BATCH_MAX_CAND = 8
@@ -104,8 +112,17 @@ def lib() -> ctypes.CDLL:
     L.cvtpm_get_stats.argtypes = [vp, ctypes.POINTER(CvtpmStats)]
     L.cvtpm_tool_fp32_peak.argtypes = [i, vp, ctypes.POINTER(ctypes.c_float)]
     L.cvtpm_cost_eval_noalloc.argtypes = [P, vp, vp, i, i, sz, vp, vp, vp]
+    IP = ctypes.POINTER(CvtpmImage)
+    L.cvtpm_iformat_bpp.argtypes = [i]
+    L.cvtpm_iformat_bpp.restype = sz
+    L.cvtpm_image_to_rgbaf.argtypes = [IP, vp, sz, vp]
+    L.cvtpm_depthmap_image.argtypes = [vp, vp, sz, IP, IP, i, f, i, i, f, vp, sz, ctypes.POINTER(CvtpmTrace), vp]
+    L.cvtpm_raw_read.argtypes = [ctypes.c_char_p, IP]
+    L.cvtpm_raw_write.argtypes = [ctypes.c_char_p, IP]
+    L.cvtpm_ppm_read.argtypes = [ctypes.c_char_p, IP]
+    L.cvtpm_pfm_write.argtypes = [ctypes.c_char_p, IP]
     for name in EXPORTS:
-        if name not in ("cvtpm_version", "cvtpm_status_string", "cvtpm_last_error"):
+        if name not in ("cvtpm_version", "cvtpm_status_string", "cvtpm_last_error", "cvtpm_iformat_bpp"):
             getattr(L, name).restype = ctypes.c_int
     _lib = L
     return L

@@ -18,7 +18,7 @@ ROOT = os.path.dirname(PKG)
 CSRC = os.path.join(PKG, "csrc")
 BUILD = os.path.join(ROOT, "_build")
 LIB = os.path.join(PKG, "libcvtpm.so")
-SOURCES = ["pm_kernels.cu", "pm_capi.cu", "pm_noalloc.cu", "pm_adjoint.cu"]
+SOURCES = ["pm_kernels.cu", "pm_capi.cu", "pm_noalloc.cu", "pm_adjoint.cu", "pm_image.cu", "pm_io.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -33,7 +33,7 @@ def _deps():
     out = []
     for d in (CSRC, os.path.join(ROOT, "include")):
         for f in os.listdir(d):
-            if f.endswith((".cu", ".cuh", ".h", ".hpp")):
+            if f.endswith((".cu", ".cpp", ".cuh", ".h", ".hpp")):
                 out.append(os.path.join(d, f))
     return out
 
@@ -55,7 +55,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
     procs = []
     objs = []
     for src in SOURCES:
-        obj = os.path.join(BUILD, src.replace(".cu", ".o"))
+        obj = os.path.join(BUILD, os.path.splitext(src)[0] + ".o")
         objs.append(obj)
         cmd = common + ["-c", os.path.join(CSRC, src), "-o", obj]
         if verbose:

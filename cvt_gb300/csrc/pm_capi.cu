@@ -70,6 +70,9 @@ struct cvtpm_ctx {
     /* staging for the *_host entry points */
     void* stage = nullptr;
     size_t stage_bytes = 0;
+    /* cvtpm_depthmap_image: left and right converted to RGBA float32 */
+    void* istage = nullptr;
+    size_t istage_bytes = 0;
     /* observability (cvtpm_get_stats) */
     cvtpm_stats stats{};
     bool timing = false;
@@ -532,6 +535,7 @@ const char* cvtpm_status_string(cvtpm_status s) {
         case CVTPM_ERR_ALLOC: return "device allocation failed";
         case CVTPM_ERR_TIMEOUT: return "device wait timed out";
         case CVTPM_ERR_NOT_SUPPORTED: return "not supported";
+        case CVTPM_ERR_IO: return "file error";
     }
     return "unknown status";
 }
@@ -616,6 +620,7 @@ cvtpm_status cvtpm_destroy(cvtpm_ctx* ctx) {
     if (ctx->bjoin) cudaEventDestroy(ctx->bjoin);
     if (ctx->stage) cudaFree(ctx->stage);
     if (ctx->nbcost) cudaFree(ctx->nbcost);
+    if (ctx->istage) cudaFree(ctx->istage);
     if (ctx->dcount) cudaFree(ctx->dcount);
     for (auto& pr : ctx->ev_prop) { cudaEventDestroy(pr.first); cudaEventDestroy(pr.second); }
     for (auto& pr : ctx->ev_pd) { cudaEventDestroy(pr.first); cudaEventDestroy(pr.second); }
@@ -638,7 +643,7 @@ cvtpm_status cvtpm_get_params(const cvtpm_ctx* ctx, cvtpm_params* p) {
     return CVTPM_OK;
 }
 
-const char* cvtpm_last_error(const cvtpm_ctx* ctx) { return ctx ? ctx->err.c_str() : "null context"; }
+const char* cvtpm_last_error(const cvtpm_ctx* ctx) { return ctx ? ctx->err.c_str() : pm_free_error(); }
 
 cvtpm_status cvtpm_synchronize(cvtpm_ctx* ctx, void* stream) {
     if (!ctx) return CVTPM_ERR_INVALID_ARGUMENT;
@@ -659,6 +664,45 @@ cvtpm_status cvtpm_depthmap(cvtpm_ctx* ctx, float* dmap, size_t dmap_pitch, cons
     p.dscale = dscale;
     return run_depthmap(ctx, p, dmap, dmap_pitch, left, right, width, height, pitch, normalmap, normalmap_pitch,
                         trace, (cudaStream_t)stream);
+}
+
+cvtpm_status cvtpm_depthmap_image(cvtpm_ctx* ctx, float* dmap, size_t dmap_pitch, const cvtpm_image* left,
+                                  const cvtpm_image* right, int patchsize, float depthmax, int iterations,
+                                  int viewsamples, float dscale, float* normalmap, size_t normalmap_pitch,
+                                  const cvtpm_trace* trace, void* stream) {
+    if (!ctx) return CVTPM_ERR_INVALID_ARGUMENT;
+    if (!left || !right) return fail(ctx, CVTPM_ERR_INVALID_ARGUMENT, "left or right descriptor is NULL");
+    /* PMHuberStereo.cpp:66-68: sizes must agree; formats may differ */
+    if (left->width != right->width || left->height != right->height)
+        return fail(ctx, CVTPM_ERR_INCONSISTENT, "Left/Right stereo images inconsistent");
+    if (left->width < 1 || left->height < 1) return fail(ctx, CVTPM_ERR_SIZE, "empty image");
+    CK(cudaSetDevice(ctx->device), "cudaSetDevice");
+    const int W = left->width, H = left->height;
+    const size_t pitch = (size_t)W * 16, need = 2 * pitch * (size_t)H;
+    cudaStream_t st = (cudaStream_t)stream;
+    if (ctx->istage_bytes < need) {
+        if (ctx->istage) {
+            CK(cudaStreamSynchronize(st), "image staging");
+            CK(cudaFree(ctx->istage), "free image staging");
+            ctx->istage = nullptr;
+            ctx->istage_bytes = 0;
+        }
+        if (cudaMalloc(&ctx->istage, need) != cudaSuccess) {
+            cudaGetLastError();
+            ctx->istage = nullptr;
+            return fail(ctx, CVTPM_ERR_ALLOC, "image staging allocation failed");
+        }
+        ctx->istage_bytes = need;
+    }
+    float4* l = (float4*)ctx->istage;
+    float4* r = (float4*)((char*)ctx->istage + pitch * (size_t)H);
+    std::string msg;
+    cvtpm_status s;
+    if ((s = pm_image_to_rgbaf_checked(left, "left", l, pitch, st, &msg)) != CVTPM_OK) return fail(ctx, s, msg);
+    if ((s = pm_image_to_rgbaf_checked(right, "right", r, pitch, st, &msg)) != CVTPM_OK) return fail(ctx, s, msg);
+    ctx->stats.launches += 2;
+    return cvtpm_depthmap(ctx, dmap, dmap_pitch, (const float*)l, (const float*)r, W, H, pitch, patchsize, depthmax,
+                          iterations, viewsamples, dscale, normalmap, normalmap_pitch, trace, stream);
 }
 
 cvtpm_status cvtpm_depthmap_inpaint(cvtpm_ctx* ctx, float* dmap, size_t dmap_pitch, const float* left,

@@ -7,6 +7,7 @@
 
 #include <cuda_runtime.h>
 #include <stdint.h>
+#include <string>
 #include "cvtpm.h"
 #include "pm_device.cuh"
 
@@ -71,5 +72,13 @@ cudaError_t pm_launch_cost_adjoint(const PmCostConsts& k, const PmView& v1, cons
 cudaError_t pm_launch_adjoint_finish(const float4* dI, const float4* dG, int W, int H, float* out, cudaStream_t st);
 cudaError_t pm_launch_gn_polish(const PmCostConsts& k, const PmView& v1, const PmView& v2, float4* planes, int lr,
                                 int steps, float* cost, cudaStream_t st);
+
+/* pm_image.cu: one image in a cvt::IFormat (validated) into RGBA float32 rows
+ * of dst_pitch bytes; *msg receives the reason of a failure. */
+cvtpm_status pm_image_to_rgbaf_checked(const cvtpm_image* img, const char* what, float4* dst, size_t dst_pitch,
+                                       cudaStream_t st, std::string* msg);
+/* The calling thread's last error message of a context-free entry point. */
+const char* pm_free_error();
+void pm_set_free_error(const std::string& m);
 
 #endif

@@ -130,6 +130,40 @@ class PMHuberStereo:
         self._check(rc)
         return dmap
 
+    def depthMapImage(self, dmap: torch.Tensor | None, left: torch.Tensor, left_fmt: int, right: torch.Tensor,
+                      right_fmt: int, patchsize: int, depthmax: float, iterations: int, viewsamples: int,
+                      dscale: float = -1.0, normalmap: torch.Tensor | None = None,
+                      trace: dict | None = None) -> torch.Tensor:
+        """PMHuberStereo::depthMap with left/right in any cvt::IFormat (CUDA
+        tensors holding the storage, see ``imageio.device_desc``); each is
+        read as the reference's read_imagef reads it."""
+        from . import imageio
+        dl, dr = imageio.device_desc(left, left_fmt), imageio.device_desc(right, right_fmt)
+        if (dl.width, dl.height) != (dr.width, dr.height) or left.device != right.device:
+            raise CVTException("Left/Right stereo images inconsistent or incompatible memory type")
+        H, W = dl.height, dl.width
+        if dmap is None:
+            dmap = torch.empty((H, W), dtype=torch.float32, device=left.device)
+        if dmap.shape != (H, W) or not dmap.is_contiguous():
+            dmap.resize_(H, W)
+        nm_ptr, nm_pitch = None, 0
+        if normalmap is not None:
+            if normalmap.shape != (H, W, 4) or not normalmap.is_contiguous():
+                normalmap.resize_(H, W, 4)
+            nm_ptr, nm_pitch = normalmap.data_ptr(), W * 16
+        tr = None
+        if trace is not None:
+            trace["winners"] = torch.empty((2, H, W), dtype=torch.uint8, device=left.device)
+            trace["valid"] = torch.empty((H, W), dtype=torch.uint8, device=left.device)
+            trace["states"] = torch.empty((2, H, W, 4), dtype=torch.float32, device=left.device)
+            tr = _lib.CvtpmTrace(trace["winners"].data_ptr(), trace["valid"].data_ptr(), trace["states"].data_ptr())
+        rc = _lib.lib().cvtpm_depthmap_image(
+            self._h, dmap.data_ptr(), W * 4, ctypes.byref(dl), ctypes.byref(dr), int(patchsize), float(depthmax),
+            int(iterations), int(viewsamples), float(dscale), nm_ptr, nm_pitch,
+            ctypes.byref(tr) if tr is not None else None, _stream_ptr(left))
+        self._check(rc)
+        return dmap
+
     def depthMapHost(self, left, right, patchsize: int, depthmax: float, iterations: int, viewsamples: int,
                      dscale: float = -1.0, dmap=None):
         """depthMap on host (numpy / CPU torch) buffers: copies in, runs,

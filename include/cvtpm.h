@@ -43,7 +43,9 @@ typedef enum cvtpm_status {
     CVTPM_ERR_CUDA = 4,             /* a CUDA runtime call failed             */
     CVTPM_ERR_ALLOC = 5,            /* device allocation failed               */
     CVTPM_ERR_TIMEOUT = 6,          /* a bounded device wait gave up          */
-    CVTPM_ERR_NOT_SUPPORTED = 7
+    CVTPM_ERR_NOT_SUPPORTED = 7,
+    CVTPM_ERR_IO = 8                /* a file could not be opened, read or
+                                       written, or its header is corrupt    */
 } cvtpm_status;
 
 enum { CVTPM_RNG_MWC64X = 0, CVTPM_RNG_PHILOX = 1 };
@@ -133,6 +135,9 @@ cvtpm_status cvtpm_create(cvtpm_ctx** ctx, int device);
 cvtpm_status cvtpm_destroy(cvtpm_ctx* ctx);
 cvtpm_status cvtpm_set_params(cvtpm_ctx* ctx, const cvtpm_params* p);
 cvtpm_status cvtpm_get_params(const cvtpm_ctx* ctx, cvtpm_params* p);
+/* The message of the context's last failure; with ctx == NULL, the message
+ * of the calling thread's last failed context-free call (image conversion,
+ * file readers and writers, cvtpm_cost_eval_noalloc). */
 const char*  cvtpm_last_error(const cvtpm_ctx* ctx);
 cvtpm_status cvtpm_synchronize(cvtpm_ctx* ctx, void* stream);
 
@@ -286,6 +291,91 @@ typedef struct cvtpm_batch_info {
 /* Fix the lane count of cvtpm_depthmap_batched (0: autotune). */
 cvtpm_status cvtpm_set_batch_lanes(cvtpm_ctx* ctx, int lanes);
 cvtpm_status cvtpm_get_batch_info(const cvtpm_ctx* ctx, cvtpm_batch_info* out);
+
+/* ------------------------------------------------------------------
+ * Input side: the reference's image formats and files.
+ *
+ * cvt::PMHuberStereo::depthMap accepts left/right cvt::Image objects of any
+ * format backed by OpenCL images (PMHuberStereo.cpp:64-68 checks only sizes
+ * and the memory type; the two may differ in format); its kernels read them
+ * with read_imagef, which returns RGBA floats.  The identifiers below are
+ * cvt::IFormatID (cvt/gfx/IFormat.h:36-63) and each is read the way its
+ * OpenCL image format (IFormat::toCLImageFormat, IFormat.h:293-328) makes
+ * read_imagef return it:
+ *   GRAY_*, BAYER_*  CL_INTENSITY  (I, I, I, I)
+ *   GRAYALPHA_*      CL_RG         (R, G, 0, 1)
+ *   RGBA_*           CL_RGBA       (R, G, B, A)
+ *   BGRA_*           CL_BGRA       stored B, G, R, A; returned (R, G, B, A)
+ *   YUYV, UYVY       CL_RA         (R, 0, 0, A): byte 0 and byte 1 of a pixel
+ * with UINT8 = CL_UNORM_INT8 (c / 255), UINT16 = CL_UNORM_INT16
+ * (c / 65535), INT16 = CL_SNORM_INT16 (max(-1, c / 32767)), FLOAT as is
+ * (OpenCL 1.2, 8.3.1.1; the division is correctly rounded).  16-bit
+ * channels are in host byte order.
+ * ------------------------------------------------------------------ */
+enum {
+    CVTPM_IFORMAT_GRAY_UINT8 = 1, CVTPM_IFORMAT_GRAY_UINT16, CVTPM_IFORMAT_GRAY_INT16, CVTPM_IFORMAT_GRAY_FLOAT,
+    CVTPM_IFORMAT_GRAYALPHA_UINT8, CVTPM_IFORMAT_GRAYALPHA_UINT16, CVTPM_IFORMAT_GRAYALPHA_INT16,
+    CVTPM_IFORMAT_GRAYALPHA_FLOAT,
+    CVTPM_IFORMAT_RGBA_UINT8, CVTPM_IFORMAT_RGBA_UINT16, CVTPM_IFORMAT_RGBA_INT16, CVTPM_IFORMAT_RGBA_FLOAT,
+    CVTPM_IFORMAT_BGRA_UINT8, CVTPM_IFORMAT_BGRA_UINT16, CVTPM_IFORMAT_BGRA_INT16, CVTPM_IFORMAT_BGRA_FLOAT,
+    CVTPM_IFORMAT_BAYER_RGGB_UINT8, CVTPM_IFORMAT_BAYER_GRBG_UINT8, CVTPM_IFORMAT_BAYER_GBRG_UINT8,
+    CVTPM_IFORMAT_YUYV_UINT8, CVTPM_IFORMAT_UYVY_UINT8
+};
+
+/* A cvt::Image's storage: format, size and row stride in bytes.  `data` is
+ * device memory for the conversion and depthMap calls, host memory for the
+ * file readers and writers. */
+typedef struct cvtpm_image {
+    int format;             /* CVTPM_IFORMAT_* */
+    int width, height;
+    size_t stride;          /* bytes per row, >= width * bytes per pixel */
+    void* data;
+} cvtpm_image;
+
+/* Bytes per pixel of a format (0 for an unknown one). */
+size_t cvtpm_iformat_bpp(int format);
+
+/* src (device) as read_imagef sees it, into RGBA float32 rows of dst_pitch
+ * bytes (a multiple of 16).  No counterpart function in the reference: there
+ * the OpenCL image sampler does this on every read. */
+cvtpm_status cvtpm_image_to_rgbaf(const cvtpm_image* src, float* dst, size_t dst_pitch, void* stream);
+
+/* PMHuberStereo::depthMap with left/right in any of the formats above
+ * (device memory; formats may differ, sizes may not).  The images are
+ * converted into context scratch, then the call is cvtpm_depthmap's. */
+cvtpm_status cvtpm_depthmap_image(cvtpm_ctx* ctx,
+                                  float* dmap, size_t dmap_pitch,
+                                  const cvtpm_image* left, const cvtpm_image* right,
+                                  int patchsize, float depthmax, int iterations,
+                                  int viewsamples, float dscale,
+                                  float* normalmap, size_t normalmap_pitch,
+                                  const cvtpm_trace* trace, void* stream);
+
+/* Files (host memory).  Readers fill the descriptor in two steps: with
+ * img->data == NULL they set format, width, height and the stride of a tight
+ * copy (width * bytes per pixel) and return; then, with data pointing to
+ * height * stride bytes, they read the pixels.
+ *
+ * CVTRaw (plugins/iloader/CVTRaw/CVTRawLoader.cpp,
+ * plugins/isaver/CVTRaw/CVTRawSaver.cpp): a header of four uint32 in host
+ * byte order, width, height, stride and IFormatID, then height rows of
+ * `stride` bytes. */
+cvtpm_status cvtpm_raw_read(const char* path, cvtpm_image* img);
+cvtpm_status cvtpm_raw_write(const char* path, const cvtpm_image* img);
+
+/* PPM / PGM (plugins/iloader/PPM/PPMLoader.cpp): P2 and P5 (gray) read as
+ * GRAY_UINT8, P3 and P6 (RGB) as RGBA_UINT8 with alpha 255; lines starting
+ * with '#' are comments; maximum values above 255 are refused
+ * (CVTPM_ERR_NOT_SUPPORTED), as in the reference, whose 16-bit formats have
+ * no reader. */
+cvtpm_status cvtpm_ppm_read(const char* path, cvtpm_image* img);
+
+/* PFM (plugins/isaver/PFM/PFMSaver.cpp): GRAY_FLOAT as "Pf", RGBA_FLOAT and
+ * BGRA_FLOAT as "PF" with the alpha channel dropped (BGRA written in its
+ * stored order, as the reference's alpha stripping keeps the channel order);
+ * rows bottom to top; scale -1.0 on little-endian hosts.  Other formats:
+ * CVTPM_ERR_NOT_SUPPORTED. */
+cvtpm_status cvtpm_pfm_write(const char* path, const cvtpm_image* img);
 
 #ifdef __cplusplus
 }

@@ -308,3 +308,48 @@ def pd_apply_inpaint(output, inp, wgt, mask, lam, iters):
     h, w = inp.shape[:2]
     lib().orc_pd_apply_inpaint(out, inp, wgt, mask, float(lam), int(iters), w, h)
     return out
+
+
+# ----------------------------------------------------------------------
+# Image formats as the reference's kernels read them.  cvt::IFormatID
+# (cvt/gfx/IFormat.h:36-63) -> OpenCL image format (IFormat::toCLImageFormat,
+# IFormat.h:293-328) -> what read_imagef returns (OpenCL 1.2, 6.12.14.1 for
+# the channel orders, 8.3.1.1 for normalized integers).  float32 numpy
+# division is the correctly rounded IEEE division.
+
+
+def image_to_rgbaf(arr: np.ndarray, fmt: int) -> np.ndarray:
+    """(H, W[, C]) storage of format `fmt` -> (H, W, 4) float32 RGBA."""
+    a = np.asarray(arr)
+    if 1 <= fmt <= 16:
+        kind = (fmt - 1) % 4          # 0 unorm8, 1 unorm16, 2 snorm16, 3 float
+        order = ("I", "RG", "RGBA", "BGRA")[(fmt - 1) // 4]
+    elif 17 <= fmt <= 19:
+        kind, order = 0, "I"          # Bayer: CL_INTENSITY, CL_UNORM_INT8
+    elif fmt in (20, 21):
+        kind, order = 0, "RA"         # YUYV / UYVY: CL_RA, CL_UNORM_INT8
+    else:
+        raise ValueError(fmt)
+    if kind == 0:
+        v = a.astype(np.float32) / np.float32(255.0)
+    elif kind == 1:
+        v = a.astype(np.float32) / np.float32(65535.0)
+    elif kind == 2:
+        v = np.maximum(np.float32(-1.0), a.astype(np.float32) / np.float32(32767.0))
+    else:
+        v = a.astype(np.float32)
+    if v.ndim == 2:
+        v = v[..., None]
+    H, W = v.shape[:2]
+    out = np.zeros((H, W, 4), np.float32)
+    if order == "I":
+        out[...] = v[..., :1]
+    elif order == "RG":
+        out[..., 0], out[..., 1], out[..., 3] = v[..., 0], v[..., 1], 1.0
+    elif order == "RA":
+        out[..., 0], out[..., 3] = v[..., 0], v[..., 1]
+    elif order == "RGBA":
+        out[...] = v
+    else:                             # stored B, G, R, A
+        out[..., 0], out[..., 1], out[..., 2], out[..., 3] = v[..., 2], v[..., 1], v[..., 0], v[..., 3]
+    return out

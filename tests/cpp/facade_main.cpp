@@ -1,9 +1,13 @@
 /* Drop-in check for C++ callers: reads two RGBA float32 images (raw, W*H*4),
  * runs cvt::PMHuberStereo::depthMap through include/cvt/PMHuberStereo.hpp and
  * writes the disparity map (raw, W*H floats).
- * usage: facade_main W H patchsize depthmax iterations left.raw right.raw out.raw */
+ * usage: facade_main W H patchsize depthmax iterations left.raw right.raw out.raw
+ *    or: facade_main --files patchsize depthmax iterations left right out.pfm
+ * The second form loads the pair with cvt::Image::load (CVTRaw or PPM files
+ * in any format), runs depthMap and saves the disparity map as PFM. */
 #include <cstdio>
 #include <cstdlib>
+#include <string>
 #include <vector>
 
 #include "cvt/PMHuberStereo.hpp"
@@ -16,7 +20,23 @@ static bool read_all(const char* path, std::vector<float>& v) {
     return n == v.size();
 }
 
+static int files(char** argv) {
+    try {
+        cvt::Image left, right, dmap;
+        left.load(argv[5]);
+        right.load(argv[6]);
+        cvt::PMHuberStereo stereo;                         /* REFERENCE preset */
+        stereo.depthMap(dmap, left, right, (size_t)atoi(argv[2]), (float)atof(argv[3]), (size_t)atoi(argv[4]), 4);
+        dmap.save(argv[7]);
+    } catch (const std::exception& e) {
+        fprintf(stderr, "error: %s\n", e.what());
+        return 4;
+    }
+    return 0;
+}
+
 int main(int argc, char** argv) {
+    if (argc == 8 && std::string(argv[1]) == "--files") return files(argv);
     if (argc != 9) { fprintf(stderr, "usage\n"); return 2; }
     size_t W = (size_t)atoi(argv[1]), H = (size_t)atoi(argv[2]);
     size_t patch = (size_t)atoi(argv[3]);

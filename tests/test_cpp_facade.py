@@ -53,3 +53,36 @@ def test_facade_matches_oracle(tmp_path, cuda, oracle):
     want, _ = oracle.depthmap(default_params(PRESET_REFERENCE, patchsize=5, depthmax=10.0, iterations=2),
                               sc.left, sc.right)
     assert not bit_diff(got, want).any()
+
+
+@pytest.mark.gpu
+def test_facade_loads_files_and_reads_any_format(tmp_path, cuda, oracle):
+    """cvt::Image::load of a CVTRaw RGBA_UINT8 left and a BGRA_UINT8 right,
+    depthMap, cvt::Image::save as PFM: the oracle's disparities on the
+    read_imagef conversion of both."""
+    g = _gxx()
+    from cvt_gb300 import scenes, imageio
+    from cvt_gb300.params import default_params, PRESET_REFERENCE
+    from cvt_gb300._lib import LIB_PATH
+    exe = str(tmp_path / "facade")
+    r = subprocess.run([g, "-std=c++17", "-O1", "-I", os.path.join(ROOT, "include"), "-I", CUDA_INC,
+                        os.path.join(ROOT, "tests", "cpp", "facade_main.cpp"), "-o", exe,
+                        LIB_PATH, f"-Wl,-rpath,{os.path.dirname(LIB_PATH)}", "-L", CUDA_LIB, "-lcudart",
+                        f"-Wl,-rpath,{CUDA_LIB}"], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    sc = scenes.make_scene(45, 33, 3, 10.0, seed=13)
+    lu8 = np.round(sc.left * 255).astype(np.uint8)
+    ru8 = np.ascontiguousarray(np.round(sc.right * 255).astype(np.uint8)[..., [2, 1, 0, 3]])
+    imageio.write_raw(tmp_path / "l.raw", lu8, imageio.RGBA_UINT8)
+    imageio.write_raw(tmp_path / "r.raw", ru8, imageio.BGRA_UINT8)
+    out = tmp_path / "d.pfm"
+    r = subprocess.run([exe, "--files", "5", "10", "2", str(tmp_path / "l.raw"), str(tmp_path / "r.raw"), str(out)],
+                       capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr
+    data = out.read_bytes().split(b"\n", 3)
+    assert data[0] == b"Pf" and data[1] == b"45 33"
+    got = np.frombuffer(data[3], "<f4").reshape(33, 45)[::-1]
+    want, _ = oracle.depthmap(default_params(PRESET_REFERENCE, patchsize=5, depthmax=10.0, iterations=2),
+                              oracle.image_to_rgbaf(lu8, imageio.RGBA_UINT8),
+                              oracle.image_to_rgbaf(ru8, imageio.BGRA_UINT8))
+    assert not bit_diff(got, want).any()
