@@ -23,7 +23,7 @@ EXPORTS = (
     "cvtpm_set_timing", "cvtpm_reset_stats", "cvtpm_get_stats", "cvtpm_tool_fp32_peak",
     "cvtpm_cost_eval_noalloc",
     "cvtpm_iformat_bpp", "cvtpm_image_to_rgbaf", "cvtpm_depthmap_image", "cvtpm_raw_read", "cvtpm_raw_write",
-    "cvtpm_ppm_read", "cvtpm_pfm_write",
+    "cvtpm_ppm_read", "cvtpm_pfm_write", "cvtpm_stereo_rectify", "cvtpm_warp_apply",
 )
 
 
@@ -41,6 +41,16 @@ class CvtpmImage(ctypes.Structure):
     """cvtpm_image: a cvt::Image's storage (format, size, row stride in bytes, data)."""
     _fields_ = [("format", ctypes.c_int), ("width", ctypes.c_int), ("height", ctypes.c_int),
                 ("stride", ctypes.c_size_t), ("data", ctypes.c_void_p)]
+
+
+class CvtpmCamera(ctypes.Structure):
+    """cvtpm_camera: intrinsics (row-major 3x3), radial k1..k3, tangential p1, p2."""
+    _fields_ = [("intrinsics", ctypes.c_float * 9), ("radial", ctypes.c_float * 3), ("tangential", ctypes.c_float * 2)]
+
+
+class CvtpmRectification(ctypes.Structure):
+    _fields_ = [("first", CvtpmCamera), ("second", CvtpmCamera), ("extrinsics", ctypes.c_float * 16),
+                ("rot_first", ctypes.c_float * 9), ("rot_second", ctypes.c_float * 9)]
 
 
 BATCH_MAX_CAND = 8
@@ -121,6 +131,10 @@ def lib() -> ctypes.CDLL:
     L.cvtpm_raw_write.argtypes = [ctypes.c_char_p, IP]
     L.cvtpm_ppm_read.argtypes = [ctypes.c_char_p, IP]
     L.cvtpm_pfm_write.argtypes = [ctypes.c_char_p, IP]
+    CP = ctypes.POINTER(CvtpmCamera)
+    L.cvtpm_stereo_rectify.argtypes = [CP, CP, ctypes.POINTER(ctypes.c_float), i, ctypes.POINTER(CvtpmRectification),
+                                       i, i, vp, vp, sz, vp]
+    L.cvtpm_warp_apply.argtypes = [IP, IP, vp, sz, vp]
     for name in EXPORTS:
         if name not in ("cvtpm_version", "cvtpm_status_string", "cvtpm_last_error", "cvtpm_iformat_bpp"):
             getattr(L, name).restype = ctypes.c_int

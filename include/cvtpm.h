@@ -377,6 +377,56 @@ cvtpm_status cvtpm_ppm_read(const char* path, cvtpm_image* img);
  * CVTPM_ERR_NOT_SUPPORTED. */
 cvtpm_status cvtpm_pfm_write(const char* path, const cvtpm_image* img);
 
+/* ------------------------------------------------------------------
+ * Input side: stereo rectification (cvt/vision/StereoCameraCalibration.h,
+ * cvt/vision/StereoRectification.h, cvt/gfx/ifilter/IWarp.cpp).
+ * ------------------------------------------------------------------ */
+
+/* A camera of cvt::CameraCalibration: intrinsics and lens distortion. */
+typedef struct cvtpm_camera {
+    float intrinsics[9];    /* row-major 3x3: fx, skew, cx / 0, fy, cy / 0, 0, 1 */
+    float radial[3];        /* k1, k2, k3 */
+    float tangential[2];    /* p1, p2 */
+} cvtpm_camera;
+
+/* What StereoCameraCalibration::undistortRectify produces besides the maps. */
+typedef struct cvtpm_rectification {
+    cvtpm_camera first, second;  /* rectified cameras: common focal length, no distortion */
+    float extrinsics[16];        /* rectified stereo extrinsics (row-major 4x4) */
+    float rot_first[9];          /* rectifying rotations (row-major), as  */
+    float rot_second[9];         /* rectificationMatrices returns them    */
+} cvtpm_rectification;
+
+/* StereoCameraCalibration(first, second, extrinsics).undistortRectify(out,
+ * warp_first, warp_second, width, height, vertical)
+ * (StereoCameraCalibration.h:124-130, 166-277): `extrinsics` is the stereo
+ * extrinsics (row-major 4x4, the pose of the second camera relative to the
+ * first, as StereoCameraCalibration stores and loads it).  The rectified
+ * calibration is computed on the host; with warp_first / warp_second non-NULL
+ * the two warp maps (IFormat::GRAYALPHA_FLOAT, width x height, rows of
+ * warp_pitch bytes: per output pixel the (x, y) to sample the source at) are
+ * written on the device, stream-ordered on `stream`.  As in the reference,
+ * the rectifying rotations are always those of horizontal stereo
+ * (undistortRectify calls rectificationMatrices without its `verticalstereo`
+ * flag); `vertical` only selects which principal-point coordinate the two
+ * cameras share. */
+cvtpm_status cvtpm_stereo_rectify(const cvtpm_camera* first, const cvtpm_camera* second, const float* extrinsics,
+                                  int vertical, cvtpm_rectification* out, int width, int height,
+                                  float* warp_first, float* warp_second, size_t warp_pitch, void* stream);
+
+/* IWarp::apply(dst, src, warp) (cvt/gfx/ifilter/IWarp.cpp:49-66, 254-376):
+ * dst (warp's size, src's format) = src resampled at the warp map's (x, y),
+ * bilinear, with the reference's fill outside the image.  Formats:
+ * GRAY_FLOAT (fill 0), RGBA_FLOAT / BGRA_FLOAT (fill 0, 0, 0, 1), GRAY_UINT8
+ * (fill 0, 16-bit fixed-point weights), RGBA_UINT8 / BGRA_UINT8 (fill
+ * opaque black, 8-bit fixed-point weights).  Map coordinates that are not
+ * finite or beyond the fixed-point range (|x|, |y| >= 32768 for GRAY_UINT8,
+ * >= 2^23 for the 4-channel 8-bit formats, >= 2^31 for float) give the fill
+ * value (the reference's float-to-int conversion is undefined there).  All
+ * device memory. */
+cvtpm_status cvtpm_warp_apply(const cvtpm_image* dst, const cvtpm_image* src, const float* warp, size_t warp_pitch,
+                              void* stream);
+
 #ifdef __cplusplus
 }
 #endif

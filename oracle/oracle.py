@@ -353,3 +353,58 @@ def image_to_rgbaf(arr: np.ndarray, fmt: int) -> np.ndarray:
     else:                             # stored B, G, R, A
         out[..., 0], out[..., 1], out[..., 2], out[..., 3] = v[..., 2], v[..., 1], v[..., 0], v[..., 3]
     return out
+
+
+# ----------------------------------------------------------------------
+# Stereo rectification and IWarp::apply (orc_stereo_rectify, orc_warp in
+# pm_oracle.cpp).  A camera is a dict: "K" (3, 3), "radial" (3,),
+# "tangential" (2,) float32.
+
+WARP_KIND = {4: 0, 12: 1, 16: 1, 1: 2, 9: 3, 13: 3}   # IFormatID -> IWarp::apply variant
+
+
+def _rect_call(fn, cam0, cam1, E, vertical, W, H):
+    f = lambda a, n: np.ascontiguousarray(np.asarray(a, np.float32).reshape(n))
+    map0 = np.empty((H, W, 2), np.float32)
+    map1 = np.empty((H, W, 2), np.float32)
+    K0n, K1n, Rl, Rr = (np.empty(9, np.float32) for _ in range(4))
+    En = np.empty(16, np.float32)
+    args = [f(cam0["K"], 9), f(cam0["radial"], 3), f(cam0["tangential"], 2), f(cam1["K"], 9), f(cam1["radial"], 3),
+            f(cam1["tangential"], 2), f(E, 16)]
+    rc = fn(*[a.ctypes.data for a in args], int(vertical), int(W), int(H), map0.ctypes.data, map1.ctypes.data,
+            K0n.ctypes.data, K1n.ctypes.data, En.ctypes.data, Rl.ctypes.data, Rr.ctypes.data)
+    if rc:
+        raise RuntimeError("rectification failed")
+    return {"map0": map0, "map1": map1, "K0": K0n.reshape(3, 3), "K1": K1n.reshape(3, 3),
+            "E": En.reshape(4, 4), "R0": Rl.reshape(3, 3), "R1": Rr.reshape(3, 3)}
+
+
+def _warp_call(fn, fmt, src, warp_map):
+    src = np.ascontiguousarray(src)
+    warp_map = np.ascontiguousarray(warp_map, np.float32)
+    H, W = warp_map.shape[:2]
+    kind = WARP_KIND[fmt]
+    sh, sw = src.shape[:2]
+    dst = np.empty((H, W) + src.shape[2:], src.dtype)
+    rc = fn(kind, src.ctypes.data, src.strides[0], sw, sh, warp_map.ctypes.data, warp_map.strides[0], W, H,
+            dst.ctypes.data, dst.strides[0])
+    if rc:
+        raise RuntimeError("warp failed")
+    return dst
+
+
+def _rect_lib(L):
+    vp, c_int, sz = ctypes.c_void_p, ctypes.c_int, ctypes.c_size_t
+    L.orc_stereo_rectify.argtypes = [vp] * 7 + [c_int, c_int, c_int] + [vp] * 7
+    L.orc_warp.argtypes = [c_int, vp, sz, c_int, c_int, vp, sz, c_int, c_int, vp, sz]
+    return L
+
+
+def stereo_rectify(cam0, cam1, E, vertical, W, H):
+    """StereoCameraCalibration(cam0, cam1, E).undistortRectify on W x H maps."""
+    return _rect_call(_rect_lib(lib()).orc_stereo_rectify, cam0, cam1, E, vertical, W, H)
+
+
+def warp(fmt, src, warp_map):
+    """IWarp::apply(dst, src, warp) for GRAY/RGBA/BGRA float and uint8 storage."""
+    return _warp_call(_rect_lib(lib()).orc_warp, fmt, src, warp_map)

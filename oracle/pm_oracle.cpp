@@ -1323,3 +1323,262 @@ int orc_cost_adjoint_f64(const cvtpm_params* prm, const double* img1, const doub
 }
 
 }  // extern "C"
+
+/* ---------------------------------------------------------------------
+ * Stereo rectification and bilinear warps (the input side of the path).
+ *
+ *   orc_stereo_rectify  StereoCameraCalibration(first, second, extrinsics)
+ *                       .undistortRectify (cvt/vision/StereoCameraCalibration.h:
+ *                       124-130, 166-277) with UndistortRectifyWarp (:79-92)
+ *                       evaluated per map pixel as IWarp::warpGeneric does
+ *                       (cvt/gfx/ifilter/IWarp.h:80-99)
+ *   orc_warp            IWarp::apply's row loops (cvt/gfx/ifilter/IWarp.cpp:
+ *                       254-376) over SIMD::warpBilinear1f / 4f / 1u8 / 4u8
+ *                       (cvt/util/SIMD.cpp:4497-4710, _floor :732-739,
+ *                       _mix4U8 :702-717)
+ * Float arithmetic in the reference's order (flat row-major arrays here),
+ * the C library's sqrtf / sinf / cosf / acosf as the reference's Math::
+ * wrappers call them.  Map coordinates that are not finite or beyond the
+ * fixed-point range give the fill value (undefined in the reference).
+ * --------------------------------------------------------------------- */
+namespace {
+
+void mat3_mul(const float* a, const float* b, float* r) {      /* Matrix3.h:275-286 */
+    float t[9];
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) t[i * 3 + j] = a[i * 3] * b[j] + a[i * 3 + 1] * b[3 + j] + a[i * 3 + 2] * b[6 + j];
+    memcpy(r, t, sizeof t);
+}
+
+void mat3_vec(const float* a, const float* v, float* r) {      /* Matrix3.h:257-262 */
+    float t[3];
+    for (int i = 0; i < 3; ++i) t[i] = a[i * 3] * v[0] + a[i * 3 + 1] * v[1] + a[i * 3 + 2] * v[2];
+    memcpy(r, t, sizeof t);
+}
+
+void vec3_normalize(float* v) {                                 /* Vector3.h:344-352 */
+    const float ls = v[0] * v[0] + v[1] * v[1] + v[2] * v[2];
+    const float inv = 1.0f / sqrtf(ls);
+    v[0] *= inv; v[1] *= inv; v[2] *= inv;
+}
+
+void set_rotation(const float* ax_in, float rad, float* m) {    /* Matrix3.h:508-553 */
+    float a[3] = {ax_in[0], ax_in[1], ax_in[2]};
+    vec3_normalize(a);
+    const float c = cosf(rad * 0.5f), s = sinf(rad * 0.5f);
+    const float x = a[0] * s, y = a[1] * s, z = a[2] * s;
+    const float x2 = x + x, y2 = y + y, z2 = z + z;
+    const float xx = x * x2, xy = x * y2, xz = x * z2, yy = y * y2, yz = y * z2, zz = z * z2;
+    const float wx = c * x2, wy = c * y2, wz = c * z2;
+    const float r[9] = {1.0f - (yy + zz), xy - wz, xz + wy,
+                        xy + wz, 1.0f - (xx + zz), yz - wx,
+                        xz - wy, yz + wx, 1.0f - (xx + yy)};
+    memcpy(m, r, sizeof r);
+}
+
+/* Quaternion(Matrix3) (Quaternion.h:128-164) + toAxisAngle (:517-523) */
+void to_axis_angle(const float* m, float* axis, float* angle) {
+    float q[4];    /* x, y, z, w */
+    const float tr = m[0] + m[4] + m[8];
+    if (tr > 0.0f) {
+        float root = sqrtf(tr + 1.0f);
+        q[3] = 0.5f * root;
+        root = 0.5f / root;
+        q[0] = (m[7] - m[5]) * root;
+        q[1] = (m[2] - m[6]) * root;
+        q[2] = (m[3] - m[1]) * root;
+    } else {
+        int i = 0;
+        if (m[4] > m[0]) i = 1;
+        if (m[8] > m[i * 4]) i = 2;
+        const int j = (i + 1) % 3, k = (j + 1) % 3;
+        float root = sqrtf(m[i * 4] - m[j * 4] - m[k * 4] + 1.0f);
+        q[i] = 0.5f * root;
+        root = 0.5f / root;
+        q[3] = (m[k * 3 + j] - m[j * 3 + k]) * root;
+        q[j] = (m[j * 3 + i] + m[i * 3 + j]) * root;
+        q[k] = (m[k * 3 + i] + m[i * 3 + k]) * root;
+    }
+    *angle = acosf(q[3]) * 2.0f;
+    const float s = sinf(*angle * 0.5f);
+    axis[0] = q[0] / s; axis[1] = q[1] / s; axis[2] = q[2] / s;
+    vec3_normalize(axis);
+}
+
+void homog_col3(const float* E, float* t) {                     /* Vector3(Vector4), Vector3.h:120-126 */
+    const float invw = (float)(1.0 / (double)E[15]);
+    t[0] = invw * E[3]; t[1] = invw * E[7]; t[2] = invw * E[11];
+}
+
+/* rectificationMatrices(Rleft, Rright), horizontal (:166-197) */
+void rect_rotations(const float* E, float* Rl, float* Rr) {
+    const float R[9] = {E[0], E[1], E[2], E[4], E[5], E[6], E[8], E[9], E[10]};
+    float axis[3], angle, t[3], c[3];
+    to_axis_angle(R, axis, &angle);
+    set_rotation(axis, 0.5f * angle, Rl);
+    set_rotation(axis, -0.5f * angle, Rr);
+    homog_col3(E, c);
+    mat3_vec(Rr, c, t);
+    float u[3] = {1.0f, 0.0f, 0.0f};
+    if (t[0] * u[0] + t[1] * u[1] + t[2] * u[2] < 0.0f) { u[0] = -u[0]; u[1] = -u[1]; u[2] = -u[2]; }
+    float ax[3] = {t[1] * u[2] - t[2] * u[1], t[2] * u[0] - t[0] * u[2], t[0] * u[1] - t[1] * u[0]};
+    vec3_normalize(ax);
+    const float d = u[0] * t[0] + u[1] * t[1] + u[2] * t[2];
+    const float len = sqrtf(t[0] * t[0] + t[1] * t[1] + t[2] * t[2]);
+    const float ang = acosf(fabsf(d) / len);
+    float R2[9];
+    set_rotation(ax, ang, R2);
+    mat3_mul(R2, Rr, Rr);
+    mat3_mul(R2, Rl, Rl);
+}
+
+/* UndistortRectifyWarp::operator()(Vector2f(x, y)) (:79-92) */
+void rect_point(float x, float y, float fn, float cnx, float cny, const float* rt, const float* K, const float* rad,
+                const float* tan, float* mx, float* my) {
+    const float dx = (x - cnx) / fn, dy = (y - cny) / fn;
+    float px = rt[0] * dx + rt[1] * dy + rt[2];
+    float py = rt[3] * dx + rt[4] * dy + rt[5];
+    const float w = rt[6] * dx + rt[7] * dy + rt[8];
+    px /= w;
+    py /= w;
+    const float r2 = px * px + py * py, r4 = r2 * r2, r6 = r2 * r4;
+    const float poly = 1.0f + rad[0] * r2 + rad[1] * r4 + rad[2] * r6;
+    const float xy2 = 2.0f * px * py;
+    *mx = K[0] * (px * poly + xy2 * tan[0] + tan[1] * (r2 + 2.0f * px * px)) + K[2];
+    *my = K[4] * (py * poly + xy2 * tan[1] + tan[0] * (r2 + 2.0f * py * py)) + K[5];
+}
+
+int floor_ref(float v) {                                        /* SIMD.cpp:732-739 */
+    uint32_t bits;
+    memcpy(&bits, &v, 4);
+    return (int)v - (int)(bits >> 31);
+}
+
+uint32_t mix4(uint32_t a, uint32_t b, uint32_t t) {             /* SIMD.cpp:702-717 */
+    uint32_t hi = (((b >> 8) & 0xff00ffu) - ((a >> 8) & 0xff00ffu)) * t;
+    hi = (hi + (a & 0xff00ff00u)) & 0xff00ff00u;
+    uint32_t lo = ((b & 0xff00ffu) - (a & 0xff00ffu)) * t;
+    lo = ((lo >> 8) + (a & 0xff00ffu)) & 0xff00ffu;
+    return hi + lo;
+}
+
+}  // namespace
+
+extern "C" {
+
+/* maps: W*H (x, y) pairs each; K0new/K1new 9, Enew 16, Rl/Rr 9 floats. */
+int orc_stereo_rectify(const float* K0, const float* rad0, const float* tan0, const float* K1, const float* rad1,
+                       const float* tan1, const float* E, int vertical, int W, int H, float* map0, float* map1,
+                       float* K0new, float* K1new, float* Enew, float* Rl, float* Rr) {
+    rect_rotations(E, Rl, Rr);
+    float c[3], t[3], u[3];
+    homog_col3(E, c);
+    mat3_vec(Rr, c, t);
+    mat3_vec(Rr, t, u);
+    for (int i = 0; i < 16; ++i) Enew[i] = (i % 5 == 0) ? 1.0f : 0.0f;
+    Enew[3] = u[0]; Enew[7] = u[1]; Enew[11] = u[2];
+    const float fl = K0[4], fr = K1[4];
+    const float fn = (fl < fr) ? fl : fr;
+    float clx = K0[2], cly = K0[5], crx = K1[2], cry = K1[5];
+    if (vertical) {
+        clx = crx = (clx + crx) * 0.5f;
+    } else {
+        const float ny = (cly + cry) * 0.5f;
+        cly = ny;
+        cry = ny;
+    }
+    const float a0[9] = {fn, 0.0f, clx, 0.0f, fn, cly, 0.0f, 0.0f, 1.0f};
+    const float a1[9] = {fn, 0.0f, crx, 0.0f, fn, cry, 0.0f, 0.0f, 1.0f};
+    memcpy(K0new, a0, sizeof a0);
+    memcpy(K1new, a1, sizeof a1);
+    float RlT[9], RrT[9];
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) { RlT[i * 3 + j] = Rl[j * 3 + i]; RrT[i * 3 + j] = Rr[j * 3 + i]; }
+    for (int y = 0; y < H; ++y)
+        for (int x = 0; x < W; ++x) {
+            const size_t o = 2 * ((size_t)y * W + x);
+            rect_point((float)x, (float)y, fn, clx, cly, RlT, K0, rad0, tan0, &map0[o], &map0[o + 1]);
+            rect_point((float)x, (float)y, fn, crx, cry, RrT, K1, rad1, tan1, &map1[o], &map1[o + 1]);
+        }
+    return 0;
+}
+
+/* kind: 0 GRAY_FLOAT, 1 RGBA/BGRA_FLOAT, 2 GRAY_UINT8, 3 RGBA/BGRA_UINT8;
+ * map W*H (x, y) pairs (rows of mstride bytes); strides in bytes. */
+int orc_warp(int kind, const void* src, size_t sstride, int sw, int sh, const float* map, size_t mstride, int W, int H,
+             void* dst, size_t dstride) {
+    const uint8_t* s = (const uint8_t*)src;
+    for (int y = 0; y < H; ++y) {
+        const float* m = (const float*)((const uint8_t*)map + (size_t)y * mstride);
+        uint8_t* d = (uint8_t*)dst + (size_t)y * dstride;
+        for (int x = 0; x < W; ++x) {
+            const float cx = m[2 * x], cy = m[2 * x + 1];
+            if (kind == 0 || kind == 1) {
+                const int C = kind == 0 ? 1 : 4;
+                const float fill[4] = {0.0f, 0.0f, 0.0f, kind == 0 ? 0.0f : 1.0f};
+                float* o = (float*)d + (size_t)x * C;
+                const bool rep = std::isfinite(cx) && std::isfinite(cy) && fabsf(cx) < 2147483520.0f &&
+                                 fabsf(cy) < 2147483520.0f;
+                const int lx = rep ? floor_ref(cx) : -2, ly = rep ? floor_ref(cy) : -2;
+                if (lx < -1 || lx >= sw || ly < -1 || ly >= sh) {
+                    for (int k = 0; k < C; ++k) o[k] = fill[k];
+                    continue;
+                }
+                const float a1 = cx - (float)lx, a2 = cy - (float)ly;
+                for (int k = 0; k < C; ++k) {
+                    auto at = [&](int px, int py) {
+                        return (px >= 0 && px < sw && py >= 0 && py < sh)
+                                   ? ((const float*)(s + (size_t)py * sstride))[(size_t)px * C + k] : fill[k];
+                    };
+                    const float v00 = at(lx, ly), v10 = at(lx + 1, ly), v01 = at(lx, ly + 1), v11 = at(lx + 1, ly + 1);
+                    const float v1 = v00 + (v10 - v00) * a1;
+                    const float v2 = v01 + (v11 - v01) * a1;
+                    o[k] = v1 + (v2 - v1) * a2;
+                }
+            } else if (kind == 2) {
+                if (!(std::isfinite(cx) && std::isfinite(cy) && fabsf(cx) < 32768.0f && fabsf(cy) < 32768.0f)) {
+                    d[x] = 0;
+                    continue;
+                }
+                const int fx = (int)(cx * 65536.0f), fy = (int)(cy * 65536.0f);
+                const int lx = fx >> 16, ly = fy >> 16, ax = fx & 0xffff, ay = fy & 0xffff;
+                if (lx < -1 || lx >= sw || ly < -1 || ly >= sh) {
+                    d[x] = 0;
+                    continue;
+                }
+                auto at = [&](int px, int py) {
+                    return (px >= 0 && px < sw && py >= 0 && py < sh) ? (int)s[(size_t)py * sstride + px] : 0;
+                };
+                const int v1 = at(lx, ly) + (((at(lx + 1, ly) - at(lx, ly)) * ax) >> 16);
+                const int v2 = at(lx, ly + 1) + (((at(lx + 1, ly + 1) - at(lx, ly + 1)) * ax) >> 16);
+                d[x] = (uint8_t)(v1 + (((v2 - v1) * ay) >> 16));
+            } else {
+                const uint32_t fill = 0xff000000u;
+                uint32_t* o = (uint32_t*)d + x;
+                if (!(std::isfinite(cx) && std::isfinite(cy) && fabsf(cx) < 8388608.0f && fabsf(cy) < 8388608.0f)) {
+                    *o = fill;
+                    continue;
+                }
+                const int fx = (int)(cx * 256.0f), fy = (int)(cy * 256.0f);
+                const int lx = fx >> 8, ly = fy >> 8;
+                if (lx < -1 || lx >= sw || ly < -1 || ly >= sh) {
+                    *o = fill;
+                    continue;
+                }
+                auto at = [&](int px, int py) {
+                    uint32_t v;
+                    if (!(px >= 0 && px < sw && py >= 0 && py < sh)) return fill;
+                    memcpy(&v, s + (size_t)py * sstride + (size_t)px * 4, 4);
+                    return v;
+                };
+                const uint32_t a1 = (uint32_t)fx & 0xffu, a2 = (uint32_t)fy & 0xffu;
+                const uint32_t v1 = mix4(at(lx, ly), at(lx + 1, ly), a1);
+                const uint32_t v2 = mix4(at(lx, ly + 1), at(lx + 1, ly + 1), a1);
+                *o = mix4(v1, v2, a2);
+            }
+        }
+    }
+    return 0;
+}
+
+}  // extern "C"

@@ -121,5 +121,50 @@ def build(force: bool = False, verbose: bool = False) -> str | None:
     return LIB
 
 
+RECT_LIB = os.path.join(OUT, "libpmref_rect.so")
+RECT_SHIM = os.path.join(HERE, "rect_shim")
+
+
+def build_rect(force: bool = False, verbose: bool = False) -> str | None:
+    """oracle/_ref/libpmref_rect.so: the reference's stereo rectification
+    (cvt/vision/StereoCameraCalibration.h with cvt/math) and bilinear warps
+    (cvt/util/SIMD.cpp) behind rect_harness.cpp.  SIMD.cpp is compiled with
+    hidden visibility and linked with --gc-sections, so SIMD::instance() and
+    the SSE variants it would construct (other translation units) drop out;
+    the harness calls the generic SIMD methods."""
+    if not available():
+        return None
+    own = [os.path.join(HERE, "rect_harness.cpp"), os.path.join(HERE, "rect_stubs.cpp"), __file__]
+    own += [os.path.join(dp, f) for dp, _, fs in os.walk(RECT_SHIM) for f in fs]
+    if not force and os.path.exists(RECT_LIB) and all(os.path.getmtime(s) <= os.path.getmtime(RECT_LIB) for s in own):
+        return RECT_LIB
+    os.makedirs(OUT, exist_ok=True)
+    os.makedirs(GEN, exist_ok=True)
+    base = ["g++", "-std=c++11", "-O2", "-fPIC", "-ffp-contract=off", "-fno-fast-math", "-w", "-fvisibility=hidden",
+            "-ffunction-sections", "-fdata-sections", "-include", "cstring", "-I", RECT_SHIM, "-I", REF]
+    srcs = [os.path.join(HERE, "rect_harness.cpp"), os.path.join(HERE, "rect_stubs.cpp"),
+            os.path.join(REF, "cvt", "util", "SIMD.cpp")]
+    objs, jobs = [], []
+    for src in srcs:
+        obj = os.path.join(GEN, "rect_" + os.path.basename(src).replace(".cpp", ".o"))
+        cmd = base + ["-c", src, "-o", obj]
+        if verbose:
+            print(" ".join(cmd), file=sys.stderr)
+        jobs.append((src, subprocess.Popen(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)))
+        objs.append(obj)
+    bad = []
+    for src, p in jobs:
+        out, _ = p.communicate()
+        if p.returncode:
+            print(out, file=sys.stderr)
+            bad.append(src)
+    if bad:
+        raise RuntimeError(f"rectification harness: compile failed for {bad}")
+    subprocess.run(["g++", "-shared", "-Wl,--gc-sections", "-Wl,-z,now", "-o", RECT_LIB + ".tmp", *objs], check=True)
+    os.replace(RECT_LIB + ".tmp", RECT_LIB)
+    return RECT_LIB
+
+
 if __name__ == "__main__":
     print(build(force=True, verbose="-v" in sys.argv))
+    print(build_rect(force=True, verbose="-v" in sys.argv))
