@@ -24,6 +24,8 @@ EXPORTS = (
     "cvtpm_cost_eval_noalloc",
     "cvtpm_iformat_bpp", "cvtpm_image_to_rgbaf", "cvtpm_depthmap_image", "cvtpm_raw_read", "cvtpm_raw_write",
     "cvtpm_ppm_read", "cvtpm_pfm_write", "cvtpm_stereo_rectify", "cvtpm_warp_apply",
+    "cvtpm_tsdf_create", "cvtpm_tsdf_destroy", "cvtpm_tsdf_info", "cvtpm_tsdf_clear", "cvtpm_tsdf_projection",
+    "cvtpm_tsdf_add_depthmap", "cvtpm_tsdf_raycast", "cvtpm_tsdf_slice", "cvtpm_tsdf_save_raw",
 )
 
 
@@ -135,6 +137,17 @@ def lib() -> ctypes.CDLL:
     L.cvtpm_stereo_rectify.argtypes = [CP, CP, ctypes.POINTER(ctypes.c_float), i, ctypes.POINTER(CvtpmRectification),
                                        i, i, vp, vp, sz, vp]
     L.cvtpm_warp_apply.argtypes = [IP, IP, vp, sz, vp]
+    FP = ctypes.POINTER(ctypes.c_float)
+    L.cvtpm_tsdf_create.argtypes = [ctypes.POINTER(vp), i, FP, i, i, i, f]
+    L.cvtpm_tsdf_destroy.argtypes = [vp]
+    IPp = ctypes.POINTER(ctypes.c_int)
+    L.cvtpm_tsdf_info.argtypes = [vp, IPp, IPp, IPp, ctypes.POINTER(vp)]
+    L.cvtpm_tsdf_clear.argtypes = [vp, f, vp]
+    L.cvtpm_tsdf_projection.argtypes = [FP, FP, FP]
+    L.cvtpm_tsdf_add_depthmap.argtypes = [vp, FP, vp, i, i, sz, f, vp]
+    L.cvtpm_tsdf_raycast.argtypes = [vp, FP, vp, i, i, sz, f, vp]
+    L.cvtpm_tsdf_slice.argtypes = [vp, i, i, vp, sz, vp]
+    L.cvtpm_tsdf_save_raw.argtypes = [vp, ctypes.c_char_p, i]
     for name in EXPORTS:
         if name not in ("cvtpm_version", "cvtpm_status_string", "cvtpm_last_error", "cvtpm_iformat_bpp"):
             getattr(L, name).restype = ctypes.c_int

@@ -427,6 +427,47 @@ cvtpm_status cvtpm_stereo_rectify(const cvtpm_camera* first, const cvtpm_camera*
 cvtpm_status cvtpm_warp_apply(const cvtpm_image* dst, const cvtpm_image* src, const float* warp, size_t warp_pitch,
                               void* stream);
 
+/* ------------------------------------------------------------------
+ * Output side: TSDF fusion of depth maps (cvt::TSDFVolume,
+ * cvt/vision/TSDFVolume.h, TSDFVolume.cpp; kernels
+ * cvt/cl/kernel/TSDFVolume/TSDFVolume.cl).  Matrices are row-major 4x4
+ * (cvt::Matrix4f).  The volume is width*height*depth float2 (tsdf, weight) in
+ * device memory, x fastest.
+ * ------------------------------------------------------------------ */
+typedef struct cvtpm_tsdf cvtpm_tsdf;
+
+/* TSDFVolume(gridtoworld, width, height, depth, truncation)
+ * (TSDFVolume.cpp:31-45); the volume is not cleared (call cvtpm_tsdf_clear). */
+cvtpm_status cvtpm_tsdf_create(cvtpm_tsdf** vol, int device, const float* grid_to_world,
+                               int width, int height, int depth, float truncation);
+cvtpm_status cvtpm_tsdf_destroy(cvtpm_tsdf* vol);
+/* Size and the device pointer of the volume. */
+cvtpm_status cvtpm_tsdf_info(const cvtpm_tsdf* vol, int* width, int* height, int* depth, void** data);
+/* clear(weight) (:47-58): every voxel (1, weight). */
+cvtpm_status cvtpm_tsdf_clear(cvtpm_tsdf* vol, float weight, void* stream);
+/* The projection of addDepthMap / rayCastDepthMap from intrinsics (3x3) and
+ * extrinsics (4x4): intrinsics.toMatrix4() * extrinsics (:79-84, :87-92). */
+cvtpm_status cvtpm_tsdf_projection(const float* intrinsics, const float* extrinsics, float* proj);
+/* addDepthMap(proj, depthmap, scale) (:61-77): depth map GRAY_FLOAT on the
+ * device (rows of dpitch bytes), depth = value * scale. */
+cvtpm_status cvtpm_tsdf_add_depthmap(cvtpm_tsdf* vol, const float* proj, const float* depthmap,
+                                     int dwidth, int dheight, size_t dpitch, float scale, void* stream);
+/* rayCastDepthMap(depthmap, proj, scale) (:94-110): depth of the first
+ * surface along each pixel's ray, 0 where there is none.  A ray whose march
+ * cannot advance in float (a camera about 2^24 voxels from the volume) stops
+ * after 2 * max(width, height, depth) + 16 steps with 0, where the
+ * reference's loop does not end. */
+cvtpm_status cvtpm_tsdf_raycast(cvtpm_tsdf* vol, const float* proj, float* depthmap,
+                                int dwidth, int dheight, size_t dpitch, float scale, void* stream);
+/* The slice kernels TSDFVolume_sliceX/Y/Z (axis 0/1/2, plane `index`) into
+ * RGBA float rows of `pitch` bytes: (c, c, c, 1), c = clamp(tsdf + 0.5, 0, 1);
+ * the image is height x depth (x), width x depth (y) or width x height (z).
+ * (The reference's host functions sliceX/Y/Z are empty.) */
+cvtpm_status cvtpm_tsdf_slice(cvtpm_tsdf* vol, int axis, int index, float* rgba, size_t pitch, void* stream);
+/* saveRaw(path, weighted) (:130-152): (tsdf, weight) pairs or the tsdf
+ * values alone; synchronizes the device. */
+cvtpm_status cvtpm_tsdf_save_raw(cvtpm_tsdf* vol, const char* path, int weighted);
+
 #ifdef __cplusplus
 }
 #endif

@@ -408,3 +408,65 @@ def stereo_rectify(cam0, cam1, E, vertical, W, H):
 def warp(fmt, src, warp_map):
     """IWarp::apply(dst, src, warp) for GRAY/RGBA/BGRA float and uint8 storage."""
     return _warp_call(_rect_lib(lib()).orc_warp, fmt, src, warp_map)
+
+
+# ----------------------------------------------------------------------
+# TSDF fusion (orc_tsdf_* in pm_oracle.cpp).  Volumes are (D, H, W, 2)
+# float32 arrays of (tsdf, weight); matrices (4, 4) float32 row-major.
+
+def _tsdf_lib():
+    L = lib()
+    vp, c_int, c_float = ctypes.c_void_p, ctypes.c_int, ctypes.c_float
+    L.orc_tsdf_matrices.argtypes = [vp, vp, vp, vp]
+    L.orc_tsdf_clear.argtypes = [vp, c_int, c_int, c_int, c_float]
+    L.orc_tsdf_add.argtypes = [vp, c_int, c_int, c_int, vp, c_int, c_int, c_float, vp, c_float]
+    L.orc_tsdf_raycast.argtypes = [vp, c_int, c_int, vp, c_int, c_int, c_int, vp, vp, c_float, c_int]
+    L.orc_tsdf_slice.argtypes = [vp, c_int, c_int, vp, c_int, c_int, c_int]
+    return L
+
+
+def _m4(a):
+    return np.ascontiguousarray(np.asarray(a, np.float32).reshape(4, 4))
+
+
+def tsdf_matrices(proj, g2w):
+    """(proj * g2w, its inverse) as TSDFVolume::addDepthMap / rayCastDepthMap form them."""
+    t, ti = np.empty((4, 4), np.float32), np.empty((4, 4), np.float32)
+    p, g = _m4(proj), _m4(g2w)
+    _tsdf_lib().orc_tsdf_matrices(p.ctypes.data, g.ctypes.data, t.ctypes.data, ti.ctypes.data)
+    return t, ti
+
+
+def tsdf_clear(W, H, D, weight=0.0):
+    v = np.empty((D, H, W, 2), np.float32)
+    _tsdf_lib().orc_tsdf_clear(v.ctypes.data, W, H, D, float(weight))
+    return v
+
+
+def tsdf_add(vol, dmap, dscale, tg2cam, trunc):
+    """In place: TSDFVolume_add with the kernel matrix TG2CAM."""
+    D, H, W = vol.shape[:3]
+    dm = np.ascontiguousarray(dmap, np.float32)
+    t = _m4(tg2cam)
+    _tsdf_lib().orc_tsdf_add(vol.ctypes.data, W, H, D, dm.ctypes.data, dm.shape[1], dm.shape[0], float(dscale),
+                             t.ctypes.data, float(trunc))
+    return vol
+
+
+def tsdf_raycast(vol, iw, ih, tcam2g, tg2cam, scale, max_steps=None):
+    D, H, W = vol.shape[:3]
+    if max_steps is None:
+        max_steps = 2 * max(W, H, D) + 16
+    out = np.empty((ih, iw), np.float32)
+    ti, t = _m4(tcam2g), _m4(tg2cam)
+    _tsdf_lib().orc_tsdf_raycast(out.ctypes.data, iw, ih, vol.ctypes.data, W, H, D, ti.ctypes.data, t.ctypes.data,
+                                 float(scale), int(max_steps))
+    return out
+
+
+def tsdf_slice(vol, axis, index):
+    D, H, W = vol.shape[:3]
+    shape = {0: (D, H), 1: (D, W), 2: (H, W)}[axis]
+    out = np.empty(shape + (4,), np.float32)
+    _tsdf_lib().orc_tsdf_slice(out.ctypes.data, axis, index, vol.ctypes.data, W, H, D)
+    return out

@@ -34,6 +34,7 @@
  * separate colour/gradient accumulators); it is the bit-exact CPU mirror of
  * that kernel.
  */
+#include <cfloat>
 #include "cvtpm.h"
 #include "pm_math.h"
 
@@ -1578,6 +1579,173 @@ int orc_warp(int kind, const void* src, size_t sstride, int sw, int sh, const fl
             }
         }
     }
+    return 0;
+}
+
+}  // extern "C"
+
+/* ---------------------------------------------------------------------
+ * TSDF fusion (cvt::TSDFVolume, cvt/vision/TSDFVolume.cpp; kernels
+ * cvt/cl/kernel/TSDFVolume/TSDFVolume.cl) on the CPU.  Volume: W*H*D pairs
+ * (tsdf, weight), x fastest.  Matrices row-major 4x4.
+ *   orc_tsdf_matrices  projall = proj * g2w (Matrix4.h:269-288) and its
+ *                      inverse (Matrix.cpp:109-196; unchanged if |det| <
+ *                      FLT_EPSILON)
+ *   orc_tsdf_clear / orc_tsdf_add / orc_tsdf_raycast / orc_tsdf_slice
+ *                      the kernels, with OpenCL's dot summed left to right and
+ *                      normalize = v * (1 / sqrt(dot(v, v))); the ray march
+ *                      stops after max_steps steps (its float loop need not
+ *                      end otherwise).
+ * --------------------------------------------------------------------- */
+namespace {
+
+void m4mul(const float* a, const float* b, float* r) {
+    float t[16];
+    for (int i = 0; i < 4; ++i)
+        for (int j = 0; j < 4; ++j)
+            t[i * 4 + j] = a[i * 4 + 0] * b[0 * 4 + j] + a[i * 4 + 1] * b[1 * 4 + j] + a[i * 4 + 2] * b[2 * 4 + j] +
+                           a[i * 4 + 3] * b[3 * 4 + j];
+    memcpy(r, t, sizeof t);
+}
+
+void m4inv(const float* m, float* out) {
+    auto A = [&](int i, int j) { return m[i * 4 + j]; };
+    /* 2x2 minors of rows (r0, r1), columns (c0, c1) */
+    auto d2 = [&](int r0, int r1, int c0, int c1) { return A(r0, c0) * A(r1, c1) - A(r1, c0) * A(r0, c1); };
+    /* 3x3 minors: row r with the 2x2 minors of rows (p, q) */
+    auto d3 = [&](int r, int p, int q, int c0, int c1, int c2) {
+        return A(r, c0) * d2(p, q, c1, c2) - A(r, c1) * d2(p, q, c0, c2) + A(r, c2) * d2(p, q, c0, c1);
+    };
+    const float det = A(0, 0) * d3(1, 2, 3, 1, 2, 3) - A(0, 1) * d3(1, 2, 3, 0, 2, 3) +
+                      A(0, 2) * d3(1, 2, 3, 0, 1, 3) - A(0, 3) * d3(1, 2, 3, 0, 1, 2);
+    if (fabsf(det) < FLT_EPSILON) { memcpy(out, m, 16 * sizeof(float)); return; }
+    const float inv = 1.0f / det;
+    /* cofactor of element (j, i): rows without j, columns without i */
+    const int rows[4][3] = {{1, 2, 3}, {0, 2, 3}, {0, 1, 3}, {0, 1, 2}};
+    float r[16];
+    for (int i = 0; i < 4; ++i)
+        for (int j = 0; j < 4; ++j) {
+            const int* rr = rows[j];
+            const int* cc = rows[i];
+            const float c = d3(rr[0], rr[1], rr[2], cc[0], cc[1], cc[2]);
+            r[i * 4 + j] = ((i + j) & 1) ? -c * inv : c * inv;
+        }
+    memcpy(out, r, sizeof r);
+}
+
+struct V4 { float x, y, z, w; };
+inline float dot4f(const float* r, V4 v) { return ((r[0] * v.x + r[1] * v.y) + r[2] * v.z) + r[3] * v.w; }
+inline float mixo(float a, float b, float t) { return a + (b - a) * t; }
+
+float tsdf_trilinear(const float* cv, int W, int H, int D, float px, float py, float pz) {
+    px = std::fmin(std::fmax(0.0f, px), (float)(W - 2));
+    py = std::fmin(std::fmax(0.0f, py), (float)(H - 2));
+    pz = std::fmin(std::fmax(0.0f, pz), (float)(D - 2));
+    const float bx = std::floor(px), by = std::floor(py), bz = std::floor(pz);
+    const int ix = (int)bx, iy = (int)by, iz = (int)bz;
+    float v[8];
+    for (int k = 0; k < 8; ++k) {
+        const size_t o = 2 * (((size_t)(iz + (k >> 2)) * H + (size_t)(iy + ((k >> 1) & 1))) * W + (size_t)(ix + (k & 1)));
+        if (cv[o + 1] < 1.0f) return 1e10f;
+        v[k] = cv[o];
+    }
+    const float az = pz - bz, ay = py - by, ax = px - bx;
+    const float y0 = mixo(mixo(v[0], v[4], az), mixo(v[2], v[6], az), ay);
+    const float y1 = mixo(mixo(v[1], v[5], az), mixo(v[3], v[7], az), ay);
+    return mixo(y0, y1, ax);
+}
+
+}  // namespace
+
+extern "C" {
+
+int orc_tsdf_matrices(const float* proj, const float* g2w, float* tg2cam, float* tcam2g) {
+    m4mul(proj, g2w, tg2cam);
+    m4inv(tg2cam, tcam2g);
+    return 0;
+}
+
+int orc_tsdf_clear(float* cv, int W, int H, int D, float init) {
+    for (size_t i = 0; i < (size_t)W * H * D; ++i) { cv[2 * i] = 1.0f; cv[2 * i + 1] = init; }
+    return 0;
+}
+
+int orc_tsdf_add(float* cv, int W, int H, int D, const float* dmap, int iw, int ih, float dscale, const float* T,
+                 float trunc) {
+    for (int z = 0; z < D; ++z)
+        for (int y = 0; y < H; ++y)
+            for (int x = 0; x < W; ++x) {
+                const V4 p{(float)x, (float)y, (float)z, 1.0f};
+                const float gx = dot4f(T, p), gy = dot4f(T + 4, p), gz = dot4f(T + 8, p);
+                const float u = gx / gz, v = gy / gz;
+                if (!(u < (float)iw && v < (float)ih && u >= 0.0f && v >= 0.0f)) continue;
+                const float d = dmap[(size_t)(int)std::floor(v) * iw + (size_t)(int)std::floor(u)] * dscale;
+                if (!(d > 0.0f && gz > 0.0f)) continue;
+                const float sdf = d - gz;
+                const float t = sdf / trunc;
+                if (!(std::fabs(sdf) <= trunc)) continue;
+                float* c = cv + 2 * (((size_t)z * H + y) * W + x);
+                const float w = 1.0f;
+                const float nx = (c[0] * c[1] + t * w) / (c[1] + w), ny = c[1] + w;
+                c[0] = nx;
+                c[1] = ny;
+            }
+    return 0;
+}
+
+int orc_tsdf_raycast(float* out, int iw, int ih, const float* cv, int W, int H, int D, const float* Ti,
+                     const float* T, float scale, int max_steps) {
+    for (int gy = 0; gy < ih; ++gy)
+        for (int gx = 0; gx < iw; ++gx) {
+            const V4 z0{0.0f, 0.0f, 0.0f, 1.0f}, p1{(float)gx, (float)gy, 1.0f, 1.0f};
+            const float ox = dot4f(Ti, z0), oy = dot4f(Ti + 4, z0), oz = dot4f(Ti + 8, z0);
+            float dx = dot4f(Ti, p1) - ox, dy = dot4f(Ti + 4, p1) - oy, dz = dot4f(Ti + 8, p1) - oz;
+            const float n = 1.0f / std::sqrt((dx * dx + dy * dy) + dz * dz);
+            dx *= n; dy *= n; dz *= n;
+            const float sx = ((dx > 0.0f ? 0.0f : (float)W) - ox) / dx, sy = ((dy > 0.0f ? 0.0f : (float)H) - oy) / dy;
+            const float sz = ((dz > 0.0f ? 0.0f : (float)D) - oz) / dz;
+            const float ex = ((dx > 0.0f ? (float)W : 0.0f) - ox) / dx, ey = ((dy > 0.0f ? (float)H : 0.0f) - oy) / dy;
+            const float ez = ((dz > 0.0f ? (float)D : 0.0f) - oz) / dz;
+            const float rs = std::fmax(std::fmax(sx, sy), sz), re = std::fmin(std::fmin(ex, ey), ez);
+            float ret = 0.0f;
+            if (rs < re && std::isfinite(rs) && std::isfinite(re) && std::isfinite(dx) && std::isfinite(dy) &&
+                std::isfinite(dz)) {
+                const float span = re - rs;
+                const float vx = std::fabs(dx * span), vy = std::fabs(dy * span), vz = std::fabs(dz * span);
+                const float len = std::sqrt((vx * vx + vy * vy) + vz * vz);
+                const float step = 0.5f * len / std::fmax(vx, std::fmax(vy, vz));
+                float qx = ox + dx * rs, qy = oy + dy * rs, qz = oz + dz * rs;
+                float prev = tsdf_trilinear(cv, W, H, D, qx, qy, qz);
+                int k = 0;
+                for (float lam = rs + step; lam <= re && k < max_steps; lam += step, ++k) {
+                    const float px = ox + dx * lam, py = oy + dy * lam, pz = oz + dz * lam;
+                    const float val = tsdf_trilinear(cv, W, H, D, px, py, pz);
+                    if (prev < 0.0f && val > 0.0f) break;
+                    if (prev > 0.0f && val < 0.0f) {
+                        const float a = -val / (prev - val);
+                        const float g = mixo(pz, qz, a);
+                        ret = std::fmax(-dot4f(T + 8, V4{g, g, g, 1.0f}) * scale, 0.0f);
+                        break;
+                    }
+                    prev = val;
+                    qx = px; qy = py; qz = pz;
+                }
+            }
+            out[(size_t)gy * iw + gx] = ret;
+        }
+    return 0;
+}
+
+int orc_tsdf_slice(float* rgba, int axis, int v, const float* cv, int W, int H, int D) {
+    const int ow = axis == 0 ? H : W, oh = axis == 2 ? H : D;
+    for (int b = 0; b < oh; ++b)
+        for (int a = 0; a < ow; ++a) {
+            const int x = axis == 0 ? v : a, y = axis == 0 ? a : (axis == 1 ? v : b), z = axis == 2 ? v : b;
+            const float t = std::fmin(std::fmax(cv[2 * (((size_t)z * H + y) * W + x)] + 0.5f, 0.0f), 1.0f);
+            float* o = rgba + 4 * ((size_t)b * ow + a);
+            o[0] = o[1] = o[2] = t;
+            o[3] = 1.0f;
+        }
     return 0;
 }
 

@@ -4,7 +4,7 @@ they lie, under /root/reference, and copies none into the repository), so it
 runs only where they are present.
 
   1. translate.py rewrites cvt/cl/kernel/{pmhstereo,RNG,PDHuberWeighted,
-     PDHuberWeightedInpaint,fill}.cl
+     PDHuberWeightedInpaint,fill,Matrix4,TSDFVolume/TSDFVolume}.cl
      into _build/ref_gen/*.inc (generated, never committed);
   2. one C++ unit per kernel file wraps its .inc in a namespace and registers
      the kernels with clemu;
@@ -26,7 +26,9 @@ REF = "/root/reference"
 GEN = os.path.join(ROOT, "_build", "ref_gen")
 OUT = os.path.join(ORACLE, "_ref")
 LIB = os.path.join(OUT, "libpmref.so")
-KERNEL_FILES = ["RNG", "pmhstereo", "PDHuberWeighted", "PDHuberWeightedInpaint", "fill"]
+KERNEL_FILES = ["RNG", "Matrix4", "pmhstereo", "PDHuberWeighted", "PDHuberWeightedInpaint", "fill",
+                "TSDFVolume/TSDFVolume"]
+INCLUDE_ONLY = ("RNG", "Matrix4")     # #import-ed by other kernel files, no kernels of their own
 
 sys.path.insert(0, HERE)
 import translate  # noqa: E402
@@ -39,12 +41,13 @@ def available() -> bool:
 def generate():
     os.makedirs(GEN, exist_ok=True)
     units = []
-    for name in KERNEL_FILES:
-        src = open(os.path.join(REF, "cvt", "cl", "kernel", name + ".cl")).read()
+    for path in KERNEL_FILES:
+        name = os.path.basename(path)
+        src = open(os.path.join(REF, "cvt", "cl", "kernel", path + ".cl")).read()
         tr = translate.translate(src)
         with open(os.path.join(GEN, name + ".inc"), "w") as f:
             f.write(tr)
-        if name == "RNG":
+        if name in INCLUDE_ONLY:
             continue
         ns = "k_" + name
         lines = ['#include "clemu.h"', "namespace clemu { namespace %s {" % ns, '#include "%s.inc"' % name, "}}",

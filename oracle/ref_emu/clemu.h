@@ -24,6 +24,8 @@
 #define CLEMU_H
 
 #include <cmath>
+#include <cstdio>
+#include <cstdlib>
 #include <cstddef>
 #include <cstdint>
 #include <cstring>
@@ -78,6 +80,10 @@ struct float2 {
     float2() : x(0), y(0) {}
     float2(float s) : x(s), y(s) {}
     template <class A, class B> float2(A a, B b) : x(to_float(a)), y(to_float(b)) {}
+    float& s0() { return x; }
+    float& s1() { return y; }
+    float s0() const { return x; }
+    float s1() const { return y; }
 };
 struct float3 {
     float x, y, z;
@@ -91,7 +97,11 @@ struct int2 {
     int2(int s) : x(s), y(s) {}
     template <class A, class B> int2(A a, B b) : x(to_int(a)), y(to_int(b)) {}
 };
-struct int3 { int x, y, z; };
+struct int3 {
+    int x, y, z;
+    int3() : x(0), y(0), z(0) {}
+    template <class A, class B, class C> int3(A a, B b, C c) : x(to_int(a)), y(to_int(b)), z(to_int(c)) {}
+};
 struct int4 { int x, y, z, w; };
 struct uint2 {
     uint x, y;
@@ -120,15 +130,29 @@ struct alignas(16) float4 {
     float4(float s) : x(s), y(s), z(s), w(s) {}
     template <class A, class B, class C, class D>
     float4(A a, B b, C c, D d) : x(to_float(a)), y(to_float(b)), z(to_float(c)), w(to_float(d)) {}
+    float4(const float3& v, float w);   /* (float4)(v, w) */
     Swz2 xy() const { float* q = const_cast<float*>(&x); return Swz2{{q, q + 1}}; }
     Swz3 xyz() const { float* q = const_cast<float*>(&x); return Swz3{{q, q + 1, q + 2}}; }
+    float2 s01() const { return float2(x, y); }
+    float2 s23() const { return float2(z, w); }
     float4& operator+=(const float4& o);
 };
+inline float4::float4(const float3& v, float w_) : x(v.x), y(v.y), z(v.z), w(w_) {}
 struct alignas(32) float8 {
     float4 l, h;
     float8() {}
     float8(float s) : l(s), h(s) {}
     float8(const float4& a, const float4& b) : l(a), h(b) {}
+    float& s0() { return l.x; }
+    float& s1() { return l.y; }
+    float& s2() { return l.z; }
+    float& s3() { return l.w; }
+    float& s4() { return h.x; }
+    float& s5() { return h.y; }
+    float& s6() { return h.z; }
+    float& s7() { return h.w; }
+    float4 s0123() const { return l; }
+    float4 s4567() const { return h; }
     float4& lo() { return l; }
     float4& hi() { return h; }
     const float4& lo() const { return l; }
@@ -183,6 +207,31 @@ inline float pow(float a, float b) { return pm_pow(a, b); }
 inline float acospi(float v) { return pm_acospi(v); }
 inline float round(float v) { return std::round(v); }
 inline float floor(float v) { return std::floor(v); }
+inline float3 floor(const float3& v) { return float3(std::floor(v.x), std::floor(v.y), std::floor(v.z)); }
+inline float3 fmin(const float3& a, const float3& b) {
+    return float3(std::fmin(a.x, b.x), std::fmin(a.y, b.y), std::fmin(a.z, b.z));
+}
+inline float3 fmax(const float3& a, const float3& b) {
+    return float3(std::fmax(a.x, b.x), std::fmax(a.y, b.y), std::fmax(a.z, b.z));
+}
+/* mix(x, y, a) = x + (y - x) * a (OpenCL 1.2, 6.12.4), per component */
+inline float mix(float a, float b, float t) { return a + (b - a) * t; }
+inline float2 mix(const float2& a, const float2& b, float t) { return float2(mix(a.x, b.x, t), mix(a.y, b.y, t)); }
+inline float4 mix(const float4& a, const float4& b, float t) {
+    return float4(mix(a.x, b.x, t), mix(a.y, b.y, t), mix(a.z, b.z, t), mix(a.w, b.w, t));
+}
+/* sincos(float3, float3*) appears in helpers of Matrix4.cl (mat4f_rotation)
+ * that no emulated kernel calls; it is not emulated. */
+inline float3 sincos(const float3&, float3*) {
+    std::fprintf(stderr, "clemu: sincos(float3) is not emulated\n");
+    std::abort();
+}
+/* normalize: OpenCL leaves its rounding to the implementation; here
+ * v * (1 / sqrt(dot(v, v))), the native_rsqrt convention above */
+inline float3 normalize(const float3& v) {
+    const float r = 1.0f / std::sqrt((v.x * v.x + v.y * v.y) + v.z * v.z);
+    return float3(v.x * r, v.y * r, v.z * r);
+}
 inline float dot(const float2& a, const float2& b) { return a.x * b.x + a.y * b.y; }
 inline float dot(const float3& a, const float3& b) { return (a.x * b.x + a.y * b.y) + a.z * b.z; }
 inline float dot(const float4& a, const float4& b) { return ((a.x * b.x + a.y * b.y) + a.z * b.z) + a.w * b.w; }
@@ -260,7 +309,14 @@ typedef std::function<void(const std::vector<Arg>&)> ItemFn;   /* runs one work-
 void reg(const std::string& name, bool uses_barrier, ItemFn fn);
 void* local_arena(int index, size_t bytes);
 
-template <class T> struct ArgConv;
+/* any other argument type: a struct passed by value (Arg::BYTES) */
+template <class T> struct ArgConv {
+    static T get(const Arg& a, int) {
+        T t;
+        std::memcpy((void*)&t, a.bytes.data(), sizeof(T));
+        return t;
+    }
+};
 template <> struct ArgConv<image2d_t> { static image2d_t get(const Arg& a, int) { return a.img; } };
 template <> struct ArgConv<int> { static int get(const Arg& a, int) { return a.kind == Arg::FLOAT ? (int)a.f : a.i; } };
 template <> struct ArgConv<float> { static float get(const Arg& a, int) { return a.kind == Arg::INT ? (float)a.i : a.f; } };

@@ -21,17 +21,21 @@ struct Img {
 };
 
 struct Arg {
-    enum Kind { NONE, IMAGE, BUFFER, INT, FLOAT, FLOAT4, LOCAL } kind = NONE;
+    enum Kind { NONE, IMAGE, BUFFER, INT, FLOAT, FLOAT4, LOCAL, BYTES } kind = NONE;
     Img* img = nullptr;
     void* ptr = nullptr;
     int i = 0;
     float f = 0.0f;
     float f4[4] = {0, 0, 0, 0};
     size_t local_size = 0;
+    std::vector<unsigned char> bytes;   /* BYTES: a struct passed by value (clSetKernelArg with its size) */
 };
 
 /* Runs kernel `name` over a 2-D NDRange (global gx x gy, local lx x ly). */
 void launch(const std::string& name, const std::vector<Arg>& args, size_t gx, size_t gy, size_t lx, size_t ly);
+/* The same over a 3-D NDRange with local size lx x ly x 1. */
+void launch3(const std::string& name, const std::vector<Arg>& args, size_t gx, size_t gy, size_t gz, size_t lx,
+             size_t ly);
 bool has_kernel(const std::string& name);
 
 /* Called after every launch with the kernel name and its arguments. */

@@ -96,14 +96,20 @@ void reg(const std::string& name, bool uses_barrier, ItemFn fn) { registry()[nam
 bool has_kernel(const std::string& name) { return registry().count(name) != 0; }
 
 void launch(const std::string& name, const std::vector<Arg>& args, size_t gx, size_t gy, size_t lx, size_t ly) {
+    launch3(name, args, gx, gy, 1, lx, ly);
+}
+
+void launch3(const std::string& name, const std::vector<Arg>& args, size_t gx, size_t gy, size_t gz, size_t lx,
+             size_t ly) {
     auto it = registry().find(name);
     if (it == registry().end()) { fprintf(stderr, "clemu: unknown kernel %s\n", name.c_str()); abort(); }
     const Entry& e = it->second;
     if (gx % lx || gy % ly) { fprintf(stderr, "clemu: global size not a multiple of local size\n"); abort(); }
-    const long ngx = (long)(gx / lx), ngy = (long)(gy / ly);
+    const long ngx = (long)(gx / lx), ngy = (long)(gy / ly), ngz = (long)gz;
     const int n = (int)(lx * ly);
 #pragma omp parallel for schedule(dynamic, 1)
-    for (long gyi = 0; gyi < ngy; ++gyi) {
+    for (long gyz = 0; gyz < ngy * ngz; ++gyz) {
+        const long gyi = gyz % ngy, gzi = gyz / ngy;   /* z-planes of groups one after another */
         static thread_local std::unique_ptr<Sched> sched;
         if (!sched || (int)sched->fibers.size() < n) {
             sched.reset(new Sched());
@@ -118,9 +124,9 @@ void launch(const std::string& name, const std::vector<Arg>& args, size_t gx, si
             for (int i = 0; i < n; ++i) {
                 WorkItem& w = s->fibers[i].wi;
                 w.lid[0] = i % lx; w.lid[1] = i / lx; w.lid[2] = 0;
-                w.grp[0] = gxi; w.grp[1] = gyi; w.grp[2] = 0;
+                w.grp[0] = gxi; w.grp[1] = gyi; w.grp[2] = gzi;
                 w.lsz[0] = lx; w.lsz[1] = ly; w.lsz[2] = 1;
-                w.gid[0] = gxi * lx + w.lid[0]; w.gid[1] = gyi * ly + w.lid[1]; w.gid[2] = 0;
+                w.gid[0] = gxi * lx + w.lid[0]; w.gid[1] = gyi * ly + w.lid[1]; w.gid[2] = gzi;
                 s->fibers[i].state = 0;
             }
             if (!e.barrier) {

@@ -114,3 +114,14 @@ EXPORT int ref_warp(int kind, const void* src, size_t sstride, int sw, int sh, c
     }
     return 0;
 }
+
+/* cvt::Matrix4f operator* (cvt/math/Matrix4.h:269-288), row-major in and out;
+ * the product TSDFVolume::addDepthMap forms (proj * grid-to-world). */
+EXPORT int ref_mat4_mul(const float* a, const float* b, float* out) {
+    Matrix4f A(a[0], a[1], a[2], a[3], a[4], a[5], a[6], a[7], a[8], a[9], a[10], a[11], a[12], a[13], a[14], a[15]);
+    Matrix4f B(b[0], b[1], b[2], b[3], b[4], b[5], b[6], b[7], b[8], b[9], b[10], b[11], b[12], b[13], b[14], b[15]);
+    const Matrix4f C = A * B;
+    for (int i = 0; i < 4; ++i)
+        for (int j = 0; j < 4; ++j) out[i * 4 + j] = C[i][j];
+    return 0;
+}

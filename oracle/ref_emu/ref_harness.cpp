@@ -209,4 +209,56 @@ int ref_pdrof_inpaint(float* output, const float* input, const float* weight, co
     return 0;
 }
 
+/* TSDFVolume (cvt/vision/TSDFVolume.cpp:47-104, kernels
+ * cvt/cl/kernel/TSDFVolume/TSDFVolume.cl).  The volume is W*H*D float2
+ * (tsdf, weight); matrices row-major 4x4 as the kernels' Mat4f; NDRanges as
+ * the host code sets them (pad16 in x and y, 16 x 16 groups). */
+static clemu::Arg buf_arg(void* p) { clemu::Arg a; a.kind = clemu::Arg::BUFFER; a.ptr = p; return a; }
+static clemu::Arg mat_arg(const float* m) {
+    clemu::Arg a;
+    a.kind = clemu::Arg::BYTES;
+    a.bytes.assign((const unsigned char*)m, (const unsigned char*)m + 16 * sizeof(float));
+    return a;
+}
+
+int ref_tsdf_clear(float* vol, int W, int H, int D, float weight) {
+    clemu::launch3("TSDFVolume_clear", {buf_arg(vol), int_arg(W), int_arg(H), int_arg(D), float_arg(weight)}, pad16(W),
+                   pad16(H), (size_t)D, 16, 16);
+    return 0;
+}
+
+/* TSDFVolume::addDepthMap(proj, depthmap, scale) with TG2CAM = proj * g2w;
+ * the depth map is a GRAY_FLOAT image (read .x). */
+int ref_tsdf_add(float* vol, int W, int H, int D, const float* dmap, int iw, int ih, float dscale, const float* tg2cam,
+                 float trunc) {
+    Image dm((size_t)iw, (size_t)ih, IFormat::GRAY_FLOAT, IALLOCATOR_CL);
+    memcpy(dm.data(), dmap, sizeof(float) * (size_t)iw * ih);
+    clemu::launch3("TSDFVolume_add", {buf_arg(vol), int_arg(W), int_arg(H), int_arg(D), img_arg(dm), float_arg(dscale),
+                                      mat_arg(tg2cam), float_arg(trunc)}, pad16(W), pad16(H), (size_t)D, 16, 16);
+    return 0;
+}
+
+/* TSDFVolume::rayCastDepthMap(depthmap, proj, scale): TCAM2G = (proj * g2w)^-1. */
+int ref_tsdf_raycast(float* out, int iw, int ih, float* vol, int W, int H, int D, const float* tcam2g,
+                     const float* tg2cam, float scale) {
+    Image o((size_t)iw, (size_t)ih, IFormat::GRAY_FLOAT, IALLOCATOR_CL);
+    clemu::launch("TSDFVolume_rayCastDepthmap", {img_arg(o), buf_arg(vol), int_arg(W), int_arg(H), int_arg(D),
+                                                 mat_arg(tcam2g), mat_arg(tg2cam), float_arg(scale)},
+                  pad16(iw), pad16(ih), 16, 16);
+    memcpy(out, o.data(), sizeof(float) * (size_t)iw * ih);
+    return 0;
+}
+
+/* TSDFVolume_sliceX/Y/Z (TSDFVolume.cl) at plane v into an RGBA image of
+ * the slice's size (the NDRange as large as the image). */
+int ref_tsdf_slice(float* rgba, int axis, int v, float* vol, int W, int H, int D) {
+    const int ow = axis == 0 ? H : W, oh = axis == 2 ? H : D;
+    Image o((size_t)ow, (size_t)oh, IFormat::RGBA_FLOAT, IALLOCATOR_CL);
+    const char* k = axis == 0 ? "TSDFVolume_sliceX" : (axis == 1 ? "TSDFVolume_sliceY" : "TSDFVolume_sliceZ");
+    clemu::launch(k, {img_arg(o), int_arg(v), buf_arg(vol), int_arg(W), int_arg(H), int_arg(D)}, pad16(ow), pad16(oh),
+                  16, 16);
+    memcpy(rgba, o.data(), sizeof(float) * 4 * (size_t)ow * oh);
+    return 0;
+}
+
 }  // extern "C"

@@ -3,11 +3,12 @@ sources into C++ that compiles against clemu.h.
 
 It changes spelling only, never arithmetic:
   * comments are dropped;
-  * `#import "X.cl"` (the reference's textual include, util/glcltoheader.cpp)
-    becomes `#include "X.inc"`;
+  * `#import "X.cl"` or `#import "../X.cl"` (the reference's textual
+    include, util/glcltoheader.cpp) becomes `#include "X.inc"`;
   * vector literals `(float4)( a, b, ... )` become `float4{ a, b, ... }`
     (brace initialisation: components evaluated left to right);
-  * swizzles `.xy .xyz .lo .hi` become calls `.xy()` ... (proxy objects);
+  * swizzles `.xy .xyz .lo .hi` and `.s0` ... `.s7`, `.s01`, `.s0123` ...
+    become calls `.xy()` ... (proxy objects or accessors of the vector type);
   * `local T x[..]` declared in a kernel body becomes
     `static thread_local T x[..]`, shared by the work-items of a group
     (clemu runs one group at a time per thread).
@@ -50,9 +51,10 @@ def vector_literals(src: str) -> str:
 
 def translate(src: str) -> str:
     src = strip_comments(src)
-    src = re.sub(r'#import\s+"(\w+)\.cl"', r'#include "\1.inc"', src)
+    src = re.sub(r'#import\s+"(?:\.\./)?(\w+)\.cl"', r'#include "\1.inc"', src)
     src = vector_literals(src)
     src = re.sub(r"\.(xyz|xy|lo|hi)\b(?!\s*\()", r".\1()", src)
+    src = re.sub(r"\.(s[0-7]{1,4})\b(?!\s*\()", r".\1()", src)
     src = re.sub(r"(?m)^(\s*)local\s+", r"\1static thread_local ", src)
     return src
 
