@@ -515,6 +515,121 @@ def run_combined(args):
     return 0
 
 
+def run_rectify(args):
+    """Input-side workload: a 3840x2160 RGBA8 stereo pair undistorted and
+    rectified (two warp maps, IWarp::apply's 8-bit sampler), about 264 MB of
+    traffic per step (beyond L2).  Algorithmic bytes per output pixel: map 8 +
+    source 4 (each texel read about once) + destination 4."""
+    import torch
+    from cvt_gb300 import imageio, rectify
+    W, H = 3840, 2160
+    K0 = np.array([[2800.0, 0, 1915.0], [0, 2795.0, 1082.0], [0, 0, 1]], np.float32)
+    K1 = np.array([[2790.0, 0, 1925.0], [0, 2788.0, 1076.0], [0, 0, 1]], np.float32)
+    c0 = {"K": K0, "radial": np.array([-0.12, 0.04, 0.0], np.float32), "tangential": np.array([1e-4, -2e-4], np.float32)}
+    c1 = {"K": K1, "radial": np.array([-0.11, 0.035, 0.0], np.float32), "tangential": np.array([-1e-4, 1e-4], np.float32)}
+    a, t = 0.01, np.array([-0.12, 0.001, 0.002])
+    E = np.eye(4, dtype=np.float32)
+    E[:3, :3] = [[np.cos(a), 0, np.sin(a)], [0, 1, 0], [-np.sin(a), 0, np.cos(a)]]
+    E[:3, 3] = t
+    rng = np.random.default_rng(5)
+    left = torch.from_numpy(rng.integers(0, 256, (H, W, 4), dtype=np.uint8)).cuda()
+    right = torch.from_numpy(rng.integers(0, 256, (H, W, 4), dtype=np.uint8)).cuda()
+    stream = torch.cuda.current_stream()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    r = rectify.StereoRectification(c0, c1, E, W, H)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    r = rectify.StereoRectification(c0, c1, E, W, H)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    maps_ms = e0.elapsed_time(e1)
+    outl, outr = torch.empty_like(left), torch.empty_like(right)
+    for _ in range(max(3, args.warmup)):
+        r.undistortLeft(left, imageio.RGBA_UINT8, outl)
+        r.undistortRight(right, imageio.RGBA_UINT8, outr)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(args.steps):
+        r.undistortLeft(left, imageio.RGBA_UINT8, outl)
+        r.undistortRight(right, imageio.RGBA_UINT8, outr)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / args.steps
+    npx = 2 * W * H
+    peak, src = peaks()
+    gbs = 16.0 * npx / (ms * 1e-3) / 1e9
+    print(json.dumps({"workload": "rectify", "metric": "rectified Mpix/s (IWarp::apply, RGBA8, both views)",
+                      "value": npx / 1e6 / (ms * 1e-3), "unit": "Mpix/s", "ms_per_step": ms, "steps": args.steps,
+                      "maps_ms": maps_ms, "config": {"workload": f"{W}x{H} RGBA8 pair, radial + tangential distortion, "
+                                                                 "undistort + rectify both views per step"},
+                      "roofline": {"kernel": "k_warp_apply<U8C4>", "bound": "hbm", "achieved": gbs, "peak": peak,
+                                   "unit": "GB/s", "frac": gbs / peak, "peak_source": src,
+                                   "bytes_per_px": 16}}), flush=True)
+    return 0
+
+
+def run_tsdf(args):
+    """Output-side workload: TSDF fusion into a 512^3 volume of 1 cm voxels
+    (1 GB of (tsdf, weight)), per step 4 depth maps of 640x480 integrated and
+    one ray cast of 640x480.  Bytes: clear writes 8 per voxel; integration
+    reads 8 and writes 8 per voxel inside the truncation band and projects
+    every voxel (the depth-map reads stay in L2)."""
+    import torch
+    from cvt_gb300 import scenes, tsdf
+    N = 512
+    g2w = np.eye(4, dtype=np.float32)
+    g2w[:3, :3] *= 0.01
+    g2w[:3, 3] = [-2.56, -2.56, 0.5]
+    K = np.array([[525.0, 0, 319.5], [0, 525.0, 239.5], [0, 0, 1]], np.float32)
+    spheres = ((0.0, 0.0, 2.6, 0.8), (0.9, -0.4, 2.2, 0.35))
+    planes = ((0.0, 0.0, 1.0, 4.5), (0.0, -1.0, 0.0, -1.4))
+
+    def pose(angle, tx):
+        E = np.eye(4, dtype=np.float32)
+        E[:3, :3] = [[np.cos(angle), 0, np.sin(angle)], [0, 1, 0], [-np.sin(angle), 0, np.cos(angle)]]
+        E[:3, 3] = [tx, 0.0, 0.0]
+        return E
+    poses = [pose(a, tx) for a, tx in ((0.0, 0.0), (0.05, -0.1), (-0.05, 0.1), (0.1, -0.2))]
+    depths = [torch.from_numpy(scenes.render_depth(K, E, 640, 480, spheres, planes)).cuda() for E in poses]
+    vol = tsdf.TSDFVolume(g2w, N, N, N, truncation=0.04)
+    out = torch.empty((480, 640), device="cuda")
+    stream = torch.cuda.current_stream()
+
+    def timed(fn, reps):
+        fn()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(reps):
+            fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / reps
+    clear_ms = timed(lambda: vol.clear(), args.steps)
+    vol.clear()
+    add_ms = timed(lambda: [vol.addDepthMap(K, E, d, 1.0) for E, d in zip(poses, depths)], args.steps) / 4
+    ray_ms = timed(lambda: vol.rayCastDepthMap(K, poses[0], 640, 480, -1.0, out=out), args.steps)
+    v = vol.volume()
+    band = int((v[..., 1] > 0).sum())
+    hit = float((out > 0).float().mean())
+    err = float(((out - depths[0]).abs()[(out > 0) & (depths[0] > 0)]).median())
+    peak, src = peaks()
+    nvox = N ** 3
+    clear_gbs = 8.0 * nvox / (clear_ms * 1e-3) / 1e9
+    print(json.dumps({"workload": "tsdf", "metric": "TSDF integration Gvoxel/s (512^3, 640x480 depth maps)",
+                      "value": nvox / (add_ms * 1e-3) / 1e9, "unit": "Gvoxel/s", "steps": args.steps,
+                      "add_ms": add_ms, "raycast_ms": ray_ms, "clear_ms": clear_ms,
+                      "raycast_mpix_per_s": 640 * 480 / 1e6 / (ray_ms * 1e-3),
+                      "voxels_with_weight": band, "raycast_hit_fraction": hit,
+                      "raycast_median_abs_error_m": err,
+                      "config": {"workload": "512^3 volume of 1 cm voxels, truncation 4 cm, 4 depth maps 640x480 "
+                                             "(2 spheres, 2 planes, 4 poses) per step, ray cast from the first pose"},
+                      "roofline_clear": {"kernel": "k_tsdf_clear", "bound": "hbm", "achieved": clear_gbs, "peak": peak,
+                                         "unit": "GB/s", "frac": clear_gbs / peak, "peak_source": src},
+                      "add_bytes_per_launch_algorithmic": 16 * band / 4.0}), flush=True)
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -526,7 +641,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--profile", action="store_true", help="short run for ncu captures")
     ap.add_argument("--profile-iters", type=int, default=1)
-    ap.add_argument("--workload", choices=["pair", "batch", "adjoint", "combined"], default="pair",
+    ap.add_argument("--workload", choices=["pair", "batch", "adjoint", "combined", "rectify", "tsdf"], default="pair",
                     help="pair: the 1242x375 headline; batch: uneven pairs, plain loop vs batched graph; "
                          "adjoint: forward + adjoint, 8 x 640x480; combined: 16 pairs batched + plane polishing")
     ap.add_argument("--pairs", type=int, default=64)
@@ -538,6 +653,10 @@ def main():
         return run_batch(args)
     if args.workload == "adjoint":
         return run_adjoint(args)
+    if args.workload == "rectify":
+        return run_rectify(args)
+    if args.workload == "tsdf":
+        return run_tsdf(args)
     if args.workload == "combined":
         if args.pairs == 64:
             args.pairs = 16

@@ -270,10 +270,12 @@ __global__ void __launch_bounds__(256) k_propagate(PmPassArgs a) {
  * shared-memory ring exposed the latency of the record loads.)  The minimum
  * of 2 blocks per SM makes the allocator use up to 128 registers: without
  * it, it chose 97 and the kernel ran 8 % slower. */
-__global__ void __launch_bounds__(256, 2) k_nbcost(PmPassArgs a) {
+#define NB_COLS 30   /* planes per warp; lanes 30 and 31 feed the shuffles of the row pipeline */
+#define NB_PIPE 1    /* interior warps share weights along the row through shuffles */
+
+/* Plane (mx, my) with every weight formed by its own lane. */
+__device__ __forceinline__ void nbcost_lane(const PmPassArgs& a, int mx, int my) {
     const int W = a.k.W, H = a.k.H, P = a.k.P;
-    const int mx = blockIdx.x * 32 + threadIdx.x, my = blockIdx.y * 8 + threadIdx.y;
-    if (mx >= W || my >= H) return;
     const size_t n = (size_t)W * H, m = (size_t)my * W + mx;
     const float4 s = a.old[m];
     long long S0, S1, XA;
@@ -349,6 +351,114 @@ __global__ void __launch_bounds__(256, 2) k_nbcost(PmPassArgs a) {
         const float v = fmaf(a.k.alpha, r1[k], a.k.oma * r2[k]) / ws[k];
         a.nbcost[(size_t)k * n + m - (size_t)(oy * W + ox)] = (!fin || ws[k] <= 1.1f) ? 1e5f : v;
     }
+}
+
+/* Plane (mx, my) of a warp whose 32 columns and windows lie inside the image
+ * (mx0 - P - 1 >= 0, mx0 + 31 + P + 1 < W): all lanes walk the same tap
+ * offsets in lockstep.  The weight of user u = m - (ox, oy) at tap q is
+ * tap_weight(colour(u), colour(q), profile(q - u)); lane L forms, per user row
+ * oy, the one for ox = +1 (u one column left of its plane).  Lane L - 1 needs
+ * that value one offset later as its ox = 0 weight (same u, same q), lane
+ * L - 2 two offsets later as its ox = -1 weight: two shuffles per row and
+ * offset replace five weight evaluations.  Lanes 30 and 31 own no plane and
+ * only supply those values.  Each user still receives its taps in raster
+ * order through the operations of eval_costs. */
+__device__ __forceinline__ void nbcost_pipe(const PmPassArgs& a, int mx, int my, bool own) {
+    const int W = a.k.W, H = a.k.H, P = a.k.P;
+    const size_t n = (size_t)W * H, m = (size_t)my * W + mx;
+    const float4 s = a.old[m];
+    long long S0, S1, XA;
+    const bool fin = finite3(s);
+    pm_fix_plane(fin, s.x, s.y, s.z, W / 2, H / 2, &S0, &S1, &XA);
+    unsigned uok = 0;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+        const int oy = (k < 4 ? k : k + 1) / 3 - 1;
+        if (my - oy >= 0 && my - oy < H) uok |= 1u << k;   /* columns are inside */
+    }
+    float4 uc[3];                                  /* colours of the ox = +1 users, rows oy = -1, 0, 1 */
+#pragma unroll
+    for (int r = 0; r < 3; ++r) uc[r] = __ldg(&a.v1.col[(size_t)min(max(my - (r - 1), 0), H - 1) * W + mx - 1]);
+    float r1[8], r2[8], ws[8];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) { r1[k] = 0.0f; r2[k] = 0.0f; ws[k] = 0.0f; }
+    const int qy0 = max(my - P - 1, 0), qy1 = min(my + P + 1, H - 1);
+    for (int qy = qy0; qy <= qy1; ++qy) {
+        const int ry = qy - my;
+        unsigned rmask = 0;
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+            const int oy = (k < 4 ? k : k + 1) / 3 - 1;
+            if (abs(ry + oy) <= P) rmask |= 1u << k;
+        }
+        rmask &= uok;                              /* the same in every lane: my is */
+        if (!rmask) continue;
+        const float4* c1row = a.v1.col + (size_t)qy * W;
+        const float4* g1row = a.v1.grad + (size_t)qy * W;
+        const size_t jrow = (size_t)qy * a.k.rp;
+        long long X = XA + (long long)(qy - H / 2) * S1 + (long long)(mx - P - 1 - W / 2) * S0;
+        float p1[3] = {0.0f, 0.0f, 0.0f}, q1[3] = {0.0f, 0.0f, 0.0f};   /* own ox=+1 and received ox=0 of the last offset */
+        for (int rx = -P - 1; rx <= P + 1; ++rx) {
+            const int qx = mx + rx;
+            const float4 a1 = __ldg(&c1row[qx]);
+            const float4 g1 = __ldg(&g1row[qx]);
+            float wn[3], w0[3], wm[3];
+#pragma unroll
+            for (int r = 0; r < 3; ++r) {
+                const int dy = ry + (r - 1);
+                wn[r] = (abs(dy) <= P && abs(rx + 1) <= P)
+                            ? tap_weight(uc[r], a1, c_prof[(dy + PM_PMAX) * PM_PROF_N + PM_PMAX + rx + 1]) : 0.0f;
+                wm[r] = __shfl_down_sync(0xffffffffu, q1[r], 1);   /* lane L+2's ox=+1 of two offsets ago */
+                w0[r] = __shfl_down_sync(0xffffffffu, p1[r], 1);   /* lane L+1's ox=+1 of the last offset */
+                p1[r] = wn[r];
+                q1[r] = w0[r];
+            }
+            const long long Xt = X;
+            X += S0;
+            const int xi = (int)(Xt >> 32);
+            if (!own || (unsigned)xi >= (unsigned)W) continue;
+            unsigned mask = rmask;
+            if (rx <= -P || rx >= P) {
+#pragma unroll
+                for (int k = 0; k < 8; ++k) {
+                    const int ox = (k < 4 ? k : k + 1) % 3 - 1;
+                    if (abs(rx + ox) > P) mask &= ~(1u << k);
+                }
+            }
+            float cc, gc;
+            fast_tap_terms(a.k, a.v2, jrow + xi, pm_fix_frac(Xt), a1, g1, cc, gc);
+#pragma unroll
+            for (int k = 0; k < 8; ++k) {
+                if (!((mask >> k) & 1u)) continue;
+                const int nn = k < 4 ? k : k + 1, ox = nn % 3 - 1, r = nn / 3;
+                const float w = ox > 0 ? wn[r] : (ox == 0 ? w0[r] : wm[r]);
+                r1[k] = fmaf(w, cc, r1[k]);
+                r2[k] = fmaf(w, gc, r2[k]);
+                ws[k] = ws[k] + w;
+            }
+        }
+    }
+    if (!own) return;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+        if (!((uok >> k) & 1u)) continue;
+        const int nn = k < 4 ? k : k + 1, ox = nn % 3 - 1, oy = nn / 3 - 1;
+        const float v = fmaf(a.k.alpha, r1[k], a.k.oma * r2[k]) / ws[k];
+        a.nbcost[(size_t)k * n + m - (size_t)(oy * W + ox)] = (!fin || ws[k] <= 1.1f) ? 1e5f : v;
+    }
+}
+
+__global__ void __launch_bounds__(256, 2) k_nbcost(PmPassArgs a) {
+    const int W = a.k.W, H = a.k.H, P = a.k.P;
+    const int mx0 = blockIdx.x * NB_COLS, lane = threadIdx.x;
+    const int mx = mx0 + lane, my = blockIdx.y * 8 + threadIdx.y;
+    if (my >= H) return;                                   /* the whole warp */
+    if (NB_PIPE && mx0 - P - 1 >= 0 && mx0 + 31 + P + 1 <= W - 1) {
+        nbcost_pipe(a, mx, my, lane < NB_COLS);
+        return;
+    }
+    if (lane >= NB_COLS || mx >= W) return;
+    nbcost_lane(a, mx, my);
 }
 
 /* -------------------------------------------------------- view lists -- */
@@ -770,7 +880,7 @@ cudaError_t pm_launch_propagate(const PmPassArgs& a, bool exact, cudaStream_t st
         PmPassArgs b = a;
         if (b.color >= 0) b.nbcost = nullptr;   /* red/black: neighbours per pixel */
         if (b.nbcost) {
-            k_nbcost<<<pix_grid(a.k.W, a.k.H), dim3(32, 8), 0, st>>>(b);
+            k_nbcost<<<dim3((a.k.W + NB_COLS - 1) / NB_COLS, (a.k.H + 7) / 8), dim3(32, 8), 0, st>>>(b);
             PM_LAUNCH_CHECK();
         }
         k_propagate<false><<<grid, dim3(32, 8), 0, st>>>(b);

@@ -227,14 +227,10 @@ __device__ __forceinline__ uint32_t mix4u8(uint32_t s1, uint32_t s2, uint32_t a)
     return t + t2;
 }
 
+/* One output pixel of IWarp::apply: source coordinates c, output row `out`. */
 template <int KIND>
-__global__ void __launch_bounds__(256) k_warp_apply(const unsigned char* __restrict__ src, size_t sstride, int sw, int sh,
-                                                    const float2* __restrict__ map, size_t mpitch2, int W, int H,
-                                                    unsigned char* __restrict__ dst, size_t dstride) {
-    const int x = blockIdx.x * 32 + threadIdx.x, y = blockIdx.y * 8 + threadIdx.y;
-    if (x >= W || y >= H) return;
-    const float2 c = map[(size_t)y * mpitch2 + x];
-    unsigned char* out = dst + (size_t)y * dstride;
+__device__ __forceinline__ void warp_px(const unsigned char* __restrict__ src, size_t sstride, int sw, int sh,
+                                        float2 c, unsigned char* __restrict__ out, int x) {
     if (KIND == WARP_F1 || KIND == WARP_F4) {
         constexpr int C = KIND == WARP_F1 ? 1 : 4;
         const float fill[4] = {0.0f, 0.0f, 0.0f, C == 1 ? 0.0f : 1.0f};
@@ -309,6 +305,27 @@ __global__ void __launch_bounds__(256) k_warp_apply(const unsigned char* __restr
             *o = fill;
         }
     }
+}
+
+/* WARP_PX output pixels per thread, 32 apart (a warp covers WARP_PX runs of 32
+ * consecutive pixels): the map loads of all of them are in flight before the
+ * dependent texel reads.  3840x2160 RGBA8 pair: 1 px 0.095 ms, 2 px 0.075 ms,
+ * 4 px 0.071 ms per step (GB300). */
+#define WARP_PX 4
+template <int KIND>
+__global__ void __launch_bounds__(256) k_warp_apply(const unsigned char* __restrict__ src, size_t sstride, int sw, int sh,
+                                                    const float2* __restrict__ map, size_t mpitch2, int W, int H,
+                                                    unsigned char* __restrict__ dst, size_t dstride) {
+    const int y = blockIdx.y * 8 + threadIdx.y;
+    if (y >= H) return;
+    const int x0 = blockIdx.x * (32 * WARP_PX) + threadIdx.x;
+    float2 c[WARP_PX];
+#pragma unroll
+    for (int k = 0; k < WARP_PX; ++k)   /* the map loads first, then the dependent texel reads */
+        if (x0 + 32 * k < W) c[k] = map[(size_t)y * mpitch2 + x0 + 32 * k];
+#pragma unroll
+    for (int k = 0; k < WARP_PX; ++k)
+        if (x0 + 32 * k < W) warp_px<KIND>(src, sstride, sw, sh, c[k], dst + (size_t)y * dstride, x0 + 32 * k);
 }
 
 cvtpm_status fail(cvtpm_status s, const std::string& m) {
@@ -403,7 +420,7 @@ cvtpm_status cvtpm_warp_apply(const cvtpm_image* dst, const cvtpm_image* src, co
         return fail(CVTPM_ERR_INVALID_ARGUMENT, "warp: bad stride or alignment");
     if (warp_pitch % 8 || warp_pitch < (size_t)dst->width * 8 || (uintptr_t)warp % 8)
         return fail(CVTPM_ERR_INVALID_ARGUMENT, "warp: bad warp pitch or alignment");
-    const dim3 grid((dst->width + 31) / 32, (dst->height + 7) / 8);
+    const dim3 grid((dst->width + 32 * WARP_PX - 1) / (32 * WARP_PX), (dst->height + 7) / 8);
     cudaStream_t st = (cudaStream_t)stream;
     const unsigned char* s = (const unsigned char*)src->data;
     unsigned char* d = (unsigned char*)dst->data;

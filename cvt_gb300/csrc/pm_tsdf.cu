@@ -21,8 +21,9 @@
  * matrix with |det| < FLT_EPSILON is returned unchanged, as inverseSelf
  * leaves it).  Device arithmetic is the kernels' own, compiled without
  * contraction; OpenCL's normalize is v * (1 / sqrt(dot(v, v))) and dot is
- * summed left to right.  Clear and add are HBM-bound streams (8 B read and
- * written per voxel); the ray cast is a latency-bound gather.
+ * summed left to right.  Clear is an HBM write stream (8 B per voxel); add
+ * projects every voxel (two divisions: issue-bound) and reads and writes 16 B
+ * only inside the truncation band; the ray cast is a latency-bound gather.
  *
  * The ray loop of the reference (`for (lambda = start + step; lambda <= end;
  * lambda += step)`) never ends where lambda + step rounds to lambda (a camera
@@ -116,17 +117,29 @@ __device__ __forceinline__ float4 xform(const DMat4& m, float4 v) {   /* mat4f_t
 }
 __device__ __forceinline__ float mixf(float a, float b, float t) { return a + (b - a) * t; }
 
+/* clear: two voxels per 16-byte store over the linear volume (512^3: 0.141 ms
+ * = 7.6 TB/s, against 0.267 ms with one 8-byte store per voxel).  add:
+ * TSDF_ZPT z-planes per thread (512^3, 640x480 map: 1 plane 0.310 ms, 2 0.306,
+ * 4 0.249, 8 0.220). */
+#define TSDF_CLEAR_VEC 1
+#define TSDF_ZPT 8
 __global__ void __launch_bounds__(256) k_tsdf_clear(float2* __restrict__ cv, int W, int H, int D, float init) {
     const int x = blockIdx.x * 32 + threadIdx.x, y = blockIdx.y * 8 + threadIdx.y, z = blockIdx.z;
     if (x >= W || y >= H || z >= D) return;
     cv[((size_t)z * H + y) * W + x] = make_float2(1.0f, init);
 }
 
-__global__ void __launch_bounds__(256) k_tsdf_add(float2* __restrict__ cv, int W, int H, int D,
-                                                  const float* __restrict__ dmap, size_t dpitch4, int iw, int ih,
-                                                  float dscale, DMat4 tg2cam, float trunc) {
-    const int x = blockIdx.x * 32 + threadIdx.x, y = blockIdx.y * 8 + threadIdx.y, z = blockIdx.z;
-    if (x >= W || y >= H || z >= D) return;
+/* The same over the volume as n voxels: thread i writes voxels 2i and 2i+1
+ * with one 16-byte store (the allocation is 256-byte aligned). */
+__global__ void __launch_bounds__(256) k_tsdf_clear_vec(float4* __restrict__ cv4, size_t n, float init) {
+    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (2 * i + 1 < n) cv4[i] = make_float4(1.0f, init, 1.0f, init);
+    else if (2 * i < n) ((float2*)cv4)[2 * i] = make_float2(1.0f, init);
+}
+
+__device__ __forceinline__ void tsdf_add_voxel(float2* __restrict__ cv, int W, int H, int x, int y, int z,
+                                               const float* __restrict__ dmap, size_t dpitch4, int iw, int ih,
+                                               float dscale, const DMat4& tg2cam, float trunc) {
     const float4 g = xform(tg2cam, make_float4((float)x, (float)y, (float)z, 1.0f));
     const float ix = g.x / g.z, iy = g.y / g.z;
     if (ix < (float)iw && iy < (float)ih && ix >= 0.0f && iy >= 0.0f) {
@@ -141,6 +154,16 @@ __global__ void __launch_bounds__(256) k_tsdf_add(float2* __restrict__ cv, int W
             }
         }
     }
+}
+
+__global__ void __launch_bounds__(256) k_tsdf_add(float2* __restrict__ cv, int W, int H, int D,
+                                                  const float* __restrict__ dmap, size_t dpitch4, int iw, int ih,
+                                                  float dscale, DMat4 tg2cam, float trunc) {
+    const int x = blockIdx.x * 32 + threadIdx.x, y = blockIdx.y * 8 + threadIdx.y;
+    if (x >= W || y >= H) return;
+#pragma unroll 1
+    for (int z = blockIdx.z * TSDF_ZPT; z < min(D, (int)(blockIdx.z + 1) * TSDF_ZPT); ++z)
+        tsdf_add_voxel(cv, W, H, x, y, z, dmap, dpitch4, iw, ih, dscale, tg2cam, trunc);
 }
 
 /* TSDFVolume_trilinearValue: 1e10 if a corner has weight < 1 */
@@ -290,8 +313,13 @@ cvtpm_status cvtpm_tsdf_info(const cvtpm_tsdf* v, int* width, int* height, int* 
 cvtpm_status cvtpm_tsdf_clear(cvtpm_tsdf* v, float weight, void* stream) {
     if (!v) return fail(CVTPM_ERR_INVALID_ARGUMENT, "tsdf clear: NULL volume");
     cudaSetDevice(v->device);
-    k_tsdf_clear<<<dim3((v->W + 31) / 32, (v->H + 7) / 8, v->D), dim3(32, 8), 0, (cudaStream_t)stream>>>(
-        v->vol, v->W, v->H, v->D, weight);
+    if (TSDF_CLEAR_VEC) {
+        const size_t n = (size_t)v->W * v->H * v->D, th = (n + 1) / 2;
+        k_tsdf_clear_vec<<<(unsigned)((th + 255) / 256), 256, 0, (cudaStream_t)stream>>>((float4*)v->vol, n, weight);
+    } else {
+        k_tsdf_clear<<<dim3((v->W + 31) / 32, (v->H + 7) / 8, v->D), dim3(32, 8), 0, (cudaStream_t)stream>>>(
+            v->vol, v->W, v->H, v->D, weight);
+    }
     const cudaError_t e = cudaGetLastError();
     return e == cudaSuccess ? CVTPM_OK : fail(CVTPM_ERR_CUDA, std::string("tsdf clear: ") + cudaGetErrorString(e));
 }
@@ -306,7 +334,8 @@ cvtpm_status cvtpm_tsdf_add_depthmap(cvtpm_tsdf* v, const float* proj, const flo
     memcpy(P.m, proj, sizeof P.m);
     const DMat4 T = to_dev(mat4_mul(P, v->g2w));   /* projall = proj * g2w (TSDFVolume.cpp:64) */
     cudaSetDevice(v->device);
-    k_tsdf_add<<<dim3((v->W + 31) / 32, (v->H + 7) / 8, v->D), dim3(32, 8), 0, (cudaStream_t)stream>>>(
+    k_tsdf_add<<<dim3((v->W + 31) / 32, (v->H + 7) / 8, (v->D + TSDF_ZPT - 1) / TSDF_ZPT), dim3(32, 8), 0,
+                 (cudaStream_t)stream>>>(
         v->vol, v->W, v->H, v->D, depthmap, dpitch / 4, dwidth, dheight, scale, T, v->trunc);
     const cudaError_t e = cudaGetLastError();
     return e == cudaSuccess ? CVTPM_OK : fail(CVTPM_ERR_CUDA, std::string("tsdf add: ") + cudaGetErrorString(e));

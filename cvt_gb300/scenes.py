@@ -217,3 +217,31 @@ def end_point_error(dmap_px: np.ndarray, scene: StereoScene, nonocc: bool = True
     e = err[m]
     e = e[np.isfinite(e)]
     return float(e.mean()) if e.size else float("nan")
+
+
+def render_depth(K, E, width: int, height: int, spheres=((0.0, 0.0, 2.0, 0.5),),
+                 planes=((0.0, 0.0, 1.0, 3.0),)) -> np.ndarray:
+    """Camera-space depth (z) of the first surface along each pixel's ray, 0
+    where none: spheres (cx, cy, cz, r) and planes n . X = d (nx, ny, nz, d)
+    in world coordinates; K 3x3 intrinsics, E 4x4 world-to-camera.  Inputs for
+    the TSDF fusion workloads."""
+    Ki = np.linalg.inv(np.asarray(K, np.float64))
+    Ei = np.linalg.inv(np.asarray(E, np.float64))
+    v, u = np.mgrid[0:height, 0:width].astype(np.float64)
+    dirs = (np.stack([u, v, np.ones_like(u)], -1) @ Ki.T) @ Ei[:3, :3].T   # camera z = 1 per unit of t
+    o = Ei[:3, 3]
+    best = np.full((height, width), np.inf)
+    a = (dirs * dirs).sum(-1)
+    for cx, cy, cz, r in spheres:
+        oc = o - np.array([cx, cy, cz])
+        b = dirs @ oc
+        disc = b * b - a * ((oc * oc).sum() - r * r)
+        t = (-b - np.sqrt(np.maximum(disc, 0.0))) / a
+        best = np.where((disc > 0) & (t > 0) & (t < best), t, best)
+    for nx, ny, nz, d in planes:
+        n = np.array([nx, ny, nz])
+        den = dirs @ n
+        with np.errstate(divide="ignore", invalid="ignore"):
+            t = (d - o @ n) / den
+        best = np.where((t > 0) & (t < best), t, best)
+    return np.where(np.isfinite(best), best, 0.0).astype(np.float32)
