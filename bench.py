@@ -630,6 +630,40 @@ def run_tsdf(args):
     return 0
 
 
+def run_gcv(args):
+    """The comparison baseline (cvt::StereoGCVFilter) on the headline pair:
+    1242x375, disparities 0..127 in steps of 1, both views and the fused
+    check (apply), against PatchMatch's bad-1px on the same pair."""
+    import torch
+    from cvt_gb300 import gcv, scenes
+    sc = scene_for(0)
+    H, W = sc.left.shape[:2]
+    left, right = torch.from_numpy(sc.left).cuda(), torch.from_numpy(sc.right).cuda()
+    f = gcv.StereoGCVFilter()
+    stream = torch.cuda.current_stream()
+    for _ in range(max(1, args.warmup)):
+        f.apply(right, left, 0.0, DMAX, 1.0)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        out, d0, d1 = f.apply(right, left, 0.0, DMAX, 1.0)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / args.steps
+    disp = d0.cpu().numpy() * DMAX
+    bad = scenes.bad_pixel_rate(disp, sc)
+    nd = int(DMAX)
+    print(json.dumps({"workload": "gcv", "metric": "StereoGCVFilter::apply ms (1242x375, 128 disparities, both views)",
+                      "value": ms, "unit": "ms", "steps": args.steps,
+                      "mpix_disp_per_s": 2 * W * H * nd / 1e6 / (ms * 1e-3),
+                      "launches_per_apply": 2 * (17 + 24 * nd + 1) + 1,
+                      "bad1_nonocc_pct_left_view": bad,
+                      "config": {"workload": "pair 0 of the headline scene family (1242x375, dmax 128), point cost, "
+                                             "guided filter r 9, eps 1e-3; right image as cam0, left as cam1"}}), flush=True)
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -641,7 +675,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--profile", action="store_true", help="short run for ncu captures")
     ap.add_argument("--profile-iters", type=int, default=1)
-    ap.add_argument("--workload", choices=["pair", "batch", "adjoint", "combined", "rectify", "tsdf"], default="pair",
+    ap.add_argument("--workload", choices=["pair", "batch", "adjoint", "combined", "rectify", "tsdf", "gcv"],
+                    default="pair",
                     help="pair: the 1242x375 headline; batch: uneven pairs, plain loop vs batched graph; "
                          "adjoint: forward + adjoint, 8 x 640x480; combined: 16 pairs batched + plane polishing")
     ap.add_argument("--pairs", type=int, default=64)
@@ -653,6 +688,8 @@ def main():
         return run_batch(args)
     if args.workload == "adjoint":
         return run_adjoint(args)
+    if args.workload == "gcv":
+        return run_gcv(args)
     if args.workload == "rectify":
         return run_rectify(args)
     if args.workload == "tsdf":

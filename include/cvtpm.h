@@ -468,6 +468,33 @@ cvtpm_status cvtpm_tsdf_slice(cvtpm_tsdf* vol, int axis, int index, float* rgba,
  * values alone; synchronizes the device. */
 cvtpm_status cvtpm_tsdf_save_raw(cvtpm_tsdf* vol, const char* path, int weighted);
 
+/* ------------------------------------------------------------------
+ * The comparison baseline: cvt::StereoGCVFilter
+ * (cvt/gfx/ifilter/StereoGCVFilter.cpp), cost-volume stereo with a
+ * colour-guided filter over integral images.  Images are tight RGBA float
+ * rows on the device (pitch = width * 16).  The depth is normalised:
+ * |d - dmin| / |dmax - dmin| for the best d of dmin, dmin + dt, ... (0 where
+ * no cost fell below its start).  As in the reference, the map belongs to
+ * cam1 and its match in cam0 lies at x - d: with a left/right pair, pass the
+ * right image as cam0 and the left as cam1 for the left view's disparity.
+ * Scratch (47 floats per pixel, 49 for apply) belongs to the calling host
+ * thread and is kept between calls.  Calls are stream-ordered.
+ * ------------------------------------------------------------------ */
+
+/* StereoGCVFilter::depthmap(dst, cam0, cam1, dmin, dmax, dt) (:97-242). */
+cvtpm_status cvtpm_gcv_depthmap(float* dst, size_t dst_pitch, const float* cam0, const float* cam1,
+                                int width, int height, size_t pitch, float dmin, float dmax, float dt,
+                                void* stream);
+
+/* StereoGCVFilter::apply(dst, cam0, cam1, dmin, dmax, dt) (:75-95): both
+ * views' depth maps (d0, d1 tight float rows, or NULL) and their
+ * consistency check into a GRAY_UINT8 image (CL_UNORM_INT8 write:
+ * convert_uchar_sat_rte(v * 255)).  The reference also saves d0 and d1 as
+ * PNG files; that is not done. */
+cvtpm_status cvtpm_gcv_apply(uint8_t* dst, size_t dst_pitch, float* d0, float* d1, size_t dpitch,
+                             const float* cam0, const float* cam1, int width, int height, size_t pitch,
+                             float dmin, float dmax, float dt, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -4,7 +4,9 @@ they lie, under /root/reference, and copies none into the repository), so it
 runs only where they are present.
 
   1. translate.py rewrites cvt/cl/kernel/{pmhstereo,RNG,PDHuberWeighted,
-     PDHuberWeightedInpaint,fill,Matrix4,TSDFVolume/TSDFVolume}.cl
+     PDHuberWeightedInpaint,fill,Matrix4,TSDFVolume/TSDFVolume}.cl and the
+     kernels of cvt::StereoGCVFilter (gradx, prefixsum/*, boxfilter/*,
+     guidedfilter/*, stereogcv/*)
      into _build/ref_gen/*.inc (generated, never committed);
   2. one C++ unit per kernel file wraps its .inc in a namespace and registers
      the kernels with clemu;
@@ -27,7 +29,12 @@ GEN = os.path.join(ROOT, "_build", "ref_gen")
 OUT = os.path.join(ORACLE, "_ref")
 LIB = os.path.join(OUT, "libpmref.so")
 KERNEL_FILES = ["RNG", "Matrix4", "pmhstereo", "PDHuberWeighted", "PDHuberWeightedInpaint", "fill",
-                "TSDFVolume/TSDFVolume"]
+                "TSDFVolume/TSDFVolume", "gradx", "prefixsum/prefixsum_pblock", "prefixsum/prefixsum_pblock_mul2",
+                "prefixsum/prefixsum_pblock_outerrgb", "prefixsum/prefixsum_horiz", "prefixsum/prefixsum_vert",
+                "prefixsum/prefixsum_block2", "boxfilter/boxfilter_prefixsum",
+                "guidedfilter/guidedfilter_calcab_outerrgb", "guidedfilter/guidedfilter_applyab_gc_outer",
+                "stereogcv/costdepthgrad", "stereogcv/costmin", "stereogcv/costdepthconv",
+                "stereogcv/occlusioncheck"]
 INCLUDE_ONLY = ("RNG", "Matrix4")     # #import-ed by other kernel files, no kernels of their own
 
 sys.path.insert(0, HERE)

@@ -115,6 +115,8 @@ struct Swz2 {
     operator float2() const { return float2(*p[0], *p[1]); }
     Swz2& operator=(const float2& v) { *p[0] = v.x; *p[1] = v.y; return *this; }
     Swz2& operator=(float s) { *p[0] = s; *p[1] = s; return *this; }
+    Swz2& operator-=(const float2& v) { *p[0] = *p[0] - v.x; *p[1] = *p[1] - v.y; return *this; }
+    Swz2& operator+=(const float2& v) { *p[0] = *p[0] + v.x; *p[1] = *p[1] + v.y; return *this; }
 };
 struct Swz3 {
     float* p[3];
@@ -122,6 +124,8 @@ struct Swz3 {
     Swz3& operator=(const float3& v) { *p[0] = v.x; *p[1] = v.y; *p[2] = v.z; return *this; }
     Swz3& operator=(float s) { *p[0] = s; *p[1] = s; *p[2] = s; return *this; }
     Swz3& operator*=(float s) { *p[0] = *p[0] * s; *p[1] = *p[1] * s; *p[2] = *p[2] * s; return *this; }
+    Swz3& operator-=(const float3& v) { *p[0] = *p[0] - v.x; *p[1] = *p[1] - v.y; *p[2] = *p[2] - v.z; return *this; }
+    Swz3& operator+=(const float3& v) { *p[0] = *p[0] + v.x; *p[1] = *p[1] + v.y; *p[2] = *p[2] + v.z; return *this; }
 };
 
 struct alignas(16) float4 {
@@ -131,11 +135,17 @@ struct alignas(16) float4 {
     template <class A, class B, class C, class D>
     float4(A a, B b, C c, D d) : x(to_float(a)), y(to_float(b)), z(to_float(c)), w(to_float(d)) {}
     float4(const float3& v, float w);   /* (float4)(v, w) */
+    float4(float a, const float2& v, float d) : x(a), y(v.x), z(v.y), w(d) {}   /* (float4)(a, v, d) */
     Swz2 xy() const { float* q = const_cast<float*>(&x); return Swz2{{q, q + 1}}; }
     Swz3 xyz() const { float* q = const_cast<float*>(&x); return Swz3{{q, q + 1, q + 2}}; }
     float2 s01() const { return float2(x, y); }
     float2 s23() const { return float2(z, w); }
+    Swz2 yz() const { float* q = const_cast<float*>(&x); return Swz2{{q + 1, q + 2}}; }
+    Swz2 zw() const { float* q = const_cast<float*>(&x); return Swz2{{q + 2, q + 3}}; }
     float4& operator+=(const float4& o);
+    float4& operator-=(const float4& o) { x = x - o.x; y = y - o.y; z = z - o.z; w = w - o.w; return *this; }
+    float4& operator*=(const float4& o) { x = x * o.x; y = y * o.y; z = z * o.z; w = w * o.w; return *this; }
+    float4& operator/=(const float4& o) { x = x / o.x; y = y / o.y; z = z / o.z; w = w / o.w; return *this; }
 };
 inline float4::float4(const float3& v, float w_) : x(v.x), y(v.y), z(v.z), w(w_) {}
 struct alignas(32) float8 {
@@ -143,6 +153,9 @@ struct alignas(32) float8 {
     float8() {}
     float8(float s) : l(s), h(s) {}
     float8(const float4& a, const float4& b) : l(a), h(b) {}
+    /* (float8)(float3, float, float2, float, float) */
+    float8(const float3& a, float b, const float2& c, float d, float e) : l(a, b), h(c.x, c.y, d, e) {}
+    float8& operator+=(const float8& o) { l += o.l; h += o.h; return *this; }
     float& s0() { return l.x; }
     float& s1() { return l.y; }
     float& s2() { return l.z; }
@@ -179,6 +192,12 @@ inline float3 operator-(const Swz3& a, const Swz3& b) { return float3(a) - float
 inline float2 operator/(const Swz2& a, float s) { return float2(a) / s; }
 inline float2 operator*(const Swz2& a, float s) { return float2(a) * s; }
 inline float3 operator*(const Swz3& a, float s) { return float3(a) * s; }
+inline float3 operator*(float s, const Swz3& a) { return s * float3(a); }
+inline float2 operator*(float s, const Swz2& a) { return s * float2(a); }
+inline int2 operator-(const int2& a, const int2& b) { return int2(a.x - b.x, a.y - b.y); }
+inline int2 min(const int2& a, const int2& b) { return int2(a.x < b.x ? a.x : b.x, a.y < b.y ? a.y : b.y); }
+inline int2 max(const int2& a, const int2& b) { return int2(a.x > b.x ? a.x : b.x, a.y > b.y ? a.y : b.y); }
+inline int mul24(int a, int b) { return a * b; }   /* exact for the 24-bit operands of these kernels */
 inline float4 operator-(const float4& a) { return float4(-a.x, -a.y, -a.z, -a.w); }
 inline float4& float4::operator+=(const float4& o) { x = x + o.x; y = y + o.y; z = z + o.z; w = w + o.w; return *this; }
 inline float8 operator/(const float8& a, const float8& b) { return float8(a.l / b.l, a.h / b.h); }
@@ -196,6 +215,12 @@ inline float4 fmin(const float4& a, float s) { return float4(std::fmin(a.x, s), 
 inline float4 fmax(const float4& a, const float4& b) { return float4(std::fmax(a.x, b.x), std::fmax(a.y, b.y), std::fmax(a.z, b.z), std::fmax(a.w, b.w)); }
 inline int min(int a, int b) { return a < b ? a : b; }
 inline int max(int a, int b) { return a > b ? a : b; }
+/* OpenCL min/max of floats: y < x ? y : x and x < y ? y : x (6.12.4) */
+inline float min(float a, float b) { return b < a ? b : a; }
+inline float max(float a, float b) { return a < b ? b : a; }
+inline float4 cross(const float4& a, const float4& b) {   /* OpenCL 6.12.5: w = 0 */
+    return float4(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x, 0.0f);
+}
 inline float clamp(float v, float lo, float hi) { return std::fmin(std::fmax(v, lo), hi); }
 inline float sqrt(float v) { return std::sqrt(v); }
 inline float4 sqrt(const float4& v) { return float4(std::sqrt(v.x), std::sqrt(v.y), std::sqrt(v.z), std::sqrt(v.w)); }
@@ -266,7 +291,11 @@ inline float4 texel(image2d_t img, int x, int y, int addr) {
     } else if (x < 0 || y < 0 || x >= img->w || y >= img->h) {
         return float4(0.0f);    /* CLK_ADDRESS_CLAMP border colour */
     }
-    if (img->channels == 1) return float4(img->data[(size_t)y * img->w + x]);
+    if (img->channels == 1) return float4(img->data[(size_t)y * img->w + x]);   /* CL_INTENSITY: (I, I, I, I) */
+    if (img->channels == 2) {                                                    /* CL_RG: (R, G, 0, 1) */
+        const float* q = img->data + ((size_t)y * img->w + x) * 2;
+        return float4(q[0], q[1], 0.0f, 1.0f);
+    }
     const float* p = img->data + ((size_t)y * img->w + x) * 4;
     return float4(p[0], p[1], p[2], p[3]);
 }
@@ -291,6 +320,7 @@ inline float4 read_imagef(image2d_t img, sampler_t s, float2 c) {
 inline void write_imagef(image2d_t img, int2 c, float4 v) {
     if (c.x < 0 || c.y < 0 || c.x >= img->w || c.y >= img->h) return;
     if (img->channels == 1) { img->data[(size_t)c.y * img->w + c.x] = v.x; return; }
+    if (img->channels == 2) { float* q = img->data + ((size_t)c.y * img->w + c.x) * 2; q[0] = v.x; q[1] = v.y; return; }
     float* p = img->data + ((size_t)c.y * img->w + c.x) * 4;
     p[0] = v.x; p[1] = v.y; p[2] = v.z; p[3] = v.w;
 }

@@ -16,7 +16,7 @@ namespace clemu {
 
 struct Img {
     int w, h;
-    int channels;     /* 4: CL_RGBA/CL_FLOAT, 1: CL_INTENSITY/CL_FLOAT */
+    int channels;     /* 4: CL_RGBA/CL_FLOAT, 2: CL_RG/CL_FLOAT, 1: CL_INTENSITY/CL_FLOAT */
     float* data;
 };
 

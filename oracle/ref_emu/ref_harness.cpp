@@ -7,6 +7,7 @@
  * cvt/cl/kernel/pmhstereo.cl.  It produces the golden fixtures under
  * tests/golden/ (tests/golden/make_golden.py) and never ships.
  */
+#include <cmath>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -258,6 +259,132 @@ int ref_tsdf_slice(float* rgba, int axis, int v, float* vol, int W, int H, int D
     clemu::launch(k, {img_arg(o), int_arg(v), buf_arg(vol), int_arg(W), int_arg(H), int_arg(D)}, pad16(ow), pad16(oh),
                   16, 16);
     memcpy(rgba, o.data(), sizeof(float) * 4 * (size_t)ow * oh);
+    return 0;
+}
+
+/* ---- cvt::StereoGCVFilter (cvt/gfx/ifilter/StereoGCVFilter.cpp:75-242) ----
+ * The kernels are the reference's; the launch sequence below repeats
+ * StereoGCVFilter::depthmap / apply, IntegralFilter::apply / applyOuterRGB
+ * (cvt/gfx/ifilter/IntegralFilter.cpp:68-170, block size 16) and
+ * BoxFilter::apply (cvt/gfx/ifilter/BoxFilter.cpp:48-62) with their NDRanges.
+ * The integral images of the box-SAD and NCC cost variants (imeanG1, G0, G12,
+ * G02), which the point-SAD cost the reference compiles does not read, are not
+ * formed.  The occlusion result is written to a GRAY_UINT8 image: the float
+ * kernel output is converted as write_imagef does for CL_UNORM_INT8
+ * (convert_uchar_sat_rte(v * 255)). */
+namespace gcv {
+struct Im {
+    clemu::Img img;
+    std::vector<float> d;
+    Im(int w, int h, int ch) : d((size_t)w * h * ch, 0.0f) { img.w = w; img.h = h; img.channels = ch; img.data = d.data(); }
+    void set(int ch) { d.assign((size_t)img.w * img.h * ch, 0.0f); img.channels = ch; img.data = d.data(); }
+};
+clemu::Arg I(Im& m) { clemu::Arg a; a.kind = clemu::Arg::IMAGE; a.img = &m.img; return a; }
+clemu::Arg L(size_t bytes) { clemu::Arg a; a.kind = clemu::Arg::LOCAL; a.local_size = bytes; return a; }
+clemu::Arg F4(const float* v) { clemu::Arg a; a.kind = clemu::Arg::FLOAT4; for (int k = 0; k < 4; ++k) a.f4[k] = v[k]; return a; }
+const int BS = 16;
+
+/* IntegralFilter::apply(dst, src, src2): dst takes src's channel count */
+void integral(Im& dst, Im& src, Im* src2) {
+    const int W = src.img.w, H = src.img.h;
+    dst.set(src.img.channels);
+    if (src2) {   /* (the squared variant, src2 == &src, serves only the unused NCC cost) */
+        clemu::launch("prefixsum_pblock_mul2", {I(dst), I(src), I(*src2), L(16 * BS * BS)}, pad16(W), pad16(H), BS, BS);
+    } else {
+        clemu::launch("prefixsum_pblock", {I(dst), I(src), L(16 * BS * BS)}, pad16(W), pad16(H), BS, BS);
+    }
+    clemu::launch("prefixsum_horiz", {I(dst), I(dst), int_arg(BS)}, pad16(H), 1, BS, 1);
+    clemu::launch("prefixsum_vert", {I(dst), I(dst), int_arg(BS)}, pad16(W), 1, BS, 1);
+    clemu::launch("prefixsum_block2", {I(dst), I(dst)}, pad16(W), pad16(H), BS, BS);
+}
+
+void integral_outer(Im& rr, Im& gg, Im& src) {
+    const int W = src.img.w, H = src.img.h;
+    rr.set(4);
+    gg.set(4);
+    clemu::launch("prefixsum_pblock_outerrgb", {I(rr), I(gg), I(src), L(32 * BS * BS)}, pad16(W), pad16(H), BS, BS);
+    for (Im* m : {&rr, &gg}) clemu::launch("prefixsum_horiz", {I(*m), I(*m), int_arg(BS)}, pad16(H), 1, BS, 1);
+    for (Im* m : {&rr, &gg}) clemu::launch("prefixsum_vert", {I(*m), I(*m), int_arg(BS)}, pad16(W), 1, BS, 1);
+    for (Im* m : {&rr, &gg}) clemu::launch("prefixsum_block2", {I(*m), I(*m)}, pad16(W), pad16(H), BS, BS);
+}
+
+void box(Im& dst, Im& src, int r) {   /* dst keeps its channel count */
+    clemu::launch("boxfilter_prefixsum", {I(dst), I(src), int_arg(r)}, pad16(src.img.w), pad16(src.img.h), 16, 16);
+}
+
+/* StereoGCVFilter::depthmap (:75-242) with the point-SAD cost */
+void depthmap(Im& dst, Im& cam0, Im& cam1, float dmin, float dmax, float dt) {
+    const int W = cam0.img.w, H = cam0.img.h;
+    const int RADIUS = 9;
+    const float EPSILON = 1e-3f;
+    Im cost(W, H, 1), costgf(W, H, 1), c0(W, H, 2), c1(W, H, 2), g0(W, H, 4), g1(W, H, 4);
+    Im ia(W, H, 4), ib(W, H, 4), iint(W, H, 4), iint2(W, H, 4), imeanG(W, H, 4), imeanS(W, H, 1), imeanGS(W, H, 4);
+    Im mRR(W, H, 4), mGG(W, H, 4);
+    Im* c[2] = {&c0, &c1};
+    int index = 0;
+    const float fill[4] = {1e9f, 0.0f, 0.0f, 0.0f};
+    clemu::launch("fill", {I(*c[!index]), F4(fill)}, pad16(W), pad16(H), 16, 16);
+    clemu::launch("gradx", {I(g0), I(cam0), L(16 * 18 * 16)}, pad16(W), pad16(H), 16, 16);
+    clemu::launch("gradx", {I(g1), I(cam1), L(16 * 18 * 16)}, pad16(W), pad16(H), 16, 16);
+    integral(iint, cam1, nullptr);
+    box(imeanG, iint, RADIUS);
+    integral_outer(iint, iint2, cam1);
+    box(mRR, iint, RADIUS);
+    box(mGG, iint2, RADIUS);
+    if (dmax < dmin && dt > 0) dt = -dt;
+    size_t n = (size_t)(std::fabs(dmax - dmin) / std::fabs(dt));
+    for (float d = dmin; n--; d += dt) {
+        clemu::launch("stereogcv_costdepthgrad", {I(cost), I(cam1), I(cam0), I(g1), I(g0), float_arg(d)},
+                      pad16(W), pad16(H), 16, 16);
+        integral(iint, cost, nullptr);
+        box(imeanS, iint, RADIUS);
+        integral(iint, cam1, &cost);
+        box(imeanGS, iint, RADIUS);
+        clemu::launch("guidedfilter_calcab_outerrgb", {I(ia), I(ib), I(imeanG), I(imeanS), I(imeanGS), I(mRR), I(mGG),
+                                                       float_arg(EPSILON)}, pad16(W), pad16(H), 16, 16);
+        integral(iint, ia, nullptr);
+        box(ia, iint, RADIUS);
+        integral(iint, ib, nullptr);
+        box(ib, iint, RADIUS);
+        clemu::launch("guidedfilter_applyab_gc_outer", {I(costgf), I(cam1), I(ia), I(ib)}, pad16(W), pad16(H), 16, 16);
+        clemu::launch("stereogcv_costmin", {I(*c[index]), I(costgf), I(*c[!index]),
+                                            float_arg(std::fabs(d - dmin) / (std::fabs(dmax - dmin)))},
+                      pad16(W), pad16(H), 16, 16);
+        index = 1 - index;
+    }
+    clemu::launch("stereogcv_costdepthconv", {I(dst), I(*c[!index]), float_arg(1.0f), float_arg(0.0f)},
+                  pad16(W), pad16(H), 16, 16);
+}
+}  // namespace gcv
+
+/* StereoGCVFilter::depthmap on RGBA float images: dst W*H normalized depth. */
+int ref_gcv_depthmap(float* out, const float* cam0, const float* cam1, int W, int H, float dmin, float dmax, float dt) {
+    gcv::Im a(W, H, 4), b(W, H, 4), d(W, H, 1);
+    memcpy(a.d.data(), cam0, sizeof(float) * 4 * (size_t)W * H);
+    memcpy(b.d.data(), cam1, sizeof(float) * 4 * (size_t)W * H);
+    gcv::depthmap(d, a, b, dmin, dmax, dt);
+    memcpy(out, d.d.data(), sizeof(float) * (size_t)W * H);
+    return 0;
+}
+
+/* StereoGCVFilter::apply (:75-95): both depth maps and the occlusion check
+ * into GRAY_UINT8 (d0, d1 returned too; the reference also saves them as PNG
+ * files, which is not done here). */
+int ref_gcv_apply(uint8_t* out, float* d0out, float* d1out, const float* cam0, const float* cam1, int W, int H,
+                  float dmin, float dmax, float dt) {
+    gcv::Im a(W, H, 4), b(W, H, 4), d0(W, H, 1), d1(W, H, 1), o(W, H, 1);
+    memcpy(a.d.data(), cam0, sizeof(float) * 4 * (size_t)W * H);
+    memcpy(b.d.data(), cam1, sizeof(float) * 4 * (size_t)W * H);
+    gcv::depthmap(d0, a, b, dmin, dmax, dt);
+    gcv::depthmap(d1, b, a, -dmin, -dmax, -dt);
+    clemu::launch("stereogcv_occlusioncheck", {gcv::I(o), gcv::I(d0), gcv::I(d1), float_arg(std::fabs(dmax))},
+                  pad16(W), pad16(H), 16, 16);
+    for (size_t i = 0; i < (size_t)W * H; ++i) {
+        const float v = std::nearbyint(o.d[i] * 255.0f);   /* round to nearest even (default mode), saturate */
+        out[i] = (uint8_t)(v < 0.0f ? 0.0f : (v > 255.0f ? 255.0f : v));
+    }
+    memcpy(d0out, d0.d.data(), sizeof(float) * (size_t)W * H);
+    memcpy(d1out, d1.d.data(), sizeof(float) * (size_t)W * H);
     return 0;
 }
 

@@ -53,7 +53,7 @@ def translate(src: str) -> str:
     src = strip_comments(src)
     src = re.sub(r'#import\s+"(?:\.\./)?(\w+)\.cl"', r'#include "\1.inc"', src)
     src = vector_literals(src)
-    src = re.sub(r"\.(xyz|xy|lo|hi)\b(?!\s*\()", r".\1()", src)
+    src = re.sub(r"\.(xyz|xy|yz|zw|lo|hi)\b(?!\s*\()", r".\1()", src)
     src = re.sub(r"\.(s[0-7]{1,4})\b(?!\s*\()", r".\1()", src)
     src = re.sub(r"(?m)^(\s*)local\s+", r"\1static thread_local ", src)
     return src
