@@ -640,6 +640,7 @@ def run_gcv(args):
     H, W = sc.left.shape[:2]
     left, right = torch.from_numpy(sc.left).cuda(), torch.from_numpy(sc.right).cuda()
     f = gcv.StereoGCVFilter()
+    plan = gcv.plan(W, H, 0.0, DMAX, 1.0)
     stream = torch.cuda.current_stream()
     for _ in range(max(1, args.warmup)):
         f.apply(right, left, 0.0, DMAX, 1.0)
@@ -657,7 +658,7 @@ def run_gcv(args):
     print(json.dumps({"workload": "gcv", "metric": "StereoGCVFilter::apply ms (1242x375, 128 disparities, both views)",
                       "value": ms, "unit": "ms", "steps": args.steps,
                       "mpix_disp_per_s": 2 * W * H * nd / 1e6 / (ms * 1e-3),
-                      "launches_per_apply": 2 * (17 + 24 * nd + 1) + 1,
+                      "launches_per_apply": 2 * plan["launches"] + 1, "disparities_per_batch": plan["batch"],
                       "bad1_nonocc_pct_left_view": bad,
                       "config": {"workload": "pair 0 of the headline scene family (1242x375, dmax 128), point cost, "
                                              "guided filter r 9, eps 1e-3; right image as cam0, left as cam1"}}), flush=True)

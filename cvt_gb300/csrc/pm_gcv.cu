@@ -23,18 +23,28 @@
  * order; a linear sampler at integer coordinates (costdepthconv, undefined in
  * OpenCL) reads the texel.  dot sums left to right.
  *
- * Kernels are HBM-bound per-pixel passes, the scans latency-bound; a
- * disparity costs 24 launches.
+ * The disparities run in batches (the grid's z index is the disparity in
+ * the batch): per batch one pass forms the cost and block-scans its two
+ * integral images, three launches finish them, one pass forms the guided
+ * filter's (a, b) from their box means and block-scans a and b, three launches
+ * finish those, and one pass per pixel walks the batch's disparities in order
+ * through the box means of a and b, the filter output and the running
+ * minimum: 9 launches per batch, where the reference launches 24 kernels per
+ * disparity.  The passes are HBM- or L2-bound; the boundary scans are
+ * latency-bound chains.
  */
 #include <math.h>
 #include <stdint.h>
 
+#include <atomic>
 #include <string>
 
 #include "cvtpm.h"
 #include "pm_kernels.cuh"
 
 namespace {
+
+const int GCV_BATCH_MAX = 256;   /* disparities per batch, at most */
 
 struct Img {
     float* d;
@@ -122,33 +132,65 @@ __global__ void __launch_bounds__(256) k_scan_block_outer(Img rr, Img gg, Img in
     put(gg, x, y, b);
 }
 
-/* prefixsum_horiz: per row, running sum over the block-boundary columns */
-__global__ void k_scan_horiz(Img m) {
+/* A stack of images of one shape: slice z starts at d + z * zs. */
+struct Stk {
+    float* d;
+    int w, h, c;
+    size_t zs;
+    __host__ __device__ __forceinline__ Img at(int z) const { return Img{d + (size_t)z * zs, w, h, c}; }
+};
+
+/* One or two stacks scanned by one launch: blockIdx.z = slice * n + which. */
+struct Stk2 {
+    Stk s[2];
+    int n;
+    __device__ __forceinline__ Img at(int bz) const { return (bz % n) ? s[1].at(bz / n) : s[0].at(bz / n); }
+};
+
+/* prefixsum_horiz: per row, running sum over the block-boundary columns.
+ * The sum runs in the reference's order; the loads of 8 boundary columns are
+ * issued before their sums are stored. */
+__global__ void k_scan_horiz(Stk2 p) {
+    const Img m = p.at(blockIdx.z);
     const int y = blockIdx.x * blockDim.x + threadIdx.x;
     if (y >= m.h) return;
     float4 acc = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-    for (int x = 15; x < m.w; x += 16) {
-        acc = add4(acc, tex(m, x, y));
-        put(m, x, y, acc);
+    for (int x0 = 15; x0 < m.w; x0 += 16 * 8) {
+        float4 v[8];
+#pragma unroll
+        for (int k = 0; k < 8; ++k) v[k] = tex(m, x0 + 16 * k, y);
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+            acc = add4(acc, v[k]);
+            put(m, x0 + 16 * k, y, acc);
+        }
     }
 }
 
 /* prefixsum_vert: per column, running sum over the block-boundary rows */
-__global__ void k_scan_vert(Img m) {
+__global__ void k_scan_vert(Stk2 p) {
+    const Img m = p.at(blockIdx.z);
     const int x = blockIdx.x * blockDim.x + threadIdx.x;
     if (x >= m.w) return;
     float4 acc = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-    for (int y = 15; y < m.h; y += 16) {
-        acc = add4(acc, tex(m, x, y));
-        put(m, x, y, acc);
+    for (int y0 = 15; y0 < m.h; y0 += 16 * 8) {
+        float4 v[8];
+#pragma unroll
+        for (int k = 0; k < 8; ++k) v[k] = tex(m, x, y0 + 16 * k);
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+            acc = add4(acc, v[k]);
+            put(m, x, y0 + 16 * k, acc);
+        }
     }
 }
 
 /* prefixsum_block2, in place: each block's window shifted by (-1, -1) gets
  * the block's boundary row and column added; windows of different blocks are
  * disjoint. */
-__global__ void __launch_bounds__(256) k_scan_block2(Img m) {
+__global__ void __launch_bounds__(256) k_scan_block2(Stk2 p) {
     __shared__ float4 buf[16][16];
+    const Img m = p.at(blockIdx.z);
     const int lx = threadIdx.x, ly = threadIdx.y;
     const int bx = blockIdx.x * 16, by = blockIdx.y * 16;
     buf[ly][lx] = tex(m, bx + lx - 1, by + ly - 1);
@@ -165,17 +207,21 @@ __global__ void __launch_bounds__(256) k_scan_block2(Img m) {
 
 /* boxfilter_prefixsum: the mean over the box of radius r from the integral
  * image (window clamped to the image, as the reference clamps it) */
-__global__ void __launch_bounds__(256) k_box(Img out, Img in, int r) {
-    const int x = blockIdx.x * 32 + threadIdx.x, y = blockIdx.y * 8 + threadIdx.y;
-    if (x >= out.w || y >= out.h) return;
+__device__ __forceinline__ float4 box_px(const Img& in, int x, int y, int r) {
     const int x0 = max(0, x - (r + 1)), y0 = max(0, y - (r + 1));
-    const int x1 = min(out.w - 1, x + r), y1 = min(out.h - 1, y + r);
+    const int x1 = min(in.w - 1, x + r), y1 = min(in.h - 1, y + r);
     float4 v = tex(in, x0, y0);
     v = sub4(v, tex(in, x0, y1));
     v = sub4(v, tex(in, x1, y0));
     v = add4(v, tex(in, x1, y1));
     const float area = (float)((x1 - x0) * (y1 - y0));
-    put(out, x, y, make_float4(v.x / area, v.y / area, v.z / area, v.w / area));
+    return make_float4(v.x / area, v.y / area, v.z / area, v.w / area);
+}
+
+__global__ void __launch_bounds__(256) k_box(Img out, Img in, int r) {
+    const int x = blockIdx.x * 32 + threadIdx.x, y = blockIdx.y * 8 + threadIdx.y;
+    if (x >= out.w || y >= out.h) return;
+    put(out, x, y, box_px(in, x, y, r));
 }
 
 /* ------------------------------------------------------------ steps -- */
@@ -191,33 +237,61 @@ __global__ void __launch_bounds__(256) k_gradx(Img out, Img src) {
     put(out, x, y, sub4(tex(src, x + 1, y), tex(src, x - 1, y)));
 }
 
-/* stereogcv_costdepthgrad (point cost): img0 at the pixel, img1 at x - d */
-__global__ void __launch_bounds__(256) k_cost(Img cost, Img img0, Img img1, Img grad0, Img grad1, float depth) {
-    const int x = blockIdx.x * 32 + threadIdx.x, y = blockIdx.y * 8 + threadIdx.y;
+/* stereogcv_costdepthgrad (point cost) at (x, y) for disparity depth:
+ * img0 at the pixel, img1 at x - depth */
+__device__ __forceinline__ float point_cost(const Img& img0, const Img& img1, const Img& grad0, const Img& grad1,
+                                            int x, int y, float depth) {
     const int W = img0.w, H = img1.h;
-    if (x >= W || y >= H) return;
     const float u = (float)x + 0.5f - depth, v = (float)y + 0.5f;
-    float c;
-    if (u < 0.0f || u >= (float)W || v < 0.0f || v >= (float)H) {
-        c = 0.008f + 0.028f;
-    } else {
-        const float4 dm = make_float4(0.3333f, 0.3333f, 0.3333f, 0.0f);
-        const float4 I0 = tex(img0, x, y), G0 = tex(grad0, x, y);
-        const float4 I1 = bilinear(img1, u, v), G1 = bilinear(grad1, u, v);
-        const float ci = fminf(dotf4(abs4(sub4(I1, I0)), dm), 0.028f);
-        const float cg = fminf(dotf4(abs4(sub4(G1, G0)), dm), 0.008f);
-        c = ci + (cg - ci) * 0.10f;   /* mix(ci, cg, ALPHA) */
-    }
-    put(cost, x, y, make_float4(c, c, c, c));
+    if (u < 0.0f || u >= (float)W || v < 0.0f || v >= (float)H) return 0.008f + 0.028f;
+    const float4 dm = make_float4(0.3333f, 0.3333f, 0.3333f, 0.0f);
+    const float4 I0 = tex(img0, x, y), G0 = tex(grad0, x, y);
+    const float4 I1 = bilinear(img1, u, v), G1 = bilinear(grad1, u, v);
+    const float ci = fminf(dotf4(abs4(sub4(I1, I0)), dm), 0.028f);
+    const float cg = fminf(dotf4(abs4(sub4(G1, G0)), dm), 0.008f);
+    return ci + (cg - ci) * 0.10f;   /* mix(ci, cg, ALPHA) */
 }
 
-/* guidedfilter_calcab_outerrgb: per pixel the 3x3 system (covariance of the
- * guide + epsilon) solved by the reference's LU steps */
-__global__ void __launch_bounds__(256) k_calcab(Img ia, Img ib, Img mG, Img mS, Img mSG, Img mRR, Img mGG, float eps) {
-    const int x = blockIdx.x * 32 + threadIdx.x, y = blockIdx.y * 8 + threadIdx.y;
-    if (x >= ia.w || y >= ia.h) return;
-    const float4 g = tex(mG, x, y), s = tex(mS, x, y), sg = tex(mSG, x, y);
-    float4 rr = tex(mRR, x, y), gg = tex(mGG, x, y);
+/* Disparities of one batch: slice z of every stack belongs to d[z]. */
+struct Depths {
+    float d[GCV_BATCH_MAX];
+};
+
+/* The cost image of disparity dl.d[z] and the 16 x 16 block scans of its two
+ * integral images, the cost (GRAY) and img0 * cost (prefixsum_pblock_mul2),
+ * in one pass: the same sums in the same order as the two block scans of the
+ * stored cost image.  Pixels outside the image scan as 0, as the reference's
+ * out-of-image reads return 0. */
+__global__ void __launch_bounds__(256) k_cost_scan(Stk ig, Stk iint, Img img0, Img img1, Img grad0, Img grad1,
+                                                   Depths dl) {
+    __shared__ float4 b4[256];
+    __shared__ float b1[256];
+    const int lx = threadIdx.x, ly = threadIdx.y, lid = ly * 16 + lx;
+    const int x = blockIdx.x * 16 + lx, y = blockIdx.y * 16 + ly, z = blockIdx.z;
+    float c = 0.0f;
+    if (x < img0.w && y < img0.h) c = point_cost(img0, img1, grad0, grad1, x, y, dl.d[z]);
+    float4 t = mul4(tex(img0, x, y), make_float4(c, c, c, c));
+    b4[lid] = t;
+    b1[lid] = c;
+    for (int off = 1; off < 16; off <<= 1) {
+        __syncthreads();
+        if (lx >= off) { t = add4(t, b4[lid - off]); c = c + b1[lid - off]; }
+        __syncthreads();
+        b4[lid] = t; b1[lid] = c;
+        __syncthreads();
+        if (ly >= off) { t = add4(t, b4[lid - 16 * off]); c = c + b1[lid - 16 * off]; }
+        __syncthreads();
+        b4[lid] = t; b1[lid] = c;
+    }
+    put(iint.at(z), x, y, t);
+    put(ig.at(z), x, y, make_float4(c, c, c, c));
+}
+
+/* guidedfilter_calcab_outerrgb at one pixel: the 3x3 system (covariance of
+ * the guide + epsilon) solved by the reference's LU steps; s is the mean
+ * cost (a GRAY image, read as (s, s, s, s)). */
+__device__ __forceinline__ float4 calcab_px(float4 g, float4 s, float4 sg, float4 rr, float4 gg, float eps,
+                                            float* b) {
     float4 cov = sub4(sg, mul4(g, s));
     cov.w = 0.0f;
     rr.x = rr.x - g.x * g.x; rr.y = rr.y - g.x * g.y; rr.z = rr.z - g.x * g.z;
@@ -243,28 +317,78 @@ __global__ void __launch_bounds__(256) k_calcab(Img ia, Img ib, Img mG, Img mS, 
     const float xy = (by - m1z * xz) / m1y;
     const float xx = (bx - (m0y * xy + m0z * xz)) / m0x;
     const float4 a = make_float4(xx, xy, xz, 0.0f);
-    const float d = dotf4(g, a);
-    put(ia, x, y, a);
-    put(ib, x, y, make_float4(s.x - d, s.y - d, s.z - d, s.w - d));
+    *b = s.x - dotf4(g, a);
+    return a;
 }
 
-/* guidedfilter_applyab_gc_outer: dot(a, guide) + b */
-__global__ void __launch_bounds__(256) k_applyab(Img out, Img in, Img ia, Img ib) {
-    const int x = blockIdx.x * 32 + threadIdx.x, y = blockIdx.y * 8 + threadIdx.y;
-    if (x >= out.w || y >= out.h) return;
-    const float d = dotf4(tex(ia, x, y), tex(in, x, y));
-    const float4 b = tex(ib, x, y);
-    put(out, x, y, make_float4(d + b.x, d + b.y, d + b.z, 1.0f));
+/* Per pixel of disparity slice z: the box means of the cost and of
+ * guide * cost, the guided filter's (a, b), and the 16 x 16 block scans of a
+ * and b — the first steps of their integral images.  b's four channels are
+ * equal (s - dot(g, a) with s a GRAY mean), so one is stored. */
+__global__ void __launch_bounds__(256) k_calcab_scan(Stk iaI, Stk ibI, Stk ig, Stk iint, Img mG, Img mRR, Img mGG,
+                                                     float eps, int r) {
+    __shared__ float4 b4[256];
+    __shared__ float b1[256];
+    const int lx = threadIdx.x, ly = threadIdx.y, lid = ly * 16 + lx;
+    const int x = blockIdx.x * 16 + lx, y = blockIdx.y * 16 + ly, z = blockIdx.z;
+    float4 a = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    float b = 0.0f;
+    if (x < mG.w && y < mG.h) {
+        const float s = box_px(ig.at(z), x, y, r).x;
+        a = calcab_px(tex(mG, x, y), make_float4(s, s, s, s), box_px(iint.at(z), x, y, r), tex(mRR, x, y),
+                      tex(mGG, x, y), eps, &b);
+    }
+    b4[lid] = a;
+    b1[lid] = b;
+    for (int off = 1; off < 16; off <<= 1) {
+        __syncthreads();
+        if (lx >= off) { a = add4(a, b4[lid - off]); b = b + b1[lid - off]; }
+        __syncthreads();
+        b4[lid] = a; b1[lid] = b;
+        __syncthreads();
+        if (ly >= off) { a = add4(a, b4[lid - 16 * off]); b = b + b1[lid - 16 * off]; }
+        __syncthreads();
+        b4[lid] = a; b1[lid] = b;
+    }
+    put(iaI.at(z), x, y, a);
+    put(ibI.at(z), x, y, make_float4(b, b, b, b));
 }
 
-/* stereogcv_costmin: keep (cost, depth) of the smaller cost; ties keep the old */
-__global__ void __launch_bounds__(256) k_costmin(Img out, Img cnew, Img cin, float newdepth) {
-    const int x = blockIdx.x * 32 + threadIdx.x, y = blockIdx.y * 8 + threadIdx.y;
-    if (x >= out.w || y >= out.h) return;
-    float4 c = tex(cin, x, y);
-    const float n = tex(cnew, x, y).x;
-    if (n < c.x) { c.x = n; c.y = newdepth; }
-    put(out, x, y, c);
+/* Per pixel, the batch's disparities in order: the box means of a and b,
+ * guidedfilter_applyab_gc_outer (dot(a, guide) + b) and stereogcv_costmin
+ * (keep (cost, depth) of the smaller cost; ties keep the old).  A block is 32
+ * pixels of a row x FM_CHUNKS consecutive runs of the batch's disparities:
+ * each warp keeps its run's first strict minimum, and the runs are folded in
+ * order into the pixel's (cost, depth) with the same strict comparison.  The
+ * sequential rule picks the first disparity of the smallest cost below the
+ * start (NaN never compares less), and so does this. */
+#define FM_CHUNKS 8
+__global__ void __launch_bounds__(32 * FM_CHUNKS) k_filter_min(Img c, Stk iaI, Stk ibI, Img guide, Depths nd, int nz,
+                                                              int r) {
+    __shared__ float bv[FM_CHUNKS][32];
+    __shared__ int bz[FM_CHUNKS][32];
+    const int lx = threadIdx.x, k = threadIdx.y;
+    const int x = blockIdx.x * 32 + lx, y = blockIdx.y;
+    float best = __int_as_float(0x7f800000);   /* +inf: never taken, as no cost beats the start of 1e9 with it */
+    int bi = -1;
+    if (x < c.w) {
+        const float4 g = tex(guide, x, y);
+        const int z1 = (k + 1) * nz / FM_CHUNKS;
+#pragma unroll 2
+        for (int z = k * nz / FM_CHUNKS; z < z1; ++z) {
+            const float d = dotf4(box_px(iaI.at(z), x, y, r), g);
+            const float n = d + box_px(ibI.at(z), x, y, r).x;
+            if (n < best) { best = n; bi = z; }
+        }
+    }
+    bv[k][lx] = best;
+    bz[k][lx] = bi;
+    __syncthreads();
+    if (k || x >= c.w) return;
+    float4 cc = tex(c, x, y);
+    for (int j = 0; j < FM_CHUNKS; ++j)
+        if (bz[j][lx] >= 0 && bv[j][lx] < cc.x) { cc.x = bv[j][lx]; cc.y = nd.d[bz[j][lx]]; }
+    put(c, x, y, cc);
 }
 
 /* stereogcv_costdepthconv: depth * scale + add, 0 where it reached 1 */
@@ -305,69 +429,100 @@ struct Scratch {
     int device = -1;
 };
 
-void integral(Img dst, Img src, const Img* src2, cudaStream_t st) {
-    if (src2) k_scan_block<SCAN_MUL2><<<g16(src.w, src.h), dim3(16, 16), 0, st>>>(dst, src, *src2);
-    else k_scan_block<SCAN_PLAIN><<<g16(src.w, src.h), dim3(16, 16), 0, st>>>(dst, src, src);
-    k_scan_horiz<<<(dst.h + 127) / 128, 128, 0, st>>>(dst);
-    k_scan_vert<<<(dst.w + 127) / 128, 128, 0, st>>>(dst);
-    k_scan_block2<<<g16(dst.w, dst.h), dim3(16, 16), 0, st>>>(dst);
+Stk2 one(Stk a) { return Stk2{{a, a}, 1}; }
+Stk2 two(Stk a, Stk b) { return Stk2{{a, b}, 2}; }
+
+/* prefixsum_horiz, prefixsum_vert and prefixsum_block2 over nz slices of
+ * the stacks in p */
+void scan_rest(Stk2 p, int nz, cudaStream_t st) {
+    const int W = p.s[0].w, H = p.s[0].h, nb = nz * p.n;
+    k_scan_horiz<<<dim3((H + 127) / 128, 1, nb), 128, 0, st>>>(p);
+    k_scan_vert<<<dim3((W + 127) / 128, 1, nb), 128, 0, st>>>(p);
+    k_scan_block2<<<dim3((W + 15) / 16, (H + 15) / 16, nb), dim3(16, 16), 0, st>>>(p);
 }
 
-void integral_outer(Img rr, Img gg, Img src, cudaStream_t st) {
-    k_scan_block_outer<<<g16(src.w, src.h), dim3(16, 16), 0, st>>>(rr, gg, src);
-    for (Img m : {rr, gg}) k_scan_horiz<<<(m.h + 127) / 128, 128, 0, st>>>(m);
-    for (Img m : {rr, gg}) k_scan_vert<<<(m.w + 127) / 128, 128, 0, st>>>(m);
-    for (Img m : {rr, gg}) k_scan_block2<<<g16(m.w, m.h), dim3(16, 16), 0, st>>>(m);
+Stk stack(float* d, int W, int H, int c) { return Stk{d, W, H, c, (size_t)W * H * c}; }
+
+/* Scratch: GCV_VIEW_FLOATS per pixel for a view, GCV_SLICE_FLOATS per pixel
+ * and disparity of a batch (cost integral 1, guide * cost integral 4, the
+ * integrals of a 4 and b 1). */
+const int GCV_VIEW_FLOATS = 22, GCV_SLICE_FLOATS = 10;
+
+std::atomic<int> g_batch{0};
+
+size_t count_steps(float dmin, float dmax, float dt) { return (size_t)(fabsf(dmax - dmin) / fabsf(dt)); }
+
+/* Disparities per batch: the set value, else as many as 4 GiB of slices
+ * hold, at most GCV_BATCH_MAX and at most the number of steps. */
+int batch_for(int W, int H, size_t steps) {
+    const int set = g_batch.load();
+    size_t b = set > 0 ? (size_t)set : ((size_t)4 << 30) / ((size_t)GCV_SLICE_FLOATS * 4 * W * H);
+    b = b < 1 ? 1 : (b > GCV_BATCH_MAX ? GCV_BATCH_MAX : b);
+    if (steps && b > steps) b = steps;
+    return (int)b;
 }
 
-/* Scratch of one depthmap: 47 floats per pixel. */
-const int GCV_FLOATS = 47;
+size_t scratch_floats(int W, int H, int batch, int extra) {
+    return (size_t)W * H * (GCV_VIEW_FLOATS + (size_t)GCV_SLICE_FLOATS * batch + extra);
+}
 
-/* StereoGCVFilter::depthmap (StereoGCVFilter.cpp:97-242), point cost.  The
- * integral images of the box-SAD and NCC cost variants, which it forms but the
- * point cost does not read, are not formed. */
-void depthmap(float* dst, size_t dpitch, Img cam0, Img cam1, float dmin, float dmax, float dt, float* s,
-              cudaStream_t st, int* launches) {
+int launches_for(size_t steps, int batch) {
+    const size_t nb = (steps + batch - 1) / batch;
+    return (int)(3 + 5 + 6 + nb * 9 + 1);
+}
+
+/* StereoGCVFilter::depthmap (StereoGCVFilter.cpp:97-242), point cost, with
+ * the disparities processed in batches: the grid's z index is the disparity
+ * within the batch, and each launch covers the batch.  Every disparity's
+ * values are formed by the reference's arithmetic in its order; the running
+ * minimum takes the disparities in the reference's order.  The integral
+ * images of the box-SAD and NCC cost variants, which the reference forms but
+ * the point cost does not read, are not formed. */
+void depthmap(float* dst, size_t dpitch, Img cam0, Img cam1, float dmin, float dmax, float dt, float* s, int batch,
+              cudaStream_t st) {
     const int W = cam0.w, H = cam0.h;
     const size_t n = (size_t)W * H;
     auto take = [&](int c) { Img m{s, W, H, c}; s += n * (size_t)c; return m; };
-    Img g0 = take(4), g1 = take(4), ia = take(4), ib = take(4), iint = take(4), iint2 = take(4), mG = take(4);
-    Img mGS = take(4), mRR = take(4), mGG = take(4), cost = take(1), costgf = take(1), mS = take(1);
-    Img c[2] = {take(2), take(2)};
-    int index = 0;
+    /* RGBA images and stacks first: every float4 buffer starts on a
+     * multiple of 4 floats whatever W * H is */
+    const Img g0 = take(4), g1 = take(4), mG = take(4), mRR = take(4), mGG = take(4);
+    const Stk iint = stack(s, W, H, 4), iaI = stack(s + 4 * n * batch, W, H, 4);
+    s += 8 * n * batch;
+    const Img c = take(2);
+    const Stk ig = stack(s, W, H, 1), ibI = stack(s + n * batch, W, H, 1);
+    /* the view's set-up integrals, before the first batch: 8 floats per pixel
+     * of the RGBA stacks */
+    const Stk t0 = stack(iint.d, W, H, 4), t1 = stack(iint.d + 4 * n, W, H, 4);
     const int R = 9;
-    k_fill2<<<g32(W, H), dim3(32, 8), 0, st>>>(c[!index], 1e9f, 0.0f);
+    k_fill2<<<g32(W, H), dim3(32, 8), 0, st>>>(c, 1e9f, 0.0f);
     k_gradx<<<g32(W, H), dim3(32, 8), 0, st>>>(g0, cam0);
     k_gradx<<<g32(W, H), dim3(32, 8), 0, st>>>(g1, cam1);
-    integral(iint, cam1, nullptr, st);
-    k_box<<<g32(W, H), dim3(32, 8), 0, st>>>(mG, iint, R);
-    integral_outer(iint, iint2, cam1, st);
-    k_box<<<g32(W, H), dim3(32, 8), 0, st>>>(mRR, iint, R);
-    k_box<<<g32(W, H), dim3(32, 8), 0, st>>>(mGG, iint2, R);
-    *launches += 3 + 4 + 1 + 7 + 2;
+    k_scan_block<SCAN_PLAIN><<<g16(W, H), dim3(16, 16), 0, st>>>(t0.at(0), cam1, cam1);
+    scan_rest(one(t0), 1, st);
+    k_box<<<g32(W, H), dim3(32, 8), 0, st>>>(mG, t0.at(0), R);
+    k_scan_block_outer<<<g16(W, H), dim3(16, 16), 0, st>>>(t0.at(0), t1.at(0), cam1);
+    scan_rest(two(t0, t1), 1, st);
+    k_box<<<g32(W, H), dim3(32, 8), 0, st>>>(mRR, t0.at(0), R);
+    k_box<<<g32(W, H), dim3(32, 8), 0, st>>>(mGG, t1.at(0), R);
     if (dmax < dmin && dt > 0) dt = -dt;
-    size_t steps = (size_t)(fabsf(dmax - dmin) / fabsf(dt));
-    for (float d = dmin; steps--; d += dt) {
-        Img g = cost;
-        Img ig = iint;
-        ig.c = 1;                                   /* the integral of a GRAY image is GRAY */
-        k_cost<<<g32(W, H), dim3(32, 8), 0, st>>>(cost, cam1, cam0, g1, g0, d);
-        integral(ig, g, nullptr, st);
-        k_box<<<g32(W, H), dim3(32, 8), 0, st>>>(mS, ig, R);
-        integral(iint, cam1, &cost, st);
-        k_box<<<g32(W, H), dim3(32, 8), 0, st>>>(mGS, iint, R);
-        k_calcab<<<g32(W, H), dim3(32, 8), 0, st>>>(ia, ib, mG, mS, mGS, mRR, mGG, 1e-3f);
-        integral(iint, ia, nullptr, st);
-        k_box<<<g32(W, H), dim3(32, 8), 0, st>>>(ia, iint, R);
-        integral(iint, ib, nullptr, st);
-        k_box<<<g32(W, H), dim3(32, 8), 0, st>>>(ib, iint, R);
-        k_applyab<<<g32(W, H), dim3(32, 8), 0, st>>>(costgf, cam1, ia, ib);
-        k_costmin<<<g32(W, H), dim3(32, 8), 0, st>>>(c[index], costgf, c[!index], fabsf(d - dmin) / fabsf(dmax - dmin));
-        index = 1 - index;
-        *launches += 24;
+    size_t steps = count_steps(dmin, dmax, dt);
+    float d = dmin;
+    while (steps) {
+        const int nz = (int)(steps < (size_t)batch ? steps : (size_t)batch);
+        Depths dd, nd;
+        for (int z = 0; z < nz; ++z, d += dt) {
+            dd.d[z] = d;
+            nd.d[z] = fabsf(d - dmin) / fabsf(dmax - dmin);
+        }
+        steps -= nz;
+        const dim3 gz((W + 15) / 16, (H + 15) / 16, nz);
+        k_cost_scan<<<gz, dim3(16, 16), 0, st>>>(ig, iint, cam1, cam0, g1, g0, dd);
+        scan_rest(two(ig, iint), nz, st);
+        k_calcab_scan<<<gz, dim3(16, 16), 0, st>>>(iaI, ibI, ig, iint, mG, mRR, mGG, 1e-3f, R);
+        scan_rest(two(iaI, ibI), nz, st);
+        k_filter_min<<<dim3((W + 31) / 32, H), dim3(32, FM_CHUNKS), 0, st>>>(c, iaI, ibI, cam1, nd, nz, R);
     }
-    k_depthconv<<<g32(W, H), dim3(32, 8), 0, st>>>(dst, dpitch / 4, c[!index], 1.0f, 0.0f);
-    *launches += 1;
+    k_depthconv<<<g32(W, H), dim3(32, 8), 0, st>>>(dst, dpitch / 4, c, 1.0f, 0.0f);
 }
 
 cvtpm_status check_args(const float* cam0, const float* cam1, int W, int H, size_t pitch, float dmin, float dmax,
@@ -375,6 +530,8 @@ cvtpm_status check_args(const float* cam0, const float* cam1, int W, int H, size
     if (!cam0 || !cam1) return fail(CVTPM_ERR_INVALID_ARGUMENT, "gcv: NULL image");
     if (W < 2 || H < 2) return fail(CVTPM_ERR_SIZE, "gcv: images must be at least 2 x 2");
     if (pitch != (size_t)W * 16) return fail(CVTPM_ERR_INVALID_ARGUMENT, "gcv: images must be tight RGBA float rows");
+    if ((uintptr_t)cam0 % 16 || (uintptr_t)cam1 % 16)
+        return fail(CVTPM_ERR_INVALID_ARGUMENT, "gcv: images must start on a 16-byte boundary");
     if (!isfinite(dmin) || !isfinite(dmax) || !isfinite(dt) || dt == 0.0f || dmin == dmax)
         return fail(CVTPM_ERR_INVALID_ARGUMENT, "gcv: dmin, dmax, dt must be finite, dt and dmax - dmin non-zero");
     if (fabsf(dmax - dmin) / fabsf(dt) > 65536.0f) return fail(CVTPM_ERR_INVALID_ARGUMENT, "gcv: more than 65536 steps");
@@ -408,16 +565,37 @@ float* scratch(size_t bytes) {
 
 extern "C" {
 
+cvtpm_status cvtpm_gcv_set_batch(int disparities) {
+    if (disparities < 0 || disparities > GCV_BATCH_MAX)
+        return fail(CVTPM_ERR_INVALID_ARGUMENT, "gcv: batch must be 0 (automatic) .. " + std::to_string(GCV_BATCH_MAX));
+    g_batch.store(disparities);
+    return CVTPM_OK;
+}
+
+cvtpm_status cvtpm_gcv_plan(int width, int height, float dmin, float dmax, float dt, int* steps, int* batch,
+                            size_t* scratch_bytes, int* launches) {
+    if (width < 2 || height < 2) return fail(CVTPM_ERR_SIZE, "gcv: images must be at least 2 x 2");
+    if (!isfinite(dmin) || !isfinite(dmax) || !isfinite(dt) || dt == 0.0f || dmin == dmax)
+        return fail(CVTPM_ERR_INVALID_ARGUMENT, "gcv: dmin, dmax, dt must be finite, dt and dmax - dmin non-zero");
+    const size_t n = count_steps(dmin, dmax, dt);
+    const int b = batch_for(width, height, n);
+    if (steps) *steps = (int)n;
+    if (batch) *batch = b;
+    if (scratch_bytes) *scratch_bytes = scratch_floats(width, height, b, 0) * sizeof(float);
+    if (launches) *launches = launches_for(n, b);
+    return CVTPM_OK;
+}
+
 cvtpm_status cvtpm_gcv_depthmap(float* dst, size_t dst_pitch, const float* cam0, const float* cam1, int width,
                                 int height, size_t pitch, float dmin, float dmax, float dt, void* stream) {
     cvtpm_status s = check_args(cam0, cam1, width, height, pitch, dmin, dmax, dt);
     if (s != CVTPM_OK) return s;
     if (!dst || dst_pitch % 4 || dst_pitch < (size_t)width * 4) return fail(CVTPM_ERR_INVALID_ARGUMENT, "gcv: bad dst");
-    float* sc = scratch(sizeof(float) * GCV_FLOATS * (size_t)width * height);
+    const int b = batch_for(width, height, count_steps(dmin, dmax, dt));
+    float* sc = scratch(sizeof(float) * scratch_floats(width, height, b, 0));
     if (!sc) return fail(CVTPM_ERR_ALLOC, "gcv: scratch allocation failed");
-    int launches = 0;
     depthmap(dst, dst_pitch, Img{(float*)cam0, width, height, 4}, Img{(float*)cam1, width, height, 4}, dmin, dmax, dt,
-             sc, (cudaStream_t)stream, &launches);
+             sc, b, (cudaStream_t)stream);
     const cudaError_t e = cudaGetLastError();
     return e == cudaSuccess ? CVTPM_OK : fail(CVTPM_ERR_CUDA, std::string("gcv: ") + cudaGetErrorString(e));
 }
@@ -431,18 +609,18 @@ cvtpm_status cvtpm_gcv_apply(uint8_t* dst, size_t dst_pitch, float* d0, float* d
     if ((d0 == nullptr) != (d1 == nullptr) || (d0 && dpitch != (size_t)width * 4))
         return fail(CVTPM_ERR_INVALID_ARGUMENT, "gcv: give both depth maps (tight rows, pitch width * 4) or neither");
     const size_t n = (size_t)width * height;
-    float* sc = scratch(sizeof(float) * (GCV_FLOATS + 2) * n);
+    const int b = batch_for(width, height, count_steps(dmin, dmax, dt));
+    float* sc = scratch(sizeof(float) * scratch_floats(width, height, b, 2));
     if (!sc) return fail(CVTPM_ERR_ALLOC, "gcv: scratch allocation failed");
-    float* own0 = sc + GCV_FLOATS * n;
+    float* own0 = sc + scratch_floats(width, height, b, 0);
     float* own1 = own0 + n;
     float* p0 = d0 ? d0 : own0;
     float* p1 = d1 ? d1 : own1;
     const size_t pp = d0 ? dpitch : (size_t)width * 4;
     cudaStream_t st = (cudaStream_t)stream;
-    int launches = 0;
-    const Img a{(float*)cam0, width, height, 4}, b{(float*)cam1, width, height, 4};
-    depthmap(p0, pp, a, b, dmin, dmax, dt, sc, st, &launches);
-    depthmap(p1, pp, b, a, -dmin, -dmax, -dt, sc, st, &launches);
+    const Img a{(float*)cam0, width, height, 4}, c1{(float*)cam1, width, height, 4};
+    depthmap(p0, pp, a, c1, dmin, dmax, dt, sc, b, st);
+    depthmap(p1, pp, c1, a, -dmin, -dmax, -dt, sc, b, st);
     /* the two depth maps as GRAY images of pitch pp */
     const Img i0{p0, width, height, 1}, i1{p1, width, height, 1};
     k_occlusion<<<g32(width, height), dim3(32, 8), 0, st>>>(dst, dst_pitch, i0, i1, fabsf(dmax));

@@ -28,6 +28,25 @@ def _img(t: torch.Tensor, name: str) -> torch.Tensor:
     return t.contiguous()
 
 
+def set_batch(disparities: int = 0) -> None:
+    """Disparities per batch for later calls (0: automatic); results do not
+    depend on it."""
+    rc = _lib.lib().cvtpm_gcv_set_batch(int(disparities))
+    if rc:
+        _fail(rc)
+
+
+def plan(width: int, height: int, dmin: float, dmax: float, dt: float) -> dict:
+    """steps, batch, scratch bytes and kernel launches of one depthmap call."""
+    steps, batch, launches = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+    nbytes = ctypes.c_size_t()
+    rc = _lib.lib().cvtpm_gcv_plan(int(width), int(height), float(dmin), float(dmax), float(dt), ctypes.byref(steps),
+                                   ctypes.byref(batch), ctypes.byref(nbytes), ctypes.byref(launches))
+    if rc:
+        _fail(rc)
+    return {"steps": steps.value, "batch": batch.value, "scratch_bytes": nbytes.value, "launches": launches.value}
+
+
 class StereoGCVFilter:
     def _stream(self, t):
         return ctypes.c_void_p(torch.cuda.current_stream(t.device).cuda_stream)

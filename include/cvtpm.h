@@ -477,9 +477,21 @@ cvtpm_status cvtpm_tsdf_save_raw(cvtpm_tsdf* vol, const char* path, int weighted
  * no cost fell below its start).  As in the reference, the map belongs to
  * cam1 and its match in cam0 lies at x - d: with a left/right pair, pass the
  * right image as cam0 and the left as cam1 for the left view's disparity.
- * Scratch (47 floats per pixel, 49 for apply) belongs to the calling host
- * thread and is kept between calls.  Calls are stream-ordered.
+ * The disparities are processed in batches; scratch is (22 + 10 x batch)
+ * floats per pixel (2 more for apply), belongs to the calling host thread and
+ * is kept between calls.  Calls are stream-ordered.  The batch does not
+ * change results.
  * ------------------------------------------------------------------ */
+
+/* Disparities per batch for later calls: 0 (the default) takes as many as
+ * 4 GiB of scratch holds, at most 256; 1..256 sets it.  Process-wide. */
+cvtpm_status cvtpm_gcv_set_batch(int disparities);
+
+/* The plan of a depthmap call of these arguments: the number of
+ * disparities, the batch, the scratch bytes and the kernel launches (each
+ * optional).  An apply call runs two such depth maps and one more launch. */
+cvtpm_status cvtpm_gcv_plan(int width, int height, float dmin, float dmax, float dt, int* steps, int* batch,
+                            size_t* scratch_bytes, int* launches);
 
 /* StereoGCVFilter::depthmap(dst, cam0, cam1, dmin, dmax, dt) (:97-242). */
 cvtpm_status cvtpm_gcv_depthmap(float* dst, size_t dst_pitch, const float* cam0, const float* cam1,

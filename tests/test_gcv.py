@@ -40,3 +40,23 @@ def test_argument_checks():
     assert L.cvtpm_gcv_depthmap(16, 32, 16, 16, 1, 8, 16, 0.0, 4.0, 1.0, None) == 2
     assert L.cvtpm_gcv_depthmap(16, 32, 16, 16, 8, 8, 128, 0.0, 4.0, 0.0, None) == 1   # dt = 0
     assert "dt" in L.cvtpm_last_error(None).decode()
+
+
+def test_batch_plan():
+    from cvt_gb300 import gcv
+    p = gcv.plan(1242, 375, 0.0, 128.0, 1.0)
+    assert p["steps"] == 128 and p["batch"] == 128
+    assert p["scratch_bytes"] == 1242 * 375 * (22 + 10 * 128) * 4
+    assert p["launches"] == 14 + 9 + 1
+    try:
+        gcv.set_batch(5)
+        p = gcv.plan(1242, 375, 0.0, 128.0, 1.0)
+        assert p["batch"] == 5 and p["launches"] == 14 + 9 * 26 + 1
+        assert gcv.plan(40, 30, 3.0, 1.0, 1.0)["batch"] == 2          # never more than the steps
+        assert gcv.plan(40, 30, 0.0, 1.0, 0.25)["steps"] == 4
+    finally:
+        gcv.set_batch(0)
+    assert gcv.plan(7680, 4320, 0.0, 256.0, 1.0)["batch"] == (4 << 30) // (10 * 4 * 7680 * 4320)
+    L = _lib.lib()
+    assert L.cvtpm_gcv_set_batch(-1) == 1 and L.cvtpm_gcv_set_batch(257) == 1
+    assert L.cvtpm_gcv_plan(1, 8, 0.0, 4.0, 1.0, None, None, None, None) == 2

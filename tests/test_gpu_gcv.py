@@ -1,7 +1,9 @@
 """The comparison baseline (cvt::StereoGCVFilter) on the GPU, bit for bit
 against the golden outputs of the reference's own kernels
 (tests/golden/make_gcv_golden.py): both views, the fused map, a fractional
-step and a descending range, sizes on and off the 16-pixel scan blocks."""
+step and a descending range, sizes on and off the 16-pixel scan blocks,
+each with disparity batches of 1, 3 and the automatic size; and, at the
+headline size, the same output for every batch size."""
 import os
 
 import numpy as np
@@ -20,8 +22,15 @@ def G():
     return np.load(GOLDEN)
 
 
+@pytest.fixture(params=[0, 1, 3])
+def batch(request):
+    gcv.set_batch(request.param)
+    yield request.param
+    gcv.set_batch(0)
+
+
 @pytest.mark.parametrize("name", ["apply_a", "apply_b"])
-def test_apply_matches_reference(cuda, G, name):
+def test_apply_matches_reference(cuda, G, name, batch):
     dmin, dmax, dt = (float(v) for v in G[f"{name}_args"])
     out, d0, d1 = gcv.StereoGCVFilter().apply(torch.from_numpy(G[f"{name}_cam0"]).cuda(),
                                               torch.from_numpy(G[f"{name}_cam1"]).cuda(), dmin, dmax, dt)
@@ -32,9 +41,26 @@ def test_apply_matches_reference(cuda, G, name):
 
 
 @pytest.mark.parametrize("name", ["dm_frac", "dm_desc"])
-def test_depthmap_matches_reference(cuda, G, name):
+def test_depthmap_matches_reference(cuda, G, name, batch):
     dmin, dmax, dt = (float(v) for v in G[f"{name}_args"])
     d = gcv.StereoGCVFilter().depthmap(torch.from_numpy(G[f"{name}_cam0"]).cuda(),
                                        torch.from_numpy(G[f"{name}_cam1"]).cuda(), dmin, dmax, dt)
     torch.cuda.synchronize()
     assert not bit_diff(d.cpu().numpy(), G[f"{name}_d0"]).any()
+
+
+def test_batch_size_does_not_change_the_headline_pair(cuda):
+    from cvt_gb300 import scenes
+    sc = scenes.config_scene(2, pair=0)
+    left, right = torch.from_numpy(sc.left).cuda(), torch.from_numpy(sc.right).cuda()
+    outs = []
+    try:
+        for b in (0, 5, 64):
+            gcv.set_batch(b)
+            assert gcv.plan(1242, 375, 0.0, 128.0, 1.0)["batch"] == (b or 128)
+            outs.append([t.cpu().numpy() for t in gcv.StereoGCVFilter().apply(right, left, 0.0, 128.0, 1.0)])
+    finally:
+        gcv.set_batch(0)
+    for o in outs[1:]:
+        for a, b in zip(outs[0], o):
+            assert a.tobytes() == b.tobytes()
