@@ -23,7 +23,7 @@ EXPORTS = (
     "cvtpm_set_timing", "cvtpm_reset_stats", "cvtpm_get_stats", "cvtpm_tool_fp32_peak",
     "cvtpm_cost_eval_noalloc",
     "cvtpm_iformat_bpp", "cvtpm_image_to_rgbaf", "cvtpm_depthmap_image", "cvtpm_raw_read", "cvtpm_raw_write",
-    "cvtpm_ppm_read", "cvtpm_pfm_write", "cvtpm_stereo_rectify", "cvtpm_warp_apply",
+    "cvtpm_ppm_read", "cvtpm_pfm_write", "cvtpm_png_read", "cvtpm_png_write", "cvtpm_float_to_srgb_u8", "cvtpm_stereo_rectify", "cvtpm_warp_apply",
     "cvtpm_tsdf_create", "cvtpm_tsdf_destroy", "cvtpm_tsdf_info", "cvtpm_tsdf_clear", "cvtpm_tsdf_projection",
     "cvtpm_tsdf_add_depthmap", "cvtpm_tsdf_raycast", "cvtpm_tsdf_slice", "cvtpm_tsdf_save_raw",
     "cvtpm_gcv_set_batch", "cvtpm_gcv_plan", "cvtpm_gcv_depthmap", "cvtpm_gcv_apply",
@@ -134,6 +134,10 @@ def lib() -> ctypes.CDLL:
     L.cvtpm_raw_write.argtypes = [ctypes.c_char_p, IP]
     L.cvtpm_ppm_read.argtypes = [ctypes.c_char_p, IP]
     L.cvtpm_pfm_write.argtypes = [ctypes.c_char_p, IP]
+    L.cvtpm_png_read.argtypes = [ctypes.c_char_p, IP]
+    L.cvtpm_png_write.argtypes = [ctypes.c_char_p, IP]
+    L.cvtpm_float_to_srgb_u8.argtypes = [f]
+    L.cvtpm_float_to_srgb_u8.restype = ctypes.c_uint8
     CP = ctypes.POINTER(CvtpmCamera)
     L.cvtpm_stereo_rectify.argtypes = [CP, CP, ctypes.POINTER(ctypes.c_float), i, ctypes.POINTER(CvtpmRectification),
                                        i, i, vp, vp, sz, vp]
@@ -154,7 +158,8 @@ def lib() -> ctypes.CDLL:
     L.cvtpm_gcv_depthmap.argtypes = [vp, sz, vp, vp, i, i, sz, f, f, f, vp]
     L.cvtpm_gcv_apply.argtypes = [vp, sz, vp, vp, sz, vp, vp, i, i, sz, f, f, f, vp]
     for name in EXPORTS:
-        if name not in ("cvtpm_version", "cvtpm_status_string", "cvtpm_last_error", "cvtpm_iformat_bpp"):
+        if name not in ("cvtpm_version", "cvtpm_status_string", "cvtpm_last_error", "cvtpm_iformat_bpp",
+                        "cvtpm_float_to_srgb_u8"):
             getattr(L, name).restype = ctypes.c_int
     _lib = L
     return L

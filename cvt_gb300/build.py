@@ -18,7 +18,7 @@ ROOT = os.path.dirname(PKG)
 CSRC = os.path.join(PKG, "csrc")
 BUILD = os.path.join(ROOT, "_build")
 LIB = os.path.join(PKG, "libcvtpm.so")
-SOURCES = ["pm_kernels.cu", "pm_capi.cu", "pm_noalloc.cu", "pm_adjoint.cu", "pm_image.cu", "pm_io.cpp", "pm_rectify.cu", "pm_tsdf.cu", "pm_gcv.cu"]
+SOURCES = ["pm_kernels.cu", "pm_capi.cu", "pm_noalloc.cu", "pm_adjoint.cu", "pm_image.cu", "pm_io.cpp", "pm_png.cpp", "pm_rectify.cu", "pm_tsdf.cu", "pm_gcv.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

@@ -97,6 +97,23 @@ def read_ppm(path: str):
     return _read(_lib.lib().cvtpm_ppm_read, path)
 
 
+def read_png(path: str):
+    """PNG (plugins/iloader/PNG/PNGLoader.cpp) -> (array, fmt): GRAY_UINT8/16,
+    GRAYALPHA_UINT8/16 or RGBA_UINT8/16 as the reference's libpng set-up
+    gives them."""
+    return _read(_lib.lib().cvtpm_png_read, path)
+
+
+def write_png(path: str, arr: np.ndarray, fmt: int) -> None:
+    """PNG (plugins/isaver/PNG/PNGSaver.cpp) of a GRAY, GRAYALPHA, RGBA or
+    BGRA image of 8 or 16 bits, or of a float one converted to 8 bits as the
+    reference converts it (sRGB for colour and gray, linear for alpha)."""
+    d = _host_desc(np.ascontiguousarray(arr), fmt)
+    rc = _lib.lib().cvtpm_png_write(str(path).encode(), ctypes.byref(d))
+    if rc:
+        _fail(rc)
+
+
 def write_pfm(path: str, arr: np.ndarray, fmt: int) -> None:
     """PFM (plugins/isaver/PFM/PFMSaver.cpp) of a GRAY/RGBA/BGRA float image."""
     d = _host_desc(np.ascontiguousarray(arr), fmt)

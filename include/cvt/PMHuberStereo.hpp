@@ -76,15 +76,16 @@ class Image {
             throw CVTException("cvt::Image: download failed");
     }
     /* Image::load / Image::save by file extension (the reference picks its
-     * loader / saver plugin the same way): .raw is CVTRaw, .ppm and .pgm are
-     * read as RGBA_UINT8 / GRAY_UINT8, .pfm is written from float formats. */
+     * loader / saver plugin the same way): .raw is CVTRaw, .png is PNG, .ppm
+     * and .pgm are read as RGBA_UINT8 / GRAY_UINT8, .pfm is written from
+     * float formats. */
     void load(const std::string& path) {
         cvtpm_image d{};
-        const bool raw = ends_with(path, ".raw");
-        if (!raw && !ends_with(path, ".ppm") && !ends_with(path, ".pgm") && !ends_with(path, ".PPM") &&
+        const bool raw = ends_with(path, ".raw"), png = ends_with(path, ".png") || ends_with(path, ".PNG");
+        if (!raw && !png && !ends_with(path, ".ppm") && !ends_with(path, ".pgm") && !ends_with(path, ".PPM") &&
             !ends_with(path, ".PGM"))
             throw CVTException("cvt::Image::load: no loader for " + path);
-        auto rd = raw ? cvtpm_raw_read : cvtpm_ppm_read;
+        auto rd = raw ? cvtpm_raw_read : (png ? cvtpm_png_read : cvtpm_ppm_read);
         if (rd(path.c_str(), &d) != CVTPM_OK) throw CVTException(cvtpm_last_error(NULL));
         std::vector<unsigned char> host(d.stride * (size_t)d.height);
         d.data = host.data();
@@ -99,6 +100,7 @@ class Image {
         cvtpm_status s;
         if (ends_with(path, ".raw")) s = cvtpm_raw_write(path.c_str(), &d);
         else if (ends_with(path, ".pfm")) s = cvtpm_pfm_write(path.c_str(), &d);
+        else if (ends_with(path, ".png") || ends_with(path, ".PNG")) s = cvtpm_png_write(path.c_str(), &d);
         else throw CVTException("cvt::Image::save: no saver for " + path);
         if (s != CVTPM_OK) throw CVTException(cvtpm_last_error(NULL));
     }

@@ -377,6 +377,28 @@ cvtpm_status cvtpm_ppm_read(const char* path, cvtpm_image* img);
  * CVTPM_ERR_NOT_SUPPORTED. */
 cvtpm_status cvtpm_pfm_write(const char* path, const cvtpm_image* img);
 
+/* PNG (plugins/iloader/PNG/PNGLoader.cpp, plugins/isaver/PNG/PNGSaver.cpp;
+ * no libpng: the zlib/DEFLATE streams are decoded and encoded here).  Read
+ * in the two-call protocol above: gray 1-8 bit -> GRAY_UINT8 (low depths
+ * scaled), gray 16 -> GRAY_UINT16, gray+alpha -> GRAYALPHA_UINT8/16, RGB 8
+ * and palette -> RGBA_UINT8, RGB 16 -> RGBA_UINT16 (alpha 255 as the
+ * reference's 0xff filler), RGBA -> RGBA_UINT8/16; a tRNS chunk becomes the
+ * alpha channel (gray + tRNS -> GRAYALPHA); Adam7 interlacing is undone;
+ * 16-bit samples in host order.  Unsupported PNG types give
+ * CVTPM_ERR_NOT_SUPPORTED, corrupt files (bad CRC, Adler-32, codes)
+ * CVTPM_ERR_IO. */
+cvtpm_status cvtpm_png_read(const char* path, cvtpm_image* img);
+/* Writes GRAY, GRAYALPHA, RGBA or BGRA (as RGBA) host images of 8 or 16
+ * bits; float images are converted to 8 bits as the reference's
+ * Image::convert: colour and gray through cvtpm_float_to_srgb_u8, alpha and
+ * GRAYALPHA_FLOAT channels as (uint8)(clamp(v * 255 + 0.5, 0, 255)).  Other
+ * formats: CVTPM_ERR_NOT_SUPPORTED. */
+cvtpm_status cvtpm_png_write(const char* path, const cvtpm_image* img);
+/* The reference's float-to-8-bit sRGB conversion (F_TO_SRGB_U8,
+ * cvt/util/SIMD.cpp): the table entry round(255 * sRGB(i / 8192)) at
+ * i = (int)(v * 8192), 0 below 0 (and for NaN), 255 from 1 on. */
+uint8_t cvtpm_float_to_srgb_u8(float v);
+
 /* ------------------------------------------------------------------
  * Input side: stereo rectification (cvt/vision/StereoCameraCalibration.h,
  * cvt/vision/StereoRectification.h, cvt/gfx/ifilter/IWarp.cpp).

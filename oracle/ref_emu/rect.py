@@ -27,6 +27,7 @@ def lib():
         vp, c_int, sz = ctypes.c_void_p, ctypes.c_int, ctypes.c_size_t
         L.ref_rectify.argtypes = [vp] * 7 + [c_int, c_int, c_int] + [vp] * 7
         L.ref_warp.argtypes = [c_int, vp, sz, c_int, c_int, vp, sz, c_int, c_int, vp, sz]
+        L.ref_conv_f_u8.argtypes = [c_int, vp, vp, sz]
         _L = L
     return _L
 
@@ -37,3 +38,14 @@ def stereo_rectify(cam0, cam1, E, vertical, W, H):
 
 def warp(fmt, src, warp_map):
     return _orc._warp_call(lib().ref_warp, fmt, src, warp_map)
+
+
+def conv_f_u8(kind: int, src):
+    """Image::convert of float samples to 8 bits: kind 0 GRAY (sRGB), 1
+    GRAYALPHA (linear), 2 RGBA/BGRA (sRGB colour, linear alpha)."""
+    import numpy as np
+    a = np.ascontiguousarray(np.asarray(src, np.float32).reshape(-1))
+    out = np.zeros(a.size, np.uint8)
+    if lib().ref_conv_f_u8(int(kind), a.ctypes.data, out.ctypes.data, a.size):
+        raise ValueError("bad kind")
+    return out

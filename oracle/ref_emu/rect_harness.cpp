@@ -115,6 +115,21 @@ EXPORT int ref_warp(int kind, const void* src, size_t sstride, int sw, int sh, c
     return 0;
 }
 
+/* The float-to-8-bit conversions Image::convert applies before the PNG
+ * saver writes a float image (cvt/gfx/IConvert.cpp: GRAY_FLOAT ->
+ * Conv_GRAYf_to_GRAYu8, GRAYALPHA_FLOAT -> Conv_f_to_u8, RGBA/BGRA_FLOAT ->
+ * Conv_XXXAf_to_XXXAu8): kind 0, 1, 2; n floats (kind 2: n / 4 pixels). */
+EXPORT int ref_conv_f_u8(int kind, const float* src, uint8_t* dst, size_t n) {
+    GenericSIMD simd;
+    switch (kind) {
+        case 0: simd.Conv_GRAYf_to_GRAYu8(dst, src, n); break;
+        case 1: simd.Conv_f_to_u8(dst, src, n); break;
+        case 2: simd.Conv_XXXAf_to_XXXAu8(dst, src, n / 4); break;
+        default: return 1;
+    }
+    return 0;
+}
+
 /* cvt::Matrix4f operator* (cvt/math/Matrix4.h:269-288), row-major in and out;
  * the product TSDFVolume::addDepthMap forms (proj * grid-to-world). */
 EXPORT int ref_mat4_mul(const float* a, const float* b, float* out) {

@@ -2,9 +2,10 @@
  * runs cvt::PMHuberStereo::depthMap through include/cvt/PMHuberStereo.hpp and
  * writes the disparity map (raw, W*H floats).
  * usage: facade_main W H patchsize depthmax iterations left.raw right.raw out.raw
- *    or: facade_main --files patchsize depthmax iterations left right out.pfm
- * The second form loads the pair with cvt::Image::load (CVTRaw or PPM files
- * in any format), runs depthMap and saves the disparity map as PFM. */
+ *    or: facade_main --files patchsize depthmax iterations left right out.{pfm,png,raw}
+ * The second form loads the pair with cvt::Image::load (CVTRaw, PNG or PPM
+ * files in any format), runs depthMap and saves the disparity map by the
+ * output's extension (PFM, PNG or CVTRaw). */
 #include <cstdio>
 #include <cstdlib>
 #include <string>
