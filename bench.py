@@ -515,6 +515,17 @@ def run_combined(args):
     return 0
 
 
+def cpu_port_ms(fn, reps=1):
+    """Wall time of the oracle port on the host cores (OpenMP, all threads):
+    the CPU baseline of the input/output-side workloads."""
+    import time
+    fn()
+    t = time.perf_counter()
+    for _ in range(reps):
+        fn()
+    return (time.perf_counter() - t) * 1e3 / reps
+
+
 def run_rectify(args):
     """Input-side workload: a 3840x2160 RGBA8 stereo pair undistorted and
     rectified (two warp maps, IWarp::apply's 8-bit sampler), about 264 MB of
@@ -558,13 +569,22 @@ def run_rectify(args):
     npx = 2 * W * H
     peak, src = peaks()
     gbs = 16.0 * npx / (ms * 1e-3) / 1e9
+    cpu = None
+    if not args.no_cpu_baseline:
+        from oracle import oracle
+        hl, hr = left.cpu().numpy(), right.cpu().numpy()
+        ml, mr = r.maps[0].cpu().numpy(), r.maps[1].cpu().numpy()
+        cms = cpu_port_ms(lambda: (oracle.warp(imageio.RGBA_UINT8, hl, ml), oracle.warp(imageio.RGBA_UINT8, hr, mr)))
+        cpu = {"value": npx / 1e6 / (cms * 1e-3), "unit": "Mpix/s", "ms_per_step": cms, "cores": os.cpu_count(),
+               "kind": "port", "sample": "the full step: both views warped by the oracle (IWarp::apply's 8-bit "
+                                         "sampler restated), OpenMP over rows"}
     print(json.dumps({"workload": "rectify", "metric": "rectified Mpix/s (IWarp::apply, RGBA8, both views)",
                       "value": npx / 1e6 / (ms * 1e-3), "unit": "Mpix/s", "ms_per_step": ms, "steps": args.steps,
                       "maps_ms": maps_ms, "config": {"workload": f"{W}x{H} RGBA8 pair, radial + tangential distortion, "
                                                                  "undistort + rectify both views per step"},
                       "roofline": {"kernel": "k_warp_apply<U8C4>", "bound": "hbm", "achieved": gbs, "peak": peak,
                                    "unit": "GB/s", "frac": gbs / peak, "peak_source": src,
-                                   "bytes_per_px": 16}}), flush=True)
+                                   "bytes_per_px": 16}, "cpu_baseline": cpu}), flush=True)
     return 0
 
 
@@ -616,6 +636,16 @@ def run_tsdf(args):
     peak, src = peaks()
     nvox = N ** 3
     clear_gbs = 8.0 * nvox / (clear_ms * 1e-3) / 1e9
+    cpu = None
+    if not args.no_cpu_baseline:
+        from oracle import oracle
+        hv = oracle.tsdf_clear(N, N, N, 0.0)
+        T0, _ = oracle.tsdf_matrices(tsdf.projection(K, poses[0]), g2w)
+        hd = depths[0].cpu().numpy()
+        cms = cpu_port_ms(lambda: oracle.tsdf_add(hv, hd, 1.0, T0, 0.04))
+        cpu = {"value": nvox / (cms * 1e-3) / 1e9, "unit": "Gvoxel/s", "add_ms": cms, "cores": os.cpu_count(),
+               "kind": "port", "sample": "one depth map integrated into the 512^3 volume by the oracle "
+                                         "(TSDFVolume_add restated), OpenMP over z"}
     print(json.dumps({"workload": "tsdf", "metric": "TSDF integration Gvoxel/s (512^3, 640x480 depth maps)",
                       "value": nvox / (add_ms * 1e-3) / 1e9, "unit": "Gvoxel/s", "steps": args.steps,
                       "add_ms": add_ms, "raycast_ms": ray_ms, "clear_ms": clear_ms,
@@ -626,7 +656,7 @@ def run_tsdf(args):
                                              "(2 spheres, 2 planes, 4 poses) per step, ray cast from the first pose"},
                       "roofline_clear": {"kernel": "k_tsdf_clear", "bound": "hbm", "achieved": clear_gbs, "peak": peak,
                                          "unit": "GB/s", "frac": clear_gbs / peak, "peak_source": src},
-                      "add_bytes_per_launch_algorithmic": 16 * band / 4.0}), flush=True)
+                      "add_bytes_per_launch_algorithmic": 16 * band / 4.0, "cpu_baseline": cpu}), flush=True)
     return 0
 
 
@@ -655,11 +685,18 @@ def run_gcv(args):
     disp = d0.cpu().numpy() * DMAX
     bad = scenes.bad_pixel_rate(disp, sc)
     nd = int(DMAX)
+    cpu = None
+    if not args.no_cpu_baseline:
+        from oracle import oracle
+        cms = cpu_port_ms(lambda: oracle.gcv_apply(sc.right, sc.left, 0.0, DMAX, 1.0), reps=1)
+        cpu = {"value": cms, "unit": "ms", "cores": os.cpu_count(), "kind": "port",
+               "sample": "the full apply (128 disparities, both views, check) by the oracle's restatement of the "
+                         "reference's kernels, OpenMP over rows"}
     print(json.dumps({"workload": "gcv", "metric": "StereoGCVFilter::apply ms (1242x375, 128 disparities, both views)",
                       "value": ms, "unit": "ms", "steps": args.steps,
                       "mpix_disp_per_s": 2 * W * H * nd / 1e6 / (ms * 1e-3),
                       "launches_per_apply": 2 * plan["launches"] + 1, "disparities_per_batch": plan["batch"],
-                      "bad1_nonocc_pct_left_view": bad,
+                      "bad1_nonocc_pct_left_view": bad, "cpu_baseline": cpu,
                       "config": {"workload": "pair 0 of the headline scene family (1242x375, dmax 128), point cost, "
                                              "guided filter r 9, eps 1e-3; right image as cam0, left as cam1"}}), flush=True)
     return 0

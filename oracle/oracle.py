@@ -470,3 +470,38 @@ def tsdf_slice(vol, axis, index):
     out = np.empty(shape + (4,), np.float32)
     _tsdf_lib().orc_tsdf_slice(out.ctypes.data, axis, index, vol.ctypes.data, W, H, D)
     return out
+
+
+# ----------------------------------------------------------------------
+# StereoGCVFilter (orc_gcv_* in pm_oracle.cpp).  Images (H, W, 4) float32.
+
+def _gcv_lib():
+    L = lib()
+    vp, c_int, c_float = ctypes.c_void_p, ctypes.c_int, ctypes.c_float
+    L.orc_gcv_depthmap.argtypes = [vp, vp, vp, c_int, c_int, c_float, c_float, c_float]
+    L.orc_gcv_apply.argtypes = [vp, vp, vp, vp, vp, c_int, c_int, c_float, c_float, c_float]
+    return L
+
+
+def gcv_depthmap(cam0, cam1, dmin, dmax, dt):
+    """StereoGCVFilter::depthmap: the normalised depth map of cam1's view."""
+    a = np.ascontiguousarray(cam0, np.float32)
+    b = np.ascontiguousarray(cam1, np.float32)
+    H, W = a.shape[:2]
+    out = np.empty((H, W), np.float32)
+    _gcv_lib().orc_gcv_depthmap(out.ctypes.data, a.ctypes.data, b.ctypes.data, W, H, float(dmin), float(dmax),
+                                float(dt))
+    return out
+
+
+def gcv_apply(cam0, cam1, dmin, dmax, dt):
+    """StereoGCVFilter::apply: (GRAY_UINT8 fused map, d0, d1)."""
+    a = np.ascontiguousarray(cam0, np.float32)
+    b = np.ascontiguousarray(cam1, np.float32)
+    H, W = a.shape[:2]
+    out = np.empty((H, W), np.uint8)
+    d0 = np.empty((H, W), np.float32)
+    d1 = np.empty((H, W), np.float32)
+    _gcv_lib().orc_gcv_apply(out.ctypes.data, d0.ctypes.data, d1.ctypes.data, a.ctypes.data, b.ctypes.data, W, H,
+                             float(dmin), float(dmax), float(dt))
+    return out, d0, d1

@@ -1509,6 +1509,7 @@ int orc_stereo_rectify(const float* K0, const float* rad0, const float* tan0, co
 int orc_warp(int kind, const void* src, size_t sstride, int sw, int sh, const float* map, size_t mstride, int W, int H,
              void* dst, size_t dstride) {
     const uint8_t* s = (const uint8_t*)src;
+#pragma omp parallel for schedule(static)   /* rows are independent */
     for (int y = 0; y < H; ++y) {
         const float* m = (const float*)((const uint8_t*)map + (size_t)y * mstride);
         uint8_t* d = (uint8_t*)dst + (size_t)y * dstride;
@@ -1672,6 +1673,7 @@ int orc_tsdf_clear(float* cv, int W, int H, int D, float init) {
 
 int orc_tsdf_add(float* cv, int W, int H, int D, const float* dmap, int iw, int ih, float dscale, const float* T,
                  float trunc) {
+#pragma omp parallel for schedule(static)   /* voxels are independent */
     for (int z = 0; z < D; ++z)
         for (int y = 0; y < H; ++y)
             for (int x = 0; x < W; ++x) {
@@ -1745,6 +1747,343 @@ int orc_tsdf_slice(float* rgba, int axis, int v, const float* cv, int W, int H, 
             float* o = rgba + 4 * ((size_t)b * ow + a);
             o[0] = o[1] = o[2] = t;
             o[3] = 1.0f;
+        }
+    return 0;
+}
+
+}  // extern "C"
+
+/* ---------------------------------------------------------------------
+ * StereoGCVFilter (cvt/gfx/ifilter/StereoGCVFilter.cpp:71-244) on the CPU,
+ * in the reference's order: per disparity, whole-image passes of its
+ * kernels, every 16 x 16 work-group executed as OpenCL defines it.
+ *   orc_gcv_depthmap   StereoGCVFilter::depthmap (:91-244), point cost
+ *                      (USEPOINTSAD); the integral images that only the
+ *                      box-SAD and NCC costs read (:143-153) are not formed
+ *   orc_gcv_apply      StereoGCVFilter::apply (:71-89): both views and
+ *                      stereogcv_occlusioncheck, without the PNG saves
+ * Images follow the formats the reference allocates: GRAY (CL_INTENSITY, read
+ * as (v, v, v, v), written from .x), GRAYALPHA (CL_RG, read as (r, g, 0, 1))
+ * and RGBA.  Reads outside the image return 0 (CLK_ADDRESS_CLAMP's border;
+ * also where a CLK_ADDRESS_NONE kernel reads outside, which OpenCL leaves
+ * undefined); a linear sampler at integer coordinates (costdepthconv.cl:38,
+ * undefined in OpenCL) reads the texel; linear reads at float coordinates
+ * follow OpenCL 1.2 section 8.2.  dot sums left to right; mix(a, b, t) =
+ * a + (b - a) * t.
+ * --------------------------------------------------------------------- */
+namespace gcv {
+
+struct F4 {
+    float x, y, z, w;
+};
+inline F4 operator+(F4 a, F4 b) { return {a.x + b.x, a.y + b.y, a.z + b.z, a.w + b.w}; }
+inline F4 operator-(F4 a, F4 b) { return {a.x - b.x, a.y - b.y, a.z - b.z, a.w - b.w}; }
+inline F4 operator*(F4 a, F4 b) { return {a.x * b.x, a.y * b.y, a.z * b.z, a.w * b.w}; }
+inline F4 splat(float v) { return {v, v, v, v}; }
+inline float dot(F4 a, F4 b) { return ((a.x * b.x + a.y * b.y) + a.z * b.z) + a.w * b.w; }
+inline F4 fabs4(F4 a) { return {std::fabs(a.x), std::fabs(a.y), std::fabs(a.z), std::fabs(a.w)}; }
+
+struct Img {
+    int w = 0, h = 0, c = 4;
+    std::vector<float> d;
+    Img() {}
+    Img(int w_, int h_, int c_) : w(w_), h(h_), c(c_), d((size_t)w_ * h_ * c_, 0.0f) {}
+    F4 rd(int x, int y) const {
+        if (x < 0 || y < 0 || x >= w || y >= h) return splat(0.0f);
+        const float* p = &d[((size_t)y * w + x) * c];
+        if (c == 1) return splat(p[0]);
+        if (c == 2) return {p[0], p[1], 0.0f, 1.0f};
+        return {p[0], p[1], p[2], p[3]};
+    }
+    void wr(int x, int y, F4 v) {
+        if (x < 0 || y < 0 || x >= w || y >= h) return;
+        float* p = &d[((size_t)y * w + x) * c];
+        p[0] = v.x;
+        if (c >= 2) p[1] = v.y;
+        if (c == 4) { p[2] = v.z; p[3] = v.w; }
+    }
+    /* read_imagef with a linear sampler at (u, v), OpenCL 1.2 section 8.2 */
+    F4 lin(float u, float v) const {
+        const float tu = u - 0.5f, tv = v - 0.5f;
+        const float fu = std::floor(tu), fv = std::floor(tv);
+        const float a = tu - fu, b = tv - fv;
+        const int i0 = (int)fu, j0 = (int)fv;
+        const F4 t00 = rd(i0, j0), t10 = rd(i0 + 1, j0), t01 = rd(i0, j0 + 1), t11 = rd(i0 + 1, j0 + 1);
+        return ((splat((1.0f - a) * (1.0f - b)) * t00 + splat(a * (1.0f - b)) * t10) + splat((1.0f - a) * b) * t01) +
+               splat(a * b) * t11;
+    }
+};
+
+const int BS = 16;   /* the integral filter's block size (IntegralFilter.cpp) */
+
+/* prefixsum_pblock / _mul2 / _outerrgb (prefixsum/prefixsum_pblock*.cl:25-63):
+ * per 16 x 16 work-group, Hillis-Steele steps, x then y per offset.  The
+ * outer-product variant scans 8 channels (two outputs). */
+void pblock(Img& out, Img* out2, const Img& in, const Img* in2, bool outer) {
+    const int gw = (in.w + BS - 1) / BS, gh = (in.h + BS - 1) / BS;
+#pragma omp parallel for schedule(static)
+    for (int by = 0; by < gh; ++by)
+        for (int bx = 0; bx < gw; ++bx) {
+            std::vector<F4> lo(BS * BS), hi(BS * BS), blo(BS * BS), bhi(BS * BS);
+            for (int ly = 0; ly < BS; ++ly)
+                for (int lx = 0; lx < BS; ++lx) {
+                    const int x = bx * BS + lx, y = by * BS + ly, l = ly * BS + lx;
+                    const F4 v = in.rd(x, y);
+                    if (outer) {
+                        lo[l] = {v.x * v.x, v.x * v.y, v.x * v.z, 0.0f};   /* (rgb.x * rgb.xyz, 0, */
+                        hi[l] = {v.y * v.y, v.y * v.z, v.z * v.z, 0.0f};   /*  rgb.y * rgb.yz, rgb.z * rgb.z, 0) */
+                    } else {
+                        lo[l] = in2 ? v * in2->rd(x, y) : v;
+                    }
+                }
+            for (int off = 1; off < BS; off <<= 1) {
+                blo = lo;
+                bhi = hi;
+                for (int l = 0; l < BS * BS; ++l)
+                    if (l % BS >= off) {
+                        lo[l] = lo[l] + blo[l - off];
+                        if (outer) hi[l] = hi[l] + bhi[l - off];
+                    }
+                blo = lo;
+                bhi = hi;
+                for (int l = 0; l < BS * BS; ++l)
+                    if (l / BS >= off) {
+                        lo[l] = lo[l] + blo[l - BS * off];
+                        if (outer) hi[l] = hi[l] + bhi[l - BS * off];
+                    }
+            }
+            for (int ly = 0; ly < BS; ++ly)
+                for (int lx = 0; lx < BS; ++lx) {
+                    out.wr(bx * BS + lx, by * BS + ly, lo[ly * BS + lx]);
+                    if (outer) out2->wr(bx * BS + lx, by * BS + ly, hi[ly * BS + lx]);
+                }
+        }
+}
+
+/* prefixsum_horiz / prefixsum_vert (:25-45), in place: running sums over
+ * the block-boundary columns of each row, then the boundary rows of each
+ * column */
+void horiz_vert(Img& m) {
+#pragma omp parallel for schedule(static)
+    for (int y = 0; y < m.h; ++y) {
+        F4 acc = splat(0.0f);
+        for (int x = BS - 1; x < m.w; x += BS) {
+            acc = acc + m.rd(x, y);
+            m.wr(x, y, acc);
+        }
+    }
+#pragma omp parallel for schedule(static)
+    for (int x = 0; x < m.w; ++x) {
+        F4 acc = splat(0.0f);
+        for (int y = BS - 1; y < m.h; y += BS) {
+            acc = acc + m.rd(x, y);
+            m.wr(x, y, acc);
+        }
+    }
+}
+
+/* prefixsum_block2 (prefixsum_block2.cl:79-152), in place: each work-group's
+ * window shifted by (-1, -1) gets its left column and top row added; the
+ * rows and columns that no window covers get the fix-ups of :139-149.
+ * Windows of different work-groups are disjoint, and the fix-ups read only
+ * pixels no window writes, so work-group order does not matter. */
+void block2(Img& m) {
+    const int gw = (m.w + BS - 1) / BS, gh = (m.h + BS - 1) / BS;
+#pragma omp parallel for schedule(static)
+    for (int gy = 0; gy < gh; ++gy)
+        for (int gx = 0; gx < gw; ++gx) {
+            F4 buf[BS][BS];
+            const int bx = gx * BS, by = gy * BS;
+            for (int ly = 0; ly < BS; ++ly)
+                for (int lx = 0; lx < BS; ++lx) buf[ly][lx] = m.rd(bx + lx - 1, by + ly - 1);
+            for (int ly = 0; ly < BS; ++ly)
+                for (int lx = 1; lx < BS; ++lx) buf[ly][lx] = buf[ly][lx] + buf[ly][0];
+            for (int ly = 1; ly < BS; ++ly)
+                for (int lx = 0; lx < BS; ++lx) buf[ly][lx] = buf[ly][lx] + buf[0][lx];
+            std::vector<std::pair<std::pair<int, int>, F4>> fix;
+            for (int ly = 0; ly < BS; ++ly)
+                for (int lx = 0; lx < BS; ++lx) {
+                    const int x = bx + lx, y = by + ly;
+                    if (x > m.w || y > m.h || !x || !y) continue;
+                    m.wr(x - 1, y - 1, buf[ly][lx]);
+                    if (y == m.h - 1 && lx < BS - 1 && ly == BS - 1 && x < m.w)
+                        fix.push_back({{x, y}, m.rd(x, y) + m.rd(bx - 1, by + ly)});
+                    if (x == m.w - 1 && ly < BS - 1 && lx == BS - 1 && y < m.h)
+                        fix.push_back({{x, y}, m.rd(x, y) + m.rd(bx + lx, by - 1)});
+                }
+            for (auto& f : fix) m.wr(f.first.first, f.first.second, f.second);
+        }
+}
+
+/* IntegralFilter::apply / applyOuterRGB: the four passes */
+void integral(Img& dst, const Img& src, const Img* src2) {
+    pblock(dst, nullptr, src, src2, false);
+    horiz_vert(dst);
+    block2(dst);
+}
+
+/* boxfilter_prefixsum (boxfilter/boxfilter_prefixsum.cl:46-71) */
+void box(Img& out, const Img& in, int r) {
+#pragma omp parallel for schedule(static)
+    for (int y = 0; y < out.h; ++y)
+        for (int x = 0; x < out.w; ++x) {
+            const int x0 = std::max(0, x - (r + 1)), y0 = std::max(0, y - (r + 1));
+            const int x1 = std::min(out.w - 1, x + r), y1 = std::min(out.h - 1, y + r);
+            F4 v = in.rd(x0, y0);
+            v = v - in.rd(x0, y1);
+            v = v - in.rd(x1, y0);
+            v = v + in.rd(x1, y1);
+            const float area = (float)((x1 - x0) * (y1 - y0));
+            out.wr(x, y, {v.x / area, v.y / area, v.z / area, v.w / area});
+        }
+}
+
+/* StereoGCVFilter::depthmap (:91-244) */
+void depthmap(float* dst, const Img& cam0, const Img& cam1, float dmin, float dmax, float dt) {
+    const int W = cam0.w, H = cam0.h, R = 9;
+    const float EPS = 1e-3f;
+    Img cost(W, H, 1), costgf(W, H, 1), c[2] = {Img(W, H, 2), Img(W, H, 2)}, g0(W, H, 4), g1(W, H, 4);
+    Img ia(W, H, 4), ib(W, H, 4), iint(W, H, 4), iint2(W, H, 4), meanG(W, H, 4), meanS(W, H, 1), meanGS(W, H, 4);
+    Img mRR(W, H, 4), mGG(W, H, 4);
+    int index = 0;
+    for (int y = 0; y < H; ++y)                                        /* fill (:124-128) */
+        for (int x = 0; x < W; ++x) c[!index].wr(x, y, {1e9f, 0.0f, 0.0f, 0.0f});
+    for (int y = 0; y < H; ++y)                                        /* gradx.cl:25-54 */
+        for (int x = 0; x < W; ++x) {
+            g0.wr(x, y, cam0.rd(x + 1, y) - cam0.rd(x - 1, y));
+            g1.wr(x, y, cam1.rd(x + 1, y) - cam1.rd(x - 1, y));
+        }
+    integral(iint, cam1, nullptr);                                     /* :141-142 */
+    box(meanG, iint, R);
+    pblock(iint, &iint2, cam1, nullptr, true);                         /* :156-158 */
+    horiz_vert(iint);
+    horiz_vert(iint2);
+    block2(iint);
+    block2(iint2);
+    box(mRR, iint, R);
+    box(mGG, iint2, R);
+    if (dmax < dmin && dt > 0) dt = -dt;
+    size_t n = (size_t)(std::fabs(dmax - dmin) / std::fabs(dt));
+    const F4 dm = {0.3333f, 0.3333f, 0.3333f, 0.0f};
+    for (float d = dmin; n--; d += dt) {
+        /* stereogcv_costdepthgrad (costdepthgrad.cl:61-135): img0 = cam1,
+         * img1 = cam0, grad0 = g1, grad1 = g0 (:169-175) */
+#pragma omp parallel for schedule(static)
+        for (int y = 0; y < H; ++y)
+            for (int x = 0; x < W; ++x) {
+                const float u = (float)x + 0.5f - d, v = (float)y + 0.5f;
+                float cv;
+                if (u < 0.0f || u >= (float)W || v < 0.0f || v >= (float)H) {
+                    cv = 0.008f + 0.028f;
+                } else {
+                    const F4 I0 = cam1.rd(x, y), G0 = g1.rd(x, y), I1 = cam0.lin(u, v), G1 = g0.lin(u, v);
+                    const float ci = std::fmin(dot(fabs4(I1 - I0), dm), 0.028f);
+                    const float cg = std::fmin(dot(fabs4(G1 - G0), dm), 0.008f);
+                    cv = ci + (cg - ci) * 0.10f;
+                }
+                cost.wr(x, y, splat(cv));
+            }
+        /* the guided filter (:203-227) */
+        Img ig(W, H, 1);
+        integral(ig, cost, nullptr);
+        box(meanS, ig, R);
+        integral(iint, cam1, &cost);
+        box(meanGS, iint, R);
+#pragma omp parallel for schedule(static)
+        for (int y = 0; y < H; ++y)                                    /* guidedfilter_calcab_outerrgb.cl:76-128 */
+            for (int x = 0; x < W; ++x) {
+                const F4 g = meanG.rd(x, y), s = meanS.rd(x, y), sg = meanGS.rd(x, y);
+                F4 rr = mRR.rd(x, y), gg = mGG.rd(x, y);
+                F4 cov = sg - g * s;
+                cov.w = 0.0f;
+                rr.x = rr.x - g.x * g.x; rr.y = rr.y - g.x * g.y; rr.z = rr.z - g.x * g.z;
+                gg.x = gg.x - g.y * g.y; gg.y = gg.y - g.y * g.z;
+                gg.z = gg.z - g.z * g.z;
+                float m0[3] = {rr.x, rr.y, rr.z}, m1[3] = {rr.y, gg.x, gg.y}, m2[3] = {rr.z, gg.y, gg.z};
+                m0[0] = m0[0] + 1.0f * EPS;
+                m1[1] = m1[1] + 1.0f * EPS;
+                m2[2] = m2[2] + 1.0f * EPS;
+                /* LUSolve (:51-74) */
+                m1[0] = m1[0] / m0[0];
+                m2[0] = m2[0] / m0[0];
+                m1[1] = m1[1] - m1[0] * m0[1]; m1[2] = m1[2] - m1[0] * m0[2];
+                m2[1] = m2[1] - m2[0] * m0[1]; m2[2] = m2[2] - m2[0] * m0[2];
+                m2[1] = m2[1] / m1[1];
+                m2[2] = m2[2] - m2[1] * m1[2];
+                float bx = cov.x, byv = cov.y, bz = cov.z;
+                byv = byv - m1[0] * bx;
+                bz = bz - (m2[0] * bx + m2[1] * byv);
+                const float xz = bz / m2[2];
+                const float xy = (byv - m1[2] * xz) / m1[1];
+                const float xx = (bx - (m0[1] * xy + m0[2] * xz)) / m0[0];
+                const F4 a = {xx, xy, xz, 0.0f};
+                ia.wr(x, y, a);
+                ib.wr(x, y, s - splat(dot(g, a)));
+            }
+        integral(iint, ia, nullptr);
+        box(ia, iint, R);
+        integral(iint, ib, nullptr);
+        box(ib, iint, R);
+#pragma omp parallel for schedule(static)
+        for (int y = 0; y < H; ++y)                                    /* guidedfilter_applyab_gc_outer.cl:25-47 */
+            for (int x = 0; x < W; ++x) {
+                F4 o = splat(dot(ia.rd(x, y), cam1.rd(x, y))) + ib.rd(x, y);
+                o.w = 1.0f;
+                costgf.wr(x, y, o);
+            }
+        const float nd = std::fabs(d - dmin) / std::fabs(dmax - dmin);
+#pragma omp parallel for schedule(static)
+        for (int y = 0; y < H; ++y)                                    /* stereogcv_costmin (costmin.cl:26-52) */
+            for (int x = 0; x < W; ++x) {
+                F4 cc = c[!index].rd(x, y);
+                const float nv = costgf.rd(x, y).x;
+                if (nv < cc.x) { cc.x = nv; cc.y = nd; }
+                c[index].wr(x, y, cc);
+            }
+        index = 1 - index;
+    }
+    for (int y = 0; y < H; ++y)                                        /* stereogcv_costdepthconv (:25-43) */
+        for (int x = 0; x < W; ++x) {
+            const float v = c[!index].rd(x, y).y;
+            dst[(size_t)y * W + x] = v >= 1.0f ? 0.0f : v * 1.0f + 0.0f;
+        }
+}
+
+Img rgba(const float* p, int W, int H) {
+    Img m(W, H, 4);
+    memcpy(m.d.data(), p, sizeof(float) * 4 * (size_t)W * H);
+    return m;
+}
+
+}  // namespace gcv
+
+extern "C" {
+
+int orc_gcv_depthmap(float* dst, const float* cam0, const float* cam1, int W, int H, float dmin, float dmax,
+                     float dt) {
+    gcv::depthmap(dst, gcv::rgba(cam0, W, H), gcv::rgba(cam1, W, H), dmin, dmax, dt);
+    return 0;
+}
+
+int orc_gcv_apply(uint8_t* dst, float* d0, float* d1, const float* cam0, const float* cam1, int W, int H, float dmin,
+                  float dmax, float dt) {
+    const gcv::Img a = gcv::rgba(cam0, W, H), b = gcv::rgba(cam1, W, H);
+    gcv::depthmap(d0, a, b, dmin, dmax, dt);
+    gcv::depthmap(d1, b, a, -dmin, -dmax, -dt);
+    gcv::Img i0(W, H, 1), i1(W, H, 1);
+    memcpy(i0.d.data(), d0, sizeof(float) * (size_t)W * H);
+    memcpy(i1.d.data(), d1, sizeof(float) * (size_t)W * H);
+    const float ds = std::fabs(dmax);
+    for (int y = 0; y < H; ++y)                                        /* stereogcv_occlusioncheck (:27-52) */
+        for (int x = 0; x < W; ++x) {
+            const float din0 = i0.rd(x, y).x;
+            const float dd0 = din0 * ds;
+            const float din1 = i1.lin(-dd0 + (float)x + 0.5f, (float)y + 0.5f).x;
+            const float dd1 = din1 * ds;
+            const float v = std::fabs(-dd0 + dd1) <= 2.0f ? (din0 + din1) * 0.5f : 0.0f;
+            /* CL_UNORM_INT8 write: convert_uchar_sat_rte(v * 255) */
+            const float q = std::nearbyint(v * 255.0f);
+            dst[(size_t)y * W + x] = (uint8_t)(q > 0.0f ? (q < 255.0f ? q : 255.0f) : 0.0f);
         }
     return 0;
 }

@@ -60,3 +60,37 @@ def test_batch_plan():
     L = _lib.lib()
     assert L.cvtpm_gcv_set_batch(-1) == 1 and L.cvtpm_gcv_set_batch(257) == 1
     assert L.cvtpm_gcv_plan(1, 8, 0.0, 4.0, 1.0, None, None, None, None) == 2
+
+
+@pytest.mark.parametrize("name", ["apply_a", "apply_b"])
+def test_oracle_apply_matches_golden(oracle, name):
+    """the oracle's restatement (oracle/pm_oracle.cpp) against the golden
+    outputs of the reference's own kernels"""
+    G = np.load(GOLDEN)
+    dmin, dmax, dt = (float(v) for v in G[f"{name}_args"])
+    out, d0, d1 = oracle.gcv_apply(G[f"{name}_cam0"], G[f"{name}_cam1"], dmin, dmax, dt)
+    assert d0.tobytes() == G[f"{name}_d0"].tobytes()
+    assert d1.tobytes() == G[f"{name}_d1"].tobytes()
+    assert np.array_equal(out, G[f"{name}_out"])
+
+
+@pytest.mark.parametrize("name", ["dm_frac", "dm_desc"])
+def test_oracle_depthmap_matches_golden(oracle, name):
+    G = np.load(GOLDEN)
+    dmin, dmax, dt = (float(v) for v in G[f"{name}_args"])
+    d = oracle.gcv_depthmap(G[f"{name}_cam0"], G[f"{name}_cam1"], dmin, dmax, dt)
+    assert d.tobytes() == G[f"{name}_d0"].tobytes()
+
+
+def test_oracle_matches_reference_kernels_live(oracle):
+    """random sizes on and off the 16-pixel blocks, random steps, against the
+    reference's kernels run through the OpenCL emulation"""
+    from oracle.ref_emu import gcv
+    if not gcv.available():
+        pytest.skip("reference sources absent")
+    rng = np.random.default_rng(77)
+    for W, H, dmin, dmax, dt in ((33, 17, 0.0, 6.0, 1.0), (16, 32, 1.5, 5.0, 0.5), (41, 23, 7.0, 2.0, 1.25)):
+        sc = scenes.make_scene(W, H, 2, 6.0, seed=int(rng.integers(1000)))
+        want = gcv.depthmap(sc.right, sc.left, dmin, dmax, dt)
+        got = oracle.gcv_depthmap(sc.right, sc.left, dmin, dmax, dt)
+        assert got.tobytes() == want.tobytes(), (W, H)

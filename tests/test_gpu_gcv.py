@@ -64,3 +64,25 @@ def test_batch_size_does_not_change_the_headline_pair(cuda):
     for o in outs[1:]:
         for a, b in zip(outs[0], o):
             assert a.tobytes() == b.tobytes()
+
+
+@pytest.mark.parametrize("W,H,dmin,dmax,dt,batch", [(96, 64, 0.0, 16.0, 1.0, 0), (130, 47, 2.0, 20.0, 0.75, 7),
+                                                    (257, 129, 0.0, 32.0, 1.0, 0), (64, 80, 24.0, 3.0, 1.5, 4)])
+def test_apply_matches_oracle(cuda, oracle, W, H, dmin, dmax, dt, batch):
+    """sizes on and off the 16-pixel blocks, fractional and descending steps,
+    several batch sizes, against the oracle's restatement of the reference's
+    kernels (pinned on the golden vectors)"""
+    from cvt_gb300 import scenes
+    sc = scenes.make_scene(W, H, 4, max(abs(dmin), abs(dmax)), seed=300 + W)
+    want = oracle.gcv_apply(sc.right, sc.left, dmin, dmax, dt)
+    gcv.set_batch(batch)
+    try:
+        got = gcv.StereoGCVFilter().apply(torch.from_numpy(sc.right).cuda(), torch.from_numpy(sc.left).cuda(),
+                                          dmin, dmax, dt)
+        torch.cuda.synchronize()
+    finally:
+        gcv.set_batch(0)
+    out, d0, d1 = (t.cpu().numpy() for t in got)
+    assert not bit_diff(d0, want[1]).any()
+    assert not bit_diff(d1, want[2]).any()
+    assert np.array_equal(out, want[0])
