@@ -258,6 +258,18 @@ struct cvtpm_tsdf {
     float2* vol;
 };
 
+/* Vision::disparityToDepthmap (cvt/vision/Vision.cpp:147-168): the depth
+ * (focallength * baseline) / (disparity * dispscale) where the scaled
+ * disparity exceeds dispthres, else 0.  8 bytes per pixel: HBM-bound. */
+__global__ void __launch_bounds__(256) k_disparity_to_depth(float* __restrict__ depth, size_t dp,
+                                                            const float* __restrict__ disp, size_t sp, int W, int H,
+                                                            float dispscale, float fb, float thres) {
+    const int x = blockIdx.x * 64 + threadIdx.x, y = blockIdx.y * 4 + threadIdx.y;
+    if (x >= W || y >= H) return;
+    const float d = disp[(size_t)y * sp + x] * dispscale;
+    depth[(size_t)y * dp + x] = d > thres ? fb / d : 0.0f;
+}
+
 extern "C" {
 
 cvtpm_status cvtpm_tsdf_projection(const float* intrinsics, const float* extrinsics, float* proj) {
@@ -394,3 +406,17 @@ cvtpm_status cvtpm_tsdf_save_raw(cvtpm_tsdf* v, const char* path, int weighted) 
 }
 
 }  // extern "C"
+
+extern "C" cvtpm_status cvtpm_disparity_to_depth(float* depth, size_t depth_pitch, const float* disparity,
+                                                 size_t disp_pitch, int width, int height, float dispscale,
+                                                 float focallength, float baseline, float dispthres, void* stream) {
+    if (!depth || !disparity) return fail(CVTPM_ERR_INVALID_ARGUMENT, "disparity to depth: NULL argument");
+    if (width < 1 || height < 1) return fail(CVTPM_ERR_SIZE, "disparity to depth: empty image");
+    if (depth_pitch % 4 || disp_pitch % 4 || depth_pitch < (size_t)width * 4 || disp_pitch < (size_t)width * 4)
+        return fail(CVTPM_ERR_INVALID_ARGUMENT, "disparity to depth: bad pitch");
+    const float fb = focallength * baseline;   /* Vision.cpp:153, in float */
+    k_disparity_to_depth<<<dim3((width + 63) / 64, (height + 3) / 4), dim3(64, 4), 0, (cudaStream_t)stream>>>(
+        depth, depth_pitch / 4, disparity, disp_pitch / 4, width, height, dispscale, fb, dispthres);
+    const cudaError_t e = cudaGetLastError();
+    return e == cudaSuccess ? CVTPM_OK : fail(CVTPM_ERR_CUDA, std::string("disparity to depth: ") + cudaGetErrorString(e));
+}

@@ -470,6 +470,16 @@ cvtpm_status cvtpm_tsdf_clear(cvtpm_tsdf* vol, float weight, void* stream);
 /* The projection of addDepthMap / rayCastDepthMap from intrinsics (3x3) and
  * extrinsics (4x4): intrinsics.toMatrix4() * extrinsics (:79-84, :87-92). */
 cvtpm_status cvtpm_tsdf_projection(const float* intrinsics, const float* extrinsics, float* proj);
+/* Vision::disparityToDepthmap(depthmap, disparity, dispscale, focallength,
+ * baseline, dispthres) (cvt/vision/Vision.cpp:147-168), the step between
+ * depthMap and addDepthMap: depth = (focallength * baseline) / (disparity *
+ * dispscale) where the scaled disparity exceeds dispthres (the reference's
+ * default 0.01), else 0.  GRAY_FLOAT images on the device, rows of the given
+ * pitches in bytes.  With depthMap's default dscale (1 / depthmax), pass
+ * dispscale = depthmax. */
+cvtpm_status cvtpm_disparity_to_depth(float* depth, size_t depth_pitch, const float* disparity, size_t disp_pitch,
+                                      int width, int height, float dispscale, float focallength, float baseline,
+                                      float dispthres, void* stream);
 /* addDepthMap(proj, depthmap, scale) (:61-77): depth map GRAY_FLOAT on the
  * device (rows of dpitch bytes), depth = value * scale. */
 cvtpm_status cvtpm_tsdf_add_depthmap(cvtpm_tsdf* vol, const float* proj, const float* depthmap,

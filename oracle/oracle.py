@@ -505,3 +505,15 @@ def gcv_apply(cam0, cam1, dmin, dmax, dt):
     _gcv_lib().orc_gcv_apply(out.ctypes.data, d0.ctypes.data, d1.ctypes.data, a.ctypes.data, b.ctypes.data, W, H,
                              float(dmin), float(dmax), float(dt))
     return out, d0, d1
+
+
+def disparity_to_depth(disp, dispscale, focallength, baseline, dispthres=0.01):
+    """Vision::disparityToDepthmap (orc_disparity_to_depth)."""
+    L = lib()
+    vp, c_int, c_float = ctypes.c_void_p, ctypes.c_int, ctypes.c_float
+    L.orc_disparity_to_depth.argtypes = [vp, vp, c_int, c_int, c_float, c_float, c_float, c_float]
+    d = np.ascontiguousarray(disp, np.float32)
+    out = np.empty_like(d)
+    L.orc_disparity_to_depth(out.ctypes.data, d.ctypes.data, d.shape[1], d.shape[0], float(dispscale),
+                             float(focallength), float(baseline), float(dispthres))
+    return out

@@ -2089,3 +2089,14 @@ int orc_gcv_apply(uint8_t* dst, float* d0, float* d1, const float* cam0, const f
 }
 
 }  // extern "C"
+
+/* Vision::disparityToDepthmap (cvt/vision/Vision.cpp:147-168) */
+extern "C" int orc_disparity_to_depth(float* depth, const float* disp, int W, int H, float dispscale,
+                                      float focallength, float baseline, float dispthres) {
+    const float fb = focallength * baseline;
+    for (size_t i = 0; i < (size_t)W * H; ++i) {
+        const float d = disp[i] * dispscale;
+        depth[i] = d > dispthres ? fb / d : 0.0f;
+    }
+    return 0;
+}

@@ -80,3 +80,56 @@ def test_far_camera_raycast_is_bounded(cuda, G, oracle):
     T, Ti = oracle.tsdf_matrices(proj, G["g2w"])
     want = oracle.tsdf_raycast(v.volume().cpu().numpy(), 16, 12, Ti, T, -1.0)
     assert not bit_diff(d.cpu().numpy(), want).any()
+
+
+def test_disparity_to_depth_matches_oracle(cuda, oracle):
+    from cvt_gb300 import vision
+    rng = np.random.default_rng(3)
+    d = rng.uniform(-0.1, 1.1, (37, 53)).astype(np.float32)
+    d.flat[:8] = [0.0, -0.0, np.nan, np.inf, -np.inf, 1e-30, 0.01 / 64, np.nextafter(np.float32(0.01 / 64), 1)]
+    for args in ((64.0, 525.0, 0.12, 0.01), (1.0, 700.5, 0.54, 0.0), (128.0, 1.0, -0.3, 0.5)):
+        got = vision.disparityToDepthmap(torch.from_numpy(d).cuda(), *args)
+        torch.cuda.synchronize()
+        assert not bit_diff(got.cpu().numpy(), oracle.disparity_to_depth(d, *args)).any(), args
+    # a pitched view of a wider buffer
+    wide = torch.zeros((37, 64), device="cuda")
+    wide[:, :53] = torch.from_numpy(d).cuda()
+    got = vision.disparityToDepthmap(wide[:, :53], 64.0, 525.0, 0.12)
+    assert not bit_diff(got.cpu().numpy(), oracle.disparity_to_depth(d, 64.0, 525.0, 0.12)).any()
+
+
+def test_stereo_to_tsdf_chain_matches_oracle(cuda, oracle):
+    """The output side end to end: PatchMatch depthMap of a rectified pair ->
+    disparityToDepthmap -> TSDFVolume::addDepthMap, on the GPU and in the
+    oracle, volumes bit for bit."""
+    from cvt_gb300 import scenes, vision
+    from cvt_gb300.params import default_params, PRESET_REFERENCE
+    from cvt_gb300.stereo import PMHuberStereo
+    W, H, dmax = 64, 48, 12.0
+    sc = scenes.make_scene(W, H, 3, dmax, seed=21)
+    p = default_params(PRESET_REFERENCE, patchsize=5, depthmax=dmax, iterations=2, pd_iterations=20)
+    st = PMHuberStereo(0)
+    st.set_params(p)
+    dm = torch.empty(0, device="cuda")
+    st.depthMap(dm, torch.from_numpy(sc.left).cuda(), torch.from_numpy(sc.right).cuda(), p.patchsize, dmax,
+                p.iterations, 4)
+    want_dm, _ = oracle.depthmap(p, sc.left, sc.right)
+    assert not bit_diff(dm.cpu().numpy(), want_dm).any()
+    f, B = 60.0, 0.1
+    depth = vision.disparityToDepthmap(dm, dmax, f, B)
+    want_depth = oracle.disparity_to_depth(want_dm, dmax, f, B)
+    assert not bit_diff(depth.cpu().numpy(), want_depth).any()
+    K = np.array([[f, 0, W / 2 - 0.5], [0, f, H / 2 - 0.5], [0, 0, 1]], np.float32)
+    E = np.eye(4, dtype=np.float32)
+    g2w = np.eye(4, dtype=np.float32)
+    g2w[:3, :3] *= 0.05
+    g2w[:3, 3] = [-0.8, -0.6, 0.3]
+    v = tsdf.TSDFVolume(g2w, 32, 24, 40, 0.1)
+    v.clear()
+    v.addDepthMap(K, E, depth, 1.0)
+    torch.cuda.synchronize()
+    T, _ = oracle.tsdf_matrices(tsdf.projection(K, E), g2w)
+    want = oracle.tsdf_add(oracle.tsdf_clear(32, 24, 40), want_depth, 1.0, T, 0.1)
+    got = v.volume().cpu().numpy()
+    assert not bit_diff(got, want).any()
+    assert (got[..., 1] > 0).sum() > 100        # the surface band is populated

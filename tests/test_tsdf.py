@@ -89,3 +89,23 @@ def test_argument_checks():
     assert L.cvtpm_tsdf_create(None, 0, g, 8, 8, 8, 0.1) == 1
     assert L.cvtpm_tsdf_clear(None, 0.0, None) == 1
     assert "NULL" in L.cvtpm_last_error(None).decode()
+
+
+def _edge_disparities():
+    rng = np.random.default_rng(3)
+    d = rng.uniform(-0.1, 1.1, (37, 53)).astype(np.float32)
+    d.flat[:8] = [0.0, -0.0, np.nan, np.inf, -np.inf, 1e-30, 0.01 / 64, np.nextafter(np.float32(0.01 / 64), 1)]
+    return d
+
+
+def test_oracle_disparity_to_depth():
+    """Vision::disparityToDepthmap restated: float32 products and IEEE
+    division, 0 at or below the threshold (NaN included)"""
+    from oracle import oracle
+    d = _edge_disparities()
+    got = oracle.disparity_to_depth(d, 64.0, 525.0, 0.12, 0.01)
+    fb = np.float32(525.0) * np.float32(0.12)
+    s = d * np.float32(64.0)
+    with np.errstate(divide="ignore", invalid="ignore"):
+        want = np.where(s > np.float32(0.01), fb / s, np.float32(0.0)).astype(np.float32)
+    assert same_bits(got, want)
