@@ -222,35 +222,33 @@ int decode(BitReader* br, const Huffman* h) {
     return -1;
 }
 
+/* the fixed codes of RFC 1951 section 3.2.6, built once (function-local
+ * statics are initialised once, thread-safely) */
 const Huffman& fixed_lit() {
-    static Huffman h;
-    static bool done = false;
-    if (!done) {
+    static const Huffman h = [] {
+        Huffman t;
         uint8_t l[288];
         for (int i = 0; i < 288; ++i) l[i] = i < 144 ? 8 : (i < 256 ? 9 : (i < 280 ? 7 : 8));
-        build(&h, l, 288);
-        done = true;
-    }
+        build(&t, l, 288);
+        return t;
+    }();
     return h;
 }
 
 const Huffman& fixed_dist() {
-    static Huffman h;
-    static bool done = false;
-    if (!done) {
+    static const Huffman h = [] {
+        Huffman t;
         uint8_t l[30];
         for (int i = 0; i < 30; ++i) l[i] = 5;
-        build(&h, l, 30);
-        done = true;
-    }
+        build(&t, l, 30);
+        return t;
+    }();
     return h;
 }
 
 /* Inflates a zlib stream into out, which must come to exactly `expect`
  * bytes.  Returns an error message or an empty string. */
 std::string inflate_zlib(const uint8_t* z, size_t n, size_t expect, std::vector<uint8_t>* out) {
-    fixed_lit();
-    fixed_dist();
     if (n < 6) return "zlib stream too short";
     const int cmf = z[0], flg = z[1];
     if ((cmf & 15) != 8 || (cmf >> 4) > 7 || (cmf * 256 + flg) % 31) return "bad zlib header";
@@ -641,21 +639,23 @@ bool read_file(const char* path, std::vector<uint8_t>* out) {
 /* ------------------------------------------------------------ write -- */
 /* F_TO_SRGB_U8: the float scaled by 8192 and truncated indexes a table of
  * round(255 * sRGB(i / 8192)); below 0 gives 0, from 8192 on 255; NaN 0. */
-uint8_t f_to_srgb_u8(float v) {
-    static uint8_t table[8192];
-    static bool done = false;
-    if (!done) {
+struct SrgbTable {
+    uint8_t t[8192];
+    SrgbTable() {
         for (int i = 0; i < 8192; ++i) {
             const double l = i / 8192.0;
             const double s = l <= 0.0031308 ? 12.92 * l : 1.055 * pow(l, 1.0 / 2.4) - 0.055;
-            table[i] = (uint8_t)floor(s * 255.0 + 0.5);
+            t[i] = (uint8_t)floor(s * 255.0 + 0.5);
         }
-        done = true;
     }
+};
+
+uint8_t f_to_srgb_u8(float v) {
+    static const SrgbTable table;   /* built once, thread-safely */
     const float t = v * 8192.0f;
     if (!(t > -1.0f)) return 0;   /* NaN and negatives truncating below 0 */
     if (t >= 8192.0f) return 255;
-    return table[(int)t];
+    return table.t[(int)t];
 }
 
 /* Conv_f_to_u8 and the alpha of Conv_XXXAf_to_XXXAu8: (uint8)(clamp(v * 255
