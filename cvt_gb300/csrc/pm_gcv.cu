@@ -72,6 +72,10 @@ __device__ __forceinline__ float4 sub4(float4 a, float4 b) { return make_float4(
 __device__ __forceinline__ float4 mul4(float4 a, float4 b) { return make_float4(a.x * b.x, a.y * b.y, a.z * b.z, a.w * b.w); }
 __device__ __forceinline__ float4 scl4(float s, float4 a) { return make_float4(s * a.x, s * a.y, s * a.z, s * a.w); }
 __device__ __forceinline__ float dotf4(float4 a, float4 b) { return ((a.x * b.x + a.y * b.y) + a.z * b.z) + a.w * b.w; }
+__device__ __forceinline__ float4 shfl4(float4 v, unsigned src) {
+    return make_float4(__shfl_sync(0xffffffffu, v.x, src), __shfl_sync(0xffffffffu, v.y, src),
+                       __shfl_sync(0xffffffffu, v.z, src), __shfl_sync(0xffffffffu, v.w, src));
+}
 __device__ __forceinline__ float4 abs4(float4 a) { return make_float4(fabsf(a.x), fabsf(a.y), fabsf(a.z), fabsf(a.w)); }
 
 __device__ __forceinline__ float4 bilinear(const Img& m, float u, float v) {
@@ -185,24 +189,43 @@ __global__ void k_scan_vert(Stk2 p) {
     }
 }
 
-/* prefixsum_block2, in place: each block's window shifted by (-1, -1) gets
- * the block's boundary row and column added; windows of different blocks are
- * disjoint. */
-__global__ void __launch_bounds__(256) k_scan_block2(Stk2 p) {
-    __shared__ float4 buf[16][16];
+/* prefixsum_block2, in place: each work-group's window (its 16 x 16 block
+ * shifted by (-1, -1)) gets the window's left column and top row added:
+ * v = pre(X, Y) [+ pre(left, Y) off the left column] [+ top(X) off the top
+ * row], top(X) = pre(X, top) [+ pre(left, top)], the reference's two steps
+ * on its local buffer.  Here 16 lanes walk the 16 columns of a window down
+ * its rows: the left column's value comes by shuffle from the window's lane
+ * 0, the top row's stays in a register — no shared memory, no barriers.
+ * Windows are disjoint, and the fix-ups of the image's last row and column
+ * read only pixels no window covers. */
+__global__ void __launch_bounds__(128) k_scan_block2(Stk2 p, int nbx, int nby) {
     const Img m = p.at(blockIdx.z);
-    const int lx = threadIdx.x, ly = threadIdx.y;
-    const int bx = blockIdx.x * 16, by = blockIdx.y * 16;
-    buf[ly][lx] = tex(m, bx + lx - 1, by + ly - 1);
-    __syncthreads();
-    if (lx) buf[ly][lx] = add4(buf[ly][lx], buf[ly][0]);
-    __syncthreads();
-    if (ly) buf[ly][lx] = add4(buf[ly][lx], buf[0][lx]);
-    const int x = bx + lx, y = by + ly;
-    if (x > m.w || y > m.h || !x || !y) return;
-    put(m, bx + lx - 1, by + ly - 1, buf[ly][lx]);
-    if (y == m.h - 1 && lx < 15 && ly == 15 && x < m.w) put(m, x, y, add4(tex(m, x, y), tex(m, bx - 1, by + ly)));
-    if (x == m.w - 1 && ly < 15 && lx == 15 && y < m.h) put(m, x, y, add4(tex(m, x, y), tex(m, bx + lx, by - 1)));
+    const int lane = threadIdx.x, lx = lane & 15;
+    const int wx = blockIdx.x * 2 + (lane >> 4), wy = blockIdx.y * 4 + threadIdx.y;
+    if (wy >= nby) return;                                  /* the whole warp */
+    const bool live = wx < nbx;
+    const int bx = wx * 16, by = wy * 16;
+    const int X = bx + lx - 1;
+    const unsigned src = lane & 16;                         /* the window's lane 0 */
+    float4 top = tex(m, X, by - 1);
+    {
+        const float4 l0 = shfl4(top, src);
+        if (lx) top = add4(top, l0);
+    }
+    for (int ly = 0; ly < 16; ++ly) {
+        float4 v = top;
+        if (ly) {
+            v = tex(m, X, by + ly - 1);
+            const float4 l = shfl4(v, src);
+            if (lx) v = add4(v, l);
+            v = add4(v, top);
+        }
+        const int x = bx + lx, y = by + ly;
+        if (!live || x > m.w || y > m.h || !x || !y) continue;
+        put(m, X, y - 1, v);
+        if (y == m.h - 1 && lx < 15 && ly == 15 && x < m.w) put(m, x, y, add4(tex(m, x, y), tex(m, bx - 1, by + ly)));
+        if (x == m.w - 1 && ly < 15 && lx == 15 && y < m.h) put(m, x, y, add4(tex(m, x, y), tex(m, bx + lx, by - 1)));
+    }
 }
 
 /* boxfilter_prefixsum: the mean over the box of radius r from the integral
@@ -438,7 +461,8 @@ void scan_rest(Stk2 p, int nz, cudaStream_t st) {
     const int W = p.s[0].w, H = p.s[0].h, nb = nz * p.n;
     k_scan_horiz<<<dim3((H + 127) / 128, 1, nb), 128, 0, st>>>(p);
     k_scan_vert<<<dim3((W + 127) / 128, 1, nb), 128, 0, st>>>(p);
-    k_scan_block2<<<dim3((W + 15) / 16, (H + 15) / 16, nb), dim3(16, 16), 0, st>>>(p);
+    const int nbx = (W + 15) / 16, nby = (H + 15) / 16;   /* the reference's work-groups */
+    k_scan_block2<<<dim3((nbx + 1) / 2, (nby + 3) / 4, nb), dim3(32, 4), 0, st>>>(p, nbx, nby);
 }
 
 Stk stack(float* d, int W, int H, int c) { return Stk{d, W, H, c, (size_t)W * H * c}; }
