@@ -256,7 +256,7 @@ cvtpm_status propagate_view(cvtpm_ctx* ctx, PmPassArgs a, bool exact, bool redbl
     return CVTPM_OK;
 }
 
-/* The neighbour-cost buffer of the FAST shared-window path (8 floats per
+/* The neighbour-cost buffer of the shared-window path (8 floats per
  * pixel).  Used when it fits the context's budget and 60 % of the free device
  * memory; otherwise the propagation evaluates every neighbour per pixel (same
  * results). */
@@ -355,10 +355,8 @@ cvtpm_status run_depthmap(cvtpm_ctx* ctx, const cvtpm_params& p, float* dmap, si
     const float dscale = p.dscale <= 0.0f ? 1.0f / dmax : p.dscale;
     const int N = p.iterations;
     PmPassArgs aL = base_args(ctx, p, W, H, 0), aR = base_args(ctx, p, W, H, 1);
-    if (!exact) {
-        if ((s = ensure_nbcost(ctx, W, H)) != CVTPM_OK) return s;
-        if (ctx->nb_on) aL.nbcost = aR.nbcost = ctx->nbcost;
-    }
+    if ((s = ensure_nbcost(ctx, W, H)) != CVTPM_OK) return s;
+    if (ctx->nb_on) aL.nbcost = aR.nbcost = ctx->nbcost;
     if (!ctx->dcount) {
         if (ctx->no_alloc) return fail(ctx, CVTPM_ERR_ALLOC, "counters not allocated before capture");
         CK(cudaMalloc(&ctx->dcount, 2 * sizeof(unsigned long long)), "counters");
@@ -449,10 +447,8 @@ cvtpm_status run_depthmap_inpaint(cvtpm_ctx* ctx, const cvtpm_params& p, float* 
     const float dmax = p.depthmax;
     const int N = p.iterations;
     PmPassArgs aL = base_args(ctx, p, W, H, 0), aR = base_args(ctx, p, W, H, 1);
-    if (!exact) {
-        if ((s = ensure_nbcost(ctx, W, H)) != CVTPM_OK) return s;
-        if (ctx->nb_on) aL.nbcost = aR.nbcost = ctx->nbcost;
-    }
+    if ((s = ensure_nbcost(ctx, W, H)) != CVTPM_OK) return s;
+    if (ctx->nb_on) aL.nbcost = aR.nbcost = ctx->nbcost;
     if (!ctx->dcount) {
         if (ctx->no_alloc) return fail(ctx, CVTPM_ERR_ALLOC, "counters not allocated before capture");
         CK(cudaMalloc(&ctx->dcount, 2 * sizeof(unsigned long long)), "counters");
@@ -961,9 +957,7 @@ cvtpm_status capture_batch(cvtpm_ctx* ctx, const cvtpm_pair* pairs, int npairs, 
         c->timing = false;
         for (int i : plan[j]) {
             if ((s = ensure_buffers(c, pairs[i].width, pairs[i].height)) != CVTPM_OK) return fail(ctx, s, c->err);
-            if (p.arith == CVTPM_ARITH_FAST &&
-                (s = ensure_nbcost(c, pairs[i].width, pairs[i].height)) != CVTPM_OK)
-                return fail(ctx, s, c->err);
+            if ((s = ensure_nbcost(c, pairs[i].width, pairs[i].height)) != CVTPM_OK) return fail(ctx, s, c->err);
         }
     }
     if (k > 0 && (s = ensure_tables(ctx->lanes[0].c, p, ctx->bstream)) != CVTPM_OK) return fail(ctx, s, ctx->lanes[0].c->err);

@@ -6,6 +6,7 @@
  *  k_records            (fast arithmetic only) value/forward-difference records of a view
  *  k_init<EXACT>        pmhstereo_init (:230-248)
  *  k_propagate<EXACT>   pmhstereo_propagate_view (:286-404) without the scatter
+ *  k_nbcost<EXACT>      its candidates 1-8 (:330-342), plane by plane over shared windows
  *  k_view_list          the scatter of :391-400, made deterministic (smallest source x first)
  *  k_consistency        pmhstereo_consistency (:428-464)
  *  k_fill_state         pmhstereo_fill_state (:466-510)
@@ -140,7 +141,7 @@ __global__ void __launch_bounds__(256) k_propagate(PmPassArgs a) {
      * (:330-342).  With the shared-window costs of k_nbcost (FAST), only
      * neighbours the clamp moves (pixels on the image border) are evaluated
      * here; the others are read. */
-    const bool shared = !EXACT && a.nbcost != nullptr;
+    const bool shared = a.nbcost != nullptr;
 #pragma unroll 1
     for (int b = 0; b < 2; ++b) {
         float4 s[4]; bool act[4]; float c[4];
@@ -273,14 +274,93 @@ __global__ void __launch_bounds__(256) k_propagate(PmPassArgs a) {
 #define NB_COLS 30   /* planes per warp; lanes 30 and 31 feed the shuffles of the row pipeline */
 #define NB_PIPE 1    /* interior warps share weights along the row through shuffles */
 
+/* The plane part of a tap for the shared windows: the position and matching
+ * terms of plane (sx, sy, sz) [EXACT] or (S0, S1, X) [FAST] at tap (qx, qy).
+ * Both depend on the tap's image coordinates and the plane only (EXACT forms
+ * x' = sx*qx + sy*qy + sz from the absolute coordinates, FAST steps its
+ * image-centre-anchored Q31.32 position), so every pixel whose window holds
+ * the tap gets the same values.  Returns false where x' is outside the other
+ * view (the tap is skipped, as eval_costs skips it). */
+template <bool EXACT>
+__device__ __forceinline__ bool nb_tap_terms(const PmCostConsts& k, const PmView& v2, int qx, int qy, size_t jrow,
+                                             float sx, float sy, float sz, long long Xt, float4 a1, float4 g1,
+                                             float& cc, float& gc) {
+    if (EXACT) {
+        const float xp = sx * (float)qx + sy * (float)qy + sz;
+        if (!(xp >= 0.0f && xp < k.Wf)) return false;
+        const float u = xp + 0.5f;
+        const float t = u - 0.5f;
+        const float fi = floorf(t);
+        const float a = t - fi;
+        const int i0 = clampi((int)fi, 0, k.W - 1);
+        const int i1 = clampi((int)fi + 1, 0, k.W - 1);
+        const size_t rb = (size_t)qy * k.W;
+        const float4 c0 = __ldg(&v2.col[rb + i0]), c1 = __ldg(&v2.col[rb + i1]);
+        const float4 h0 = __ldg(&v2.grad[rb + i0]), h1 = __ldg(&v2.grad[rb + i1]);
+        const float oa = 1.0f - a;
+        const float a2x = oa * c0.x + a * c1.x, a2y = oa * c0.y + a * c1.y, a2z = oa * c0.z + a * c1.z;
+        const float g2x = oa * h0.x + a * h1.x, g2y = oa * h0.y + a * h1.y;
+        const float g2z = oa * h0.z + a * h1.z, g2w = oa * h0.w + a * h1.w;
+        const float ci = (fminf(fabsf(a1.x - a2x), k.cmax) + fminf(fabsf(a1.y - a2y), k.cmax)) + fminf(fabsf(a1.z - a2z), k.cmax);
+        const float cg = ((fminf(fabsf(g1.x - g2x), k.gmax) + fminf(fabsf(g1.y - g2y), k.gmax)) + fminf(fabsf(g1.z - g2z), k.gmax)) + fminf(fabsf(g1.w - g2w), k.gmax);
+        cc = k.alpha * ci + k.oma * cg;               /* the tap's combined cost C */
+        gc = 0.0f;
+        return true;
+    } else {
+        const int xi = (int)(Xt >> 32);
+        if ((unsigned)xi >= (unsigned)k.W) return false;
+        fast_tap_terms(k, v2, jrow + xi, pm_fix_frac(Xt), a1, g1, cc, gc);
+        return true;
+    }
+}
+
+/* One user's sums, in eval_costs' operations: EXACT ws += w, r1 += w * C;
+ * FAST r1 = fma(w, cc, r1), r2 = fma(w, gc, r2), ws += w. */
+template <bool EXACT>
+__device__ __forceinline__ void nb_accumulate(float w, float cc, float gc, float& r1, float& r2, float& ws) {
+    if (EXACT) {
+        ws += w;
+        r1 += w * cc;
+    } else {
+        r1 = fmaf(w, cc, r1);
+        r2 = fmaf(w, gc, r2);
+        ws = ws + w;
+    }
+}
+
+/* eval_costs' final value of one user's sums */
+template <bool EXACT>
+__device__ __forceinline__ float nb_final(const PmCostConsts& k, bool fin, float r1, float r2, float ws) {
+    const float v = EXACT ? r1 / ws : fmaf(k.alpha, r1, k.oma * r2) / ws;
+    return (!fin || ws <= 1.1f) ? 1e5f : v;
+}
+
+/* The plane's EXACT coefficients (eval_costs: zero, and an offset never
+ * inside [0, W), for a non-finite state) or FAST fixed-point position. */
+template <bool EXACT>
+__device__ __forceinline__ void nb_plane(const PmCostConsts& k, float4 s, bool fin, float& sx, float& sy, float& sz,
+                                         long long& S0, long long& S1, long long& XA) {
+    if (EXACT) {
+        sx = fin ? s.x : 0.0f;
+        sy = fin ? s.y : 0.0f;
+        sz = fin ? s.z : -1.0e30f;
+        S0 = S1 = XA = 0;
+    } else {
+        sx = sy = sz = 0.0f;
+        pm_fix_plane(fin, s.x, s.y, s.z, k.W / 2, k.H / 2, &S0, &S1, &XA);
+    }
+}
+
 /* Plane (mx, my) with every weight formed by its own lane. */
+template <bool EXACT>
 __device__ __forceinline__ void nbcost_lane(const PmPassArgs& a, int mx, int my) {
     const int W = a.k.W, H = a.k.H, P = a.k.P;
     const size_t n = (size_t)W * H, m = (size_t)my * W + mx;
     const float4 s = a.old[m];
     long long S0, S1, XA;
+    float sx, sy, sz;
     const bool fin = finite3(s);
-    pm_fix_plane(fin, s.x, s.y, s.z, W / 2, H / 2, &S0, &S1, &XA);
+    nb_plane<EXACT>(a.k, s, fin, sx, sy, sz, S0, S1, XA);
     unsigned uok = 0;
 #pragma unroll
     for (int k = 0; k < 8; ++k) {
@@ -317,8 +397,6 @@ __device__ __forceinline__ void nbcost_lane(const PmPassArgs& a, int mx, int my)
         for (int qx = qx0; qx <= qx1; ++qx) {
             const long long Xt = X;
             X += S0;
-            const int xi = (int)(Xt >> 32);
-            if ((unsigned)xi >= (unsigned)W) continue;
             const int rx = qx - mx;
             unsigned mask = rmask;
             if (rx <= -P || rx >= P) {
@@ -331,16 +409,14 @@ __device__ __forceinline__ void nbcost_lane(const PmPassArgs& a, int mx, int my)
             const float4 a1 = __ldg(&c1row[qx]);
             const float4 g1 = __ldg(&g1row[qx]);
             float cc, gc;
-            fast_tap_terms(a.k, a.v2, jrow + xi, pm_fix_frac(Xt), a1, g1, cc, gc);
+            if (!nb_tap_terms<EXACT>(a.k, a.v2, qx, qy, jrow, sx, sy, sz, Xt, a1, g1, cc, gc)) continue;
 #pragma unroll
             for (int k = 0; k < 8; ++k) {
                 if (!((mask >> k) & 1u)) continue;
                 /* user k sees this tap at offset (ry + oy_k, rx + ox_k) */
                 const int nn = k < 4 ? k : k + 1, ox = nn % 3 - 1, oy = nn / 3 - 1;
                 const float w = tap_weight(uc[k], a1, c_prof[(ry + oy + PM_PMAX) * PM_PROF_N + PM_PMAX + rx + ox]);
-                r1[k] = fmaf(w, cc, r1[k]);
-                r2[k] = fmaf(w, gc, r2[k]);
-                ws[k] = ws[k] + w;
+                nb_accumulate<EXACT>(w, cc, gc, r1[k], r2[k], ws[k]);
             }
         }
     }
@@ -348,8 +424,7 @@ __device__ __forceinline__ void nbcost_lane(const PmPassArgs& a, int mx, int my)
     for (int k = 0; k < 8; ++k) {
         if (!((uok >> k) & 1u)) continue;
         const int nn = k < 4 ? k : k + 1, ox = nn % 3 - 1, oy = nn / 3 - 1;
-        const float v = fmaf(a.k.alpha, r1[k], a.k.oma * r2[k]) / ws[k];
-        a.nbcost[(size_t)k * n + m - (size_t)(oy * W + ox)] = (!fin || ws[k] <= 1.1f) ? 1e5f : v;
+        a.nbcost[(size_t)k * n + m - (size_t)(oy * W + ox)] = nb_final<EXACT>(a.k, fin, r1[k], r2[k], ws[k]);
     }
 }
 
@@ -363,13 +438,15 @@ __device__ __forceinline__ void nbcost_lane(const PmPassArgs& a, int mx, int my)
  * offset replace five weight evaluations.  Lanes 30 and 31 own no plane and
  * only supply those values.  Each user still receives its taps in raster
  * order through the operations of eval_costs. */
+template <bool EXACT>
 __device__ __forceinline__ void nbcost_pipe(const PmPassArgs& a, int mx, int my, bool own) {
     const int W = a.k.W, H = a.k.H, P = a.k.P;
     const size_t n = (size_t)W * H, m = (size_t)my * W + mx;
     const float4 s = a.old[m];
     long long S0, S1, XA;
+    float sx, sy, sz;
     const bool fin = finite3(s);
-    pm_fix_plane(fin, s.x, s.y, s.z, W / 2, H / 2, &S0, &S1, &XA);
+    nb_plane<EXACT>(a.k, s, fin, sx, sy, sz, S0, S1, XA);
     unsigned uok = 0;
 #pragma unroll
     for (int k = 0; k < 8; ++k) {
@@ -415,8 +492,7 @@ __device__ __forceinline__ void nbcost_pipe(const PmPassArgs& a, int mx, int my,
             }
             const long long Xt = X;
             X += S0;
-            const int xi = (int)(Xt >> 32);
-            if (!own || (unsigned)xi >= (unsigned)W) continue;
+            if (!own) continue;
             unsigned mask = rmask;
             if (rx <= -P || rx >= P) {
 #pragma unroll
@@ -426,15 +502,13 @@ __device__ __forceinline__ void nbcost_pipe(const PmPassArgs& a, int mx, int my,
                 }
             }
             float cc, gc;
-            fast_tap_terms(a.k, a.v2, jrow + xi, pm_fix_frac(Xt), a1, g1, cc, gc);
+            if (!nb_tap_terms<EXACT>(a.k, a.v2, qx, qy, jrow, sx, sy, sz, Xt, a1, g1, cc, gc)) continue;
 #pragma unroll
             for (int k = 0; k < 8; ++k) {
                 if (!((mask >> k) & 1u)) continue;
                 const int nn = k < 4 ? k : k + 1, ox = nn % 3 - 1, r = nn / 3;
                 const float w = ox > 0 ? wn[r] : (ox == 0 ? w0[r] : wm[r]);
-                r1[k] = fmaf(w, cc, r1[k]);
-                r2[k] = fmaf(w, gc, r2[k]);
-                ws[k] = ws[k] + w;
+                nb_accumulate<EXACT>(w, cc, gc, r1[k], r2[k], ws[k]);
             }
         }
     }
@@ -443,22 +517,22 @@ __device__ __forceinline__ void nbcost_pipe(const PmPassArgs& a, int mx, int my,
     for (int k = 0; k < 8; ++k) {
         if (!((uok >> k) & 1u)) continue;
         const int nn = k < 4 ? k : k + 1, ox = nn % 3 - 1, oy = nn / 3 - 1;
-        const float v = fmaf(a.k.alpha, r1[k], a.k.oma * r2[k]) / ws[k];
-        a.nbcost[(size_t)k * n + m - (size_t)(oy * W + ox)] = (!fin || ws[k] <= 1.1f) ? 1e5f : v;
+        a.nbcost[(size_t)k * n + m - (size_t)(oy * W + ox)] = nb_final<EXACT>(a.k, fin, r1[k], r2[k], ws[k]);
     }
 }
 
+template <bool EXACT>
 __global__ void __launch_bounds__(256, 2) k_nbcost(PmPassArgs a) {
     const int W = a.k.W, H = a.k.H, P = a.k.P;
     const int mx0 = blockIdx.x * NB_COLS, lane = threadIdx.x;
     const int mx = mx0 + lane, my = blockIdx.y * 8 + threadIdx.y;
     if (my >= H) return;                                   /* the whole warp */
     if (NB_PIPE && mx0 - P - 1 >= 0 && mx0 + 31 + P + 1 <= W - 1) {
-        nbcost_pipe(a, mx, my, lane < NB_COLS);
+        nbcost_pipe<EXACT>(a, mx, my, lane < NB_COLS);
         return;
     }
     if (lane >= NB_COLS || mx >= W) return;
-    nbcost_lane(a, mx, my);
+    nbcost_lane<EXACT>(a, mx, my);
 }
 
 /* -------------------------------------------------------- view lists -- */
@@ -874,17 +948,16 @@ cudaError_t pm_launch_cost_field(const PmPassArgs& a, bool exact, const float4* 
 
 cudaError_t pm_launch_propagate(const PmPassArgs& a, bool exact, cudaStream_t st) {
     const dim3 grid = a.color < 0 ? pix_grid(a.k.W, a.k.H) : pix_grid((a.k.W + 1) / 2, a.k.H);
-    if (exact) {
-        k_propagate<true><<<grid, dim3(32, 8), 0, st>>>(a);
-    } else {
-        PmPassArgs b = a;
-        if (b.color >= 0) b.nbcost = nullptr;   /* red/black: neighbours per pixel */
-        if (b.nbcost) {
-            k_nbcost<<<dim3((a.k.W + NB_COLS - 1) / NB_COLS, (a.k.H + 7) / 8), dim3(32, 8), 0, st>>>(b);
-            PM_LAUNCH_CHECK();
-        }
-        k_propagate<false><<<grid, dim3(32, 8), 0, st>>>(b);
+    PmPassArgs b = a;
+    if (b.color >= 0) b.nbcost = nullptr;   /* red/black: neighbours per pixel */
+    const dim3 nbgrid((a.k.W + NB_COLS - 1) / NB_COLS, (a.k.H + 7) / 8);
+    if (b.nbcost) {
+        if (exact) k_nbcost<true><<<nbgrid, dim3(32, 8), 0, st>>>(b);
+        else k_nbcost<false><<<nbgrid, dim3(32, 8), 0, st>>>(b);
+        PM_LAUNCH_CHECK();
     }
+    if (exact) k_propagate<true><<<grid, dim3(32, 8), 0, st>>>(b);
+    else k_propagate<false><<<grid, dim3(32, 8), 0, st>>>(b);
     PM_LAUNCH_CHECK();
     return cudaSuccess;
 }

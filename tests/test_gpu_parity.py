@@ -93,13 +93,18 @@ def test_depthmap_bitexact(stereo, oracle, mode):
     assert_bitexact(nm, ex["normalmap"], "normalmap")
 
 
-def test_shared_windows_match_per_pixel_neighbours(oracle):
-    """FAST: the 8 neighbour candidates evaluated plane by plane over shared
-    windows give the same bits as the per-pixel evaluation
-    (memory budget 0), and both match the oracle."""
+@pytest.mark.parametrize("mode", MODES, ids=MODE_IDS)
+def test_shared_windows_match_per_pixel_neighbours(oracle, mode):
+    """The 8 neighbour candidates evaluated plane by plane over shared
+    windows give the same bits as the per-pixel evaluation (memory budget 0),
+    and both match the oracle — in FAST and in the reference's EXACT
+    arithmetic.  150 pixels wide: the row-pipelined warps and the per-lane
+    border warps both run."""
     from cvt_gb300.stereo import PMHuberStereo
+    arith, rng = mode
     sc = scenes.make_scene(150, 70, 5, 20.0, seed=12)
-    p = default_params(PRESET_BASELINE, patchsize=11, depthmax=20.0, iterations=3, pd_iterations=10)
+    p = default_params(PRESET_BASELINE, arith=arith, rng=rng, patchsize=11, depthmax=20.0, iterations=3,
+                       pd_iterations=10)
     outs = []
     for budget in (None, 0):
         st = PMHuberStereo(0)
