@@ -230,3 +230,27 @@ def test_depthmap_inpaint_redblack_bitexact(stereo, oracle):
     want, ex = oracle.depthmap_inpaint(p, sc.left, sc.right, trace=True)
     assert_bitexact(tr["states"].cpu().numpy(), ex["states"], "states")
     assert_bitexact(dm.cpu().numpy(), want, "dmap")
+
+
+@pytest.mark.parametrize("mode", [(ARITH_FAST, RNG_PHILOX), (ARITH_EXACT, RNG_MWC64X)], ids=["bench", "reference"])
+def test_bench_configuration_band_bitexact(stereo, oracle, mode):
+    """The bench's own configuration on a band of its pair: rows 0-47 of the
+    1242x375 scene (2 % salt, gain/bias), 35x35 window, dmax 128, LR
+    threshold 1 px, 250 PD steps, 2 iterations (theta stays 0; the ramp has
+    its own test) — in the bench's arithmetic and in the reference's."""
+    arith, rng = mode
+    sc = scenes.config_scene(2, pair=0)
+    left = np.ascontiguousarray(sc.left[:48])
+    right = np.ascontiguousarray(sc.right[:48])
+    p = default_params(PRESET_BASELINE, arith=arith, rng=rng, patchsize=17, depthmax=128.0, iterations=2,
+                       maxdispdiff=1.0)
+    stereo.set_params(p)
+    dm = torch.empty(0, device="cuda")
+    tr = {}
+    stereo.depthMap(dm, to_dev(left), to_dev(right), 17, 128.0, 2, 4, trace=tr)
+    torch.cuda.synchronize()
+    want, ex = oracle.depthmap(p, left, right, trace=True)
+    assert_bitexact(tr["winners"].cpu().numpy(), ex["winners"], "winners")
+    assert_bitexact(tr["valid"].cpu().numpy(), ex["valid"], "valid")
+    assert_bitexact(tr["states"].cpu().numpy(), ex["states"], "states")
+    assert_bitexact(dm.cpu().numpy(), want, "dmap")
