@@ -1,6 +1,6 @@
 """TEST INFRASTRUCTURE: the reference's own rectification and warp code
-(oracle/_ref/libpmref_rect.so, built by build_ref.build_rect from the sources
-under /root/reference), with the signatures of oracle.oracle.stereo_rectify
+(oracle/_ref/libpmref_rect.so, built by build_ref.build_rect from the
+reference's sources where build_ref finds them), with the signatures of oracle.oracle.stereo_rectify
 and oracle.oracle.warp.  available() is False where the sources are absent."""
 from __future__ import annotations
 

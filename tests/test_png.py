@@ -242,7 +242,8 @@ def test_corrupt_and_unsupported(tmp_path):
 
 
 def test_reference_data_images():
-    files = sorted(glob.glob("/root/reference/data/*.png"))
+    from oracle.ref_emu import build_ref
+    files = sorted(glob.glob(os.path.join(build_ref.REF, "data", "*.png")))
     if not files:
         pytest.skip("reference data absent")
     for f in files[:12]:
