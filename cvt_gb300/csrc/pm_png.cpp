@@ -66,22 +66,32 @@ void put_be32(std::vector<uint8_t>* o, uint32_t v) {
 
 /* ---------------------------------------------------------- checks -- */
 /* CRC-32 of the chunks: reflected polynomial 0xEDB88320, initial and final
- * value all ones. */
+ * value all ones.  Eight bytes per step ("slicing by 8"): t[k][b] is the CRC
+ * contribution of byte b followed by k zero bytes, so the eight table
+ * lookups of one step are independent. */
 struct CrcTable {
-    uint32_t t[256];
+    uint32_t t[8][256];
     CrcTable() {
         for (uint32_t n = 0; n < 256; ++n) {
             uint32_t c = n;
             for (int k = 0; k < 8; ++k) c = (c & 1) ? 0xEDB88320u ^ (c >> 1) : c >> 1;
-            t[n] = c;
+            t[0][n] = c;
         }
+        for (int k = 1; k < 8; ++k)
+            for (uint32_t n = 0; n < 256; ++n) t[k][n] = (t[k - 1][n] >> 8) ^ t[0][t[k - 1][n] & 0xff];
     }
 };
 
 uint32_t crc32(const uint8_t* p, size_t n, uint32_t crc = 0) {
     static const CrcTable tab;
     crc = ~crc;
-    for (size_t i = 0; i < n; ++i) crc = tab.t[(crc ^ p[i]) & 0xff] ^ (crc >> 8);
+    size_t i = 0;
+    for (; i + 8 <= n; i += 8) {
+        const uint32_t lo = crc ^ ((uint32_t)p[i] | (uint32_t)p[i + 1] << 8 | (uint32_t)p[i + 2] << 16 | (uint32_t)p[i + 3] << 24);
+        crc = tab.t[7][lo & 0xff] ^ tab.t[6][(lo >> 8) & 0xff] ^ tab.t[5][(lo >> 16) & 0xff] ^ tab.t[4][lo >> 24] ^
+              tab.t[3][p[i + 4]] ^ tab.t[2][p[i + 5]] ^ tab.t[1][p[i + 6]] ^ tab.t[0][p[i + 7]];
+    }
+    for (; i < n; ++i) crc = tab.t[0][(crc ^ p[i]) & 0xff] ^ (crc >> 8);
     return ~crc;
 }
 
@@ -253,8 +263,9 @@ std::string inflate_zlib(const uint8_t* z, size_t n, size_t expect, std::vector<
     const int cmf = z[0], flg = z[1];
     if ((cmf & 15) != 8 || (cmf >> 4) > 7 || (cmf * 256 + flg) % 31) return "bad zlib header";
     if (flg & 32) return "zlib preset dictionary not allowed";
-    out->clear();
-    out->reserve(expect);
+    out->assign(expect, 0);
+    uint8_t* const o = out->data();
+    size_t on = 0;                                   /* bytes written */
     BitReader br(z + 2, n - 2);
     for (int last = 0; !last;) {
         last = (int)br.bits(1);
@@ -264,8 +275,8 @@ std::string inflate_zlib(const uint8_t* z, size_t n, size_t expect, std::vector<
             const uint32_t len = br.bits(16), nlen = br.bits(16);
             if ((len ^ 0xffff) != nlen) return "stored block length check failed";
             for (uint32_t i = 0; i < len; ++i) {
-                if (out->size() >= expect) return "more image data than the header describes";
-                out->push_back((uint8_t)br.bits(8));
+                if (on >= expect) return "more image data than the header describes";
+                o[on++] = (uint8_t)br.bits(8);
             }
             if (br.overrun) return "truncated stored block";
             continue;
@@ -311,8 +322,8 @@ std::string inflate_zlib(const uint8_t* z, size_t n, size_t expect, std::vector<
             const int s = decode(&br, lit);
             if (s < 0 || br.overrun) return "bad literal/length code";
             if (s < 256) {
-                if (out->size() >= expect) return "more image data than the header describes";
-                out->push_back((uint8_t)s);
+                if (on >= expect) return "more image data than the header describes";
+                o[on++] = (uint8_t)s;
                 continue;
             }
             if (s == 256) break;
@@ -322,14 +333,15 @@ std::string inflate_zlib(const uint8_t* z, size_t n, size_t expect, std::vector<
             if (ds < 0 || ds > 29) return "bad distance symbol";
             const size_t d = DIST_BASE[ds] + br.bits(DIST_EXTRA[ds]);
             if (br.overrun) return "truncated compressed data";
-            if (d > out->size()) return "distance before the start of the data";
-            if (out->size() + len > expect) return "more image data than the header describes";
-            const size_t from = out->size() - d;
-            for (size_t i = 0; i < len; ++i) out->push_back((*out)[from + i]);   /* overlapping copies repeat */
+            if (d > on) return "distance before the start of the data";
+            if (on + len > expect) return "more image data than the header describes";
+            const uint8_t* from = o + on - d;
+            for (size_t i = 0; i < len; ++i) o[on + i] = from[i];   /* byte by byte: overlapping copies repeat */
+            on += len;
         }
         if (br.overrun) return "truncated compressed data";
     }
-    if (out->size() != expect) return "less image data than the header describes";
+    if (on != expect) return "less image data than the header describes";
     br.align();
     uint8_t a[4];
     for (int i = 0; i < 4; ++i) a[i] = (uint8_t)br.bits(8);
@@ -469,7 +481,9 @@ struct Png {
 
 const int ADAM7[7][4] = {{0, 0, 8, 8}, {4, 0, 8, 8}, {0, 4, 4, 8}, {2, 0, 4, 4}, {0, 2, 2, 4}, {1, 0, 2, 2}, {0, 1, 1, 2}};
 
-std::string parse(const std::vector<uint8_t>& d, Png* png) {
+/* The chunks of a PNG file; with header_only, parsing stops at the first
+ * IDAT (IHDR, PLTE and tRNS precede it), which is all the format needs. */
+std::string parse(const std::vector<uint8_t>& d, Png* png, bool header_only = false) {
     static const uint8_t SIG[8] = {137, 80, 78, 71, 13, 10, 26, 10};
     if (d.size() < 8 || memcmp(d.data(), SIG, 8)) return "Invalid PNG image header";
     size_t pos = 8;
@@ -480,9 +494,10 @@ std::string parse(const std::vector<uint8_t>& d, Png* png) {
         if (len > 0x7fffffffu || d.size() - pos - 12 < len) return "truncated chunk";
         const uint8_t* type = &d[pos + 4];
         const uint8_t* data = type + 4;
-        if (crc32(type, 4 + (size_t)len) != be32(data + len)) return "chunk CRC mismatch";
         const std::string t((const char*)type, 4);
         if (!ihdr && t != "IHDR") return "IHDR is not the first chunk";
+        if (header_only && t == "IDAT") break;
+        if (crc32(type, 4 + (size_t)len) != be32(data + len)) return "chunk CRC mismatch";
         if (t == "IHDR") {
             if (ihdr || len != 13) return "bad IHDR";
             png->w = be32(data);
@@ -599,6 +614,44 @@ void emit(const Png& p, const uint8_t* row, size_t sx, uint8_t* out, size_t stri
     }
 }
 
+/* one unfiltered row of a pass into the output: 8-bit gray, gray + alpha,
+ * RGB and RGBA without tRNS by plain byte loops, the rest through emit */
+void emit_row(const Png& p, const uint8_t* row, size_t pw, uint8_t* out, size_t stride, size_t x0, size_t dx,
+              size_t y, bool le) {
+    uint8_t* o = out + y * stride;
+    if (p.depth == 8 && !p.has_trns && p.ctype != 3) {
+        switch (p.ctype) {
+        case 0:
+            for (size_t i = 0; i < pw; ++i) o[x0 + i * dx] = row[i];
+            return;
+        case 4:
+            for (size_t i = 0; i < pw; ++i) {
+                uint8_t* q = o + (x0 + i * dx) * 2;
+                q[0] = row[2 * i];
+                q[1] = row[2 * i + 1];
+            }
+            return;
+        case 2:
+            for (size_t i = 0; i < pw; ++i) {
+                uint8_t* q = o + (x0 + i * dx) * 4;
+                q[0] = row[3 * i];
+                q[1] = row[3 * i + 1];
+                q[2] = row[3 * i + 2];
+                q[3] = 255;
+            }
+            return;
+        default:
+            if (dx == 1) {
+                memcpy(o + x0 * 4, row, pw * 4);
+                return;
+            }
+            for (size_t i = 0; i < pw; ++i) memcpy(o + (x0 + i * dx) * 4, row + 4 * i, 4);
+            return;
+        }
+    }
+    for (size_t i = 0; i < pw; ++i) emit(p, row, i, out, stride, x0 + i * dx, y, le);
+}
+
 std::string decode_pixels(const Png& p, uint8_t* out, size_t stride) {
     std::vector<uint8_t> raw;
     const std::string e = inflate_zlib(p.idat.data(), p.idat.size(), stream_size(p), &raw);
@@ -616,7 +669,7 @@ std::string decode_pixels(const Png& p, uint8_t* out, size_t stride) {
         for (size_t r = 0; r < ph; ++r) {
             uint8_t* row = raw.data() + pos + 1;
             if (!unfilter(raw[pos], row, prior.data(), len, bpp)) return "bad filter type";
-            for (size_t i = 0; i < pw; ++i) emit(p, row, i, out, stride, x0 + i * dx, y0 + r * dy, le);
+            emit_row(p, row, pw, out, stride, x0, dx, y0 + r * dy, le);
             memcpy(prior.data(), row, len);
             pos += 1 + len;
         }
@@ -683,7 +736,7 @@ cvtpm_status cvtpm_png_read(const char* path, cvtpm_image* img) {
     std::vector<uint8_t> d;
     if (!read_file(path, &d)) return fail(CVTPM_ERR_IO, std::string("Cannot open PNG file: ") + path);
     Png p;
-    std::string e = parse(d, &p);
+    std::string e = parse(d, &p, !img->data);
     if (!e.empty()) return fail(e == "Unsupported PNG format" ? CVTPM_ERR_NOT_SUPPORTED : CVTPM_ERR_IO, "png read: " + e);
     const int fmt = p.out_format();
     const size_t bpp = cvtpm_iformat_bpp(fmt), row = (size_t)p.w * bpp;
