@@ -15,6 +15,7 @@
 #include <stdlib.h>
 #include <string.h>
 
+#include <new>
 #include <string>
 #include <vector>
 
@@ -28,6 +29,10 @@ cvtpm_status fail(cvtpm_status s, const std::string& m) {
     pm_set_free_error(m);
     return s;
 }
+
+/* a host allocation sized by the file or image failed: no exception leaves
+ * the C ABI */
+cvtpm_status pm_out_of_memory() { return fail(CVTPM_ERR_ALLOC, "host memory exhausted"); }
 
 bool read_file(const char* path, std::vector<unsigned char>* out) {
     FILE* f = fopen(path, "rb");
@@ -79,7 +84,7 @@ bool to_int(const std::string& t, long* v) {
 
 extern "C" {
 
-cvtpm_status cvtpm_raw_read(const char* path, cvtpm_image* img) {
+static cvtpm_status cvtpm_raw_read_impl(const char* path, cvtpm_image* img) {
     if (!path || !img) return fail(CVTPM_ERR_INVALID_ARGUMENT, "raw read: path or descriptor is NULL");
     std::vector<unsigned char> d;
     if (!read_file(path, &d)) return fail(CVTPM_ERR_IO, std::string("raw read: cannot read ") + path);
@@ -107,7 +112,15 @@ cvtpm_status cvtpm_raw_read(const char* path, cvtpm_image* img) {
     return CVTPM_OK;
 }
 
-cvtpm_status cvtpm_raw_write(const char* path, const cvtpm_image* img) {
+cvtpm_status cvtpm_raw_read(const char* path, cvtpm_image* img) {
+    try {
+        return cvtpm_raw_read_impl(path, img);
+    } catch (const std::bad_alloc&) {
+        return pm_out_of_memory();
+    }
+}
+
+static cvtpm_status cvtpm_raw_write_impl(const char* path, const cvtpm_image* img) {
     if (!path || !img || !img->data) return fail(CVTPM_ERR_INVALID_ARGUMENT, "raw write: NULL argument");
     const size_t bpp = cvtpm_iformat_bpp(img->format);
     if (!bpp) return fail(CVTPM_ERR_INVALID_ARGUMENT, "raw write: unknown format");
@@ -123,7 +136,15 @@ cvtpm_status cvtpm_raw_write(const char* path, const cvtpm_image* img) {
     return ok ? CVTPM_OK : fail(CVTPM_ERR_IO, std::string("raw write: write failed for ") + path);
 }
 
-cvtpm_status cvtpm_ppm_read(const char* path, cvtpm_image* img) {
+cvtpm_status cvtpm_raw_write(const char* path, const cvtpm_image* img) {
+    try {
+        return cvtpm_raw_write_impl(path, img);
+    } catch (const std::bad_alloc&) {
+        return pm_out_of_memory();
+    }
+}
+
+static cvtpm_status cvtpm_ppm_read_impl(const char* path, cvtpm_image* img) {
     if (!path || !img) return fail(CVTPM_ERR_INVALID_ARGUMENT, "ppm read: path or descriptor is NULL");
     std::vector<unsigned char> d;
     if (!read_file(path, &d)) return fail(CVTPM_ERR_IO, std::string("ppm read: cannot read ") + path);
@@ -190,7 +211,15 @@ cvtpm_status cvtpm_ppm_read(const char* path, cvtpm_image* img) {
     return CVTPM_OK;
 }
 
-cvtpm_status cvtpm_pfm_write(const char* path, const cvtpm_image* img) {
+cvtpm_status cvtpm_ppm_read(const char* path, cvtpm_image* img) {
+    try {
+        return cvtpm_ppm_read_impl(path, img);
+    } catch (const std::bad_alloc&) {
+        return pm_out_of_memory();
+    }
+}
+
+static cvtpm_status cvtpm_pfm_write_impl(const char* path, const cvtpm_image* img) {
     if (!path || !img || !img->data) return fail(CVTPM_ERR_INVALID_ARGUMENT, "pfm write: NULL argument");
     int ch;
     if (img->format == CVTPM_IFORMAT_GRAY_FLOAT) ch = 1;
@@ -218,6 +247,14 @@ cvtpm_status cvtpm_pfm_write(const char* path, const cvtpm_image* img) {
     }
     ok = (fclose(f) == 0) && ok;
     return ok ? CVTPM_OK : fail(CVTPM_ERR_IO, std::string("pfm write: write failed for ") + path);
+}
+
+cvtpm_status cvtpm_pfm_write(const char* path, const cvtpm_image* img) {
+    try {
+        return cvtpm_pfm_write_impl(path, img);
+    } catch (const std::bad_alloc&) {
+        return pm_out_of_memory();
+    }
 }
 
 }  // extern "C"

@@ -34,6 +34,7 @@
 #include <stdio.h>
 #include <string.h>
 
+#include <new>
 #include <string>
 #include <vector>
 
@@ -47,6 +48,10 @@ cvtpm_status fail(cvtpm_status s, const std::string& m) {
     pm_set_free_error(m);
     return s;
 }
+
+/* a host allocation sized by the file or image failed: no exception leaves
+ * the C ABI */
+cvtpm_status pm_out_of_memory() { return fail(CVTPM_ERR_ALLOC, "host memory exhausted"); }
 
 bool host_little_endian() {
     const uint16_t v = 1;
@@ -653,8 +658,13 @@ void emit_row(const Png& p, const uint8_t* row, size_t pw, uint8_t* out, size_t 
 }
 
 std::string decode_pixels(const Png& p, uint8_t* out, size_t stride) {
+    /* DEFLATE expands at most 1032:1 (258-byte matches in ~2-bit codes):
+     * refuse a header that the compressed data cannot fill before
+     * allocating for it */
+    const size_t need = stream_size(p);
+    if (need / 1032 > p.idat.size() + 64) return "less image data than the header describes";
     std::vector<uint8_t> raw;
-    const std::string e = inflate_zlib(p.idat.data(), p.idat.size(), stream_size(p), &raw);
+    const std::string e = inflate_zlib(p.idat.data(), p.idat.size(), need, &raw);
     if (!e.empty()) return e;
     const size_t bits = (size_t)p.depth * p.channels(), bpp = bits >= 8 ? bits / 8 : 1;
     const bool le = host_little_endian();
@@ -731,7 +741,7 @@ extern "C" {
 
 uint8_t cvtpm_float_to_srgb_u8(float v) { return f_to_srgb_u8(v); }
 
-cvtpm_status cvtpm_png_read(const char* path, cvtpm_image* img) {
+static cvtpm_status cvtpm_png_read_impl(const char* path, cvtpm_image* img) {
     if (!path || !img) return fail(CVTPM_ERR_INVALID_ARGUMENT, "png read: path or descriptor is NULL");
     std::vector<uint8_t> d;
     if (!read_file(path, &d)) return fail(CVTPM_ERR_IO, std::string("Cannot open PNG file: ") + path);
@@ -754,7 +764,15 @@ cvtpm_status cvtpm_png_read(const char* path, cvtpm_image* img) {
     return CVTPM_OK;
 }
 
-cvtpm_status cvtpm_png_write(const char* path, const cvtpm_image* img) {
+cvtpm_status cvtpm_png_read(const char* path, cvtpm_image* img) {
+    try {
+        return cvtpm_png_read_impl(path, img);
+    } catch (const std::bad_alloc&) {
+        return pm_out_of_memory();
+    }
+}
+
+static cvtpm_status cvtpm_png_write_impl(const char* path, const cvtpm_image* img) {
     if (!path || !img || !img->data) return fail(CVTPM_ERR_INVALID_ARGUMENT, "png write: NULL argument");
     const int f = img->format;
     const int W = img->width, H = img->height;
@@ -849,6 +867,14 @@ cvtpm_status cvtpm_png_write(const char* path, const cvtpm_image* img) {
     const bool ok = fwrite(out.data(), 1, out.size(), fp) == out.size();
     if (fclose(fp) != 0 || !ok) return fail(CVTPM_ERR_IO, std::string("png write: cannot write ") + path);
     return CVTPM_OK;
+}
+
+cvtpm_status cvtpm_png_write(const char* path, const cvtpm_image* img) {
+    try {
+        return cvtpm_png_write_impl(path, img);
+    } catch (const std::bad_alloc&) {
+        return pm_out_of_memory();
+    }
 }
 
 }  // extern "C"

@@ -262,3 +262,15 @@ def test_reference_data_images():
         want, wfmt = expected(s, ct, dp, plte, trns)
         assert fmt == wfmt, f
         assert np.array_equal(got.reshape(want.shape), want), f
+
+
+def test_header_larger_than_its_data_is_refused(tmp_path):
+    """a 20000 x 20000 header over a few bytes of IDAT: refused before the
+    decoder allocates for it (DEFLATE expands at most 1032:1)"""
+    raw = zlib.compress(b"\x00" * 1000)
+    data = pngtool.SIG + pngtool.chunk(b"IHDR", struct.pack(">IIBBBBB", 20000, 20000, 8, 0, 0, 0, 0))
+    data += pngtool.chunk(b"IDAT", raw) + pngtool.chunk(b"IEND", b"")
+    p = tmp_path / "big.png"
+    p.write_bytes(data)
+    with pytest.raises(_lib.CvtpmError, match="less image data"):
+        imageio.read_png(p)          # the 400 MB output array is allocated lazily and never written
