@@ -141,6 +141,14 @@ __device__ __forceinline__ void tsdf_add_voxel(float2* __restrict__ cv, int W, i
                                                const float* __restrict__ dmap, size_t dpitch4, int iw, int ih,
                                                float dscale, const DMat4& tg2cam, float trunc) {
     const float4 g = xform(tg2cam, make_float4((float)x, (float)y, (float)z, 1.0f));
+    /* Voxels the update would skip anyway, found without the two divisions:
+     * it needs g.z > 0 (the depth read before that test has no effect), and
+     * for g.z > 0 a numerator beyond -2 g.z or (size + 2) g.z makes the
+     * rounded quotient < 0 or > size (the product rounds by at most one part
+     * in 2^24).  NaN and infinite values fall through to the full test. */
+    if (!(g.z > 0.0f)) return;
+    const float lo = -2.0f * g.z;
+    if (g.x < lo || g.y < lo || g.x > ((float)iw + 2.0f) * g.z || g.y > ((float)ih + 2.0f) * g.z) return;
     const float ix = g.x / g.z, iy = g.y / g.z;
     if (ix < (float)iw && iy < (float)ih && ix >= 0.0f && iy >= 0.0f) {
         const float d = dmap[(size_t)(int)floorf(iy) * dpitch4 + (int)floorf(ix)] * dscale;   /* nearest texel */
