@@ -228,8 +228,8 @@ cvtpm_status cvtpm_polish_planes(cvtpm_ctx* ctx, const float* img1, const float*
                                  float* planes, int lr, int steps, float* cost,
                                  void* stream);
 
-/* Device memory the context may use for the FAST path's shared-window
- * neighbour costs: 32 bytes per pixel (the costs of the 8 neighbour
+/* Device memory the context may use for the propagation's shared-window
+ * neighbour costs (FAST and EXACT): 32 bytes per pixel (the costs of the 8 neighbour
  * candidates).  Within the budget (and 60 % of the free memory) the 8
  * neighbour candidates of a pass are evaluated once per plane over the union
  * of their windows; otherwise per pixel.  Results are identical either way.
