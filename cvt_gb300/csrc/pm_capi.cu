@@ -46,7 +46,7 @@ struct cvtpm_ctx {
     uint8_t* win[2];
     uint8_t* valid;
     float* occ;                       /* occlusion mask of depthMapInpaint */
-    /* FAST shared-window neighbour costs: the costs of candidates 1-8 per
+    /* shared-window neighbour costs (FAST and EXACT): the costs of candidates 1-8 per
      * pixel ([8][W*H] floats), when the budget allows */
     float* nbcost = nullptr;
     size_t nb_bytes = 0;

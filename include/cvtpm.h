@@ -279,7 +279,7 @@ cvtpm_status cvtpm_depthmap_batched(cvtpm_ctx* ctx, const cvtpm_pair* pairs,
 #define CVTPM_BATCH_MAX_CAND 8
 typedef struct cvtpm_batch_info {
     int lanes;                 /* lanes of the current graph */
-    int shared_windows;        /* FAST shared-window neighbour costs in use (within the memory budget) */
+    int shared_windows;        /* shared-window neighbour costs in use (within the memory budget) */
     int tuned;                 /* 1 if the autotuner chose the configuration */
     int ncand;
     int cand_lanes[CVTPM_BATCH_MAX_CAND];
