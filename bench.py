@@ -38,6 +38,9 @@ WORKLOAD = "plain PatchMatch depthMap, 1 pair 1242x375 RGBA f32, 16 planes, dmax
 METRIC = "PatchMatch Mpix-iter/s (plain depthMap, 1242x375, 8 iterations)"
 FLOPS_PER_TAP = 55.0          # per (pixel, candidate) window tap: plane, lerp, truncated L1, accumulate
 FLOPS_PER_WEIGHT_TAP = 20.0   # bilateral weight of a tap, once per pixel and launch
+RECORD_BYTES_PER_TAP = 56.0   # the other view's value/difference records one evaluated tap reads (FAST)
+L1_BYTES_PER_CLK_SM = 128.0   # L1/shared data path of one SM
+N_SM = 152
 QUALITY_PAIRS = 8
 PD_BYTES_PER_PX = 116.0       # u 16 + p 32 + f 16 + w 4 read; u 16 + p 32 written
 
@@ -300,6 +303,18 @@ def run_ours(args, rank, world, local_rank):
                    "per": "PD step (algorithmic bytes of one step / time of one step)",
                    "steps_per_launch": stats["pd_steps"] / max(1, stats["pd_launches"]),
                    "note": "the blocked kernel keeps 4 steps in shared memory, so it moves fewer bytes than one step's algorithmic count"}
+    # the propagation's limiter is the L1 data path: its record bytes against
+    # 128 B per clock and SM at the sampled clock
+    clocks = clk.summary()
+    l1_peak = (N_SM * L1_BYTES_PER_CLK_SM * clocks["sm_mhz"] * 1e6 / 1e9) if clocks.get("sm_mhz") else None
+    l1_achieved = stats["cost_taps"] / nprop * RECORD_BYTES_PER_TAP / (prop_ms * 1e-3) / 1e9
+    roofline_l1 = {"kernel": "k_propagate<fast> + k_nbcost (the propagation pass)", "bound": "l1",
+                   "achieved": l1_achieved, "peak": l1_peak, "unit": "GB/s",
+                   "frac": (l1_achieved / l1_peak) if l1_peak else None,
+                   "per": "pass: device-counted evaluated taps x 56 record bytes (a lower bound: image-1 reads, "
+                          "weights and misaligned 128-byte lines come on top; ncu measures the L1 data pipe at "
+                          "81-88 % busy) / pass time",
+                   "peak_source": "152 SMs x 128 B/clk x the median SM clock sampled during the timed region"}
     cpu = None
     if not args.no_cpu_baseline:
         from cvt_gb300.params import ARITH_EXACT, RNG_MWC64X
@@ -316,14 +331,15 @@ def run_ours(args, rank, world, local_rank):
                        "l2": "flushed between steps (256 MB write)", "parallelism": "replicas" if world > 1 else "1 GPU"},
             "e2e": {"value": e2e, "unit": "Mpix-iter/s", "h2d_bytes_per_step": 2 * W * H * 16,
                     "d2h_bytes_per_step": W * H * 4},
-            "roofline": roofline, "roofline_pd": roofline_pd, "cpu_baseline": cpu, "exact_arithmetic": exact,
+            "roofline": roofline, "roofline_l1": roofline_l1, "roofline_pd": roofline_pd, "cpu_baseline": cpu,
+            "exact_arithmetic": exact,
             "quality": {"bad1_nonocc_pct": bad1, "epe_nonocc_px": epe,
                         "pairs": QUALITY_PAIRS,
                         "bad1_nonocc_pct_mean": float(np.mean(qual["ours"])),
                         "reference_algorithm_bad1_nonocc_pct_mean": float(np.mean(qual["reference"])),
                         "note": "first two: the timed pair; means over pairs 0-7 (untimed); reference algorithm = "
                                 "EXACT arithmetic + MWC64X; a different RNG stream moves one pair's bad-1px by ~0.3 pp"},
-            "clocks": clk.summary(), "gpu_launches": stats["launches"], "wall_s": wall}
+            "clocks": clocks, "gpu_launches": stats["launches"], "wall_s": wall}
     print(json.dumps(line), flush=True)
     return 0
 
