@@ -254,3 +254,31 @@ def test_bench_configuration_band_bitexact(stereo, oracle, mode):
     assert_bitexact(tr["valid"].cpu().numpy(), ex["valid"], "valid")
     assert_bitexact(tr["states"].cpu().numpy(), ex["states"], "states")
     assert_bitexact(dm.cpu().numpy(), want, "dmap")
+
+
+@pytest.mark.parametrize("seed", [11, 12, 13])
+def test_random_configurations_bitexact(stereo, oracle, seed):
+    """Seeded random configurations: sizes 8-89 x 4-59, windows 3x3-35x35,
+    dmax, iterations, PD steps, presets, the four arithmetic/RNG modes, both
+    schedules, LR thresholds — disparity map, states and winners bit for bit
+    against the oracle."""
+    from cvt_gb300 import params as P
+    rng = np.random.default_rng(seed)
+    for case in range(12):
+        W, H = int(rng.integers(8, 90)), int(rng.integers(4, 60))
+        patch, dmax = int(rng.integers(1, 18)), float(rng.choice([4.0, 9.5, 16.0, 33.0]))
+        iters = int(rng.integers(1, 5))
+        kw = dict(arith=[P.ARITH_EXACT, P.ARITH_FAST][int(rng.integers(2))],
+                  rng=[P.RNG_MWC64X, P.RNG_PHILOX][int(rng.integers(2))], patchsize=patch, depthmax=dmax,
+                  iterations=iters, pd_iterations=int(rng.integers(0, 40)), seed=int(rng.integers(1 << 30)))
+        if rng.random() < 0.25:
+            kw["schedule"] = P.SCHEDULE_REDBLACK
+        if rng.random() < 0.3:
+            kw["maxdispdiff"] = 1.0
+        p = P.default_params([P.PRESET_REFERENCE, P.PRESET_BASELINE][int(rng.integers(2))], **kw)
+        sc = scenes.make_scene(W, H, int(rng.integers(1, 5)), dmax, seed=int(rng.integers(1 << 20)))
+        dm, _, tr, want, ex = run_both(stereo, oracle, sc, p, normalmap=False)
+        what = f"case {case}: {W}x{H} {kw}"
+        assert_bitexact(dm, want, "dmap " + what)
+        assert_bitexact(tr["states"], ex["states"], "states " + what)
+        assert_bitexact(tr["winners"], ex["winners"], "winners " + what)
