@@ -107,8 +107,13 @@ __global__ void __launch_bounds__(256) k_cost_field(PmPassArgs a, const float4* 
 }
 
 /* --------------------------------------------------------- propagate -- */
+/* Register budgets, measured per 1242x375 depthMap: EXACT allowed one block
+ * per SM takes 128 registers and still fits two (630 against 644 ms with
+ * the 111 it took under the plain 256-thread bound); FAST needs the
+ * two-block cap (it takes 153 registers and one block per SM otherwise: pass
+ * 39.2 against 31.6 ms), where it also stops spilling. */
 template <bool EXACT>
-__global__ void __launch_bounds__(256) k_propagate(PmPassArgs a) {
+__global__ void __launch_bounds__(256, EXACT ? 1 : 2) k_propagate(PmPassArgs a) {
     const int W = a.k.W, H = a.k.H;
     const int y = blockIdx.y * 8 + threadIdx.y;
     /* red/black passes: thread t of a row owns the t-th pixel of that colour */
