@@ -18,6 +18,7 @@
 #include <cstring>
 #include <mutex>
 #include <string>
+#include <new>
 #include <vector>
 
 #include "cvtpm.h"
@@ -1049,7 +1050,7 @@ cvtpm_status tune_batch(cvtpm_ctx* ctx, const cvtpm_pair* pairs, int npairs, int
 
 }  // namespace
 
-cvtpm_status cvtpm_depthmap_batched(cvtpm_ctx* ctx, const cvtpm_pair* pairs, int npairs, void* stream) {
+static cvtpm_status depthmap_batched(cvtpm_ctx* ctx, const cvtpm_pair* pairs, int npairs, void* stream) {
     if (!ctx) return CVTPM_ERR_INVALID_ARGUMENT;
     if (!pairs || npairs < 1) return fail(ctx, CVTPM_ERR_INVALID_ARGUMENT, "no pairs");
     cvtpm_status s;
@@ -1107,6 +1108,16 @@ cvtpm_status cvtpm_depthmap_batched(cvtpm_ctx* ctx, const cvtpm_pair* pairs, int
     ctx->binfo.graph_nodes = (long long)nodes;
     ctx->binfo.replays = 0;
     return launch_batch(ctx, ctx->bexec, st);
+}
+
+/* the lane plans are sized by npairs: a failed host allocation becomes a
+ * status, no exception leaves the C ABI */
+cvtpm_status cvtpm_depthmap_batched(cvtpm_ctx* ctx, const cvtpm_pair* pairs, int npairs, void* stream) {
+    try {
+        return depthmap_batched(ctx, pairs, npairs, stream);
+    } catch (const std::bad_alloc&) {
+        return ctx ? fail(ctx, CVTPM_ERR_ALLOC, "host memory exhausted") : CVTPM_ERR_ALLOC;
+    }
 }
 
 cvtpm_status cvtpm_set_batch_lanes(cvtpm_ctx* ctx, int lanes) {
