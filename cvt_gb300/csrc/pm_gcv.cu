@@ -37,6 +37,8 @@
 #include <stdint.h>
 
 #include <atomic>
+#include <map>
+#include <mutex>
 #include <string>
 
 #include "cvtpm.h"
@@ -448,11 +450,6 @@ cvtpm_status fail(cvtpm_status s, const std::string& m) {
 dim3 g16(int W, int H) { return dim3((W + 15) / 16, (H + 15) / 16); }
 dim3 g32(int W, int H) { return dim3((W + 31) / 32, (H + 7) / 8); }
 
-struct Scratch {
-    float* base = nullptr;
-    size_t bytes = 0;
-    int device = -1;
-};
 
 Stk2 one(Stk a) { return Stk2{{a, a}, 1}; }
 Stk2 two(Stk a, Stk b) { return Stk2{{a, b}, 2}; }
@@ -564,27 +561,35 @@ cvtpm_status check_args(const float* cam0, const float* cam1, int W, int H, size
     return CVTPM_OK;
 }
 
-thread_local Scratch g_scratch;
+/* Scratch comes from a stream-ordered pool of the library's own per device:
+ * allocated on the call's stream, freed on it after the call's last kernel,
+ * so concurrent calls on different streams never share bytes.  The pool
+ * keeps what it has allocated (release threshold: never) for later calls. */
+cudaMemPool_t scratch_pool(int dev) {
+    static std::mutex mu;
+    static std::map<int, cudaMemPool_t> pools;
+    std::lock_guard<std::mutex> lock(mu);
+    const auto it = pools.find(dev);
+    if (it != pools.end()) return it->second;
+    cudaMemPoolProps props = {};
+    props.allocType = cudaMemAllocationTypePinned;
+    props.location.type = cudaMemLocationTypeDevice;
+    props.location.id = dev;
+    cudaMemPool_t pool = nullptr;
+    if (cudaMemPoolCreate(&pool, &props) != cudaSuccess) { cudaGetLastError(); return nullptr; }
+    uint64_t keep = UINT64_MAX;
+    cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+    pools[dev] = pool;
+    return pool;
+}
 
-/* Scratch of the calling host thread on the current device, kept between
- * calls; it grows (after a device synchronisation) when a call needs more. */
-float* scratch(size_t bytes) {
+float* scratch(size_t bytes, cudaStream_t st) {
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess) return nullptr;
-    if (g_scratch.device == dev && g_scratch.bytes >= bytes) return g_scratch.base;
-    if (g_scratch.base) {
-        int cur = dev;
-        cudaSetDevice(g_scratch.device);
-        cudaDeviceSynchronize();
-        cudaFree(g_scratch.base);
-        cudaSetDevice(cur);
-        g_scratch.base = nullptr;
-        g_scratch.bytes = 0;
-    }
-    if (cudaMalloc(&g_scratch.base, bytes) != cudaSuccess) { cudaGetLastError(); return nullptr; }
-    g_scratch.bytes = bytes;
-    g_scratch.device = dev;
-    return g_scratch.base;
+    cudaMemPool_t pool = scratch_pool(dev);
+    void* p = nullptr;
+    if (!pool || cudaMallocFromPoolAsync(&p, bytes, pool, st) != cudaSuccess) { cudaGetLastError(); return nullptr; }
+    return (float*)p;
 }
 
 }  // namespace
@@ -618,11 +623,13 @@ cvtpm_status cvtpm_gcv_depthmap(float* dst, size_t dst_pitch, const float* cam0,
     if (s != CVTPM_OK) return s;
     if (!dst || dst_pitch % 4 || dst_pitch < (size_t)width * 4) return fail(CVTPM_ERR_INVALID_ARGUMENT, "gcv: bad dst");
     const int b = batch_for(width, height, count_steps(dmin, dmax, dt));
-    float* sc = scratch(sizeof(float) * scratch_floats(width, height, b, 0));
+    float* sc = scratch(sizeof(float) * scratch_floats(width, height, b, 0), (cudaStream_t)stream);
     if (!sc) return fail(CVTPM_ERR_ALLOC, "gcv: scratch allocation failed");
     depthmap(dst, dst_pitch, Img{(float*)cam0, width, height, 4}, Img{(float*)cam1, width, height, 4}, dmin, dmax, dt,
              sc, b, (cudaStream_t)stream);
-    const cudaError_t e = cudaGetLastError();
+    cudaError_t e = cudaGetLastError();
+    cudaFreeAsync(sc, (cudaStream_t)stream);      /* back to the pool after the call's kernels */
+    if (e == cudaSuccess) e = cudaGetLastError();
     return e == cudaSuccess ? CVTPM_OK : fail(CVTPM_ERR_CUDA, std::string("gcv: ") + cudaGetErrorString(e));
 }
 
@@ -636,7 +643,7 @@ cvtpm_status cvtpm_gcv_apply(uint8_t* dst, size_t dst_pitch, float* d0, float* d
         return fail(CVTPM_ERR_INVALID_ARGUMENT, "gcv: give both depth maps (tight rows, pitch width * 4) or neither");
     const size_t n = (size_t)width * height;
     const int b = batch_for(width, height, count_steps(dmin, dmax, dt));
-    float* sc = scratch(sizeof(float) * scratch_floats(width, height, b, 2));
+    float* sc = scratch(sizeof(float) * scratch_floats(width, height, b, 2), (cudaStream_t)stream);
     if (!sc) return fail(CVTPM_ERR_ALLOC, "gcv: scratch allocation failed");
     float* own0 = sc + scratch_floats(width, height, b, 0);
     float* own1 = own0 + n;
@@ -650,7 +657,9 @@ cvtpm_status cvtpm_gcv_apply(uint8_t* dst, size_t dst_pitch, float* d0, float* d
     /* the two depth maps as GRAY images of pitch pp */
     const Img i0{p0, width, height, 1}, i1{p1, width, height, 1};
     k_occlusion<<<g32(width, height), dim3(32, 8), 0, st>>>(dst, dst_pitch, i0, i1, fabsf(dmax));
-    const cudaError_t e = cudaGetLastError();
+    cudaError_t e = cudaGetLastError();
+    cudaFreeAsync(sc, st);                        /* back to the pool after the call's kernels */
+    if (e == cudaSuccess) e = cudaGetLastError();
     return e == cudaSuccess ? CVTPM_OK : fail(CVTPM_ERR_CUDA, std::string("gcv: ") + cudaGetErrorString(e));
 }
 

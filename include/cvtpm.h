@@ -510,9 +510,10 @@ cvtpm_status cvtpm_tsdf_save_raw(cvtpm_tsdf* vol, const char* path, int weighted
  * cam1 and its match in cam0 lies at x - d: with a left/right pair, pass the
  * right image as cam0 and the left as cam1 for the left view's disparity.
  * The disparities are processed in batches; scratch is (22 + 10 x batch)
- * floats per pixel (2 more for apply), belongs to the calling host thread and
- * is kept between calls.  Calls are stream-ordered.  The batch does not
- * change results.
+ * floats per pixel (2 more for apply), allocated on the call's stream from a
+ * stream-ordered memory pool of the library's and returned to it when the
+ * call's kernels end (the pool keeps the memory for later calls).  Calls are
+ * stream-ordered.  The batch does not change results.
  * ------------------------------------------------------------------ */
 
 /* Disparities per batch for later calls: 0 (the default) takes as many as

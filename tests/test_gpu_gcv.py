@@ -86,3 +86,30 @@ def test_apply_matches_oracle(cuda, oracle, W, H, dmin, dmax, dt, batch):
     assert not bit_diff(d0, want[1]).any()
     assert not bit_diff(d1, want[2]).any()
     assert np.array_equal(out, want[0])
+
+
+def test_scratch_does_not_grow_with_threads(cuda):
+    """calls from one host thread after another reuse the library's
+    stream-ordered scratch (here about 160 MB a call): device memory after
+    four threads equals that after the first"""
+    import threading
+    from cvt_gb300 import scenes
+    sc = scenes.make_scene(300, 200, 3, 64.0, seed=5)
+    cam0, cam1 = torch.from_numpy(sc.right).cuda(), torch.from_numpy(sc.left).cuda()
+    err, free = [], []
+
+    def work():
+        try:
+            gcv.StereoGCVFilter().apply(cam0, cam1, 0.0, 64.0, 1.0)
+            torch.cuda.synchronize()
+        except Exception as e:           # noqa: BLE001 - reported below
+            err.append(e)
+
+    for _ in range(4):
+        t = threading.Thread(target=work)
+        t.start()
+        t.join()
+        torch.cuda.synchronize()
+        free.append(torch.cuda.mem_get_info()[0])
+    assert not err, err
+    assert abs(free[0] - free[-1]) < 32 << 20, [(f - free[0]) >> 20 for f in free]
