@@ -15,7 +15,9 @@ buffers (cvtpm_depthmap_host: H2D of both images, the run, D2H of the map).
 `--impl reference` times the reference's algorithm on the host cores: the
 CPU restatement of pmhstereo.cl/PDHuberWeighted.cl/RNG.cl and the depthMap
 schedule (oracle/), EXACT arithmetic with MWC64X streams, all host threads,
-each step a bounded band of the same workload.
+each step a bounded crop of the same workload (the top-left 640x48 pixels of
+the pair, all 8 iterations, so the theta ramp and the view candidates match
+the timed run).
 """
 from __future__ import annotations
 
@@ -40,7 +42,7 @@ FLOPS_PER_TAP = 55.0          # per (pixel, candidate) window tap: plane, lerp, 
 FLOPS_PER_WEIGHT_TAP = 20.0   # bilateral weight of a tap, once per pixel and launch
 RECORD_BYTES_PER_TAP = 56.0   # the other view's value/difference records one evaluated tap reads (FAST)
 L1_BYTES_PER_CLK_SM = 128.0   # L1/shared data path of one SM
-N_SM = 152
+FP32_LANES_PER_SM = 128       # FP32 CUDA cores per SM (FMA = 2 flops)
 QUALITY_PAIRS = 8
 PD_BYTES_PER_PX = 116.0       # u 16 + p 32 + f 16 + w 4 read; u 16 + p 32 written
 
@@ -130,17 +132,24 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(rows)}
 
 
-def cpu_baseline(params, sc, rows: int, iters: int):
-    """The oracle (CPU restatement) on a band of `rows` rows for `iters`
-    iterations: Mpix-iter/s of the reference's algorithm on this host."""
+def cpu_baseline(params, sc, rows: int, cols: int, iters: int):
+    """The oracle (CPU restatement) on the top-left `cols` x `rows` crop of
+    the pair for `iters` iterations: Mpix-iter/s of the reference's algorithm
+    on this host.  A left crop keeps every match of its pixels (x' = x - d
+    < x), so the crop is a smaller pair of the same scene."""
     from oracle import oracle as orc
     p = params.replace(iterations=iters)
-    L = np.ascontiguousarray(sc.left[:rows])
-    R = np.ascontiguousarray(sc.right[:rows])
+    L = np.ascontiguousarray(sc.left[:rows, :cols])
+    R = np.ascontiguousarray(sc.right[:rows, :cols])
     t0 = time.perf_counter()
     orc.depthmap(p, L, R)
     dt = time.perf_counter() - t0
-    return sc.width * rows * iters / dt / 1e6, dt, orc.max_threads()
+    return L.shape[1] * rows * iters / dt / 1e6, dt, orc.max_threads()
+
+
+def cpu_sample_text(sc, rows, cols, iters):
+    return (f"top-left {min(cols, sc.width)}x{rows} crop of the {sc.width}x{sc.height} pair (rows 0-{rows - 1}, "
+            f"columns 0-{min(cols, sc.width) - 1}), {iters} iterations per step, exact arithmetic + MWC64X")
 
 
 def run_reference(args, rank, world):
@@ -150,16 +159,16 @@ def run_reference(args, rank, world):
     orc.lib()
     p = params_for("reference")
     sc = scene_for(0)
-    rows, iters = args.ref_rows, args.ref_iters
-    for _ in range(args.warmup):
-        cpu_baseline(p, sc, rows, iters)
+    rows, cols, iters = args.ref_rows, args.ref_cols, args.ref_iters
+    for _ in range(args.warmup):              # loads and warms the library: one iteration of the crop
+        cpu_baseline(p, sc, rows, cols, 1)
     vals, secs = [], 0.0
     for _ in range(args.steps):
-        v, dt, cores = cpu_baseline(p, sc, rows, iters)
+        v, dt, cores = cpu_baseline(p, sc, rows, cols, iters)
         vals.append(v)
         secs += dt
     value = float(np.mean(vals))
-    sample = f"rows 0-{rows - 1} of the 1242x375 pair ({sc.width}x{rows}), {iters} iterations per step"
+    sample = cpu_sample_text(sc, rows, cols, iters) + "; warm-up steps run 1 iteration of the crop"
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "Mpix-iter/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * secs / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
@@ -306,7 +315,13 @@ def run_ours(args, rank, world, local_rank):
     # the propagation's limiter is the L1 data path: its record bytes against
     # 128 B per clock and SM at the sampled clock
     clocks = clk.summary()
-    l1_peak = (N_SM * L1_BYTES_PER_CLK_SM * clocks["sm_mhz"] * 1e6 / 1e9) if clocks.get("sm_mhz") else None
+    n_sm = torch.cuda.get_device_properties(dev).multi_processor_count
+    l1_peak = (n_sm * L1_BYTES_PER_CLK_SM * clocks["sm_mhz"] * 1e6 / 1e9) if clocks.get("sm_mhz") else None
+    fp32_derived = (n_sm * FP32_LANES_PER_SM * 2 * clocks["sm_mhz"] * 1e6 / 1e12) if clocks.get("sm_mhz") else None
+    roofline["peak_derived"] = fp32_derived
+    roofline["frac_of_derived"] = (achieved / fp32_derived) if fp32_derived else None
+    roofline["peak_derived_source"] = (f"{n_sm} SMs x {FP32_LANES_PER_SM} FP32 lanes x 2 flops x the median SM clock "
+                                       "sampled during the timed region")
     l1_achieved = stats["cost_taps"] / nprop * RECORD_BYTES_PER_TAP / (prop_ms * 1e-3) / 1e9
     roofline_l1 = {"kernel": "k_propagate<fast> + k_nbcost (the propagation pass)", "bound": "l1",
                    "achieved": l1_achieved, "peak": l1_peak, "unit": "GB/s",
@@ -314,14 +329,15 @@ def run_ours(args, rank, world, local_rank):
                    "per": "pass: device-counted evaluated taps x 56 record bytes (a lower bound: image-1 reads, "
                           "weights and misaligned 128-byte lines come on top; ncu measures the L1 data pipe at "
                           "81-88 % busy) / pass time",
-                   "peak_source": "152 SMs x 128 B/clk x the median SM clock sampled during the timed region"}
+                   "peak_source": f"{n_sm} SMs (from the device) x 128 B/clk x the median SM clock sampled during "
+                                  "the timed region"}
     cpu = None
     if not args.no_cpu_baseline:
         from cvt_gb300.params import ARITH_EXACT, RNG_MWC64X
-        pv, dt, cores = cpu_baseline(p.replace(arith=ARITH_EXACT, rng=RNG_MWC64X), sc, args.ref_rows, args.ref_iters)
+        pv, dt, cores = cpu_baseline(p.replace(arith=ARITH_EXACT, rng=RNG_MWC64X), sc, args.ref_rows, args.ref_cols,
+                                     args.ref_iters)
         cpu = {"value": pv, "unit": "Mpix-iter/s", "cores": cores, "kind": "port",
-               "sample": f"rows 0-{args.ref_rows - 1} ({W}x{args.ref_rows}), {args.ref_iters} iterations, "
-                         f"exact arithmetic + MWC64X, {dt:.1f} s"}
+               "sample": cpu_sample_text(sc, args.ref_rows, args.ref_cols, args.ref_iters) + f", {dt:.1f} s"}
     line = {"metric": METRIC, "value": value, "unit": "Mpix-iter/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32",
@@ -340,6 +356,8 @@ def run_ours(args, rank, world, local_rank):
                         "note": "first two: the timed pair; means over pairs 0-7 (untimed); reference algorithm = "
                                 "EXACT arithmetic + MWC64X; a different RNG stream moves one pair's bad-1px by ~0.3 pp"},
             "clocks": clocks, "gpu_launches": stats["launches"], "wall_s": wall}
+    if not args.no_extras:
+        line["adjoint"] = adjoint_record(max(3, args.steps // 4))
     print(json.dumps(line), flush=True)
     return 0
 
@@ -431,15 +449,17 @@ def _disparity(planes, W, H):
     return planes[..., 0] * xx + planes[..., 1] * yy + planes[..., 2]
 
 
-def run_adjoint(args):
+def adjoint_record(steps: int) -> dict:
     """The differentiation workload: forward + adjoint (planes and both
     images) of the aggregated cost for 8 pairs at 640x480, plane fields =
-    ground truth + N(0, 0.01) on a, b and N(0, 1) on c."""
+    ground truth + N(0, 0.01) on a, b and N(0, 1) on c, clamped to
+    a, b in [-0.3, 0.3], c in [0, 64]; dL/dcost ~ N(0, 1).  Device-timed with
+    CUDA events over `steps` repetitions after one warm-up."""
     import torch
     from cvt_gb300 import scenes
     from cvt_gb300.stereo import PMHuberStereo
     from cvt_gb300.params import default_params, PRESET_BASELINE
-    st = PMHuberStereo(0, default_params(PRESET_BASELINE, patchsize=PATCH))
+    st = PMHuberStereo(torch.cuda.current_device(), default_params(PRESET_BASELINE, patchsize=PATCH))
     rng = np.random.default_rng(4)
     items = []
     for i in range(8):
@@ -463,14 +483,19 @@ def run_adjoint(args):
         e1.record(stream)
         torch.cuda.synchronize()
         return e0.elapsed_time(e1) / reps
-    fwd = timed(lambda: [st.cost_adjoint(a, b, p, 1) for a, b, p, g in items], args.steps)
-    full = timed(lambda: [st.cost_adjoint(a, b, p, 1, dcost=g) for a, b, p, g in items], args.steps)
+    fwd = timed(lambda: [st.cost_adjoint(a, b, p, 1) for a, b, p, g in items], steps)
+    full = timed(lambda: [st.cost_adjoint(a, b, p, 1, dcost=g) for a, b, p, g in items], steps)
     mpx = 8 * 640 * 480 / 1e6
-    print(json.dumps({"workload": "adjoint", "config": {"workload": "8 pairs 640x480, 35x35 ASW, BASELINE preset, "
-                                                                     "forward + adjoint w.r.t. planes and both images"},
-                      "forward_ms": fwd, "forward_plus_adjoint_ms": full,
-                      "forward_mpix_per_s": mpx / (fwd * 1e-3), "forward_plus_adjoint_mpix_per_s": mpx / (full * 1e-3),
-                      "unit": "Mpix/s", "steps": args.steps}), flush=True)
+    return {"workload": "adjoint", "config": {"workload": "8 pairs 640x480 RGBA f32, 35x35 ASW, BASELINE preset, "
+                                                          "perturbed ground-truth planes, forward + adjoint w.r.t. "
+                                                          "planes and both images"},
+            "forward_ms": fwd, "forward_plus_adjoint_ms": full,
+            "forward_mpix_per_s": mpx / (fwd * 1e-3), "forward_plus_adjoint_mpix_per_s": mpx / (full * 1e-3),
+            "unit": "Mpix/s", "steps": steps, "timing": "CUDA events on the launching stream, inputs in HBM"}
+
+
+def run_adjoint(args):
+    print(json.dumps(adjoint_record(args.steps)), flush=True)
     return 0
 
 
@@ -817,9 +842,11 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--ref-rows", type=int, default=96)
-    ap.add_argument("--ref-iters", type=int, default=2)
+    ap.add_argument("--ref-rows", type=int, default=48)
+    ap.add_argument("--ref-cols", type=int, default=640)
+    ap.add_argument("--ref-iters", type=int, default=ITERS)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-extras", action="store_true", help="skip the batch and adjoint sub-records")
     ap.add_argument("--profile", action="store_true", help="short run for ncu captures")
     ap.add_argument("--profile-iters", type=int, default=1)
     ap.add_argument("--workload", choices=["pair", "batch", "adjoint", "combined", "rectify", "tsdf", "gcv", "pipeline"],

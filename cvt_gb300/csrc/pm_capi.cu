@@ -760,7 +760,9 @@ cvtpm_status cvtpm_cost_eval(cvtpm_ctx* ctx, const float* img1, const float* img
     if ((s = check_params(ctx, p)) != CVTPM_OK) return s;
     if ((s = check_image(ctx, img1, width, height, pitch, "img1")) != CVTPM_OK) return s;
     if ((s = check_image(ctx, img2, width, height, pitch, "img2")) != CVTPM_OK) return s;
-    if (!states || !cost) return fail(ctx, CVTPM_ERR_INVALID_ARGUMENT, "null states/cost");
+    if (!states || ((uintptr_t)states & 15))
+        return fail(ctx, CVTPM_ERR_INVALID_ARGUMENT, "states NULL or not 16-byte aligned");
+    if (!cost || ((uintptr_t)cost & 3)) return fail(ctx, CVTPM_ERR_INVALID_ARGUMENT, "cost NULL or not 4-byte aligned");
     (void)lr;   /* the cost does not depend on the view flag (pmhstereo.cl:170-228) */
     cudaStream_t st = (cudaStream_t)stream;
     CK(cudaSetDevice(ctx->device), "cudaSetDevice");

@@ -108,6 +108,8 @@ extern "C" cvtpm_status cvtpm_cost_eval_noalloc(const cvtpm_params* params, cons
                                                 int width, int height, size_t pitch, const float* states,
                                                 float* cost, void* stream) {
     if (!params || !states || !cost) return CVTPM_ERR_INVALID_ARGUMENT;
+    /* the kernel reads the states as float4 and writes the costs as float */
+    if (((uintptr_t)states & 15) || ((uintptr_t)cost & 3)) return CVTPM_ERR_INVALID_ARGUMENT;
     if (!params_ok(params)) return CVTPM_ERR_INVALID_ARGUMENT;
     if (width < 1 || height < 1 || width > 12288 || height > 65535) return CVTPM_ERR_SIZE;
     if (!image_ok(img1, width, pitch) || !image_ok(img2, width, pitch)) return CVTPM_ERR_INVALID_ARGUMENT;

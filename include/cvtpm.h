@@ -187,7 +187,9 @@ cvtpm_status cvtpm_depthmap_inpaint(cvtpm_ctx* ctx,
  * view `lr` (1 = left is image 1, 0 = right is image 1) for the given state
  * field (float4 s0,s1,s2,unused per pixel, x_other = s0*x + s1*y + s2).
  * img1/img2 are RGBA f32 device images; gradients are computed internally
- * (pmhstereo_gradxy, pmhstereo.cl:785-831).  cost is W*H floats. */
+ * (pmhstereo_gradxy, pmhstereo.cl:785-831).  cost is W*H floats.  states
+ * must be 16-byte aligned and cost 4-byte aligned (CVTPM_ERR_INVALID_ARGUMENT
+ * otherwise, before any launch). */
 cvtpm_status cvtpm_cost_eval(cvtpm_ctx* ctx,
                              const float* img1, const float* img2,
                              int width, int height, size_t pitch,
@@ -250,10 +252,14 @@ cvtpm_status cvtpm_get_stats(cvtpm_ctx* ctx, cvtpm_stats* out);
  * their own input and output buffers.  Its intermediate images live in a
  * fixed 16 MiB device array inside the library (present on every GPU that
  * loads it, until exit): width*height is limited to about 135 000 pixels
- * (e.g. 360 x 360); larger images return CVTPM_ERR_SIZE.  The first call on
- * a device looks the array up (make it before any stream capture).  Calls
- * share the array, so calls that overlap on the GPU race; serialise them.
- * Same arguments and results as cvtpm_cost_eval, with the parameters passed
+ * (366 x 366 is the largest square); larger images return CVTPM_ERR_SIZE.  The first call on
+ * a device looks the array up (make it before any stream capture).  A call
+ * whose color_weight or weight_profile differs from the previous call's on
+ * that device uploads the spatial-profile table and synchronises `stream`
+ * before it launches.  Calls share the array, so calls that overlap on the
+ * GPU race; serialise them.  states must be 16-byte aligned and cost 4-byte
+ * aligned (CVTPM_ERR_INVALID_ARGUMENT otherwise, before any launch).  Same
+ * arguments and results as cvtpm_cost_eval, with the parameters passed
  * explicitly. */
 cvtpm_status cvtpm_cost_eval_noalloc(const cvtpm_params* params,
                                      const float* img1, const float* img2,

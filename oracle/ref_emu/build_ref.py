@@ -1,6 +1,7 @@
 """TEST INFRASTRUCTURE — build recipe of the emulated reference
 (oracle/_ref/libpmref.so).  Needs the reference sources (it reads them where
-they lie, under /root/reference, and copies none into the repository), so it
+they lie, in the directory named by the CVT_REFERENCE environment variable,
+by default /root/reference, and copies none into the repository), so it
 runs only where they are present.
 
   1. translate.py rewrites cvt/cl/kernel/{pmhstereo,RNG,PDHuberWeighted,
@@ -24,7 +25,7 @@ import sys
 HERE = os.path.dirname(os.path.abspath(__file__))
 ORACLE = os.path.dirname(HERE)
 ROOT = os.path.dirname(ORACLE)
-REF = "/root/reference"
+REF = os.environ.get("CVT_REFERENCE", "/root/reference")
 GEN = os.path.join(ROOT, "_build", "ref_gen")
 OUT = os.path.join(ORACLE, "_ref")
 LIB = os.path.join(OUT, "libpmref.so")

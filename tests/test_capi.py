@@ -64,3 +64,22 @@ def test_params_struct_layout():
     # int, float x7 ... as in include/cvtpm.h; uint64 seed aligned to 8
     assert CvtpmParams.seed.offset % 8 == 0
     assert ctypes.sizeof(CvtpmParams) == 80
+
+
+def test_noalloc_rejects_misaligned_buffers_before_any_device_call(L):
+    """cvtpm_cost_eval_noalloc reads the states as float4 and writes float
+    costs: pointers that are not 16- (states) or 4-byte (cost) aligned are
+    refused with CVTPM_ERR_INVALID_ARGUMENT before anything touches the
+    device, so fake addresses that are never dereferenced suffice here."""
+    from cvt_gb300.params import default_params, PRESET_REFERENCE
+    p = default_params(PRESET_REFERENCE, patchsize=5)
+    img, out = 0x10000, 0x20000                      # aligned, never dereferenced
+    W, H = 16, 8
+
+    def call(states, cost):
+        return L.cvtpm_cost_eval_noalloc(ctypes.byref(p), img, img, W, H, W * 16, states, cost, None)
+
+    assert call(0x30000 + 4, out) == 1               # states off by 4 bytes
+    assert call(0x30000 + 8, out) == 1               # off by 8
+    assert call(0x30000, out + 2) == 1               # cost off by 2
+    assert call(None, out) == 1

@@ -67,6 +67,49 @@ def test_noalloc_matches_cost_eval_on_consecutive_calls(cuda):
         assert not bit_diff(g, w).any()
 
 
+def test_noalloc_at_its_size_limit_matches_cost_eval(cuda):
+    """366 x 366 is the largest square image the 16 MiB array holds (its
+    layout ends 124 KB before the array does, where an off-by-one in the
+    layout would show); 367 x 367 is refused."""
+    from cvt_gb300.stereo import PMHuberStereo
+    ctx = PMHuberStereo(0)
+    sc = scenes.make_scene(366, 366, 6, 24.0, seed=43)
+    for p in (default_params(PRESET_BASELINE, patchsize=17), default_params(PRESET_REFERENCE, patchsize=17)):
+        left = torch.from_numpy(sc.left).cuda()
+        right = torch.from_numpy(sc.right).cuda()
+        states = torch.from_numpy(_plane_states(sc, 5)).cuda()
+        ctx.set_params(p)
+        want = ctx.cost(left, right, states)
+        rc, got = _noalloc(p, left, right, states)
+        assert rc == 0
+        torch.cuda.synchronize()
+        assert not bit_diff(got.cpu().numpy(), want.cpu().numpy()).any()
+    big = scenes.make_scene(367, 367, 2, 8.0, seed=44)
+    left = torch.from_numpy(big.left).cuda()
+    states = torch.zeros((367, 367, 4), dtype=torch.float32, device="cuda")
+    rc, _ = _noalloc(default_params(PRESET_BASELINE, patchsize=17), left, left, states)
+    assert rc == CVTPM_ERR_SIZE
+
+
+def test_cost_eval_rejects_misaligned_states(cuda):
+    """Both evaluators read the states as float4: a pointer that is not
+    16-byte aligned is refused before any launch."""
+    from cvt_gb300 import _lib
+    from cvt_gb300.stereo import PMHuberStereo
+    ctx = PMHuberStereo(0, default_params(PRESET_REFERENCE, patchsize=5))
+    img = torch.zeros((8, 16, 4), dtype=torch.float32, device="cuda")
+    states = torch.zeros(8 * 16 * 4 + 4, dtype=torch.float32, device="cuda")
+    cost = torch.empty((8, 16), dtype=torch.float32, device="cuda")
+    rc = _lib.lib().cvtpm_cost_eval(ctx._h, img.data_ptr(), img.data_ptr(), 16, 8, 16 * 16, states.data_ptr() + 4,
+                                    1, cost.data_ptr(), None)
+    assert rc == 1
+    p = default_params(PRESET_REFERENCE, patchsize=5)
+    rc = _lib.lib().cvtpm_cost_eval_noalloc(ctypes.byref(p), img.data_ptr(), img.data_ptr(), 16, 8, 16 * 16,
+                                           states.data_ptr() + 4, cost.data_ptr(), None)
+    assert rc == 1
+    torch.cuda.synchronize()
+
+
 def test_noalloc_rejects_images_beyond_its_limit(cuda):
     p = default_params(PRESET_REFERENCE, patchsize=5)
     small = torch.zeros((8, 8, 4), dtype=torch.float32, device="cuda")
