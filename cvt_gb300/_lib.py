@@ -18,7 +18,7 @@ LIB_PATH = os.path.join(_HERE, "libcvtpm.so")
 EXPORTS = (
     "cvtpm_version", "cvtpm_status_string", "cvtpm_params_default", "cvtpm_create", "cvtpm_destroy",
     "cvtpm_set_params", "cvtpm_get_params", "cvtpm_last_error", "cvtpm_synchronize", "cvtpm_depthmap",
-    "cvtpm_depthmap_host", "cvtpm_depthmap_inpaint", "cvtpm_cost_eval", "cvtpm_cost_adjoint", "cvtpm_polish_planes", "cvtpm_depthmap_batched", "cvtpm_set_memory_budget",
+    "cvtpm_depthmap_host", "cvtpm_depthmap_inpaint", "cvtpm_cost_eval", "cvtpm_cost_adjoint", "cvtpm_polish_planes", "cvtpm_depthmap_batched", "cvtpm_set_batch_knobs", "cvtpm_set_memory_budget",
     "cvtpm_set_batch_lanes", "cvtpm_get_batch_info",
     "cvtpm_set_timing", "cvtpm_reset_stats", "cvtpm_get_stats", "cvtpm_tool_fp32_peak",
     "cvtpm_cost_eval_noalloc",
@@ -56,20 +56,31 @@ class CvtpmRectification(ctypes.Structure):
                 ("rot_first", ctypes.c_float * 9), ("rot_second", ctypes.c_float * 9)]
 
 
-BATCH_MAX_CAND = 8
+BATCH_MAX_CAND = 16
 
 
 class CvtpmBatchInfo(ctypes.Structure):
     _fields_ = [("lanes", ctypes.c_int), ("shared_windows", ctypes.c_int), ("tuned", ctypes.c_int),
                 ("ncand", ctypes.c_int), ("cand_lanes", ctypes.c_int * BATCH_MAX_CAND),
                 ("cand_ms", ctypes.c_float * BATCH_MAX_CAND), ("graph_nodes", ctypes.c_longlong),
-                ("replays", ctypes.c_longlong)]
+                ("replays", ctypes.c_longlong), ("phased", ctypes.c_int), ("grid_mult", ctypes.c_int),
+                ("pd_rows", ctypes.c_int), ("pd_halo", ctypes.c_int),
+                ("cand_grid_mult", ctypes.c_int * BATCH_MAX_CAND), ("cand_pd_rows", ctypes.c_int * BATCH_MAX_CAND),
+                ("cand_pd_halo", ctypes.c_int * BATCH_MAX_CAND), ("launches", ctypes.c_longlong),
+                ("tune_ms", ctypes.c_float)]
 
     def as_dict(self) -> dict:
         n = self.ncand
+        cands = []
+        for i in range(n):
+            c = {"lanes": self.cand_lanes[i], "proxy_ms": self.cand_ms[i]}
+            if self.cand_lanes[i] == 0:
+                c.update(grid_mult=self.cand_grid_mult[i], pd_rows=self.cand_pd_rows[i], pd_halo=self.cand_pd_halo[i])
+            cands.append(c)
         return {"lanes": self.lanes, "shared_windows": self.shared_windows, "tuned": self.tuned,
-                "candidates": [{"lanes": self.cand_lanes[i], "proxy_ms": self.cand_ms[i]} for i in range(n)],
-                "graph_nodes": self.graph_nodes, "replays": self.replays}
+                "candidates": cands, "graph_nodes": self.graph_nodes, "replays": self.replays,
+                "phased": self.phased, "grid_mult": self.grid_mult, "pd_rows": self.pd_rows,
+                "pd_halo": self.pd_halo, "launches": self.launches, "tune_ms": self.tune_ms}
 
 
 class CvtpmStats(ctypes.Structure):
@@ -121,6 +132,7 @@ def lib() -> ctypes.CDLL:
     L.cvtpm_polish_planes.argtypes = [vp, vp, vp, i, i, sz, vp, i, i, vp, vp]
     L.cvtpm_set_batch_lanes.argtypes = [vp, i]
     L.cvtpm_get_batch_info.argtypes = [vp, ctypes.POINTER(CvtpmBatchInfo)]
+    L.cvtpm_set_batch_knobs.argtypes = [vp, i, i, i]
     L.cvtpm_reset_stats.argtypes = [vp]
     L.cvtpm_get_stats.argtypes = [vp, ctypes.POINTER(CvtpmStats)]
     L.cvtpm_tool_fp32_peak.argtypes = [i, vp, ctypes.POINTER(ctypes.c_float)]

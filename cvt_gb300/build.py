@@ -70,7 +70,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
             failed.append(src)
     if failed:
         raise RuntimeError(f"nvcc failed for {failed}")
-    link = [nvcc(), *ARCH, "-shared", "-cudart", "static", "-o", LIB + ".tmp", *objs]
+    link = [nvcc(), *ARCH, "-shared", "-cudart", "static", "-o", LIB + ".tmp", *objs, "-ldl"]
     if verbose:
         print(" ".join(link), file=sys.stderr)
     subprocess.run(link, check=True)

@@ -14,12 +14,16 @@
  *    the candidate planes (k_view_list).
  */
 #include <algorithm>
+#include <chrono>
 #include <cstdio>
 #include <cstring>
+#include <memory>
 #include <mutex>
 #include <string>
 #include <new>
 #include <vector>
+
+#include <nvtx3/nvToolsExt.h>
 
 #include "cvtpm.h"
 #include "cvtpm_tools.h"
@@ -60,6 +64,12 @@ struct cvtpm_ctx {
      * captured graph of the last batch and the tuning record */
     struct Lane { cvtpm_ctx* c = nullptr; cudaStream_t s = nullptr; cudaEvent_t done = nullptr; };
     std::vector<Lane> lanes;
+    /* phase-batched mode: one scratch context per pair of the batch, the
+     * tuned launch knobs per batch shape and the knobs of the current graph */
+    std::vector<cvtpm_ctx*> bpairs;
+    std::vector<std::pair<std::vector<unsigned char>, PmBatchKnobs>> tuned_knobs;
+    PmBatchKnobs knobs{1, 16, 4};     /* pinned by cvtpm_set_batch_knobs */
+    bool pinned_knobs = false;
     cudaStream_t bstream = nullptr;
     cudaEvent_t bfork = nullptr, bjoin = nullptr;
     cudaGraphExec_t bexec = nullptr;
@@ -116,6 +126,15 @@ struct PhaseTimer {
     void stop() {
         if (a && b) { cudaEventRecord(b, st); list->push_back({a, b}); a = b = nullptr; }
     }
+};
+
+/* An NVTX range around the host-side enqueue of a phase (a profiler shows
+ * the phase's kernels under it); no cost without a profiler attached. */
+struct NvtxRange {
+    explicit NvtxRange(const char* name) { nvtxRangePushA(name); }
+    ~NvtxRange() { nvtxRangePop(); }
+    NvtxRange(const NvtxRange&) = delete;
+    NvtxRange& operator=(const NvtxRange&) = delete;
 };
 
 size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
@@ -364,11 +383,15 @@ cvtpm_status run_depthmap(cvtpm_ctx* ctx, const cvtpm_params& p, float* dmap, si
         CK(cudaMemset(ctx->dcount, 0, 2 * sizeof(unsigned long long)), "counters");
     }
     ++ctx->stats.calls;
+    NvtxRange whole("cvtpm depthMap");
 
-    aL.out = ctx->S[0][0];                                         /* :124-143 */
-    LK(pm_launch_init(aL, exact, st), "init");
-    aR.out = ctx->S[1][0];
-    LK(pm_launch_init(aR, exact, st), "init");
+    {
+        NvtxRange r("init");
+        aL.out = ctx->S[0][0];                                     /* :124-143 */
+        LK(pm_launch_init(aL, exact, st), "init");
+        aR.out = ctx->S[1][0];
+        LK(pm_launch_init(aR, exact, st), "init");
+    }
     CK(cudaMemsetAsync(ctx->smooth[0], 0, n * 16, st), "clear");   /* :108-113 */
     CK(cudaMemsetAsync(ctx->smooth[1], 0, n * 16, st), "clear");
     CK(cudaMemsetAsync(ctx->list[1], 0xFF, n * 8, st), "clear");   /* :145-149 */
@@ -382,6 +405,7 @@ cvtpm_status run_depthmap(cvtpm_ctx* ctx, const cvtpm_params& p, float* dmap, si
         aL.viewin = ctx->list[1]; aL.viewsrc = ctx->S[1][sw]; aL.winners = ctx->win[0];
         aL.counters = aR.counters = ctx->dcount;
         {
+            NvtxRange r("propagate left");
             PhaseTimer tm(ctx, st, ctx->ev_prop);
             if ((s = propagate_view(ctx, aL, exact, p.schedule == CVTPM_SCHEDULE_REDBLACK, n, st)) != CVTPM_OK) return s;
             tm.stop();
@@ -390,6 +414,7 @@ cvtpm_status run_depthmap(cvtpm_ctx* ctx, const cvtpm_params& p, float* dmap, si
         aR.old = ctx->S[1][sw]; aR.out = ctx->S[1][1 - sw]; aR.smooth = ctx->smooth[1];
         aR.viewin = ctx->list[0]; aR.viewsrc = ctx->S[0][1 - sw]; aR.winners = ctx->win[1];
         {
+            NvtxRange r("propagate right");
             PhaseTimer tm(ctx, st, ctx->ev_prop);
             if ((s = propagate_view(ctx, aR, exact, p.schedule == CVTPM_SCHEDULE_REDBLACK, n, st)) != CVTPM_OK) return s;
             tm.stop();
@@ -398,6 +423,7 @@ cvtpm_status run_depthmap(cvtpm_ctx* ctx, const cvtpm_params& p, float* dmap, si
         LK(pm_launch_view_list(ctx->S[1][1 - sw], W, H, ctx->list[1], st), "view list");
         const float lambda = theta * p.thetascale + 5.0f;
         for (int v = 0; v < 2; ++v) {                              /* :228-261 */
+            NvtxRange r(v == 0 ? "consistency, fill, PD left" : "consistency, fill, PD right");
             LK(pm_launch_consistency(ctx->S[v][1 - sw], ctx->S[1 - v][1 - sw], W, H, p.maxdispdiff, p.maxanglediff,
                                      v == 0 ? 1 : 0, ctx->tmp, nullptr, st), "consistency");
             LK(pm_launch_fill_state(ctx->tmp, W, H, dmax, v == 0 ? 1 : 0, ctx->tmp2, st), "fill");
@@ -407,6 +433,7 @@ cvtpm_status run_depthmap(cvtpm_ctx* ctx, const cvtpm_params& p, float* dmap, si
         if (iter >= 5) theta = smoothstep01(((float)iter - 5.0f) / ((float)N - 5.0f)) * 1.0f;
     }
     const int fin = 1 - ((N - 1) & 1);                              /* :268-290 */
+    NvtxRange fr("final consistency and fill");
     LK(pm_launch_consistency(ctx->S[0][fin], ctx->S[1][fin], W, H, p.maxdispdiff, p.maxanglediff, 1, ctx->tmp,
                              ctx->valid, st), "consistency");
     LK(pm_launch_fill_output(ctx->tmp, W, H, dscale, dmap, dpitch / 4, (float4*)nmap, npitch / 16, st), "fill output");
@@ -472,6 +499,7 @@ cvtpm_status run_depthmap_inpaint(cvtpm_ctx* ctx, const cvtpm_params& p, float* 
         aL.viewin = ctx->list[1]; aL.viewsrc = ctx->S[1][sw]; aL.winners = ctx->win[0];
         aL.counters = aR.counters = ctx->dcount;
         {
+            NvtxRange r("propagate left");
             PhaseTimer tm(ctx, st, ctx->ev_prop);
             if ((s = propagate_view(ctx, aL, exact, p.schedule == CVTPM_SCHEDULE_REDBLACK, n, st)) != CVTPM_OK) return s;
             tm.stop();
@@ -480,6 +508,7 @@ cvtpm_status run_depthmap_inpaint(cvtpm_ctx* ctx, const cvtpm_params& p, float* 
         aR.old = ctx->S[1][sw]; aR.out = ctx->S[1][1 - sw]; aR.smooth = ctx->smooth[1];
         aR.viewin = ctx->list[0]; aR.viewsrc = ctx->S[0][1 - sw]; aR.winners = ctx->win[1];
         {
+            NvtxRange r("propagate right");
             PhaseTimer tm(ctx, st, ctx->ev_prop);
             if ((s = propagate_view(ctx, aR, exact, p.schedule == CVTPM_SCHEDULE_REDBLACK, n, st)) != CVTPM_OK) return s;
             tm.stop();
@@ -607,6 +636,7 @@ cvtpm_status cvtpm_destroy(cvtpm_ctx* ctx) {
     cudaSetDevice(ctx->device);
     if (ctx->pool) cudaFree(ctx->pool);
     if (ctx->bexec) cudaGraphExecDestroy(ctx->bexec);
+    for (cvtpm_ctx* c : ctx->bpairs) cvtpm_destroy(c);
     for (auto& l : ctx->lanes) {
         if (l.c) cvtpm_destroy(l.c);
         if (l.s) cudaStreamDestroy(l.s);
@@ -1039,6 +1069,7 @@ cvtpm_status tune_batch(cvtpm_ctx* ctx, const cvtpm_pair* pairs, int npairs, int
             if (!ok) { cudaEventDestroy(t0); cudaEventDestroy(t1); return cuda_fail(ctx, cudaGetLastError(), "tuning run"); }
             if (bi.ncand < CVTPM_BATCH_MAX_CAND) {
                 bi.cand_lanes[bi.ncand] = k;
+                bi.cand_grid_mult[bi.ncand] = bi.cand_pd_rows[bi.ncand] = bi.cand_pd_halo[bi.ncand] = 0;
                 bi.cand_ms[bi.ncand] = ms;
                 ++bi.ncand;
             }
@@ -1051,6 +1082,391 @@ cvtpm_status tune_batch(cvtpm_ctx* ctx, const cvtpm_pair* pairs, int npairs, int
 }
 
 }  // namespace
+
+}  // extern "C"
+
+/* ------------------------------------------------ phase-batched mode -- */
+/* PMHuberStereo::depthMap for a batch of pairs with one launch per phase of
+ * the schedule (run_depthmap's order: prep, records, init, then per
+ * iteration the neighbour costs, propagation and view lists of the left
+ * view, the same for the right view, and per view the consistency check, the
+ * fill and the PD smoother; finally the consistency check and the output
+ * fill) covering every pair.  The kernels are the plain path's tile bodies
+ * behind a persistent item loop (pm_kernels.cu, "batched phases"), so every
+ * pair gets the bits of its plain call.  Each pair keeps its own scratch (a
+ * context of its own), sized before the graph capture. */
+namespace {
+
+cvtpm_status ensure_batch_pairs(cvtpm_ctx* ctx, int n) {
+    while ((int)ctx->bpairs.size() < n) {
+        cvtpm_ctx* c = nullptr;
+        cvtpm_status s = cvtpm_create(&c, ctx->device);
+        if (s != CVTPM_OK) return fail(ctx, s, "pair context");
+        ctx->bpairs.push_back(c);
+        CK(cudaMalloc(&c->dcount, 2 * sizeof(unsigned long long)), "pair counters");
+        CK(cudaMemset(c->dcount, 0, 2 * sizeof(unsigned long long)), "pair counters");
+    }
+    return CVTPM_OK;
+}
+
+/* Builds the PmBatch of `nent` entries (make(e, args, W, H) fills entry e),
+ * in launches of at most PM_BATCH_MAX entries, and launches each. */
+template <typename A, typename Make, typename Launch>
+cvtpm_status run_phase(cvtpm_ctx* ctx, int nent, PmBatchKernel kind, const PmBatchKnobs& kn, Make make, Launch launch,
+                       const char* what, long long* launches) {
+    std::unique_ptr<PmBatch<A>> b(new PmBatch<A>());
+    for (int e0 = 0; e0 < nent; e0 += PM_BATCH_MAX) {
+        b->n = std::min(PM_BATCH_MAX, nent - e0);
+        int items = 0;
+        for (int i = 0; i < b->n; ++i) {
+            int W = 0, H = 0, tx = 1, tiles = 0;
+            make(e0 + i, b->a[i], W, H);
+            pm_batch_tiles(kind, W, H, kn, &tx, &tiles);
+            b->first[i] = items;
+            b->tx[i] = tx;
+            items += tiles;
+        }
+        b->first[b->n] = items;
+        CK(launch(*b), what);
+        ++ctx->stats.launches;
+        if (launches) ++*launches;
+    }
+    return CVTPM_OK;
+}
+
+struct PhaseState {
+    cvtpm_ctx* ctx;
+    const cvtpm_pair* pairs;
+    int n;
+    cvtpm_params p;
+    PmBatchKnobs kn;
+    cudaStream_t st;
+    int maxW;
+    long long launches;
+    std::vector<PmPassArgs> aL, aR;
+};
+
+/* Sizes every pair's scratch and neighbour-cost buffer (outside any capture). */
+cvtpm_status phase_prepare(PhaseState& S) {
+    cvtpm_status s;
+    if ((s = ensure_batch_pairs(S.ctx, S.n)) != CVTPM_OK) return s;
+    S.maxW = 1;
+    for (int i = 0; i < S.n; ++i) {
+        cvtpm_ctx* c = S.ctx->bpairs[i];
+        c->prm = S.p;
+        c->prm.depthmax = S.pairs[i].depthmax;
+        c->nb_budget = S.ctx->nb_budget;
+        c->timing = false;
+        if ((s = ensure_buffers(c, S.pairs[i].width, S.pairs[i].height)) != CVTPM_OK) return fail(S.ctx, s, c->err);
+        if ((s = ensure_nbcost(c, S.pairs[i].width, S.pairs[i].height)) != CVTPM_OK) return fail(S.ctx, s, c->err);
+        S.maxW = std::max(S.maxW, S.pairs[i].width);
+    }
+    return ensure_tables(S.ctx->bpairs[0], S.p, S.st) == CVTPM_OK ? CVTPM_OK
+                                                                   : fail(S.ctx, CVTPM_ERR_CUDA, S.ctx->bpairs[0]->err);
+}
+
+/* prep, records, init and the clears: every pair ready for iteration 0 */
+cvtpm_status phase_start(PhaseState& S) {
+    cvtpm_ctx* ctx = S.ctx;
+    const bool exact = S.p.arith == CVTPM_ARITH_EXACT;
+    cvtpm_status s;
+    auto pc = [&](int i) { return ctx->bpairs[i]; };
+    if ((s = run_phase<PmPrepArgs>(ctx, 2 * S.n, PMB_PREP, S.kn, [&](int e, PmPrepArgs& a, int& W, int& H) {
+            const int i = e >> 1, v = e & 1;
+            const cvtpm_pair& q = S.pairs[i];
+            W = q.width; H = q.height;
+            a = {(const float4*)(v ? q.right : q.left), q.pitch / 16, W, H, pc(i)->col[v], pc(i)->grad[v], pc(i)->wgt[v]};
+        }, [&](const PmBatch<PmPrepArgs>& b) { return pm_batch_prep(b, S.kn, S.st); }, "batched prep", &S.launches)) != CVTPM_OK)
+        return s;
+    if (!exact &&
+        (s = run_phase<PmRecArgs>(ctx, 2 * S.n, PMB_RECORDS, S.kn, [&](int e, PmRecArgs& a, int& W, int& H) {
+            const int i = e >> 1, v = e & 1;
+            W = S.pairs[i].width; H = S.pairs[i].height;
+            cvtpm_ctx* c = pc(i);
+            a = {c->col[v], c->grad[v], W, H, rec_pitch(W), c->recA[v], c->recB[v], c->recC[v], c->recD[v]};
+        }, [&](const PmBatch<PmRecArgs>& b) { return pm_batch_records(b, S.kn, S.st); }, "batched records", &S.launches)) != CVTPM_OK)
+        return s;
+    S.aL.resize(S.n);
+    S.aR.resize(S.n);
+    for (int i = 0; i < S.n; ++i) {
+        cvtpm_ctx* c = pc(i);
+        const int W = S.pairs[i].width, H = S.pairs[i].height;
+        S.aL[i] = base_args(c, c->prm, W, H, 0);
+        S.aR[i] = base_args(c, c->prm, W, H, 1);
+        if (c->nb_on) S.aL[i].nbcost = S.aR[i].nbcost = c->nbcost;
+        S.aL[i].counters = S.aR[i].counters = c->dcount;
+        S.aL[i].out = c->S[0][0];
+        S.aR[i].out = c->S[1][0];
+    }
+    if ((s = run_phase<PmPassArgs>(ctx, 2 * S.n, PMB_PIXEL, S.kn, [&](int e, PmPassArgs& a, int& W, int& H) {
+            const int i = e >> 1;
+            a = (e & 1) ? S.aR[i] : S.aL[i];
+            W = a.k.W; H = a.k.H;
+        }, [&](const PmBatch<PmPassArgs>& b) { return pm_batch_init(b, exact, S.kn, S.st); }, "batched init", &S.launches)) != CVTPM_OK)
+        return s;
+    for (int i = 0; i < S.n; ++i) {                                 /* :108-113, :145-149 */
+        cvtpm_ctx* c = pc(i);
+        const size_t npx = (size_t)S.pairs[i].width * S.pairs[i].height;
+        CK(cudaMemsetAsync(c->smooth[0], 0, npx * 16, S.st), "clear");
+        CK(cudaMemsetAsync(c->smooth[1], 0, npx * 16, S.st), "clear");
+        CK(cudaMemsetAsync(c->list[1], 0xFF, npx * 8, S.st), "clear");
+    }
+    return CVTPM_OK;
+}
+
+/* One view's propagation pass for every pair: neighbour costs (where the
+ * pair's shared windows are on), propagation, view lists. */
+cvtpm_status phase_propagate(PhaseState& S, std::vector<PmPassArgs>& args, short4* (*list_of)(cvtpm_ctx*),
+                             const float4* (*src_of)(cvtpm_ctx*, int), int sw) {
+    cvtpm_ctx* ctx = S.ctx;
+    const bool exact = S.p.arith == CVTPM_ARITH_EXACT;
+    cvtpm_status s;
+    std::vector<int> nb;
+    for (int i = 0; i < S.n; ++i)
+        if (args[i].nbcost) nb.push_back(i);
+    if (!nb.empty() &&
+        (s = run_phase<PmPassArgs>(ctx, (int)nb.size(), PMB_NBCOST, S.kn, [&](int e, PmPassArgs& a, int& W, int& H) {
+            a = args[nb[e]];
+            W = a.k.W; H = a.k.H;
+        }, [&](const PmBatch<PmPassArgs>& b) { return pm_batch_nbcost(b, exact, S.kn, S.st); }, "batched neighbour costs",
+           &S.launches)) != CVTPM_OK)
+        return s;
+    if ((s = run_phase<PmPassArgs>(ctx, S.n, PMB_PIXEL, S.kn, [&](int e, PmPassArgs& a, int& W, int& H) {
+            a = args[e];
+            W = a.k.W; H = a.k.H;
+        }, [&](const PmBatch<PmPassArgs>& b) { return pm_batch_propagate(b, exact, S.kn, S.st); }, "batched propagate",
+           &S.launches)) != CVTPM_OK)
+        return s;
+    return run_phase<PmViewListArgs>(ctx, S.n, PMB_ROW, S.kn, [&](int e, PmViewListArgs& a, int& W, int& H) {
+            cvtpm_ctx* c = ctx->bpairs[e];
+            W = S.pairs[e].width; H = S.pairs[e].height;
+            a = {src_of(c, sw), W, H, list_of(c)};
+        }, [&](const PmBatch<PmViewListArgs>& b) { return pm_batch_view_list(b, S.maxW, S.kn, S.st); },
+        "batched view list", &S.launches);
+}
+
+/* PDROF::apply (PDROF.h:50-96) of view v for every pair, kn.pd_halo steps per
+ * launch; pd_apply's schedule of buffers (iters == 0 runs pd_apply per pair). */
+cvtpm_status phase_pd(PhaseState& S, int v, float lambda) {
+    cvtpm_ctx* ctx = S.ctx;
+    cvtpm_status s;
+    const int iters = S.p.pd_iterations;
+    if (iters == 0) {
+        for (int i = 0; i < S.n; ++i) {
+            cvtpm_ctx* c = ctx->bpairs[i];
+            if ((s = pd_apply(c, c->smooth[v], c->tmp2, c->wgt[v], lambda, 0, S.pairs[i].width, S.pairs[i].height, S.st)) !=
+                CVTPM_OK)
+                return fail(ctx, s, c->err);
+            ++S.launches;
+        }
+        return CVTPM_OK;
+    }
+    const int total = iters + (iters & 1);
+    const int K = S.kn.pd_halo;
+    int l = 0;
+    for (int done = 0; done < total; done += K, ++l) {
+        const int steps = total - done < K ? total - done : K;
+        if ((s = run_phase<PmPdArgs>(ctx, S.n, PMB_PD, S.kn, [&](int e, PmPdArgs& a, int& W, int& H) {
+                cvtpm_ctx* c = ctx->bpairs[e];
+                W = S.pairs[e].width; H = S.pairs[e].height;
+                float4* U[2] = {c->smooth[v], c->pdT};
+                float4* Pp[2] = {c->pdP[0], c->pdP[1]};
+                a.uout = U[(l + 1) & 1]; a.pout = Pp[(l + 1) & 1];
+                a.uin = U[l & 1]; a.pin = Pp[l & 1];
+                a.f = c->tmp2; a.wgt = c->wgt[v];
+                a.pzero = l == 0 ? 1 : 0; a.nsteps = steps; a.W = W; a.H = H; a.lambda = lambda;
+            }, [&](const PmBatch<PmPdArgs>& b) { return pm_batch_pd(b, S.kn, S.st); }, "batched PD", &S.launches)) != CVTPM_OK)
+            return s;
+    }
+    if (l & 1)                                          /* the result sits in pdT */
+        for (int i = 0; i < S.n; ++i) {
+            cvtpm_ctx* c = ctx->bpairs[i];
+            CK(cudaMemcpyAsync(c->smooth[v], c->pdT, (size_t)S.pairs[i].width * S.pairs[i].height * 16,
+                               cudaMemcpyDeviceToDevice, S.st), "pd copy");
+        }
+    return CVTPM_OK;
+}
+
+short4* list0(cvtpm_ctx* c) { return c->list[0]; }
+short4* list1(cvtpm_ctx* c) { return c->list[1]; }
+
+/* The whole schedule for `iterations` iterations, stream-ordered on S.st. */
+cvtpm_status phase_schedule(PhaseState& S, int iterations) {
+    cvtpm_ctx* ctx = S.ctx;
+    cvtpm_status s;
+    NvtxRange whole("cvtpm depthMap batch (phase-batched)");
+    if ((s = phase_start(S)) != CVTPM_OK) return s;
+    float theta = 0.0f;
+    const int N = iterations;
+    for (int iter = 0; iter < N; ++iter) {                         /* PMHuberStereo.cpp:151-266 */
+        const int sw = iter & 1;
+        for (int i = 0; i < S.n; ++i) {
+            cvtpm_ctx* c = ctx->bpairs[i];
+            PmPassArgs& L = S.aL[i];
+            L.iter = iter; L.theta = theta;
+            L.old = c->S[0][sw]; L.out = c->S[0][1 - sw]; L.smooth = c->smooth[0];
+            L.viewin = c->list[1]; L.viewsrc = c->S[1][sw]; L.winners = c->win[0];
+        }
+        if ((s = phase_propagate(S, S.aL, list0, [](cvtpm_ctx* c, int sw_) { return (const float4*)c->S[0][1 - sw_]; }, sw)) !=
+            CVTPM_OK)
+            return s;
+        for (int i = 0; i < S.n; ++i) {
+            cvtpm_ctx* c = ctx->bpairs[i];
+            PmPassArgs& R = S.aR[i];
+            R.iter = iter; R.theta = theta;
+            R.old = c->S[1][sw]; R.out = c->S[1][1 - sw]; R.smooth = c->smooth[1];
+            R.viewin = c->list[0]; R.viewsrc = c->S[0][1 - sw]; R.winners = c->win[1];
+        }
+        if ((s = phase_propagate(S, S.aR, list1, [](cvtpm_ctx* c, int sw_) { return (const float4*)c->S[1][1 - sw_]; }, sw)) !=
+            CVTPM_OK)
+            return s;
+        const float lambda = theta * S.p.thetascale + 5.0f;
+        for (int v = 0; v < 2; ++v) {                              /* :228-261 */
+            if ((s = run_phase<PmConsArgs>(ctx, S.n, PMB_PIXEL, S.kn, [&](int e, PmConsArgs& a, int& W, int& H) {
+                    cvtpm_ctx* c = ctx->bpairs[e];
+                    W = S.pairs[e].width; H = S.pairs[e].height;
+                    a = {c->S[v][1 - sw], c->S[1 - v][1 - sw], W, H, S.p.maxdispdiff, S.p.maxanglediff / 180.0f,
+                         v == 0 ? 1 : 0, c->tmp, nullptr};
+                }, [&](const PmBatch<PmConsArgs>& b) { return pm_batch_consistency(b, S.kn, S.st); }, "batched consistency",
+                   &S.launches)) != CVTPM_OK)
+                return s;
+            if ((s = run_phase<PmFillArgs>(ctx, S.n, PMB_ROW, S.kn, [&](int e, PmFillArgs& a, int& W, int& H) {
+                    cvtpm_ctx* c = ctx->bpairs[e];
+                    W = S.pairs[e].width; H = S.pairs[e].height;
+                    a = {c->tmp, W, H, S.pairs[e].depthmax, v == 0 ? 1 : 0, c->tmp2};
+                }, [&](const PmBatch<PmFillArgs>& b) { return pm_batch_fill_state(b, S.maxW, S.kn, S.st); }, "batched fill",
+                   &S.launches)) != CVTPM_OK)
+                return s;
+            if ((s = phase_pd(S, v, lambda)) != CVTPM_OK) return s;
+        }
+        if (iter >= 5) theta = smoothstep01(((float)iter - 5.0f) / ((float)N - 5.0f)) * 1.0f;
+    }
+    const int fin = 1 - ((N - 1) & 1);                              /* :268-290 */
+    if ((s = run_phase<PmConsArgs>(ctx, S.n, PMB_PIXEL, S.kn, [&](int e, PmConsArgs& a, int& W, int& H) {
+            cvtpm_ctx* c = ctx->bpairs[e];
+            W = S.pairs[e].width; H = S.pairs[e].height;
+            a = {c->S[0][fin], c->S[1][fin], W, H, S.p.maxdispdiff, S.p.maxanglediff / 180.0f, 1, c->tmp, c->valid};
+        }, [&](const PmBatch<PmConsArgs>& b) { return pm_batch_consistency(b, S.kn, S.st); }, "batched consistency",
+           &S.launches)) != CVTPM_OK)
+        return s;
+    return run_phase<PmOutArgs>(ctx, S.n, PMB_ROW, S.kn, [&](int e, PmOutArgs& a, int& W, int& H) {
+            cvtpm_ctx* c = ctx->bpairs[e];
+            const cvtpm_pair& q = S.pairs[e];
+            W = q.width; H = q.height;
+            const float dscale = S.p.dscale <= 0.0f ? 1.0f / q.depthmax : S.p.dscale;
+            a = {c->tmp, W, H, dscale, q.dmap, q.dmap_pitch / 4, nullptr, 0};
+        }, [&](const PmBatch<PmOutArgs>& b) { return pm_batch_fill_output(b, S.maxW, S.kn, S.st); }, "batched fill output",
+        &S.launches);
+}
+
+/* The batch autotuner.  The knobs do not change any result, only how the
+ * launches are shaped: the persistent grid of every phase (1 or 2 times the
+ * blocks resident per SM, or one block per work item) and the PD smoother's
+ * tile (16 or 8 rows) and steps per launch (4 or 2, also its halo width).
+ * On the batch's own data (its first pairs, up to 4 Mpx, after their prep
+ * and init), it times one propagation phase of the left view per grid
+ * choice, then one PD apply of 8 steps of the left view per PD tile, halo
+ * and grid, and keeps the fastest. */
+cvtpm_status tune_phased(PhaseState& full, PmBatchKnobs* best) {
+    PhaseState S = full;
+    long long px = 0;
+    S.n = 0;
+    while (S.n < full.n && (S.n == 0 || px < 4000000)) {
+        px += (long long)full.pairs[S.n].width * full.pairs[S.n].height;
+        ++S.n;
+    }
+    cvtpm_ctx* ctx = S.ctx;
+    cvtpm_batch_info& bi = ctx->binfo;
+    cvtpm_status s;
+    bi.ncand = 0;
+    S.kn = PmBatchKnobs{1, 16, 4};
+    if ((s = phase_start(S)) != CVTPM_OK) return s;
+    for (int i = 0; i < S.n; ++i) {
+        cvtpm_ctx* c = ctx->bpairs[i];
+        PmPassArgs& L = S.aL[i];
+        L.iter = 0; L.theta = 0.0f;
+        L.old = c->S[0][0]; L.out = c->S[0][1]; L.smooth = c->smooth[0];
+        L.viewin = c->list[1]; L.viewsrc = c->S[1][0]; L.winners = c->win[0];
+    }
+    cudaEvent_t t0 = nullptr, t1 = nullptr;
+    CK(cudaEventCreate(&t0), "tune event");
+    if (cudaEventCreate(&t1) != cudaSuccess) { cudaEventDestroy(t0); return cuda_fail(ctx, cudaGetLastError(), "tune event"); }
+    auto timed = [&](auto&& body, float* ms) -> cvtpm_status {
+        cvtpm_status r;
+        if (cudaEventRecord(t0, S.st) != cudaSuccess) return cuda_fail(ctx, cudaGetLastError(), "tune record");
+        if ((r = body()) != CVTPM_OK) return r;
+        if (cudaEventRecord(t1, S.st) != cudaSuccess || cudaEventSynchronize(t1) != cudaSuccess ||
+            cudaEventElapsedTime(ms, t0, t1) != cudaSuccess)
+            return cuda_fail(ctx, cudaGetLastError(), "tune timing");
+        return CVTPM_OK;
+    };
+    auto add = [&](const PmBatchKnobs& k, float ms) {
+        if (bi.ncand < CVTPM_BATCH_MAX_CAND) {
+            bi.cand_lanes[bi.ncand] = 0;
+            bi.cand_grid_mult[bi.ncand] = k.grid_mult;
+            bi.cand_pd_rows[bi.ncand] = k.pd_rows;
+            bi.cand_pd_halo[bi.ncand] = k.pd_halo;
+            bi.cand_ms[bi.ncand] = ms;
+            ++bi.ncand;
+        }
+    };
+    PmBatchKnobs win{1, 16, 4};
+    float best_ms = -1.0f;
+    s = CVTPM_OK;
+    for (int g : {1, 2, 0}) {                             /* the propagation's grid */
+        S.kn = PmBatchKnobs{g, 16, 4};
+        float ms = 0.0f;
+        s = timed([&] { return phase_propagate(S, S.aL, list0, [](cvtpm_ctx* c, int) { return (const float4*)c->S[0][1]; }, 0); }, &ms);
+        if (s != CVTPM_OK) break;
+        add(S.kn, ms);
+        if (best_ms < 0.0f || ms < best_ms) { best_ms = ms; win.grid_mult = g; }
+    }
+    if (s == CVTPM_OK) {
+        cvtpm_params pd = S.p;
+        S.p.pd_iterations = 8;
+        best_ms = -1.0f;
+        for (int rows : {16, 8})
+            for (int halo : {4, 2})
+                for (int g : {1, 0}) {
+                    S.kn = PmBatchKnobs{g, rows, halo};
+                    float ms = 0.0f;
+                    s = timed([&] { return phase_pd(S, 0, 5.0f); }, &ms);
+                    if (s != CVTPM_OK) break;
+                    add(S.kn, ms);
+                    if (best_ms < 0.0f || ms < best_ms) { best_ms = ms; win.pd_rows = rows; win.pd_halo = halo; }
+                }
+        S.p = pd;
+    }
+    cudaEventDestroy(t0);
+    cudaEventDestroy(t1);
+    if (s != CVTPM_OK) return s;
+    *best = win;
+    return CVTPM_OK;
+}
+
+/* Captures the phase-batched schedule into one graph. */
+cvtpm_status capture_phased(PhaseState& S, cudaGraphExec_t* exec, size_t* nodes) {
+    cvtpm_ctx* ctx = S.ctx;
+    for (int i = 0; i < S.n; ++i) ctx->bpairs[i]->no_alloc = true;
+    CK(cudaStreamBeginCapture(S.st, cudaStreamCaptureModeThreadLocal), "begin capture");
+    S.launches = 0;
+    cvtpm_status err = phase_schedule(S, S.p.iterations);
+    cudaGraph_t graph = nullptr;
+    cudaError_t e = cudaStreamEndCapture(S.st, &graph);
+    for (int i = 0; i < S.n; ++i) ctx->bpairs[i]->no_alloc = false;
+    if (err != CVTPM_OK) { if (graph) cudaGraphDestroy(graph); return err; }
+    if (e != cudaSuccess) { if (graph) cudaGraphDestroy(graph); return cuda_fail(ctx, e, "end capture"); }
+    *nodes = 0;
+    cudaGraphGetNodes(graph, nullptr, nodes);
+    e = cudaGraphInstantiate(exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "graph instantiate");
+    return CVTPM_OK;
+}
+
+}  // namespace
+
+extern "C" {
 
 static cvtpm_status depthmap_batched(cvtpm_ctx* ctx, const cvtpm_pair* pairs, int npairs, void* stream) {
     if (!ctx) return CVTPM_ERR_INVALID_ARGUMENT;
@@ -1072,6 +1488,8 @@ static cvtpm_status depthmap_batched(cvtpm_ctx* ctx, const cvtpm_pair* pairs, in
     put(&pr.grad_maxdiff, sizeof(float)); put(&pr.weight_profile, sizeof(int)); put(&pr.rng, sizeof(int));
     put(&pr.seed, sizeof(uint64_t)); put(&pr.arith, sizeof(int)); put(&pr.schedule, sizeof(int));
     put(&ctx->batch_lanes, sizeof(int));
+    put(&ctx->pinned_knobs, sizeof(bool));
+    put(&ctx->knobs.grid_mult, sizeof(int)); put(&ctx->knobs.pd_rows, sizeof(int)); put(&ctx->knobs.pd_halo, sizeof(int));
     put(&ctx->nb_budget, sizeof(size_t));
     for (int i = 0; i < npairs; ++i) {
         const cvtpm_pair& q = pairs[i];
@@ -1090,10 +1508,46 @@ static cvtpm_status depthmap_batched(cvtpm_ctx* ctx, const cvtpm_pair* pairs, in
     if (ctx->bexec) { cudaGraphExecDestroy(ctx->bexec); ctx->bexec = nullptr; ctx->bkey.clear(); }
     if ((s = ensure_lanes(ctx, 1)) != CVTPM_OK) return s;
     CK(cudaStreamSynchronize(st), "batch order");      /* inputs written on `st` before tuning reads them */
-    int k = ctx->batch_lanes;
+    if (ctx->batch_lanes == 0 && ctx->prm.schedule == CVTPM_SCHEDULE_JACOBI) {
+        /* phase-batched: one launch per phase for all pairs */
+        PhaseState S{ctx, pairs, npairs, ctx->prm, PmBatchKnobs{1, 16, 4}, ctx->bstream, 1, 0, {}, {}};
+        if ((s = phase_prepare(S)) != CVTPM_OK) return s;
+        CK(cudaStreamSynchronize(ctx->bstream), "batch prepare");
+        ctx->binfo.tuned = 0;
+        bool cached = false;
+        if (ctx->pinned_knobs) { S.kn = ctx->knobs; cached = true; }
+        for (auto& tk : ctx->tuned_knobs)
+            if (!cached && tk.first == tkey) { S.kn = tk.second; cached = true; }
+        if (!cached) {
+            const auto c0 = std::chrono::steady_clock::now();
+            PmBatchKnobs best{1, 16, 4};
+            if ((s = tune_phased(S, &best)) != CVTPM_OK) return s;
+            ctx->binfo.tune_ms = std::chrono::duration<float, std::milli>(std::chrono::steady_clock::now() - c0).count();
+            ctx->tuned_knobs.push_back({tkey, best});
+            S.kn = best;
+            ctx->binfo.tuned = 1;
+        }
+        size_t nodes = 0;
+        if ((s = capture_phased(S, &ctx->bexec, &nodes)) != CVTPM_OK) return s;
+        ctx->bkey = key;
+        ctx->binfo.phased = 1;
+        ctx->binfo.lanes = 0;
+        ctx->binfo.grid_mult = S.kn.grid_mult;
+        ctx->binfo.pd_rows = S.kn.pd_rows;
+        ctx->binfo.pd_halo = S.kn.pd_halo;
+        ctx->binfo.launches = S.launches;
+        int nb = 0;
+        for (int i = 0; i < npairs; ++i) nb += ctx->bpairs[i]->nb_on ? 1 : 0;
+        ctx->binfo.shared_windows = nb == npairs ? 1 : 0;
+        ctx->binfo.graph_nodes = (long long)nodes;
+        ctx->binfo.replays = 0;
+        return launch_batch(ctx, ctx->bexec, st);
+    }
+    ctx->binfo.phased = 0;
+    int k = ctx->batch_lanes > 0 ? ctx->batch_lanes : 0;
     ctx->binfo.tuned = 0;
     if (k <= 0) {
-        if (tkey == ctx->tkey) {                         /* same shapes: keep the tuned choice */
+        if (!ctx->tkey.empty() && tkey == ctx->tkey) {   /* same shapes: keep the tuned choice */
             k = ctx->tuned_lanes;
         } else {
             if ((s = tune_batch(ctx, pairs, npairs, &k)) != CVTPM_OK) return s;
@@ -1109,6 +1563,7 @@ static cvtpm_status depthmap_batched(cvtpm_ctx* ctx, const cvtpm_pair* pairs, in
     ctx->binfo.shared_windows = ctx->prm.arith == CVTPM_ARITH_FAST && ctx->nb_budget > 0 ? 1 : 0;
     ctx->binfo.graph_nodes = (long long)nodes;
     ctx->binfo.replays = 0;
+    ctx->binfo.launches = 0;
     return launch_batch(ctx, ctx->bexec, st);
 }
 
@@ -1125,6 +1580,16 @@ cvtpm_status cvtpm_depthmap_batched(cvtpm_ctx* ctx, const cvtpm_pair* pairs, int
 cvtpm_status cvtpm_set_batch_lanes(cvtpm_ctx* ctx, int lanes) {
     if (!ctx || lanes < 0 || lanes > 64) return CVTPM_ERR_INVALID_ARGUMENT;
     ctx->batch_lanes = lanes;
+    return CVTPM_OK;
+}
+
+cvtpm_status cvtpm_set_batch_knobs(cvtpm_ctx* ctx, int grid_mult, int pd_rows, int pd_halo) {
+    if (!ctx) return CVTPM_ERR_INVALID_ARGUMENT;
+    if (grid_mult < 0) { ctx->pinned_knobs = false; return CVTPM_OK; }
+    if (grid_mult > 2 || (pd_rows != 16 && pd_rows != 8) || (pd_halo != 4 && pd_halo != 2))
+        return fail(ctx, CVTPM_ERR_INVALID_ARGUMENT, "batch knobs: grid_mult 0..2, pd_rows 16 or 8, pd_halo 4 or 2");
+    ctx->pinned_knobs = true;
+    ctx->knobs = PmBatchKnobs{grid_mult, pd_rows, pd_halo};
     return CVTPM_OK;
 }
 

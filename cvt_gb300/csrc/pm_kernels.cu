@@ -17,14 +17,18 @@
 #define PM_KERNELS_TU 1
 #include "pm_kernels.cuh"
 
+/* Blocks of 256 threads per SM the FAST propagation is compiled for. */
+#ifndef PM_PROP_MINB
+#define PM_PROP_MINB 2
+#endif
+
 
 /* ------------------------------------------------------------- prep -- */
 #define PREP_T 16
-__global__ void __launch_bounds__(PREP_T * PREP_T)
-k_prep(const float4* __restrict__ img, size_t pitch4, int W, int H,
-       float4* __restrict__ col, float4* __restrict__ grad, float* __restrict__ wgt) {
+PM_DEV void prep_tile(const float4* __restrict__ img, size_t pitch4, int W, int H, float4* __restrict__ col,
+                      float4* __restrict__ grad, float* __restrict__ wgt, int tbx, int tby) {
     __shared__ float g[PREP_T + 2][PREP_T + 2];
-    const int bx = blockIdx.x * PREP_T - 1, by = blockIdx.y * PREP_T - 1;
+    const int bx = tbx * PREP_T - 1, by = tby * PREP_T - 1;
     for (int i = threadIdx.y * PREP_T + threadIdx.x; i < (PREP_T + 2) * (PREP_T + 2); i += PREP_T * PREP_T) {
         int lx = i % (PREP_T + 2), ly = i / (PREP_T + 2);
         int x = bx + lx, y = by + ly;
@@ -36,7 +40,7 @@ k_prep(const float4* __restrict__ img, size_t pitch4, int W, int H,
         g[ly][lx] = v;
     }
     __syncthreads();
-    const int x = blockIdx.x * PREP_T + threadIdx.x, y = blockIdx.y * PREP_T + threadIdx.y;
+    const int x = tbx * PREP_T + threadIdx.x, y = tby * PREP_T + threadIdx.y;
     if (x >= W || y >= H) return;
     const int lx = threadIdx.x + 1, ly = threadIdx.y + 1;
 #define B(dx_, dy_) g[ly + (dy_)][lx + (dx_)]
@@ -53,10 +57,16 @@ k_prep(const float4* __restrict__ img, size_t pitch4, int W, int H,
     wgt[o] = pm_exp(-3.0f * pm_pow(pm_sqrt(ex * ex + ey * ey), 0.8f)) + 0.0001f;
 }
 
-__global__ void k_records(const float4* __restrict__ col, const float4* __restrict__ grad, int W, int H, int rp,
-                          float4* __restrict__ A, float4* __restrict__ Bq, float4* __restrict__ C,
-                          float2* __restrict__ D) {
-    const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y;
+__global__ void __launch_bounds__(PREP_T * PREP_T)
+k_prep(const float4* __restrict__ img, size_t pitch4, int W, int H,
+       float4* __restrict__ col, float4* __restrict__ grad, float* __restrict__ wgt) {
+    prep_tile(img, pitch4, W, H, col, grad, wgt, blockIdx.x, blockIdx.y);
+}
+
+PM_DEV void records_tile(const float4* __restrict__ col, const float4* __restrict__ grad, int W, int H, int rp,
+                         float4* __restrict__ A, float4* __restrict__ Bq, float4* __restrict__ C,
+                         float2* __restrict__ D, int tbx, int y) {
+    const int x = tbx * 128 + threadIdx.x;
     if (x >= W || y >= H) return;
     const size_t o = (size_t)y * rp + x;
     const size_t i0 = (size_t)y * W + x, i1 = (size_t)y * W + min(x + 1, W - 1);
@@ -65,6 +75,12 @@ __global__ void k_records(const float4* __restrict__ col, const float4* __restri
     Bq[o] = f4(g0.y, g0.z, g0.w, c1.x - c0.x);
     C[o] = f4(c1.y - c0.y, c1.z - c0.z, g1.x - g0.x, g1.y - g0.y);
     D[o] = make_float2(g1.z - g0.z, g1.w - g0.w);
+}
+
+__global__ void __launch_bounds__(128) k_records(const float4* __restrict__ col, const float4* __restrict__ grad, int W,
+                                                 int H, int rp, float4* __restrict__ A, float4* __restrict__ Bq,
+                                                 float4* __restrict__ C, float2* __restrict__ D) {
+    records_tile(col, grad, W, H, rp, A, Bq, C, D, blockIdx.x, blockIdx.y);
 }
 
 /* ------------------------------------------------------- init / cost -- */
@@ -81,8 +97,8 @@ PM_DEV void seed_rng(PmRng& rng, const PmPassArgs& a, int x, int y, bool init) {
 }
 
 template <bool EXACT>
-__global__ void __launch_bounds__(256) k_init(PmPassArgs a) {
-    const int x = blockIdx.x * 32 + threadIdx.x, y = blockIdx.y * 8 + threadIdx.y;
+PM_DEV void init_tile(const PmPassArgs& a, int tbx, int tby) {
+    const int x = tbx * 32 + threadIdx.x, y = tby * 8 + threadIdx.y;
     if (x >= a.k.W || y >= a.k.H) return;
     PmRng rng;
     seed_rng(rng, a, x, y, true);
@@ -93,6 +109,9 @@ __global__ void __launch_bounds__(256) k_init(PmPassArgs a) {
     s[0].w = c[0];
     a.out[(size_t)y * a.k.W + x] = s[0];
 }
+
+template <bool EXACT>
+__global__ void __launch_bounds__(256) k_init(PmPassArgs a) { init_tile<EXACT>(a, blockIdx.x, blockIdx.y); }
 
 template <bool EXACT>
 __global__ void __launch_bounds__(256) k_cost_field(PmPassArgs a, const float4* __restrict__ states,
@@ -113,12 +132,12 @@ __global__ void __launch_bounds__(256) k_cost_field(PmPassArgs a, const float4* 
  * two-block cap (it takes 153 registers and one block per SM otherwise: pass
  * 39.2 against 31.6 ms), where it also stops spilling. */
 template <bool EXACT>
-__global__ void __launch_bounds__(256, EXACT ? 1 : 2) k_propagate(PmPassArgs a) {
+PM_DEV void propagate_tile(const PmPassArgs& a, int tbx, int tby) {
     const int W = a.k.W, H = a.k.H;
-    const int y = blockIdx.y * 8 + threadIdx.y;
+    const int y = tby * 8 + threadIdx.y;
     /* red/black passes: thread t of a row owns the t-th pixel of that colour */
-    const int x = a.color < 0 ? blockIdx.x * 32 + threadIdx.x
-                              : 2 * (blockIdx.x * 32 + threadIdx.x) + ((y + a.color) & 1);
+    const int x = a.color < 0 ? tbx * 32 + threadIdx.x
+                              : 2 * (tbx * 32 + threadIdx.x) + ((y + a.color) & 1);
     const bool inside = x < W && y < H;
     const int xc = min(x, W - 1), yc = min(y, H - 1);   /* lanes outside still follow the warp */
     const float cx = (float)xc, cy = (float)yc;
@@ -171,35 +190,33 @@ __global__ void __launch_bounds__(256, EXACT ? 1 : 2) k_propagate(PmPassArgs a) 
 #pragma unroll
         for (int i = 0; i < 4; ++i) accept(s[i], c[i], 1 + b * 4 + i);
     }
-    /* candidate 9: the smoothed plane (:345-352); 10-12: random neighbours (:355-361) */
-    {
-        float4 s[4]; bool act[4] = {true, true, true, true}; float c[4];
-        float4 sc = f4(1.0f - (-smooth.x / smooth.z), 0.0f - (-smooth.y / smooth.z),
-                       0.0f - ((smooth.x * cx + smooth.y * cy) / smooth.z + smooth.w), 0.0f - 0.0f);
-        s[0] = lr ? sc : viewprop(sc);
+    /* candidates 9-16: the smoothed plane (:345-352), six random neighbours
+     * (:355-361), a fresh random plane (:364-368).  FAST evaluates the eight
+     * in one window sweep (1 % faster per pass than two sweeps of four,
+     * measured); EXACT in two, which keeps it at two blocks per SM. */
+    constexpr int NB = EXACT ? 4 : 8;
 #pragma unroll
-        for (int i = 1; i < 4; ++i) {
-            int ox = (int)(rng_float(rng) * 7.0f + 0.5f);
-            int oy = (int)(rng_float(rng) * 7.0f + 0.5f);
-            s[i] = a.old[(size_t)clampi(yc + oy, 0, H - 1) * W + clampi(xc + ox, 0, W - 1)];
+    for (int b0 = 0; b0 < 8; b0 += NB) {
+        float4 s[NB]; bool act[NB]; float c[NB];
+#pragma unroll
+        for (int j = 0; j < NB; ++j) {
+            const int i = b0 + j;
+            act[j] = true;
+            if (i == 0) {
+                const float4 sc = f4(1.0f - (-smooth.x / smooth.z), 0.0f - (-smooth.y / smooth.z),
+                                     0.0f - ((smooth.x * cx + smooth.y * cy) / smooth.z + smooth.w), 0.0f - 0.0f);
+                s[j] = lr ? sc : viewprop(sc);
+            } else if (i < 7) {
+                const int ox = (int)(rng_float(rng) * 7.0f + 0.5f);
+                const int oy = (int)(rng_float(rng) * 7.0f + 0.5f);
+                s[j] = a.old[(size_t)clampi(yc + oy, 0, H - 1) * W + clampi(xc + ox, 0, W - 1)];
+            } else {
+                s[j] = state_init(rng, cx, cy, lr, 2.0f, dmax);
+            }
         }
-        eval_costs<4, EXACT>(a.k, a.v1, a.v2, xc, yc, s, act, c);
+        eval_costs<NB, EXACT>(a.k, a.v1, a.v2, xc, yc, s, act, c);
 #pragma unroll
-        for (int i = 0; i < 4; ++i) accept(s[i], c[i], 9 + i);
-    }
-    /* 13-15: random neighbours; 16: a fresh random plane (:364-368) */
-    {
-        float4 s[4]; bool act[4] = {true, true, true, true}; float c[4];
-#pragma unroll
-        for (int i = 0; i < 3; ++i) {
-            int ox = (int)(rng_float(rng) * 7.0f + 0.5f);
-            int oy = (int)(rng_float(rng) * 7.0f + 0.5f);
-            s[i] = a.old[(size_t)clampi(yc + oy, 0, H - 1) * W + clampi(xc + ox, 0, W - 1)];
-        }
-        s[3] = state_init(rng, cx, cy, lr, 2.0f, dmax);
-        eval_costs<4, EXACT>(a.k, a.v1, a.v2, xc, yc, s, act, c);
-#pragma unroll
-        for (int i = 0; i < 4; ++i) accept(s[i], c[i], 13 + i);
+        for (int j = 0; j < NB; ++j) accept(s[j], c[j], 9 + b0 + j);
     }
     /* 17-20: candidates from the other view (:372-379) */
     int nview_total = 0;
@@ -255,6 +272,11 @@ __global__ void __launch_bounds__(256, EXACT ? 1 : 2) k_propagate(PmPassArgs a) 
             atomicAdd(&a.counters[1], taps);
         }
     }
+}
+
+template <bool EXACT>
+__global__ void __launch_bounds__(256, EXACT ? 1 : PM_PROP_MINB) k_propagate(PmPassArgs a) {
+    propagate_tile<EXACT>(a, blockIdx.x, blockIdx.y);
 }
 
 /* ---------------------------------------- shared neighbour windows -- */
@@ -527,10 +549,10 @@ __device__ __forceinline__ void nbcost_pipe(const PmPassArgs& a, int mx, int my,
 }
 
 template <bool EXACT>
-__global__ void __launch_bounds__(256, 2) k_nbcost(PmPassArgs a) {
+PM_DEV void nbcost_tile(const PmPassArgs& a, int tbx, int tby) {
     const int W = a.k.W, H = a.k.H, P = a.k.P;
-    const int mx0 = blockIdx.x * NB_COLS, lane = threadIdx.x;
-    const int mx = mx0 + lane, my = blockIdx.y * 8 + threadIdx.y;
+    const int mx0 = tbx * NB_COLS, lane = threadIdx.x;
+    const int mx = mx0 + lane, my = tby * 8 + threadIdx.y;
     if (my >= H) return;                                   /* the whole warp */
     if (NB_PIPE && mx0 - P - 1 >= 0 && mx0 + 31 + P + 1 <= W - 1) {
         nbcost_pipe<EXACT>(a, mx, my, lane < NB_COLS);
@@ -540,14 +562,14 @@ __global__ void __launch_bounds__(256, 2) k_nbcost(PmPassArgs a) {
     nbcost_lane<EXACT>(a, mx, my);
 }
 
+template <bool EXACT>
+__global__ void __launch_bounds__(256, 2) k_nbcost(PmPassArgs a) { nbcost_tile<EXACT>(a, blockIdx.x, blockIdx.y); }
+
 /* -------------------------------------------------------- view lists -- */
 /* One warp per row.  Sources are visited in increasing x; the first four
  * that map to a target pixel fill its slots in that order (pmhstereo.cl:394-400
  * executed in raster order). */
-__global__ void __launch_bounds__(32) k_view_list(const float4* __restrict__ src, int W, int H,
-                                                  short4* __restrict__ list) {
-    extern __shared__ int cnt[];
-    const int y = blockIdx.x;
+PM_DEV void view_list_row(const float4* __restrict__ src, int W, int H, short4* __restrict__ list, int* cnt, int y) {
     const int lane = threadIdx.x;
     if (y >= H) return;
     short4* row = list + (size_t)y * W;
@@ -575,11 +597,17 @@ __global__ void __launch_bounds__(32) k_view_list(const float4* __restrict__ src
     }
 }
 
+__global__ void __launch_bounds__(32) k_view_list(const float4* __restrict__ src, int W, int H,
+                                                  short4* __restrict__ list) {
+    extern __shared__ int cnt[];
+    view_list_row(src, W, H, list, cnt, blockIdx.x);
+}
+
 /* ------------------------------------------------------- consistency -- */
-__global__ void k_consistency(const float4* __restrict__ L, const float4* __restrict__ R, int W, int H,
-                              float maxdisp, float athr, int lr, float4* __restrict__ out,
-                              uint8_t* __restrict__ valid) {
-    const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
+PM_DEV void consistency_tile(const float4* __restrict__ L, const float4* __restrict__ R, int W, int H,
+                             float maxdisp, float athr, int lr, float4* __restrict__ out,
+                             uint8_t* __restrict__ valid, int tbx, int tby) {
+    const int x = tbx * 32 + threadIdx.x, y = tby * 8 + threadIdx.y;
     if (x >= W || y >= H) return;
     const size_t o = (size_t)y * W + x;
     float4 sl = L[o];
@@ -595,6 +623,12 @@ __global__ void k_consistency(const float4* __restrict__ L, const float4* __rest
     bool bad = (dm >= maxdisp) || (pm_acospi(ndiff) >= athr);
     out[o] = bad ? f4s(0.0f) : sl;
     if (valid) valid[o] = bad ? 0 : 1;
+}
+
+__global__ void __launch_bounds__(256) k_consistency(const float4* __restrict__ L, const float4* __restrict__ R, int W,
+                                                     int H, float maxdisp, float athr, int lr,
+                                                     float4* __restrict__ out, uint8_t* __restrict__ valid) {
+    consistency_tile(L, R, W, H, maxdisp, athr, lr, out, valid, blockIdx.x, blockIdx.y);
 }
 
 /* pmhstereo_occmap (pmhstereo.cl:682-712): the test of k_consistency with
@@ -659,10 +693,8 @@ PM_DEV void row_scan(const float4* row, int W, int* lftbuf, OK ok, EMIT emit) {
     }
 }
 
-__global__ void __launch_bounds__(32) k_fill_state(const float4* __restrict__ in, int W, int H, float depthmax,
-                                                   int lr, float4* __restrict__ out) {
-    extern __shared__ int lftbuf[];
-    const int y = blockIdx.x;
+PM_DEV void fill_state_row(const float4* __restrict__ in, int W, int H, float depthmax, int lr,
+                           float4* __restrict__ out, int* lftbuf, int y) {
     if (y >= H) return;
     const float4* row = in + (size_t)y * W;
     const float cy = (float)y;
@@ -684,11 +716,14 @@ __global__ void __launch_bounds__(32) k_fill_state(const float4* __restrict__ in
              });
 }
 
-__global__ void __launch_bounds__(32) k_fill_output(const float4* __restrict__ in, int W, int H, float scale,
-                                                    float* __restrict__ dmap, size_t dpitch,
-                                                    float4* __restrict__ nmap, size_t npitch) {
+__global__ void __launch_bounds__(32) k_fill_state(const float4* __restrict__ in, int W, int H, float depthmax,
+                                                   int lr, float4* __restrict__ out) {
     extern __shared__ int lftbuf[];
-    const int y = blockIdx.x;
+    fill_state_row(in, W, H, depthmax, lr, out, lftbuf, blockIdx.x);
+}
+
+PM_DEV void fill_output_row(const float4* __restrict__ in, int W, int H, float scale, float* __restrict__ dmap,
+                            size_t dpitch, float4* __restrict__ nmap, size_t npitch, int* lftbuf, int y) {
     if (y >= H) return;
     const float4* row = in + (size_t)y * W;
     const float cy = (float)y;
@@ -711,6 +746,13 @@ __global__ void __launch_bounds__(32) k_fill_output(const float4* __restrict__ i
                  dmap[(size_t)y * dpitch + x] = v * scale;
                  if (nmap) nmap[(size_t)y * npitch + x] = f4(nx, ny, nz, 0.0f);
              });
+}
+
+__global__ void __launch_bounds__(32) k_fill_output(const float4* __restrict__ in, int W, int H, float scale,
+                                                    float* __restrict__ dmap, size_t dpitch,
+                                                    float4* __restrict__ nmap, size_t npitch) {
+    extern __shared__ int lftbuf[];
+    fill_output_row(in, W, H, scale, dmap, dpitch, nmap, npitch, lftbuf, blockIdx.x);
 }
 
 /* ------------------------------------------------------------ PD step -- */
@@ -823,17 +865,22 @@ k_pd_step(float4* __restrict__ uout, float4* __restrict__ pout, const float4* __
  * tile is exact.  Image borders keep the reference's semantics: u is read
  * clamped to the edge, the dual and the weight are zero outside. */
 #define PDB_TX 32
-#define PDB_TY 16
+#define PDB_TY 16        /* the plain path's tile height; the batch tuner may choose 8 */
 #define PDB_K 4
-#define PDB_RX (PDB_TX + 2 * PDB_K)
-#define PDB_RY (PDB_TY + 2 * PDB_K)
-#define PDB_N (PDB_RX * PDB_RY)
 
-template <bool INPAINT>
-__global__ void __launch_bounds__(PDB_TX * PDB_TY)
-k_pd_block(float4* __restrict__ uout, float4* __restrict__ pout, const float4* __restrict__ uin,
-           const float4* __restrict__ pin, int pzero, const float4* __restrict__ f, const float* __restrict__ wgt,
-           const float* __restrict__ mask, float lambda, int nsteps, int W, int H) {
+/* shared memory of a TY-row tile with a K-pixel halo: u, both duals and f
+ * (float4), w and the dual denominator (float) for every cell of the region */
+constexpr size_t pd_block_smem(int TY, int K = PDB_K) {
+    return (size_t)(PDB_TX + 2 * K) * (TY + 2 * K) * (4 * 16 + 2 * 4);
+}
+
+/* TY rows, at most K steps (K is also the halo width). */
+template <bool INPAINT, int TY, int K = PDB_K>
+PM_DEV void pd_block_tile(float4* __restrict__ uout, float4* __restrict__ pout, const float4* __restrict__ uin,
+                          const float4* __restrict__ pin, int pzero, const float4* __restrict__ f,
+                          const float* __restrict__ wgt, const float* __restrict__ mask, float lambda, int nsteps,
+                          int W, int H, int tbx, int tby) {
+    constexpr int PDB_RX = PDB_TX + 2 * K, PDB_RY = TY + 2 * K, PDB_N = PDB_RX * PDB_RY;
     extern __shared__ __align__(16) float4 sm4[];
     float4* su = sm4;
     float4* slo = su + PDB_N;
@@ -841,8 +888,8 @@ k_pd_block(float4* __restrict__ uout, float4* __restrict__ pout, const float4* _
     float4* sf = shi + PDB_N;
     float* sw = (float*)(sf + PDB_N);
     float* sden = sw + PDB_N;
-    const int tid = threadIdx.y * PDB_TX + threadIdx.x, nt = PDB_TX * PDB_TY;
-    const int rx0 = blockIdx.x * PDB_TX - PDB_K, ry0 = blockIdx.y * PDB_TY - PDB_K;
+    const int tid = threadIdx.y * PDB_TX + threadIdx.x, nt = PDB_TX * TY;
+    const int rx0 = tbx * PDB_TX - K, ry0 = tby * TY - K;
     for (int i = tid; i < PDB_N; i += nt) {
         const int gx = rx0 + i % PDB_RX, gy = ry0 + i / PDB_RX;
         const bool in = gx >= 0 && gy >= 0 && gx < W && gy < H;
@@ -867,7 +914,7 @@ k_pd_block(float4* __restrict__ uout, float4* __restrict__ pout, const float4* _
     /* Step st updates the duals at ring distance >= st from the region edge and
      * the primal at distance >= st+1: by induction u is exact at distance
      * >= st+1 afterwards (its left/upper duals at distance >= st are exact), so
-     * after the last step the tile (distance PDB_K) is. */
+     * after the last step the tile (distance K) is. */
     for (int st = 0; st < nsteps; ++st) {
         const int dw = PDB_RX - 2 * st, dh = PDB_RY - 2 * st;
         for (int k = tid; k < dw * dh; k += nt) {                     /* duals */
@@ -895,8 +942,8 @@ k_pd_block(float4* __restrict__ uout, float4* __restrict__ pout, const float4* _
         }
         __syncthreads();
     }
-    for (int i = tid; i < PDB_TX * PDB_TY; i += nt) {
-        const int lx = PDB_K + i % PDB_TX, ly = PDB_K + i / PDB_TX;
+    for (int i = tid; i < PDB_TX * TY; i += nt) {
+        const int lx = K + i % PDB_TX, ly = K + i / PDB_TX;
         const int gx = rx0 + lx, gy = ry0 + ly;
         if (gx >= W || gy >= H) continue;
         const int r = ly * PDB_RX + lx;
@@ -904,6 +951,123 @@ k_pd_block(float4* __restrict__ uout, float4* __restrict__ pout, const float4* _
         uout[o] = su[r];
         pout[o * 2] = slo[r];
         pout[o * 2 + 1] = shi[r];
+    }
+}
+
+template <bool INPAINT>
+__global__ void __launch_bounds__(PDB_TX * PDB_TY)
+k_pd_block(float4* __restrict__ uout, float4* __restrict__ pout, const float4* __restrict__ uin,
+           const float4* __restrict__ pin, int pzero, const float4* __restrict__ f, const float* __restrict__ wgt,
+           const float* __restrict__ mask, float lambda, int nsteps, int W, int H) {
+    pd_block_tile<INPAINT, PDB_TY>(uout, pout, uin, pin, pzero, f, wgt, mask, lambda, nsteps, W, H, blockIdx.x,
+                                   blockIdx.y);
+}
+
+/* ------------------------------------------------------ batched phases -- */
+/* The kernels of cvtpm_depthmap_batched: one launch per phase for many
+ * pairs.  Block b walks the flat item list b, b + gridDim.x, ...; the pair
+ * of an item is found by a block-uniform binary search over first[], and
+ * the pair's arguments are read from the kernel parameter with that uniform
+ * index.  Every item runs the plain kernel's tile body, so each pair's
+ * results are those of its plain launches. */
+template <typename A>
+PM_DEV int batch_pair(const PmBatch<A>& b, int item) {
+    int lo = 0, hi = b.n - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (b.first[mid] <= item) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
+__global__ void __launch_bounds__(PREP_T * PREP_T) kb_prep(const __grid_constant__ PmBatch<PmPrepArgs> b) {
+    for (int item = blockIdx.x; item < b.first[b.n]; item += gridDim.x) {
+        const int p = batch_pair(b, item), t = item - b.first[p];
+        const PmPrepArgs& a = b.a[p];
+        __syncthreads();                                 /* the tile's shared rows are reused */
+        prep_tile(a.img, a.pitch4, a.W, a.H, a.col, a.grad, a.wgt, t % b.tx[p], t / b.tx[p]);
+    }
+}
+
+__global__ void __launch_bounds__(128) kb_records(const __grid_constant__ PmBatch<PmRecArgs> b) {
+    for (int item = blockIdx.x; item < b.first[b.n]; item += gridDim.x) {
+        const int p = batch_pair(b, item), t = item - b.first[p];
+        const PmRecArgs& a = b.a[p];
+        records_tile(a.col, a.grad, a.W, a.H, a.rp, a.A, a.B, a.C, a.D, t % b.tx[p], t / b.tx[p]);
+    }
+}
+
+template <bool EXACT>
+__global__ void __launch_bounds__(256) kb_init(const __grid_constant__ PmBatch<PmPassArgs> b) {
+    for (int item = blockIdx.x; item < b.first[b.n]; item += gridDim.x) {
+        const int p = batch_pair(b, item), t = item - b.first[p];
+        init_tile<EXACT>(b.a[p], t % b.tx[p], t / b.tx[p]);
+    }
+}
+
+template <bool EXACT>
+__global__ void __launch_bounds__(256, 2) kb_nbcost(const __grid_constant__ PmBatch<PmPassArgs> b) {
+    for (int item = blockIdx.x; item < b.first[b.n]; item += gridDim.x) {
+        const int p = batch_pair(b, item), t = item - b.first[p];
+        nbcost_tile<EXACT>(b.a[p], t % b.tx[p], t / b.tx[p]);
+    }
+}
+
+template <bool EXACT>
+__global__ void __launch_bounds__(256, 2) kb_propagate(const __grid_constant__ PmBatch<PmPassArgs> b) {
+    for (int item = blockIdx.x; item < b.first[b.n]; item += gridDim.x) {
+        const int p = batch_pair(b, item), t = item - b.first[p];
+        propagate_tile<EXACT>(b.a[p], t % b.tx[p], t / b.tx[p]);
+    }
+}
+
+__global__ void __launch_bounds__(32) kb_view_list(const __grid_constant__ PmBatch<PmViewListArgs> b) {
+    extern __shared__ int cnt[];
+    for (int item = blockIdx.x; item < b.first[b.n]; item += gridDim.x) {
+        const int p = batch_pair(b, item), t = item - b.first[p];
+        const PmViewListArgs& a = b.a[p];
+        __syncwarp();                                    /* the row counters are reused */
+        view_list_row(a.src, a.W, a.H, a.list, cnt, t);
+    }
+}
+
+__global__ void __launch_bounds__(256) kb_consistency(const __grid_constant__ PmBatch<PmConsArgs> b) {
+    for (int item = blockIdx.x; item < b.first[b.n]; item += gridDim.x) {
+        const int p = batch_pair(b, item), t = item - b.first[p];
+        const PmConsArgs& a = b.a[p];
+        consistency_tile(a.L, a.R, a.W, a.H, a.maxdisp, a.athr, a.lr, a.out, a.valid, t % b.tx[p], t / b.tx[p]);
+    }
+}
+
+__global__ void __launch_bounds__(32) kb_fill_state(const __grid_constant__ PmBatch<PmFillArgs> b) {
+    extern __shared__ int lftbuf[];
+    for (int item = blockIdx.x; item < b.first[b.n]; item += gridDim.x) {
+        const int p = batch_pair(b, item), t = item - b.first[p];
+        const PmFillArgs& a = b.a[p];
+        __syncwarp();
+        fill_state_row(a.in, a.W, a.H, a.depthmax, a.lr, a.out, lftbuf, t);
+    }
+}
+
+__global__ void __launch_bounds__(32) kb_fill_output(const __grid_constant__ PmBatch<PmOutArgs> b) {
+    extern __shared__ int lftbuf[];
+    for (int item = blockIdx.x; item < b.first[b.n]; item += gridDim.x) {
+        const int p = batch_pair(b, item), t = item - b.first[p];
+        const PmOutArgs& a = b.a[p];
+        __syncwarp();
+        fill_output_row(a.in, a.W, a.H, a.scale, a.dmap, a.dpitch, a.nmap, a.npitch, lftbuf, t);
+    }
+}
+
+template <int TY, int K>
+__global__ void __launch_bounds__(PDB_TX * TY) kb_pd_block(const __grid_constant__ PmBatch<PmPdArgs> b) {
+    for (int item = blockIdx.x; item < b.first[b.n]; item += gridDim.x) {
+        const int p = batch_pair(b, item), t = item - b.first[p];
+        const PmPdArgs& a = b.a[p];
+        __syncthreads();                                 /* the region in shared memory is reused */
+        pd_block_tile<false, TY, K>(a.uout, a.pout, a.uin, a.pin, a.pzero, a.f, a.wgt, nullptr, a.lambda, a.nsteps, a.W,
+                                 a.H, t % b.tx[p], t / b.tx[p]);
     }
 }
 
@@ -997,12 +1161,14 @@ cudaError_t pm_launch_fill_output(const float4* in, int W, int H, float scale, f
 
 int pm_pd_block_steps() { return PDB_K; }
 
-static const size_t kPdBlockSmem = (size_t)PDB_N * (4 * sizeof(float4) + 2 * sizeof(float));
+static const size_t kPdBlockSmem = pd_block_smem(PDB_TY);
 
 cudaError_t pm_prepare_kernels() {
     cudaError_t e = cudaFuncSetAttribute(k_pd_block<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kPdBlockSmem);
     if (e != cudaSuccess) return e;
-    return cudaFuncSetAttribute(k_pd_block<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kPdBlockSmem);
+    e = cudaFuncSetAttribute(k_pd_block<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kPdBlockSmem);
+    if (e != cudaSuccess) return e;
+    return pm_batch_prepare_kernels();
 }
 
 cudaError_t pm_launch_pd_block(float4* uout, float4* pout, const float4* uin, const float4* pin, int pzero,
@@ -1057,4 +1223,101 @@ cudaError_t pm_launch_ffma_peak(float* out, int blocks, int iters, cudaStream_t 
     k_ffma_peak<<<blocks, 256, 0, st>>>(out, iters, 0.999999f, 1e-6f);
     PM_LAUNCH_CHECK();
     return cudaSuccess;
+}
+
+/* ------------------------------------------------- batched launchers -- */
+void pm_batch_tiles(PmBatchKernel k, int W, int H, const PmBatchKnobs& kn, int* tx, int* tiles) {
+    int x = 1, y = 1;
+    switch (k) {
+    case PMB_PREP: x = (W + PREP_T - 1) / PREP_T; y = (H + PREP_T - 1) / PREP_T; break;
+    case PMB_RECORDS: x = (W + 127) / 128; y = H; break;
+    case PMB_PIXEL: x = (W + 31) / 32; y = (H + 7) / 8; break;
+    case PMB_NBCOST: x = (W + NB_COLS - 1) / NB_COLS; y = (H + 7) / 8; break;
+    case PMB_ROW: x = 1; y = H; break;
+    case PMB_PD: {
+        const int rows = kn.pd_rows == 8 ? 8 : 16;
+        x = (W + PDB_TX - 1) / PDB_TX;
+        y = (H + rows - 1) / rows;
+        break;
+    }
+    }
+    *tx = x;
+    *tiles = x * y;
+}
+
+namespace {
+/* Persistent grid: `mult` x the blocks of `kern` resident per SM, x the SM
+ * count, capped at the item count; mult 0 launches one block per item. */
+template <typename K>
+unsigned batch_grid(K kern, int threads, size_t smem, int items, int mult) {
+    if (mult <= 0) return (unsigned)items;
+    static int nsm = 0;
+    if (!nsm) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+        if (nsm <= 0) nsm = 1;
+    }
+    int per = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kern, threads, smem) != cudaSuccess || per < 1) per = 1;
+    const long long g = (long long)nsm * per * mult;
+    return (unsigned)(g < items ? g : items);
+}
+}  // namespace
+
+#define PM_BATCH_LAUNCH(kern, threads, smem)                                                          \
+    do {                                                                                             \
+        const int items_ = b.first[b.n];                                                             \
+        if (items_ <= 0) return cudaSuccess;                                                         \
+        kern<<<batch_grid(kern, (threads).x * (threads).y, (smem), items_, kn.grid_mult), (threads), (smem), st>>>(b); \
+        PM_LAUNCH_CHECK();                                                                           \
+        return cudaSuccess;                                                                          \
+    } while (0)
+
+cudaError_t pm_batch_prep(const PmBatch<PmPrepArgs>& b, const PmBatchKnobs& kn, cudaStream_t st) {
+    PM_BATCH_LAUNCH(kb_prep, dim3(PREP_T, PREP_T), 0);
+}
+cudaError_t pm_batch_records(const PmBatch<PmRecArgs>& b, const PmBatchKnobs& kn, cudaStream_t st) {
+    PM_BATCH_LAUNCH(kb_records, dim3(128), 0);
+}
+cudaError_t pm_batch_init(const PmBatch<PmPassArgs>& b, bool exact, const PmBatchKnobs& kn, cudaStream_t st) {
+    if (exact) PM_BATCH_LAUNCH(kb_init<true>, dim3(32, 8), 0);
+    PM_BATCH_LAUNCH(kb_init<false>, dim3(32, 8), 0);
+}
+cudaError_t pm_batch_nbcost(const PmBatch<PmPassArgs>& b, bool exact, const PmBatchKnobs& kn, cudaStream_t st) {
+    if (exact) PM_BATCH_LAUNCH(kb_nbcost<true>, dim3(32, 8), 0);
+    PM_BATCH_LAUNCH(kb_nbcost<false>, dim3(32, 8), 0);
+}
+cudaError_t pm_batch_propagate(const PmBatch<PmPassArgs>& b, bool exact, const PmBatchKnobs& kn, cudaStream_t st) {
+    if (exact) PM_BATCH_LAUNCH(kb_propagate<true>, dim3(32, 8), 0);
+    PM_BATCH_LAUNCH(kb_propagate<false>, dim3(32, 8), 0);
+}
+cudaError_t pm_batch_view_list(const PmBatch<PmViewListArgs>& b, int maxW, const PmBatchKnobs& kn, cudaStream_t st) {
+    PM_BATCH_LAUNCH(kb_view_list, dim3(32), sizeof(int) * (size_t)maxW);
+}
+cudaError_t pm_batch_consistency(const PmBatch<PmConsArgs>& b, const PmBatchKnobs& kn, cudaStream_t st) {
+    PM_BATCH_LAUNCH(kb_consistency, dim3(32, 8), 0);
+}
+cudaError_t pm_batch_fill_state(const PmBatch<PmFillArgs>& b, int maxW, const PmBatchKnobs& kn, cudaStream_t st) {
+    PM_BATCH_LAUNCH(kb_fill_state, dim3(32), sizeof(int) * (size_t)maxW);
+}
+cudaError_t pm_batch_fill_output(const PmBatch<PmOutArgs>& b, int maxW, const PmBatchKnobs& kn, cudaStream_t st) {
+    PM_BATCH_LAUNCH(kb_fill_output, dim3(32), sizeof(int) * (size_t)maxW);
+}
+/* b.tx / b.first describe tiles of kn.pd_rows rows (pm_batch_tiles). */
+cudaError_t pm_batch_pd(const PmBatch<PmPdArgs>& b, const PmBatchKnobs& kn, cudaStream_t st) {
+    if (kn.pd_rows == 8 && kn.pd_halo == 2) PM_BATCH_LAUNCH((kb_pd_block<8, 2>), dim3(PDB_TX, 8), pd_block_smem(8, 2));
+    if (kn.pd_rows == 8) PM_BATCH_LAUNCH((kb_pd_block<8, 4>), dim3(PDB_TX, 8), pd_block_smem(8, 4));
+    if (kn.pd_halo == 2) PM_BATCH_LAUNCH((kb_pd_block<16, 2>), dim3(PDB_TX, 16), pd_block_smem(16, 2));
+    PM_BATCH_LAUNCH((kb_pd_block<16, 4>), dim3(PDB_TX, 16), pd_block_smem(16, 4));
+}
+cudaError_t pm_batch_prepare_kernels() {
+    cudaError_t e;
+    if ((e = cudaFuncSetAttribute(kb_pd_block<16, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)pd_block_smem(16, 4))) != cudaSuccess) return e;
+    if ((e = cudaFuncSetAttribute(kb_pd_block<8, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)pd_block_smem(8, 4))) != cudaSuccess) return e;
+    if ((e = cudaFuncSetAttribute(kb_pd_block<16, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)pd_block_smem(16, 2))) != cudaSuccess) return e;
+    return cudaFuncSetAttribute(kb_pd_block<8, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)pd_block_smem(8, 2));
 }

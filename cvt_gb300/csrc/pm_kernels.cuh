@@ -29,6 +29,64 @@ struct PmPassArgs {
     int color;                 /* -1: every pixel (Jacobi); 0 / 1: pixels with (x + y) & 1 == color */
 };
 
+/* ------------------------------------------------------------------
+ * Batched launches (cvtpm_depthmap_batched).  One launch runs one phase of
+ * the depthMap schedule for many pairs: its blocks walk a flat list of work
+ * items, pair i owning items first[i] .. first[i+1]-1, whose item t is the
+ * tile (t % tx[i], t / tx[i]) of that pair (a row, for the row-scan
+ * kernels).  Blocks are persistent: block b takes items b, b + gridDim.x,
+ * ...  The pairs' arguments travel in the kernel parameter (at most
+ * PM_BATCH_MAX pairs per launch), read through a block-uniform index.
+ * ------------------------------------------------------------------ */
+#define PM_BATCH_MAX 64
+
+template <typename A>
+struct PmBatch {
+    int n;                          /* pairs of this launch */
+    int first[PM_BATCH_MAX + 1];    /* first item of each pair; first[n] = items */
+    int tx[PM_BATCH_MAX];           /* tiles per row of each pair */
+    A a[PM_BATCH_MAX];
+};
+
+struct PmPrepArgs { const float4* img; size_t pitch4; int W, H; float4* col; float4* grad; float* wgt; };
+struct PmRecArgs { const float4* col; const float4* grad; int W, H, rp; float4 *A, *B, *C; float2* D; };
+struct PmViewListArgs { const float4* src; int W, H; short4* list; };
+struct PmConsArgs { const float4 *L, *R; int W, H; float maxdisp, athr; int lr; float4* out; uint8_t* valid; };
+struct PmFillArgs { const float4* in; int W, H; float depthmax; int lr; float4* out; };
+struct PmOutArgs { const float4* in; int W, H; float scale; float* dmap; size_t dpitch; float4* nmap; size_t npitch; };
+struct PmPdArgs {
+    float4 *uout, *pout;
+    const float4 *uin, *pin, *f;
+    const float* wgt;
+    int pzero, nsteps, W, H;
+    float lambda;
+};
+
+/* Launch knobs the batch autotuner chooses. */
+struct PmBatchKnobs {
+    int grid_mult;     /* persistent grid: this many x the blocks resident per SM x the SMs; 0 = one block per item */
+    int pd_rows;       /* PD tile height: 16 or 8 */
+    int pd_halo;       /* PD steps per launch, which is also the tile's halo width: 4 or 2 */
+};
+
+/* Tile geometry of each batched kernel (items per pair = tiles). */
+enum PmBatchKernel { PMB_PREP, PMB_RECORDS, PMB_PIXEL, PMB_NBCOST, PMB_ROW, PMB_PD };
+void pm_batch_tiles(PmBatchKernel k, int W, int H, const PmBatchKnobs& kn, int* tx, int* tiles);
+
+cudaError_t pm_batch_prep(const PmBatch<PmPrepArgs>& b, const PmBatchKnobs& kn, cudaStream_t st);
+cudaError_t pm_batch_records(const PmBatch<PmRecArgs>& b, const PmBatchKnobs& kn, cudaStream_t st);
+cudaError_t pm_batch_init(const PmBatch<PmPassArgs>& b, bool exact, const PmBatchKnobs& kn, cudaStream_t st);
+cudaError_t pm_batch_nbcost(const PmBatch<PmPassArgs>& b, bool exact, const PmBatchKnobs& kn, cudaStream_t st);
+cudaError_t pm_batch_propagate(const PmBatch<PmPassArgs>& b, bool exact, const PmBatchKnobs& kn, cudaStream_t st);
+cudaError_t pm_batch_view_list(const PmBatch<PmViewListArgs>& b, int maxW, const PmBatchKnobs& kn, cudaStream_t st);
+cudaError_t pm_batch_consistency(const PmBatch<PmConsArgs>& b, const PmBatchKnobs& kn, cudaStream_t st);
+cudaError_t pm_batch_fill_state(const PmBatch<PmFillArgs>& b, int maxW, const PmBatchKnobs& kn, cudaStream_t st);
+cudaError_t pm_batch_pd(const PmBatch<PmPdArgs>& b, const PmBatchKnobs& kn, cudaStream_t st);
+cudaError_t pm_batch_fill_output(const PmBatch<PmOutArgs>& b, int maxW, const PmBatchKnobs& kn, cudaStream_t st);
+/* Shared-memory limits of the batched PD kernels; once per device before
+ * the first launch or capture. */
+cudaError_t pm_batch_prepare_kernels();
+
 cudaError_t pm_upload_tables(const unsigned long long* pow2, const float* prof, cudaStream_t st);
 cudaError_t pm_launch_prep(const float4* img, size_t pitch4, int W, int H, float4* col, float4* grad,
                            float* wgt, cudaStream_t st);

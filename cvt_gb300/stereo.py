@@ -260,6 +260,10 @@ class PMHuberStereo:
         """Fix the lane count of depthMapBatched (0: autotune)."""
         self._check(_lib.lib().cvtpm_set_batch_lanes(self._h, int(lanes)))
 
+    def set_batch_knobs(self, grid_mult: int = -1, pd_rows: int = 16, pd_halo: int = 4) -> None:
+        """Pin the phase-batched launch knobs (grid_mult -1: autotune)."""
+        self._check(_lib.lib().cvtpm_set_batch_knobs(self._h, int(grid_mult), int(pd_rows), int(pd_halo)))
+
     def batch_info(self) -> dict:
         info = _lib.CvtpmBatchInfo()
         self._check(_lib.lib().cvtpm_get_batch_info(self._h, ctypes.byref(info)))

@@ -271,31 +271,64 @@ cvtpm_status cvtpm_cost_eval_noalloc(const cvtpm_params* params,
  * (pair.depthmax) in one CUDA-graph launch; no counterpart in the reference,
  * which handles one pair per call.  Each pair's result is bit-identical to
  * cvtpm_depthmap on that pair with the context's parameters (normal map and
- * trace are not produced).  The pairs are spread over lanes, each with its
- * own scratch and stream; the whole launch sequence of every lane is captured
- * into one graph, which is replayed while the context's parameters and the
- * pair descriptors (pointers, sizes, depthmax) stay the same.  Capture and
- * tuning synchronise `stream` once; replays do not.  With the lane count 0
- * (default) the first call of a new batch runs the autotuner: it times
- * one-iteration proxies of the batch for 1, 2, 4 and 8 lanes and keeps the
- * fastest (cvtpm_get_batch_info reports the candidates). */
+ * trace are not produced).
+ *
+ * Default (lane count 0, Jacobi schedule): phase-batched.  Every phase of
+ * the depthMap schedule (prep, init, per iteration the neighbour costs,
+ * propagation and view lists of each view, the consistency checks, fills
+ * and PD smoother steps, the final fill) is ONE launch covering all pairs:
+ * persistent blocks walk a flat list of (pair, tile) work items, with the
+ * pairs' arguments in the kernel parameter (up to 64 pairs per launch).  So
+ * a batch takes the launches of one plain call, not one call per pair.  The
+ * first call of a batch shape runs the autotuner on the batch's own data:
+ * it times the propagation with persistent grids of 1 or 2 times the
+ * resident blocks per SM or one block per work item, and the PD smoother
+ * with 16- or 8-row tiles and 4 or 2 steps per launch (the steps are the
+ * halo width of its shared-memory tile), and keeps the fastest of each;
+ * the choice is cached per shape (widths, heights, disparity ranges and
+ * parameters) in the context.  Each pair gets its own scratch.
+ *
+ * With a lane count k >= 1 (cvtpm_set_batch_lanes), or with the red/black
+ * schedule: the pairs are spread over k lanes, each with its own scratch
+ * and stream, and each pair's plain launch sequence is captured on its
+ * lane's branch of the graph.
+ *
+ * Either graph is replayed while the context's parameters and the pair
+ * descriptors (pointers, sizes, depthmax) stay the same.  Capture and tuning
+ * synchronise `stream` once; replays do not. */
 cvtpm_status cvtpm_depthmap_batched(cvtpm_ctx* ctx, const cvtpm_pair* pairs,
                                     int npairs, void* stream);
 
-#define CVTPM_BATCH_MAX_CAND 8
+#define CVTPM_BATCH_MAX_CAND 16
 typedef struct cvtpm_batch_info {
-    int lanes;                 /* lanes of the current graph */
-    int shared_windows;        /* shared-window neighbour costs in use (within the memory budget) */
-    int tuned;                 /* 1 if the autotuner chose the configuration */
+    int lanes;                 /* lanes of the current graph (0: phase-batched) */
+    int shared_windows;        /* shared-window neighbour costs in use for every pair */
+    int tuned;                 /* 1 if the autotuner ran for the current graph */
     int ncand;
-    int cand_lanes[CVTPM_BATCH_MAX_CAND];
-    float cand_ms[CVTPM_BATCH_MAX_CAND];   /* one-iteration proxy time */
+    int cand_lanes[CVTPM_BATCH_MAX_CAND];     /* lane count of a lane candidate, 0 for a phase-batched one */
+    float cand_ms[CVTPM_BATCH_MAX_CAND];      /* its timed proxy: a one-iteration batch (lanes), one
+                                                 propagation phase or one 8-step PD apply (phase-batched) */
     long long graph_nodes;
     long long replays;
+    int phased;                /* 1: phase-batched graph */
+    int grid_mult;             /* chosen persistent grid (x resident blocks per SM; 0: a block per item) */
+    int pd_rows;               /* chosen PD tile height */
+    int pd_halo;               /* chosen PD steps per launch (= halo width) */
+    int cand_grid_mult[CVTPM_BATCH_MAX_CAND];
+    int cand_pd_rows[CVTPM_BATCH_MAX_CAND];
+    int cand_pd_halo[CVTPM_BATCH_MAX_CAND];
+    long long launches;        /* kernel launches in the phase-batched graph */
+    float tune_ms;             /* host time the last tuning took */
 } cvtpm_batch_info;
 
-/* Fix the lane count of cvtpm_depthmap_batched (0: autotune). */
+/* The lane count of cvtpm_depthmap_batched: 0 (default) for the
+ * phase-batched launches, k >= 1 for k lanes of per-pair launch sequences. */
 cvtpm_status cvtpm_set_batch_lanes(cvtpm_ctx* ctx, int lanes);
+/* Pin the phase-batched launch knobs instead of tuning them: grid_mult 0
+ * (a block per work item), 1 or 2 (persistent grid of that many times the
+ * resident blocks per SM); pd_rows 16 or 8; pd_halo 4 or 2.  grid_mult -1
+ * returns to autotuning.  Results never depend on the knobs. */
+cvtpm_status cvtpm_set_batch_knobs(cvtpm_ctx* ctx, int grid_mult, int pd_rows, int pd_halo);
 cvtpm_status cvtpm_get_batch_info(const cvtpm_ctx* ctx, cvtpm_batch_info* out);
 
 /* ------------------------------------------------------------------

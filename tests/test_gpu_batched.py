@@ -1,7 +1,10 @@
 """cvtpm_depthmap_batched: many pairs of uneven size and disparity range in
 one captured graph.  Every pair's disparity map must be bit-identical to the
-plain per-pair cvtpm_depthmap with the same parameters, for the autotuned
-lane count, on graph replays and for fixed lane counts."""
+plain per-pair cvtpm_depthmap with the same parameters: in the default
+phase-batched mode (one launch per phase for all pairs, autotuned or with
+every pinned combination of launch knobs, more pairs than one launch holds,
+PD step counts even, odd and zero), on graph replays, and in the lane mode
+with fixed lane counts."""
 import numpy as np
 import pytest
 import torch
@@ -50,9 +53,48 @@ def test_batched_matches_plain_per_pair(cuda, preset):
             assert not bit_diff(g.cpu().numpy(), w).any(), f"pair {i}, call {attempt}"
     info = bat.batch_info()
     assert info["tuned"] == 1 and info["replays"] == 1
-    assert info["lanes"] in (1, 2, 4, 8) and len(info["candidates"]) >= 2
-    assert info["shared_windows"] == (1 if preset == PRESET_BASELINE else 0)
-    assert all(c["proxy_ms"] > 0 for c in info["candidates"])
+    assert info["phased"] == 1 and info["lanes"] == 0
+    assert info["grid_mult"] in (0, 1, 2) and info["pd_rows"] in (8, 16) and info["pd_halo"] in (2, 4)
+    assert len(info["candidates"]) == 11 and all(c["proxy_ms"] > 0 for c in info["candidates"])
+    assert info["shared_windows"] == 1
+    # one launch per phase for all pairs: about one plain call's launches, not one call's per pair
+    plain.reset_stats()
+    plain.depthMap(torch.empty(0, device="cuda"), pairs[0][0], pairs[0][1], p.patchsize, pairs[0][2], p.iterations, 4)
+    torch.cuda.synchronize()
+    assert 0 < info["launches"] <= 2 * plain.stats()["launches"] < len(pairs) * plain.stats()["launches"]
+
+
+@pytest.mark.parametrize("knobs", [(0, 16, 4), (1, 8, 2), (2, 8, 4), (1, 16, 2)])
+@pytest.mark.parametrize("pd_iterations", [0, 7, 12])
+def test_phased_knobs_match_plain(cuda, knobs, pd_iterations):
+    from cvt_gb300.stereo import PMHuberStereo
+    p = default_params(PRESET_BASELINE, patchsize=5, iterations=2, pd_iterations=pd_iterations)
+    pairs = _pairs(SIZES[:4], seed0=700)
+    want = _plain(PMHuberStereo(0, p), pairs, p)
+    bat = PMHuberStereo(0, p)
+    bat.set_batch_knobs(*knobs)
+    got = bat.depthMapBatched(pairs)
+    torch.cuda.synchronize()
+    info = bat.batch_info()
+    assert info["tuned"] == 0 and (info["grid_mult"], info["pd_rows"], info["pd_halo"]) == knobs
+    for i, (g, w) in enumerate(zip(got, want)):
+        assert not bit_diff(g.cpu().numpy(), w).any(), f"pair {i}"
+
+
+def test_phased_more_pairs_than_one_launch_holds(cuda):
+    """70 small pairs: every phase takes two launches (64 + 6 pairs)."""
+    from cvt_gb300.stereo import PMHuberStereo
+    p = default_params(PRESET_BASELINE, patchsize=3, iterations=2, pd_iterations=4)
+    rng = np.random.default_rng(9)
+    sizes = [(int(rng.integers(8, 40)), int(rng.integers(6, 24)), float(rng.choice([4.0, 6.0, 9.0]))) for _ in range(70)]
+    pairs = _pairs(sizes, seed0=900)
+    want = _plain(PMHuberStereo(0, p), pairs, p)
+    bat = PMHuberStereo(0, p)
+    bat.set_batch_knobs(1, 16, 4)
+    got = bat.depthMapBatched(pairs)
+    torch.cuda.synchronize()
+    for i, (g, w) in enumerate(zip(got, want)):
+        assert not bit_diff(g.cpu().numpy(), w).any(), f"pair {i}"
 
 
 def test_batched_fixed_lanes_and_changed_batch(cuda):
@@ -68,12 +110,15 @@ def test_batched_fixed_lanes_and_changed_batch(cuda):
         assert bat.batch_info()["lanes"] == lanes and bat.batch_info()["tuned"] == 0
         for g, w in zip(got, want):
             assert not bit_diff(g.cpu().numpy(), w).any()
-    # a different batch on the same context re-captures
+    # a different batch on the same context re-captures, in either mode
     pairs2 = pairs[::-1]
-    got = bat.depthMapBatched(pairs2)
-    torch.cuda.synchronize()
-    for g, w in zip(got, want[::-1]):
-        assert not bit_diff(g.cpu().numpy(), w).any()
+    for lanes in (1, 0):
+        bat.set_batch_lanes(lanes)
+        got = bat.depthMapBatched(pairs2)
+        torch.cuda.synchronize()
+        assert bat.batch_info()["phased"] == (1 if lanes == 0 else 0)
+        for g, w in zip(got, want[::-1]):
+            assert not bit_diff(g.cpu().numpy(), w).any()
 
 
 def test_batched_rejects_bad_pairs(cuda):
