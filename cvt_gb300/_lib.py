@@ -26,7 +26,7 @@ EXPORTS = (
     "cvtpm_ppm_read", "cvtpm_pfm_write", "cvtpm_png_read", "cvtpm_png_write", "cvtpm_float_to_srgb_u8", "cvtpm_stereo_rectify", "cvtpm_warp_apply",
     "cvtpm_tsdf_create", "cvtpm_tsdf_destroy", "cvtpm_tsdf_info", "cvtpm_tsdf_clear", "cvtpm_tsdf_projection",
     "cvtpm_tsdf_add_depthmap", "cvtpm_tsdf_raycast", "cvtpm_tsdf_slice", "cvtpm_tsdf_save_raw",
-    "cvtpm_disparity_to_depth", "cvtpm_gcv_set_batch", "cvtpm_gcv_plan", "cvtpm_gcv_depthmap", "cvtpm_gcv_apply",
+    "cvtpm_disparity_to_depth", "cvtpm_gcv_set_batch", "cvtpm_gcv_trim", "cvtpm_gcv_plan", "cvtpm_gcv_depthmap", "cvtpm_gcv_apply",
 )
 
 
@@ -167,6 +167,7 @@ def lib() -> ctypes.CDLL:
     L.cvtpm_tsdf_save_raw.argtypes = [vp, ctypes.c_char_p, i]
     L.cvtpm_disparity_to_depth.argtypes = [vp, sz, vp, sz, i, i, f, f, f, f, vp]
     L.cvtpm_gcv_set_batch.argtypes = [i]
+    L.cvtpm_gcv_trim.argtypes = [i, sz]
     L.cvtpm_gcv_plan.argtypes = [i, i, f, f, f, vp, vp, vp, vp]
     L.cvtpm_gcv_depthmap.argtypes = [vp, sz, vp, vp, i, i, sz, f, f, f, vp]
     L.cvtpm_gcv_apply.argtypes = [vp, sz, vp, vp, sz, vp, vp, i, i, sz, f, f, f, vp]

@@ -137,6 +137,34 @@ struct NvtxRange {
     NvtxRange& operator=(const NvtxRange&) = delete;
 };
 
+/* Ends a stream capture that an exception interrupted (a failed host
+ * allocation inside the captured host code): the partial graph is discarded
+ * and the contexts' capture flags are cleared, so the stream and the
+ * contexts stay usable.  release() after the normal end of the capture. */
+struct CaptureGuard {
+    cudaStream_t st;
+    std::vector<cvtpm_ctx*> ctxs;
+    bool active = true;
+    CaptureGuard(cudaStream_t s, std::vector<cvtpm_ctx*> c) : st(s), ctxs(std::move(c)) {}
+    void release() { active = false; }
+    ~CaptureGuard() {
+        if (!active) return;
+        cudaGraph_t g = nullptr;
+        if (cudaStreamEndCapture(st, &g) == cudaSuccess && g) cudaGraphDestroy(g);
+        cudaGetLastError();
+        for (cvtpm_ctx* c : ctxs) c->no_alloc = false;
+    }
+};
+
+/* Two timing events, destroyed on every exit. */
+struct EventPair {
+    cudaEvent_t a = nullptr, b = nullptr;
+    ~EventPair() {
+        if (a) cudaEventDestroy(a);
+        if (b) cudaEventDestroy(b);
+    }
+};
+
 size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
 
 /* Row pitch (elements) of the record planes: even and two columns past the
@@ -995,7 +1023,10 @@ cvtpm_status capture_batch(cvtpm_ctx* ctx, const cvtpm_pair* pairs, int npairs, 
     }
     if (k > 0 && (s = ensure_tables(ctx->lanes[0].c, p, ctx->bstream)) != CVTPM_OK) return fail(ctx, s, ctx->lanes[0].c->err);
     CK(cudaStreamSynchronize(ctx->bstream), "batch prepare");
+    std::vector<cvtpm_ctx*> lane_ctx;
+    for (int j = 0; j < k; ++j) lane_ctx.push_back(ctx->lanes[j].c);
     CK(cudaStreamBeginCapture(ctx->bstream, cudaStreamCaptureModeThreadLocal), "begin capture");
+    CaptureGuard guard(ctx->bstream, std::move(lane_ctx));
     cvtpm_status err = CVTPM_OK;
     std::string msg;
     auto note = [&](cvtpm_status st, const std::string& m) { if (err == CVTPM_OK && st != CVTPM_OK) { err = st; msg = m; } };
@@ -1019,6 +1050,7 @@ cvtpm_status capture_batch(cvtpm_ctx* ctx, const cvtpm_pair* pairs, int npairs, 
     }
     cudaGraph_t graph = nullptr;
     cudaError_t e = cudaStreamEndCapture(ctx->bstream, &graph);
+    guard.release();
     if (err != CVTPM_OK) { if (graph) cudaGraphDestroy(graph); return fail(ctx, err, msg); }
     if (e != cudaSuccess) { if (graph) cudaGraphDestroy(graph); return cuda_fail(ctx, e, "end capture"); }
     *nodes = 0;
@@ -1049,16 +1081,17 @@ cvtpm_status tune_batch(cvtpm_ctx* ctx, const cvtpm_pair* pairs, int npairs, int
     cvtpm_batch_info& bi = ctx->binfo;
     bi.ncand = 0;
     float best = 0.0f;
-    cudaEvent_t t0, t1;
-    CK(cudaEventCreate(&t0), "tune event");
-    CK(cudaEventCreate(&t1), "tune event");
+    EventPair ev;
+    CK(cudaEventCreate(&ev.a), "tune event");
+    CK(cudaEventCreate(&ev.b), "tune event");
+    cudaEvent_t t0 = ev.a, t1 = ev.b;
     for (size_t ci = 0; ci < cand.size(); ++ci) {
         {
             const int k = cand[ci];
             cudaGraphExec_t ex = nullptr;
             size_t nodes = 0;
             cvtpm_status s = capture_batch(ctx, pairs, npairs, k, 1, &ex, &nodes);
-            if (s != CVTPM_OK) { cudaEventDestroy(t0); cudaEventDestroy(t1); return s; }
+            if (s != CVTPM_OK) return s;
             float ms = 0.0f;
             bool ok = cudaEventRecord(t0, ctx->bstream) == cudaSuccess &&
                       cudaGraphLaunch(ex, ctx->bstream) == cudaSuccess &&
@@ -1066,7 +1099,7 @@ cvtpm_status tune_batch(cvtpm_ctx* ctx, const cvtpm_pair* pairs, int npairs, int
                       cudaEventSynchronize(t1) == cudaSuccess &&
                       cudaEventElapsedTime(&ms, t0, t1) == cudaSuccess;
             cudaGraphExecDestroy(ex);
-            if (!ok) { cudaEventDestroy(t0); cudaEventDestroy(t1); return cuda_fail(ctx, cudaGetLastError(), "tuning run"); }
+            if (!ok) return cuda_fail(ctx, cudaGetLastError(), "tuning run");
             if (bi.ncand < CVTPM_BATCH_MAX_CAND) {
                 bi.cand_lanes[bi.ncand] = k;
                 bi.cand_grid_mult[bi.ncand] = bi.cand_pd_rows[bi.ncand] = bi.cand_pd_halo[bi.ncand] = 0;
@@ -1076,8 +1109,6 @@ cvtpm_status tune_batch(cvtpm_ctx* ctx, const cvtpm_pair* pairs, int npairs, int
             if (best == 0.0f || ms < best) { best = ms; *lanes_out = k; }
         }
     }
-    cudaEventDestroy(t0);
-    cudaEventDestroy(t1);
     return CVTPM_OK;
 }
 
@@ -1388,9 +1419,10 @@ cvtpm_status tune_phased(PhaseState& full, PmBatchKnobs* best) {
         L.old = c->S[0][0]; L.out = c->S[0][1]; L.smooth = c->smooth[0];
         L.viewin = c->list[1]; L.viewsrc = c->S[1][0]; L.winners = c->win[0];
     }
-    cudaEvent_t t0 = nullptr, t1 = nullptr;
-    CK(cudaEventCreate(&t0), "tune event");
-    if (cudaEventCreate(&t1) != cudaSuccess) { cudaEventDestroy(t0); return cuda_fail(ctx, cudaGetLastError(), "tune event"); }
+    EventPair ev;
+    CK(cudaEventCreate(&ev.a), "tune event");
+    CK(cudaEventCreate(&ev.b), "tune event");
+    cudaEvent_t t0 = ev.a, t1 = ev.b;
     auto timed = [&](auto&& body, float* ms) -> cvtpm_status {
         cvtpm_status r;
         if (cudaEventRecord(t0, S.st) != cudaSuccess) return cuda_fail(ctx, cudaGetLastError(), "tune record");
@@ -1437,8 +1469,6 @@ cvtpm_status tune_phased(PhaseState& full, PmBatchKnobs* best) {
                 }
         S.p = pd;
     }
-    cudaEventDestroy(t0);
-    cudaEventDestroy(t1);
     if (s != CVTPM_OK) return s;
     *best = win;
     return CVTPM_OK;
@@ -1447,13 +1477,19 @@ cvtpm_status tune_phased(PhaseState& full, PmBatchKnobs* best) {
 /* Captures the phase-batched schedule into one graph. */
 cvtpm_status capture_phased(PhaseState& S, cudaGraphExec_t* exec, size_t* nodes) {
     cvtpm_ctx* ctx = S.ctx;
-    for (int i = 0; i < S.n; ++i) ctx->bpairs[i]->no_alloc = true;
-    CK(cudaStreamBeginCapture(S.st, cudaStreamCaptureModeThreadLocal), "begin capture");
+    std::vector<cvtpm_ctx*> pc(ctx->bpairs.begin(), ctx->bpairs.begin() + S.n);
+    for (cvtpm_ctx* c : pc) c->no_alloc = true;
+    if (cudaStreamBeginCapture(S.st, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+        for (cvtpm_ctx* c : pc) c->no_alloc = false;
+        return cuda_fail(ctx, cudaGetLastError(), "begin capture");
+    }
+    CaptureGuard guard(S.st, pc);
     S.launches = 0;
     cvtpm_status err = phase_schedule(S, S.p.iterations);
     cudaGraph_t graph = nullptr;
     cudaError_t e = cudaStreamEndCapture(S.st, &graph);
-    for (int i = 0; i < S.n; ++i) ctx->bpairs[i]->no_alloc = false;
+    guard.release();
+    for (cvtpm_ctx* c : pc) c->no_alloc = false;
     if (err != CVTPM_OK) { if (graph) cudaGraphDestroy(graph); return err; }
     if (e != cudaSuccess) { if (graph) cudaGraphDestroy(graph); return cuda_fail(ctx, e, "end capture"); }
     *nodes = 0;

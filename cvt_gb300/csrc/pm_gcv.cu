@@ -598,6 +598,17 @@ float* scratch(size_t bytes, cudaStream_t st) {
 
 extern "C" {
 
+cvtpm_status cvtpm_gcv_trim(int device, size_t keep_bytes) {
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess) return CVTPM_ERR_CUDA;
+    if (device < 0 || device >= n) return CVTPM_ERR_INVALID_ARGUMENT;
+    cudaMemPool_t pool = scratch_pool(device);
+    if (!pool) return CVTPM_ERR_CUDA;
+    /* memory of calls still in flight stays reserved: trimming only returns
+     * what the pool holds unused */
+    return cudaMemPoolTrimTo(pool, keep_bytes) == cudaSuccess ? CVTPM_OK : CVTPM_ERR_CUDA;
+}
+
 cvtpm_status cvtpm_gcv_set_batch(int disparities) {
     if (disparities < 0 || disparities > GCV_BATCH_MAX)
         return fail(CVTPM_ERR_INVALID_ARGUMENT, "gcv: batch must be 0 (automatic) .. " + std::to_string(GCV_BATCH_MAX));

@@ -17,9 +17,17 @@
 #define PM_KERNELS_TU 1
 #include "pm_kernels.cuh"
 
-/* Blocks of 256 threads per SM the FAST propagation is compiled for. */
+/* Blocks of 256 threads per SM the FAST propagation and the neighbour
+ * costs are compiled for. */
 #ifndef PM_PROP_MINB
 #define PM_PROP_MINB 2
+#endif
+#ifndef PM_NB_MINB
+#define PM_NB_MINB 2
+#endif
+/* FAST: candidates 9-16 per window sweep (8: one sweep; 4: two) */
+#ifndef PM_FAST_SWEEP
+#define PM_FAST_SWEEP 8
 #endif
 
 
@@ -194,7 +202,7 @@ PM_DEV void propagate_tile(const PmPassArgs& a, int tbx, int tby) {
      * (:355-361), a fresh random plane (:364-368).  FAST evaluates the eight
      * in one window sweep (1 % faster per pass than two sweeps of four,
      * measured); EXACT in two, which keeps it at two blocks per SM. */
-    constexpr int NB = EXACT ? 4 : 8;
+    constexpr int NB = EXACT ? 4 : PM_FAST_SWEEP;
 #pragma unroll
     for (int b0 = 0; b0 < 8; b0 += NB) {
         float4 s[NB]; bool act[NB]; float c[NB];
@@ -563,7 +571,7 @@ PM_DEV void nbcost_tile(const PmPassArgs& a, int tbx, int tby) {
 }
 
 template <bool EXACT>
-__global__ void __launch_bounds__(256, 2) k_nbcost(PmPassArgs a) { nbcost_tile<EXACT>(a, blockIdx.x, blockIdx.y); }
+__global__ void __launch_bounds__(256, PM_NB_MINB) k_nbcost(PmPassArgs a) { nbcost_tile<EXACT>(a, blockIdx.x, blockIdx.y); }
 
 /* -------------------------------------------------------- view lists -- */
 /* One warp per row.  Sources are visited in increasing x; the first four

@@ -36,6 +36,14 @@ def set_batch(disparities: int = 0) -> None:
         _fail(rc)
 
 
+def trim(device: int = 0, keep_bytes: int = 0) -> None:
+    """Return the scratch pool's unused memory beyond keep_bytes to the
+    device (the pool otherwise keeps its largest reservation until exit)."""
+    rc = _lib.lib().cvtpm_gcv_trim(int(device), int(keep_bytes))
+    if rc:
+        _fail(rc)
+
+
 def plan(width: int, height: int, dmin: float, dmax: float, dt: float) -> dict:
     """steps, batch, scratch bytes and kernel launches of one depthmap call."""
     steps, batch, launches = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()

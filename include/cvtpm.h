@@ -559,6 +559,14 @@ cvtpm_status cvtpm_tsdf_save_raw(cvtpm_tsdf* vol, const char* path, int weighted
  * 4 GiB of scratch holds, at most 256; 1..256 sets it.  Process-wide. */
 cvtpm_status cvtpm_gcv_set_batch(int disparities);
 
+/* The scratch pool keeps what its largest call reserved (22 + 10 x batch
+ * floats per pixel per call in flight: about 1.9 GB for an apply at
+ * 1242x375 with the automatic batch of 128 disparities) until the process
+ * exits.  This returns the unused part beyond keep_bytes to the device
+ * (cudaMemPoolTrimTo); later calls reserve again.  No counterpart in the
+ * reference. */
+cvtpm_status cvtpm_gcv_trim(int device, size_t keep_bytes);
+
 /* The plan of a depthmap call of these arguments: the number of
  * disparities, the batch, the scratch bytes and the kernel launches (each
  * optional).  An apply call runs two such depth maps and one more launch. */

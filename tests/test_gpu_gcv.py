@@ -113,3 +113,26 @@ def test_scratch_does_not_grow_with_threads(cuda):
         free.append(torch.cuda.mem_get_info()[0])
     assert not err, err
     assert abs(free[0] - free[-1]) < 32 << 20, [(f - free[0]) >> 20 for f in free]
+
+
+def test_trim_returns_the_pool_memory(cuda):
+    """after an apply the pool keeps its scratch (about 160 MB here);
+    cvtpm_gcv_trim gives it back to the device, and a later apply still
+    gives the same bits"""
+    from cvt_gb300 import scenes
+    sc = scenes.make_scene(300, 200, 3, 64.0, seed=6)
+    cam0, cam1 = torch.from_numpy(sc.right).cuda(), torch.from_numpy(sc.left).cuda()
+    f = gcv.StereoGCVFilter()
+    first = f.apply(cam0, cam1, 0.0, 64.0, 1.0)
+    torch.cuda.synchronize()
+    held = torch.cuda.mem_get_info()[0]
+    gcv.trim(0, 0)
+    torch.cuda.synchronize()
+    freed = torch.cuda.mem_get_info()[0]
+    assert freed - held > 64 << 20, (freed - held) >> 20
+    again = f.apply(cam0, cam1, 0.0, 64.0, 1.0)
+    torch.cuda.synchronize()
+    for a, b in zip(first, again):
+        assert torch.equal(a.cpu(), b.cpu())
+    with pytest.raises(Exception):
+        gcv.trim(-1, 0)
