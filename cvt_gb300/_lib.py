@@ -18,7 +18,7 @@ LIB_PATH = os.path.join(_HERE, "libcvtpm.so")
 EXPORTS = (
     "cvtpm_version", "cvtpm_status_string", "cvtpm_params_default", "cvtpm_create", "cvtpm_destroy",
     "cvtpm_set_params", "cvtpm_get_params", "cvtpm_last_error", "cvtpm_synchronize", "cvtpm_depthmap",
-    "cvtpm_depthmap_host", "cvtpm_depthmap_inpaint", "cvtpm_cost_eval", "cvtpm_cost_adjoint", "cvtpm_polish_planes", "cvtpm_depthmap_batched", "cvtpm_set_batch_knobs", "cvtpm_set_memory_budget",
+    "cvtpm_depthmap_host", "cvtpm_depthmap_resumable", "cvtpm_depthmap_inpaint", "cvtpm_cost_eval", "cvtpm_cost_adjoint", "cvtpm_polish_planes", "cvtpm_depthmap_batched", "cvtpm_set_batch_knobs", "cvtpm_set_memory_budget",
     "cvtpm_set_batch_lanes", "cvtpm_get_batch_info",
     "cvtpm_set_timing", "cvtpm_reset_stats", "cvtpm_get_stats", "cvtpm_tool_fp32_peak",
     "cvtpm_cost_eval_noalloc",
@@ -28,6 +28,10 @@ EXPORTS = (
     "cvtpm_tsdf_add_depthmap", "cvtpm_tsdf_raycast", "cvtpm_tsdf_slice", "cvtpm_tsdf_save_raw",
     "cvtpm_disparity_to_depth", "cvtpm_gcv_set_batch", "cvtpm_gcv_trim", "cvtpm_gcv_plan", "cvtpm_gcv_depthmap", "cvtpm_gcv_apply",
 )
+
+
+class CvtpmCheckpoint(ctypes.Structure):
+    _fields_ = [("iteration", ctypes.c_int), ("states", ctypes.c_void_p), ("smooth", ctypes.c_void_p)]
 
 
 class CvtpmTrace(ctypes.Structure):
@@ -122,6 +126,9 @@ def lib() -> ctypes.CDLL:
     L.cvtpm_last_error.restype = ctypes.c_char_p
     L.cvtpm_synchronize.argtypes = [vp, vp]
     L.cvtpm_depthmap.argtypes = [vp, vp, sz, vp, vp, i, i, sz, i, f, i, i, f, vp, sz, ctypes.POINTER(CvtpmTrace), vp]
+    L.cvtpm_depthmap_resumable.argtypes = [vp, vp, sz, vp, vp, i, i, sz, i, f, i, i, f, vp, sz,
+                                           ctypes.POINTER(CvtpmTrace), ctypes.POINTER(CvtpmCheckpoint), i,
+                                           ctypes.POINTER(CvtpmCheckpoint), vp]
     L.cvtpm_depthmap_host.argtypes = [vp, vp, sz, vp, vp, i, i, sz, i, f, i, i, f, vp, sz, vp]
     L.cvtpm_depthmap_inpaint.argtypes = [vp, vp, sz, vp, vp, i, i, sz, i, f, i, i, ctypes.POINTER(CvtpmTrace), vp]
     L.cvtpm_cost_eval.argtypes = [vp, vp, vp, i, i, sz, vp, i, vp, vp]

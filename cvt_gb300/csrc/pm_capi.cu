@@ -382,15 +382,48 @@ float smoothstep01(float x) {                                      /* cvt/math/M
     return t * t * (3.0f - 2.0f * t);
 }
 
+/* The theta of iteration k of an N-iteration run (PMHuberStereo.cpp:264-265). */
+float theta_at(int k, int N) {
+    float theta = 0.0f;
+    for (int iter = 0; iter < k; ++iter)
+        if (iter >= 5) theta = smoothstep01(((float)iter - 5.0f) / ((float)N - 5.0f)) * 1.0f;
+    return theta;
+}
+
+cvtpm_status check_checkpoint(cvtpm_ctx* ctx, const cvtpm_checkpoint* c, int N, const char* what) {
+    if (!c) return CVTPM_OK;
+    if (c->iteration < 0 || c->iteration > N)
+        return fail(ctx, CVTPM_ERR_INVALID_ARGUMENT, std::string(what) + ": iteration out of 0..iterations");
+    if (!c->states || !c->smooth || ((uintptr_t)c->states & 15) || ((uintptr_t)c->smooth & 15))
+        return fail(ctx, CVTPM_ERR_INVALID_ARGUMENT, std::string(what) + ": states/smooth NULL or not 16-byte aligned");
+    return CVTPM_OK;
+}
+
+/* The depthMap schedule.  resume (optional) starts at iteration
+ * resume->iteration from its state instead of the random init; the run stops
+ * before iteration `stop` (stop < 0: all iterations), saves the state there
+ * into `save` (optional) and produces dmap only when it ran to the end. */
 cvtpm_status run_depthmap(cvtpm_ctx* ctx, const cvtpm_params& p, float* dmap, size_t dpitch, const float* left,
                           const float* right, int W, int H, size_t pitch, float* nmap, size_t npitch,
-                          const cvtpm_trace* trace, cudaStream_t st) {
+                          const cvtpm_trace* trace, cudaStream_t st, const cvtpm_checkpoint* resume = nullptr,
+                          int stop = -1, cvtpm_checkpoint* save = nullptr) {
     cvtpm_status s;
     if ((s = check_params(ctx, p)) != CVTPM_OK) return s;
     if ((s = check_image(ctx, left, W, H, pitch, "left")) != CVTPM_OK) return s;
     if ((s = check_image(ctx, right, W, H, pitch, "right")) != CVTPM_OK) return s;
-    if (!dmap) return fail(ctx, CVTPM_ERR_INVALID_ARGUMENT, "dmap is NULL");
-    if (dpitch % 4 != 0 || dpitch < (size_t)W * 4) return fail(ctx, CVTPM_ERR_INVALID_ARGUMENT, "dmap pitch");
+    const int first = resume ? resume->iteration : 0;
+    const int last = (stop < 0 || stop > p.iterations) ? p.iterations : stop;
+    if ((s = check_checkpoint(ctx, resume, p.iterations, "resume")) != CVTPM_OK) return s;
+    if (save && !save->states && !save->smooth) save = nullptr;
+    if (save) {
+        cvtpm_checkpoint chk = *save;
+        chk.iteration = last;
+        if ((s = check_checkpoint(ctx, &chk, p.iterations, "save")) != CVTPM_OK) return s;
+    }
+    if (last < first) return fail(ctx, CVTPM_ERR_INVALID_ARGUMENT, "stop comes before the resumed iteration");
+    const bool finish = last == p.iterations;
+    if (finish && !dmap) return fail(ctx, CVTPM_ERR_INVALID_ARGUMENT, "dmap is NULL");
+    if (finish && (dpitch % 4 != 0 || dpitch < (size_t)W * 4)) return fail(ctx, CVTPM_ERR_INVALID_ARGUMENT, "dmap pitch");
     if (nmap && (npitch % 16 != 0 || npitch < (size_t)W * 16)) return fail(ctx, CVTPM_ERR_INVALID_ARGUMENT, "normalmap pitch");
     CK(cudaSetDevice(ctx->device), "cudaSetDevice");
     if ((s = ensure_buffers(ctx, W, H)) != CVTPM_OK) return s;
@@ -413,19 +446,33 @@ cvtpm_status run_depthmap(cvtpm_ctx* ctx, const cvtpm_params& p, float* dmap, si
     ++ctx->stats.calls;
     NvtxRange whole("cvtpm depthMap");
 
-    {
+    if (!resume) {
         NvtxRange r("init");
         aL.out = ctx->S[0][0];                                     /* :124-143 */
         LK(pm_launch_init(aL, exact, st), "init");
         aR.out = ctx->S[1][0];
         LK(pm_launch_init(aR, exact, st), "init");
+        CK(cudaMemsetAsync(ctx->smooth[0], 0, n * 16, st), "clear");   /* :108-113 */
+        CK(cudaMemsetAsync(ctx->smooth[1], 0, n * 16, st), "clear");
+        CK(cudaMemsetAsync(ctx->list[1], 0xFF, n * 8, st), "clear");   /* :145-149 */
+    } else {
+        /* the state before iteration `first`: both views' planes and smoothed
+         * fields; the left pass's view list is the one the right view's
+         * planes give (or empty before iteration 0) */
+        NvtxRange r("resume");
+        const int sw0 = first & 1;
+        for (int v = 0; v < 2; ++v) {
+            CK(cudaMemcpyAsync(ctx->S[v][sw0], resume->states + (size_t)v * 4 * n, n * 16, cudaMemcpyDeviceToDevice, st),
+               "resume");
+            CK(cudaMemcpyAsync(ctx->smooth[v], resume->smooth + (size_t)v * 4 * n, n * 16, cudaMemcpyDeviceToDevice, st),
+               "resume");
+        }
+        if (first == 0) CK(cudaMemsetAsync(ctx->list[1], 0xFF, n * 8, st), "clear");
+        else LK(pm_launch_view_list(ctx->S[1][sw0], W, H, ctx->list[1], st), "view list");
     }
-    CK(cudaMemsetAsync(ctx->smooth[0], 0, n * 16, st), "clear");   /* :108-113 */
-    CK(cudaMemsetAsync(ctx->smooth[1], 0, n * 16, st), "clear");
-    CK(cudaMemsetAsync(ctx->list[1], 0xFF, n * 8, st), "clear");   /* :145-149 */
 
-    float theta = 0.0f;
-    for (int iter = 0; iter < N; ++iter) {                         /* :151-266 */
+    float theta = theta_at(first, N);
+    for (int iter = first; iter < last; ++iter) {                  /* :151-266 */
         const int sw = iter & 1;
         aL.iter = aR.iter = iter;
         aL.theta = aR.theta = theta;
@@ -460,6 +507,15 @@ cvtpm_status run_depthmap(cvtpm_ctx* ctx, const cvtpm_params& p, float* dmap, si
         }
         if (iter >= 5) theta = smoothstep01(((float)iter - 5.0f) / ((float)N - 5.0f)) * 1.0f;
     }
+    if (save) {
+        const int sw = last & 1;
+        for (int v = 0; v < 2; ++v) {
+            CK(cudaMemcpyAsync(save->states + (size_t)v * 4 * n, ctx->S[v][sw], n * 16, cudaMemcpyDeviceToDevice, st), "save");
+            CK(cudaMemcpyAsync(save->smooth + (size_t)v * 4 * n, ctx->smooth[v], n * 16, cudaMemcpyDeviceToDevice, st), "save");
+        }
+        save->iteration = last;
+    }
+    if (!finish) return CVTPM_OK;
     const int fin = 1 - ((N - 1) & 1);                              /* :268-290 */
     NvtxRange fr("final consistency and fill");
     LK(pm_launch_consistency(ctx->S[0][fin], ctx->S[1][fin], W, H, p.maxdispdiff, p.maxanglediff, 1, ctx->tmp,
@@ -719,6 +775,23 @@ cvtpm_status cvtpm_depthmap(cvtpm_ctx* ctx, float* dmap, size_t dmap_pitch, cons
     p.dscale = dscale;
     return run_depthmap(ctx, p, dmap, dmap_pitch, left, right, width, height, pitch, normalmap, normalmap_pitch,
                         trace, (cudaStream_t)stream);
+}
+
+cvtpm_status cvtpm_depthmap_resumable(cvtpm_ctx* ctx, float* dmap, size_t dmap_pitch, const float* left,
+                                      const float* right, int width, int height, size_t pitch, int patchsize,
+                                      float depthmax, int iterations, int viewsamples, float dscale, float* normalmap,
+                                      size_t normalmap_pitch, const cvtpm_trace* trace,
+                                      const cvtpm_checkpoint* resume, int stop, cvtpm_checkpoint* save,
+                                      void* stream) {
+    if (!ctx) return CVTPM_ERR_INVALID_ARGUMENT;
+    (void)viewsamples;
+    cvtpm_params p = ctx->prm;
+    p.patchsize = patchsize;
+    p.depthmax = depthmax;
+    p.iterations = iterations;
+    p.dscale = dscale;
+    return run_depthmap(ctx, p, dmap, dmap_pitch, left, right, width, height, pitch, normalmap, normalmap_pitch, trace,
+                        (cudaStream_t)stream, resume, stop, save);
 }
 
 cvtpm_status cvtpm_depthmap_image(cvtpm_ctx* ctx, float* dmap, size_t dmap_pitch, const cvtpm_image* left,

@@ -306,8 +306,7 @@ __global__ void __launch_bounds__(256, EXACT ? 1 : PM_PROP_MINB) k_propagate(PmP
  * shared-memory ring exposed the latency of the record loads.)  The minimum
  * of 2 blocks per SM makes the allocator use up to 128 registers: without
  * it, it chose 97 and the kernel ran 8 % slower. */
-#define NB_COLS 30   /* planes per warp; lanes 30 and 31 feed the shuffles of the row pipeline */
-#define NB_PIPE 1    /* interior warps share weights along the row through shuffles */
+#define NB_COLS 30   /* planes per warp; lanes 30 and 31 form the weights lanes 28 and 29 read */
 
 /* The plane part of a tap for the shared windows: the position and matching
  * terms of plane (sx, sy, sz) [EXACT] or (S0, S1, X) [FAST] at tap (qx, qy).
@@ -463,20 +462,65 @@ __device__ __forceinline__ void nbcost_lane(const PmPassArgs& a, int mx, int my)
     }
 }
 
-/* Plane (mx, my) of a warp whose 32 columns and windows lie inside the image
- * (mx0 - P - 1 >= 0, mx0 + 31 + P + 1 < W): all lanes walk the same tap
- * offsets in lockstep.  The weight of user u = m - (ox, oy) at tap q is
- * tap_weight(colour(u), colour(q), profile(q - u)); lane L forms, per user row
- * oy, the one for ox = +1 (u one column left of its plane).  Lane L - 1 needs
- * that value one offset later as its ox = 0 weight (same u, same q), lane
- * L - 2 two offsets later as its ox = -1 weight: two shuffles per row and
- * offset replace five weight evaluations.  Lanes 30 and 31 own no plane and
- * only supply those values.  Each user still receives its taps in raster
- * order through the operations of eval_costs. */
+/* Interior blocks: the weights shared across the block's rows.
+ *
+ * A block holds NB_ROWS plane rows (warps 1..NB_ROWS) and NB_WARPS user rows
+ * U_w = my0 - 1 + w (w = 0..NB_WARPS-1): the plane rows and the rows just
+ * above and below them, whose pixels are users of the edge planes.  The
+ * weight of user (mx - 1, U) at tap (mx + rx, Yq) — lane L's "ox = +1"
+ * weight — depends on
+ * U, Yq, rx and the lane only, so it is needed by the three plane rows
+ * U - 1, U and U + 1 at three different window rows.  The block walks the
+ * union of its planes' window rows (Yq = my0 - P - 1 .. my0 + NB_ROWS + P)
+ * in lockstep; per row:
+ *   A. the image-1 row Yq over the block's columns mx0 - P - 1 ..
+ *      mx0 + 32 + P (colour and gradient) is staged into shared memory by
+ *      cp.async;
+ *   B. warp w forms the weights of its user row at that image row for
+ *      every offset rx (one weight per lane and offset) into a table
+ *      T[w][rx][lane];
+ *   C. each plane warp processes its window row Yq - my: the matching terms
+ *      of its plane at each tap (the record loads from global memory
+ *      through L1), the 8 users' weights read from the table
+ *      (user (mx - ox, U) at tap column mx + rx is lane L + 1 - ox's entry
+ *      at offset rx - 1 + ox), folded into the users' sums in raster order
+ *      through the operations of eval_costs.
+ * A weight is formed once per block, where each plane row forming the
+ * weights of its three user rows would form it three times.  Same bits as
+ * nbcost_lane. */
+#define NB_ROWS 8
+#define NB_WARPS (NB_ROWS + 2)
+
+PM_DEV void cp_async16(void* smem, const void* gmem) {
+    const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem) : "memory");
+}
+PM_DEV void cp_async_wait_all() { asm volatile("cp.async.commit_group;\ncp.async.wait_group 0;\n" ::: "memory"); }
+
+/* dynamic shared memory of nbcost_block for window radius P */
+__host__ __device__ constexpr size_t nb_block_smem(int P) {
+    return (size_t)2 * (32 + 2 * (P + 1)) * 16 + (size_t)NB_WARPS * (2 * P + 5) * 32 * 4;
+}
+
 template <bool EXACT>
-__device__ __forceinline__ void nbcost_pipe(const PmPassArgs& a, int mx, int my, bool own) {
+PM_DEV void nbcost_block(const PmPassArgs& a, int mx0, int my0) {
+    extern __shared__ __align__(16) float4 nb_smem[];
     const int W = a.k.W, H = a.k.H, P = a.k.P;
-    const size_t n = (size_t)W * H, m = (size_t)my * W + mx;
+    const int NQ = 32 + 2 * (P + 1);                 /* staged columns mx0 - P - 1 .. mx0 + 32 + P */
+    const int NR = 2 * P + 5;                        /* table columns: offsets rx = -P-3 .. P+1 */
+    float4* s_col = nb_smem;
+    float4* s_grad = nb_smem + NQ;
+    float* T = reinterpret_cast<float*>(nb_smem + 2 * NQ);
+    const int lane = threadIdx.x, w = threadIdx.y, tid = w * 32 + lane;
+    const int U = my0 + w - 1;                       /* this warp's user row */
+    const float4 uc = __ldg(&a.v1.col[(size_t)clampi(U, 0, H - 1) * W + mx0 + lane - 1]);
+    T[(w * NR + 0) * 32 + lane] = 0.0f;              /* offsets before the window: no weight */
+    T[(w * NR + 1) * 32 + lane] = 0.0f;
+    /* plane role */
+    const int my = U, mx = mx0 + lane;
+    const bool prow = w >= 1 && w <= NB_ROWS && my < H;      /* warp-uniform */
+    const bool own = prow && lane < NB_COLS;
+    const size_t n = (size_t)W * H, m = (size_t)clampi(my, 0, H - 1) * W + mx;
     const float4 s = a.old[m];
     long long S0, S1, XA;
     float sx, sy, sz;
@@ -486,66 +530,74 @@ __device__ __forceinline__ void nbcost_pipe(const PmPassArgs& a, int mx, int my,
 #pragma unroll
     for (int k = 0; k < 8; ++k) {
         const int oy = (k < 4 ? k : k + 1) / 3 - 1;
-        if (my - oy >= 0 && my - oy < H) uok |= 1u << k;   /* columns are inside */
+        if (my - oy >= 0 && my - oy < H) uok |= 1u << k;
     }
-    float4 uc[3];                                  /* colours of the ox = +1 users, rows oy = -1, 0, 1 */
-#pragma unroll
-    for (int r = 0; r < 3; ++r) uc[r] = __ldg(&a.v1.col[(size_t)min(max(my - (r - 1), 0), H - 1) * W + mx - 1]);
     float r1[8], r2[8], ws[8];
 #pragma unroll
     for (int k = 0; k < 8; ++k) { r1[k] = 0.0f; r2[k] = 0.0f; ws[k] = 0.0f; }
-    const int qy0 = max(my - P - 1, 0), qy1 = min(my + P + 1, H - 1);
-    for (int qy = qy0; qy <= qy1; ++qy) {
-        const int ry = qy - my;
-        unsigned rmask = 0;
-#pragma unroll
-        for (int k = 0; k < 8; ++k) {
-            const int oy = (k < 4 ? k : k + 1) / 3 - 1;
-            if (abs(ry + oy) <= P) rmask |= 1u << k;
+    const int steps = NB_ROWS + 2 * P + 2;
+    for (int t = 0; t < steps; ++t) {
+        const int Yq = my0 - P - 1 + t;
+        if (Yq < 0 || Yq >= H) continue;             /* block-uniform */
+        /* A: the image-1 row */
+        const size_t rb = (size_t)Yq * W + (mx0 - P - 1);
+        for (int i = tid; i < 2 * NQ; i += NB_WARPS * 32)
+            cp_async16(&nb_smem[i], i < NQ ? (const void*)(a.v1.col + rb + i) : (const void*)(a.v1.grad + rb + i - NQ));
+        cp_async_wait_all();
+        __syncthreads();
+        /* B: this user row's weights at image row Yq */
+        const int dy = Yq - U;
+        if (abs(dy) <= P) {                          /* warp-uniform */
+            const float* prow = c_prof + (dy + PM_PMAX) * PM_PROF_N + PM_PMAX;
+            for (int rxi = 0; rxi < 2 * P + 3; ++rxi) {
+                const int dx = rxi - P;                  /* tap offset from the user: rx + 1 */
+                T[(w * NR + rxi + 2) * 32 + lane] = abs(dx) <= P ? tap_weight(uc, s_col[lane + rxi], prow[dx]) : 0.0f;
+            }
+        } else {
+            for (int rxi = 0; rxi < 2 * P + 3; ++rxi) T[(w * NR + rxi + 2) * 32 + lane] = 0.0f;
         }
-        rmask &= uok;                              /* the same in every lane: my is */
-        if (!rmask) continue;
-        const float4* c1row = a.v1.col + (size_t)qy * W;
-        const float4* g1row = a.v1.grad + (size_t)qy * W;
-        const size_t jrow = (size_t)qy * a.k.rp;
-        long long X = XA + (long long)(qy - H / 2) * S1 + (long long)(mx - P - 1 - W / 2) * S0;
-        float p1[3] = {0.0f, 0.0f, 0.0f}, q1[3] = {0.0f, 0.0f, 0.0f};   /* own ox=+1 and received ox=0 of the last offset */
-        for (int rx = -P - 1; rx <= P + 1; ++rx) {
-            const int qx = mx + rx;
-            const float4 a1 = __ldg(&c1row[qx]);
-            const float4 g1 = __ldg(&g1row[qx]);
-            float wn[3], w0[3], wm[3];
-#pragma unroll
-            for (int r = 0; r < 3; ++r) {
-                const int dy = ry + (r - 1);
-                wn[r] = (abs(dy) <= P && abs(rx + 1) <= P)
-                            ? tap_weight(uc[r], a1, c_prof[(dy + PM_PMAX) * PM_PROF_N + PM_PMAX + rx + 1]) : 0.0f;
-                wm[r] = __shfl_down_sync(0xffffffffu, q1[r], 1);   /* lane L+2's ox=+1 of two offsets ago */
-                w0[r] = __shfl_down_sync(0xffffffffu, p1[r], 1);   /* lane L+1's ox=+1 of the last offset */
-                p1[r] = wn[r];
-                q1[r] = w0[r];
-            }
-            const long long Xt = X;
-            X += S0;
-            if (!own) continue;
-            unsigned mask = rmask;
-            if (rx <= -P || rx >= P) {
-#pragma unroll
-                for (int k = 0; k < 8; ++k) {
-                    const int ox = (k < 4 ? k : k + 1) % 3 - 1;
-                    if (abs(rx + ox) > P) mask &= ~(1u << k);
-                }
-            }
-            float cc, gc;
-            if (!nb_tap_terms<EXACT>(a.k, a.v2, qx, qy, jrow, sx, sy, sz, Xt, a1, g1, cc, gc)) continue;
+        __syncthreads();
+        /* C: the plane rows' window row Yq */
+        const int ry = Yq - my;
+        if (prow && ry >= -P - 1 && ry <= P + 1) {
+            unsigned rmask = 0;
 #pragma unroll
             for (int k = 0; k < 8; ++k) {
-                if (!((mask >> k) & 1u)) continue;
-                const int nn = k < 4 ? k : k + 1, ox = nn % 3 - 1, r = nn / 3;
-                const float w = ox > 0 ? wn[r] : (ox == 0 ? w0[r] : wm[r]);
-                nb_accumulate<EXACT>(w, cc, gc, r1[k], r2[k], ws[k]);
+                const int oy = (k < 4 ? k : k + 1) / 3 - 1;
+                if (abs(ry + oy) <= P) rmask |= 1u << k;
+            }
+            rmask &= uok;
+            if (rmask && own) {
+                const size_t jrow = (size_t)Yq * a.k.rp;
+                long long X = XA + (long long)(Yq - H / 2) * S1 + (long long)(mx - P - 1 - W / 2) * S0;
+                for (int rx = -P - 1; rx <= P + 1; ++rx) {
+                    const int rxi = rx + P + 1;
+                    const long long Xt = X;
+                    X += S0;
+                    unsigned mask = rmask;
+                    if (rx <= -P || rx >= P) {
+#pragma unroll
+                        for (int k = 0; k < 8; ++k) {
+                            const int ox = (k < 4 ? k : k + 1) % 3 - 1;
+                            if (abs(rx + ox) > P) mask &= ~(1u << k);
+                        }
+                    }
+                    const float4 a1 = s_col[lane + rxi];
+                    const float4 g1 = s_grad[lane + rxi];
+                    float cc, gc;
+                    if (!nb_tap_terms<EXACT>(a.k, a.v2, mx + rx, Yq, jrow, sx, sy, sz, Xt, a1, g1, cc, gc)) continue;
+#pragma unroll
+                    for (int k = 0; k < 8; ++k) {
+                        if (!((mask >> k) & 1u)) continue;
+                        const int nn = k < 4 ? k : k + 1, ox = nn % 3 - 1, r = nn / 3;
+                        const int wu = w + 1 - r;                /* the warp of user row my - (r - 1) */
+                        const float wgt = T[(wu * NR + rxi + 1 + ox) * 32 + lane + 1 - ox];
+                        nb_accumulate<EXACT>(wgt, cc, gc, r1[k], r2[k], ws[k]);
+                    }
+                }
             }
         }
+        __syncthreads();
     }
     if (!own) return;
 #pragma unroll
@@ -556,22 +608,26 @@ __device__ __forceinline__ void nbcost_pipe(const PmPassArgs& a, int mx, int my,
     }
 }
 
+/* A block of NB_COLS x NB_ROWS planes: interior blocks (their columns' windows
+ * inside the image) share weights across rows (nbcost_block); the others
+ * evaluate plane by plane (nbcost_lane). */
 template <bool EXACT>
 PM_DEV void nbcost_tile(const PmPassArgs& a, int tbx, int tby) {
     const int W = a.k.W, H = a.k.H, P = a.k.P;
-    const int mx0 = tbx * NB_COLS, lane = threadIdx.x;
-    const int mx = mx0 + lane, my = tby * 8 + threadIdx.y;
-    if (my >= H) return;                                   /* the whole warp */
-    if (NB_PIPE && mx0 - P - 1 >= 0 && mx0 + 31 + P + 1 <= W - 1) {
-        nbcost_pipe<EXACT>(a, mx, my, lane < NB_COLS);
+    const int mx0 = tbx * NB_COLS, my0 = tby * NB_ROWS, lane = threadIdx.x, w = threadIdx.y;
+    if (mx0 - P - 1 >= 0 && mx0 + 31 + P + 1 <= W - 1) {   /* block-uniform */
+        nbcost_block<EXACT>(a, mx0, my0);
         return;
     }
-    if (lane >= NB_COLS || mx >= W) return;
+    const int mx = mx0 + lane, my = my0 + w - 1;
+    if (w < 1 || w > NB_ROWS || my >= H || lane >= NB_COLS || mx >= W) return;
     nbcost_lane<EXACT>(a, mx, my);
 }
 
 template <bool EXACT>
-__global__ void __launch_bounds__(256, PM_NB_MINB) k_nbcost(PmPassArgs a) { nbcost_tile<EXACT>(a, blockIdx.x, blockIdx.y); }
+__global__ void __launch_bounds__(32 * NB_WARPS, PM_NB_MINB) k_nbcost(PmPassArgs a) {
+    nbcost_tile<EXACT>(a, blockIdx.x, blockIdx.y);
+}
 
 /* -------------------------------------------------------- view lists -- */
 /* One warp per row.  Sources are visited in increasing x; the first four
@@ -1015,7 +1071,7 @@ __global__ void __launch_bounds__(256) kb_init(const __grid_constant__ PmBatch<P
 }
 
 template <bool EXACT>
-__global__ void __launch_bounds__(256, 2) kb_nbcost(const __grid_constant__ PmBatch<PmPassArgs> b) {
+__global__ void __launch_bounds__(32 * NB_WARPS, PM_NB_MINB) kb_nbcost(const __grid_constant__ PmBatch<PmPassArgs> b) {
     for (int item = blockIdx.x; item < b.first[b.n]; item += gridDim.x) {
         const int p = batch_pair(b, item), t = item - b.first[p];
         nbcost_tile<EXACT>(b.a[p], t % b.tx[p], t / b.tx[p]);
@@ -1127,10 +1183,11 @@ cudaError_t pm_launch_propagate(const PmPassArgs& a, bool exact, cudaStream_t st
     const dim3 grid = a.color < 0 ? pix_grid(a.k.W, a.k.H) : pix_grid((a.k.W + 1) / 2, a.k.H);
     PmPassArgs b = a;
     if (b.color >= 0) b.nbcost = nullptr;   /* red/black: neighbours per pixel */
-    const dim3 nbgrid((a.k.W + NB_COLS - 1) / NB_COLS, (a.k.H + 7) / 8);
+    const dim3 nbgrid((a.k.W + NB_COLS - 1) / NB_COLS, (a.k.H + NB_ROWS - 1) / NB_ROWS);
     if (b.nbcost) {
-        if (exact) k_nbcost<true><<<nbgrid, dim3(32, 8), 0, st>>>(b);
-        else k_nbcost<false><<<nbgrid, dim3(32, 8), 0, st>>>(b);
+        const size_t smem = nb_block_smem(a.k.P);
+        if (exact) k_nbcost<true><<<nbgrid, dim3(32, NB_WARPS), smem, st>>>(b);
+        else k_nbcost<false><<<nbgrid, dim3(32, NB_WARPS), smem, st>>>(b);
         PM_LAUNCH_CHECK();
     }
     if (exact) k_propagate<true><<<grid, dim3(32, 8), 0, st>>>(b);
@@ -1240,7 +1297,7 @@ void pm_batch_tiles(PmBatchKernel k, int W, int H, const PmBatchKnobs& kn, int* 
     case PMB_PREP: x = (W + PREP_T - 1) / PREP_T; y = (H + PREP_T - 1) / PREP_T; break;
     case PMB_RECORDS: x = (W + 127) / 128; y = H; break;
     case PMB_PIXEL: x = (W + 31) / 32; y = (H + 7) / 8; break;
-    case PMB_NBCOST: x = (W + NB_COLS - 1) / NB_COLS; y = (H + 7) / 8; break;
+    case PMB_NBCOST: x = (W + NB_COLS - 1) / NB_COLS; y = (H + NB_ROWS - 1) / NB_ROWS; break;
     case PMB_ROW: x = 1; y = H; break;
     case PMB_PD: {
         const int rows = kn.pd_rows == 8 ? 8 : 16;
@@ -1293,8 +1350,9 @@ cudaError_t pm_batch_init(const PmBatch<PmPassArgs>& b, bool exact, const PmBatc
     PM_BATCH_LAUNCH(kb_init<false>, dim3(32, 8), 0);
 }
 cudaError_t pm_batch_nbcost(const PmBatch<PmPassArgs>& b, bool exact, const PmBatchKnobs& kn, cudaStream_t st) {
-    if (exact) PM_BATCH_LAUNCH(kb_nbcost<true>, dim3(32, 8), 0);
-    PM_BATCH_LAUNCH(kb_nbcost<false>, dim3(32, 8), 0);
+    const size_t smem = nb_block_smem(b.a[0].k.P);           /* one window size per batch */
+    if (exact) PM_BATCH_LAUNCH(kb_nbcost<true>, dim3(32, NB_WARPS), smem);
+    PM_BATCH_LAUNCH(kb_nbcost<false>, dim3(32, NB_WARPS), smem);
 }
 cudaError_t pm_batch_propagate(const PmBatch<PmPassArgs>& b, bool exact, const PmBatchKnobs& kn, cudaStream_t st) {
     if (exact) PM_BATCH_LAUNCH(kb_propagate<true>, dim3(32, 8), 0);
@@ -1321,6 +1379,11 @@ cudaError_t pm_batch_pd(const PmBatch<PmPdArgs>& b, const PmBatchKnobs& kn, cuda
 }
 cudaError_t pm_batch_prepare_kernels() {
     cudaError_t e;
+    const int nbmax = (int)nb_block_smem(PM_PMAX);
+    if ((e = cudaFuncSetAttribute(k_nbcost<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, nbmax)) != cudaSuccess) return e;
+    if ((e = cudaFuncSetAttribute(k_nbcost<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, nbmax)) != cudaSuccess) return e;
+    if ((e = cudaFuncSetAttribute(kb_nbcost<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, nbmax)) != cudaSuccess) return e;
+    if ((e = cudaFuncSetAttribute(kb_nbcost<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, nbmax)) != cudaSuccess) return e;
     if ((e = cudaFuncSetAttribute(kb_pd_block<16, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   (int)pd_block_smem(16, 4))) != cudaSuccess) return e;
     if ((e = cudaFuncSetAttribute(kb_pd_block<8, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize,

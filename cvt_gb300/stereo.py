@@ -130,6 +130,52 @@ class PMHuberStereo:
         self._check(rc)
         return dmap
 
+    def depthMapResumable(self, dmap: torch.Tensor | None, left: torch.Tensor, right: torch.Tensor, patchsize: int,
+                          depthmax: float, iterations: int, resume: dict | None = None, stop: int = -1,
+                          save: bool = False, trace: dict | None = None):
+        """cvtpm_depthmap_resumable: the run from resume["iteration"] (with
+        resume["states"], resume["smooth"], (2, H, W, 4) float32 CUDA tensors;
+        None: from the random init) up to iteration `stop` (-1: the end).
+        Returns (dmap or None, checkpoint dict or None): the map when the run
+        reached the end, the state before `stop` when save is true."""
+        _check_img(left, "left")
+        _check_img(right, "right")
+        if left.shape != right.shape:
+            raise CVTException("Left/Right stereo images inconsistent or incompatible memory type")
+        H, W = left.shape[:2]
+        if stop < 0 or stop > iterations:
+            stop = iterations
+        finish = stop == iterations
+        if finish and dmap is None:
+            dmap = torch.empty((H, W), dtype=torch.float32, device=left.device)
+        rs = None
+        if resume is not None:
+            for k in ("states", "smooth"):
+                t = resume[k]
+                if t.shape != (2, H, W, 4) or t.dtype != torch.float32 or not t.is_contiguous() or t.device != left.device:
+                    raise CVTException(f"resume['{k}'] must be a contiguous (2, H, W, 4) float32 tensor on the images' device")
+            rs = _lib.CvtpmCheckpoint(int(resume["iteration"]), resume["states"].data_ptr(), resume["smooth"].data_ptr())
+        sv, out = None, None
+        if save:
+            out = {"states": torch.empty((2, H, W, 4), dtype=torch.float32, device=left.device),
+                   "smooth": torch.empty((2, H, W, 4), dtype=torch.float32, device=left.device)}
+            sv = _lib.CvtpmCheckpoint(-1, out["states"].data_ptr(), out["smooth"].data_ptr())
+        tr = None
+        if trace is not None and finish:
+            trace["winners"] = torch.empty((2, H, W), dtype=torch.uint8, device=left.device)
+            trace["valid"] = torch.empty((H, W), dtype=torch.uint8, device=left.device)
+            trace["states"] = torch.empty((2, H, W, 4), dtype=torch.float32, device=left.device)
+            tr = _lib.CvtpmTrace(trace["winners"].data_ptr(), trace["valid"].data_ptr(), trace["states"].data_ptr())
+        rc = _lib.lib().cvtpm_depthmap_resumable(
+            self._h, dmap.data_ptr() if finish else None, W * 4, left.data_ptr(), right.data_ptr(), W, H,
+            left.stride(0) * 4, int(patchsize), float(depthmax), int(iterations), 4, -1.0, None, 0,
+            ctypes.byref(tr) if tr is not None else None, ctypes.byref(rs) if rs is not None else None, int(stop),
+            ctypes.byref(sv) if sv is not None else None, _stream_ptr(left))
+        self._check(rc)
+        if out is not None:
+            out["iteration"] = sv.iteration
+        return (dmap if finish else None), out
+
     def depthMapImage(self, dmap: torch.Tensor | None, left: torch.Tensor, left_fmt: int, right: torch.Tensor,
                       right_fmt: int, patchsize: int, depthmax: float, iterations: int, viewsamples: int,
                       dscale: float = -1.0, normalmap: torch.Tensor | None = None,

@@ -164,6 +164,37 @@ cvtpm_status cvtpm_depthmap_host(cvtpm_ctx* ctx,
                                  float* normalmap, size_t normalmap_pitch,
                                  void* stream);
 
+/* The state of a depthMap run between two iterations: everything the
+ * iterations from `iteration` on read (the random streams are keyed by
+ * pixel, iteration and view, so they need no state).  Device memory of the
+ * caller, 16-byte aligned; W*H*4 floats per view, left view first. */
+typedef struct cvtpm_checkpoint {
+    int iteration;          /* the next iteration to run, 0..iterations     */
+    float* states;          /* 2*W*H*4: plane states (s0, s1, s2, cost)     */
+    float* smooth;          /* 2*W*H*4: PD-smoothed fields (nx, ny, d/dmax, 1) */
+} cvtpm_checkpoint;
+
+/* cvtpm_depthmap in pieces, for checkpointing long runs or inspecting the
+ * field between iterations; no counterpart in the reference, which runs
+ * the whole schedule in one call.  resume (may be NULL: start with the
+ * random init) continues from resume->iteration; the run stops before
+ * iteration `stop` (stop < 0 or >= iterations: runs to the end) and, with
+ * save given, writes the state there into save->states / save->smooth and
+ * sets save->iteration.  dmap (and normalmap, trace) are produced only by a
+ * call that runs to the end (dmap may be NULL otherwise).  A run split at
+ * any iteration into a saving call and a resuming call gives the bits of the
+ * uninterrupted call.  The other arguments are cvtpm_depthmap's. */
+cvtpm_status cvtpm_depthmap_resumable(cvtpm_ctx* ctx,
+                                      float* dmap, size_t dmap_pitch,
+                                      const float* left, const float* right,
+                                      int width, int height, size_t pitch,
+                                      int patchsize, float depthmax, int iterations,
+                                      int viewsamples, float dscale,
+                                      float* normalmap, size_t normalmap_pitch,
+                                      const cvtpm_trace* trace,
+                                      const cvtpm_checkpoint* resume, int stop,
+                                      cvtpm_checkpoint* save, void* stream);
+
 /* PMHuberStereo::depthMapInpaint (PMHuberStereo.h:41, PMHuberStereo.cpp:
  * 293-506) on device images: the depthMap schedule with the occlusion-masked
  * Huber-ROF smoother (100 steps, lambda = 20*theta + 5), theta ramped from
