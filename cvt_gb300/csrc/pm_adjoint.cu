@@ -63,8 +63,8 @@ __device__ __forceinline__ void load_tap(const PmView& v2, size_t j, float af, T
     const float4 B = __ldg(&v2.recB[j]);
     const float4 Cc = __ldg(&v2.recC[j]);
     const float2 D = __ldg(&v2.recD[j]);
-    const float T[7] = {A.x, A.y, A.z, A.w, B.x, B.y, B.z};
-    const float S[7] = {B.w, Cc.x, Cc.y, Cc.z, Cc.w, D.x, D.y};
+    const float T[7] = {A.x, A.y, A.z, A.w, Cc.x, Cc.y, D.x};
+    const float S[7] = {B.x, B.y, B.z, B.w, Cc.z, Cc.w, D.y};
 #pragma unroll
     for (int k = 0; k < 7; ++k) { t.D[k] = S[k]; t.v[k] = fmaf(af, S[k], T[k]); }
 }

@@ -205,10 +205,10 @@ __constant__ float c_prof[PM_PROF_N * PM_PROF_N];
 struct PmView {
     const float4* col;    /* RGBA, tight rows          */
     const float4* grad;   /* (dx, dy, dxy, dyx)         */
-    const float4* recA;   /* fast records: (c0,c1,c2,g0) */
-    const float4* recB;   /*               (g1,g2,g3,dc0) */
-    const float4* recC;   /*               (dc1,dc2,dg0,dg1) */
-    const float2* recD;   /*               (dg2,dg3)      */
+    const float4* recA;   /* fast records: values (c0,c1,c2,g0)          */
+    const float4* recB;   /*   their differences (dc0,dc1,dc2,dg0)        */
+    const float4* recC;   /*   (g1,g2,dg1,dg2): values and differences    */
+    const float2* recD;   /*   (g3,dg3)                                   */
 };
 
 struct PmCostConsts {
@@ -218,21 +218,63 @@ struct PmCostConsts {
     int rp;          /* row pitch (elements) of the record planes */
 };
 
+/* Packed FP32 pairs (sm_100 and later): one instruction applies the IEEE
+ * round-to-nearest add, subtract or fused multiply-add to both halves, so a
+ * pair gives the bits of the two scalar operations. */
+PM_DEV unsigned long long pk2(float2 v) {
+    unsigned long long r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(v.x), "f"(v.y));
+    return r;
+}
+PM_DEV float2 upk2(unsigned long long r) {
+    float2 v;
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(v.x), "=f"(v.y) : "l"(r));
+    return v;
+}
+PM_DEV float2 ffma2(float2 a, float2 b, float2 c) {
+    unsigned long long d;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(pk2(a)), "l"(pk2(b)), "l"(pk2(c)));
+    return upk2(d);
+}
+PM_DEV float2 fadd2(float2 a, float2 b) {
+    unsigned long long d;
+    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(pk2(a)), "l"(pk2(b)));
+    return upk2(d);
+}
+PM_DEV float2 fsub2(float2 a, float2 b) {
+    unsigned long long d;
+    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(pk2(a)), "l"(pk2(b)));
+    return upk2(d);
+}
+
 /* The matching terms of one tap in the FAST arithmetic: colour and gradient
  * truncated-L1 distances between image 1 at the tap (a1, g1) and the other
  * view interpolated from record j with weight a.  They depend on the tap
- * and the plane only, not on the pixel whose window holds the tap. */
+ * and the plane only, not on the pixel whose window holds the tap.  The
+ * record planes keep each value beside its difference partner, so the
+ * interpolations and differences run as packed pairs: channel k is
+ * fmaf(a, dT_k, T_k) and a_k - that, as the scalar form computes it. */
 PM_DEV void fast_tap_terms(const PmCostConsts& k, const PmView& v2, size_t j, float a, float4 a1, float4 g1,
                            float& cc, float& gc) {
     const float4 A = __ldg(&v2.recA[j]);
     const float4 B = __ldg(&v2.recB[j]);
     const float4 Cc = __ldg(&v2.recC[j]);
     const float2 D = __ldg(&v2.recD[j]);
-    const float v0 = fmaf(a, B.w, A.x), v1c = fmaf(a, Cc.x, A.y), v2c = fmaf(a, Cc.y, A.z);
-    const float u0 = fmaf(a, Cc.z, A.w), u1 = fmaf(a, Cc.w, B.x), u2 = fmaf(a, D.x, B.y), u3 = fmaf(a, D.y, B.z);
-    cc = (fminf(fabsf(a1.x - v0), k.cmax) + fminf(fabsf(a1.y - v1c), k.cmax)) + fminf(fabsf(a1.z - v2c), k.cmax);
-    gc = ((fminf(fabsf(g1.x - u0), k.gmax) + fminf(fabsf(g1.y - u1), k.gmax)) + fminf(fabsf(g1.z - u2), k.gmax)) +
-         fminf(fabsf(g1.w - u3), k.gmax);
+    const float2 aa = make_float2(a, a);
+    const float2 v01 = ffma2(aa, make_float2(B.x, B.y), make_float2(A.x, A.y));     /* c0, c1 */
+    const float2 v23 = ffma2(aa, make_float2(B.z, B.w), make_float2(A.z, A.w));     /* c2, g0 */
+    const float2 v45 = ffma2(aa, make_float2(Cc.z, Cc.w), make_float2(Cc.x, Cc.y)); /* g1, g2 */
+    const float v6 = fmaf(a, D.y, D.x);                                              /* g3 */
+    const float2 d01 = fsub2(make_float2(a1.x, a1.y), v01);
+    const float2 d23 = fsub2(make_float2(a1.z, g1.x), v23);
+    const float2 d45 = fsub2(make_float2(g1.y, g1.z), v45);
+    const float d6 = g1.w - v6;
+    const float m0 = fminf(fabsf(d01.x), k.cmax), m1 = fminf(fabsf(d01.y), k.cmax), m2 = fminf(fabsf(d23.x), k.cmax);
+    const float m3 = fminf(fabsf(d23.y), k.gmax), m4 = fminf(fabsf(d45.x), k.gmax), m5 = fminf(fabsf(d45.y), k.gmax);
+    const float m6 = fminf(fabsf(d6), k.gmax);
+    const float2 s = fadd2(fadd2(make_float2(m0, m3), make_float2(m1, m4)), make_float2(m2, m5));
+    cc = s.x;                                      /* (m0 + m1) + m2 */
+    gc = s.y + m6;                                 /* ((m3 + m4) + m5) + m6 */
 }
 
 /* The bilateral weight of tap (centre colour vc, tap colour a1, profile
@@ -320,8 +362,9 @@ PM_DEV void eval_costs(const PmCostConsts& k, const PmView& v1, const PmView& v2
                     if ((unsigned)xi >= (unsigned)k.W) continue;
                     float cc, gc;
                     fast_tap_terms(k, v2, (size_t)qy * k.rp + xi, pm_fix_frac(Xt), a1, g1, cc, gc);
-                    r1[c] = fmaf(w1, cc, r1[c]);
-                    r2[c] = fmaf(w1, gc, r2[c]);
+                    const float2 r = ffma2(make_float2(w1, w1), make_float2(cc, gc), make_float2(r1[c], r2[c]));
+                    r1[c] = r.x;                   /* fmaf(w1, cc, r1), fmaf(w1, gc, r2) */
+                    r2[c] = r.y;
                     ws[c] = ws[c] + w1;
                 }
             }

@@ -80,9 +80,9 @@ PM_DEV void records_tile(const float4* __restrict__ col, const float4* __restric
     const size_t i0 = (size_t)y * W + x, i1 = (size_t)y * W + min(x + 1, W - 1);
     float4 c0 = col[i0], c1 = col[i1], g0 = grad[i0], g1 = grad[i1];
     A[o] = f4(c0.x, c0.y, c0.z, g0.x);
-    Bq[o] = f4(g0.y, g0.z, g0.w, c1.x - c0.x);
-    C[o] = f4(c1.y - c0.y, c1.z - c0.z, g1.x - g0.x, g1.y - g0.y);
-    D[o] = make_float2(g1.z - g0.z, g1.w - g0.w);
+    Bq[o] = f4(c1.x - c0.x, c1.y - c0.y, c1.z - c0.z, g1.x - g0.x);
+    C[o] = f4(g0.y, g0.z, g1.y - g0.y, g1.z - g0.z);
+    D[o] = make_float2(g0.w, g1.w - g0.w);
 }
 
 __global__ void __launch_bounds__(128) k_records(const float4* __restrict__ col, const float4* __restrict__ grad, int W,
@@ -356,8 +356,9 @@ __device__ __forceinline__ void nb_accumulate(float w, float cc, float gc, float
         ws += w;
         r1 += w * cc;
     } else {
-        r1 = fmaf(w, cc, r1);
-        r2 = fmaf(w, gc, r2);
+        const float2 r = ffma2(make_float2(w, w), make_float2(cc, gc), make_float2(r1, r2));
+        r1 = r.x;                                  /* fmaf(w, cc, r1), fmaf(w, gc, r2) */
+        r2 = r.y;
         ws = ws + w;
     }
 }
