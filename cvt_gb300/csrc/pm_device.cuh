@@ -254,7 +254,12 @@ PM_DEV float2 fsub2(float2 a, float2 b) {
  * record planes keep each value beside its difference partner, so the
  * interpolations and differences run as packed pairs: channel k is
  * fmaf(a, dT_k, T_k) and a_k - that, as the scalar form computes it. */
-PM_DEV void fast_tap_terms(const PmCostConsts& k, const PmView& v2, size_t j, float a, float4 a1, float4 g1,
+/* Record and pixel indices are 64-bit: with 32-bit unsigned indices (whose
+ * wrap-around the compiler must keep) the propagation pass measured 33.4 ms
+ * against 30.7 ms. */
+typedef size_t pm_idx;
+
+PM_DEV void fast_tap_terms(const PmCostConsts& k, const PmView& v2, pm_idx j, float a, float4 a1, float4 g1,
                            float& cc, float& gc) {
     const float4 A = __ldg(&v2.recA[j]);
     const float4 B = __ldg(&v2.recB[j]);
@@ -344,7 +349,7 @@ PM_DEV void eval_costs(const PmCostConsts& k, const PmView& v1, const PmView& v2
                     const float a = t - fi;
                     const int i0 = clampi((int)fi, 0, k.W - 1);
                     const int i1 = clampi((int)fi + 1, 0, k.W - 1);
-                    const size_t rb = (size_t)qy * k.W;
+                    const pm_idx rb = (pm_idx)qy * (pm_idx)k.W;
                     const float4 c0 = __ldg(&v2.col[rb + i0]), cc1 = __ldg(&v2.col[rb + i1]);
                     const float4 h0 = __ldg(&v2.grad[rb + i0]), h1 = __ldg(&v2.grad[rb + i1]);
                     const float oa = 1.0f - a;
@@ -361,7 +366,7 @@ PM_DEV void eval_costs(const PmCostConsts& k, const PmView& v1, const PmView& v2
                     const int xi = (int)(Xt >> 32);
                     if ((unsigned)xi >= (unsigned)k.W) continue;
                     float cc, gc;
-                    fast_tap_terms(k, v2, (size_t)qy * k.rp + xi, pm_fix_frac(Xt), a1, g1, cc, gc);
+                    fast_tap_terms(k, v2, (pm_idx)qy * (pm_idx)k.rp + (pm_idx)xi, pm_fix_frac(Xt), a1, g1, cc, gc);
                     const float2 r = ffma2(make_float2(w1, w1), make_float2(cc, gc), make_float2(r1[c], r2[c]));
                     r1[c] = r.x;                   /* fmaf(w1, cc, r1), fmaf(w1, gc, r2) */
                     r2[c] = r.y;

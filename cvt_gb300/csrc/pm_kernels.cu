@@ -316,7 +316,7 @@ __global__ void __launch_bounds__(256, EXACT ? 1 : PM_PROP_MINB) k_propagate(PmP
  * the tap gets the same values.  Returns false where x' is outside the other
  * view (the tap is skipped, as eval_costs skips it). */
 template <bool EXACT>
-__device__ __forceinline__ bool nb_tap_terms(const PmCostConsts& k, const PmView& v2, int qx, int qy, size_t jrow,
+__device__ __forceinline__ bool nb_tap_terms(const PmCostConsts& k, const PmView& v2, int qx, int qy, pm_idx jrow,
                                              float sx, float sy, float sz, long long Xt, float4 a1, float4 g1,
                                              float& cc, float& gc) {
     if (EXACT) {
@@ -328,7 +328,7 @@ __device__ __forceinline__ bool nb_tap_terms(const PmCostConsts& k, const PmView
         const float a = t - fi;
         const int i0 = clampi((int)fi, 0, k.W - 1);
         const int i1 = clampi((int)fi + 1, 0, k.W - 1);
-        const size_t rb = (size_t)qy * k.W;
+        const pm_idx rb = (pm_idx)qy * (pm_idx)k.W;
         const float4 c0 = __ldg(&v2.col[rb + i0]), c1 = __ldg(&v2.col[rb + i1]);
         const float4 h0 = __ldg(&v2.grad[rb + i0]), h1 = __ldg(&v2.grad[rb + i1]);
         const float oa = 1.0f - a;
@@ -343,7 +343,7 @@ __device__ __forceinline__ bool nb_tap_terms(const PmCostConsts& k, const PmView
     } else {
         const int xi = (int)(Xt >> 32);
         if ((unsigned)xi >= (unsigned)k.W) return false;
-        fast_tap_terms(k, v2, jrow + xi, pm_fix_frac(Xt), a1, g1, cc, gc);
+        fast_tap_terms(k, v2, jrow + (pm_idx)xi, pm_fix_frac(Xt), a1, g1, cc, gc);
         return true;
     }
 }
@@ -427,7 +427,7 @@ __device__ __forceinline__ void nbcost_lane(const PmPassArgs& a, int mx, int my)
         if (!rmask) continue;
         const float4* c1row = a.v1.col + (size_t)qy * W;
         const float4* g1row = a.v1.grad + (size_t)qy * W;
-        const size_t jrow = (size_t)qy * a.k.rp;
+        const pm_idx jrow = (pm_idx)qy * (pm_idx)a.k.rp;
         long long X = XA + (long long)(qy - H / 2) * S1 + (long long)(qx0 - W / 2) * S0;
         for (int qx = qx0; qx <= qx1; ++qx) {
             const long long Xt = X;
@@ -569,7 +569,7 @@ PM_DEV void nbcost_block(const PmPassArgs& a, int mx0, int my0) {
             }
             rmask &= uok;
             if (rmask && own) {
-                const size_t jrow = (size_t)Yq * a.k.rp;
+                const pm_idx jrow = (pm_idx)Yq * (pm_idx)a.k.rp;
                 long long X = XA + (long long)(Yq - H / 2) * S1 + (long long)(mx - P - 1 - W / 2) * S0;
                 for (int rx = -P - 1; rx <= P + 1; ++rx) {
                     const int rxi = rx + P + 1;
@@ -933,6 +933,15 @@ k_pd_step(float4* __restrict__ uout, float4* __restrict__ pout, const float4* __
 #define PDB_TY 16        /* the plain path's tile height; the batch tuner may choose 8 */
 #define PDB_K 4
 
+/* (k % w, k / w) without an integer division: the fraction of (k + 0.5) / w
+ * is at least 0.5 / w away from an integer, and the product with the
+ * rounded reciprocal is off by less than 2.4e-7 (k + 0.5) / w, so its
+ * truncation is k / w for every k below 2^21. */
+PM_DEV void split_index(int k, int w, float inv_w, int& x, int& y) {
+    y = (int)(((float)k + 0.5f) * inv_w);
+    x = k - y * w;
+}
+
 /* shared memory of a TY-row tile with a K-pixel halo: u, both duals and f
  * (float4), w and the dual denominator (float) for every cell of the region */
 constexpr size_t pd_block_smem(int TY, int K = PDB_K) {
@@ -982,8 +991,11 @@ PM_DEV void pd_block_tile(float4* __restrict__ uout, float4* __restrict__ pout, 
      * after the last step the tile (distance K) is. */
     for (int st = 0; st < nsteps; ++st) {
         const int dw = PDB_RX - 2 * st, dh = PDB_RY - 2 * st;
+        const float inv_dw = 1.0f / (float)dw, inv_pw = 1.0f / (float)(dw - 2);
         for (int k = tid; k < dw * dh; k += nt) {                     /* duals */
-            const int lx = st + k % dw, ly = st + k / dw;
+            int lx, ly;
+            split_index(k, dw, inv_dw, lx, ly);
+            lx += st; ly += st;
             const int i = ly * PDB_RX + lx;
             const int gx = rx0 + lx, gy = ry0 + ly;
             float4 lo, hi;
@@ -994,7 +1006,9 @@ PM_DEV void pd_block_tile(float4* __restrict__ uout, float4* __restrict__ pout, 
         __syncthreads();
         const int pw = dw - 2, ph = dh - 2;
         for (int k = tid; k < pw * ph; k += nt) {                     /* primal */
-            const int lx = st + 1 + k % pw, ly = st + 1 + k / pw;
+            int lx, ly;
+            split_index(k, pw, inv_pw, lx, ly);
+            lx += st + 1; ly += st + 1;
             const int gx = rx0 + lx, gy = ry0 + ly;
             if (gx < 0 || gy < 0 || gx >= W || gy >= H) continue;
             const int i = ly * PDB_RX + lx;
