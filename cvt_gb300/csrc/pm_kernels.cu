@@ -26,6 +26,14 @@
 #define PM_NB_MINB 2
 #endif
 /* FAST: candidates 9-16 per window sweep (8: one sweep; 4: two) */
+/* The propagation as two launches: candidates 1-20, then the refinements
+ * at PM_REFINE_MINB blocks of 256 per SM (0: one launch). */
+#ifndef PM_PROP_SPLIT
+#define PM_PROP_SPLIT 1
+#endif
+#ifndef PM_REFINE_MINB
+#define PM_REFINE_MINB 4
+#endif
 #ifndef PM_FAST_SWEEP
 #define PM_FAST_SWEEP 8
 #endif
@@ -139,7 +147,14 @@ __global__ void __launch_bounds__(256) k_cost_field(PmPassArgs a, const float4* 
  * the 111 it took under the plain 256-thread bound); FAST needs the
  * two-block cap (it takes 153 registers and one block per SM otherwise: pass
  * 39.2 against 31.6 ms), where it also stops spilling. */
-template <bool EXACT>
+/* STAGE 0: the whole candidate schedule.  STAGE 1: candidates 1-20, the
+ * best so far written to out (and its index to winners).  STAGE 2: the two
+ * refinements of that best (read back from out), from the random stream
+ * after the 15 draws stage 1 made (12 for the random neighbours' offsets,
+ * 3 for the random plane).  Stages 1 then 2 give the bits of stage 0; the
+ * split lets the single-candidate refinement sweeps run at the occupancy
+ * their few registers allow. */
+template <bool EXACT, int STAGE>
 PM_DEV void propagate_tile(const PmPassArgs& a, int tbx, int tby) {
     const int W = a.k.W, H = a.k.H;
     const int y = tby * 8 + threadIdx.y;
@@ -157,10 +172,14 @@ PM_DEV void propagate_tile(const PmPassArgs& a, int tbx, int tby) {
     float nf = fmaxf(pm_sqrt(sm.x * sm.x + sm.y * sm.y) + 0.001f, 1.0f);
     float smx = sm.x / nf, smy = sm.y / nf;
     const float4 smooth = f4(smx, smy, pm_sqrt(1.0f - smx * smx - smy * smy), sm.z * dmax);
-    float4 self = a.old[o];
-    int win = 0;
+    float4 self = STAGE == 2 ? a.out[o] : a.old[o];
+    int win = STAGE == 2 ? -1 : 0;
     PmRng rng;
     seed_rng(rng, a, xc, yc, false);
+    if (STAGE == 2) {
+#pragma unroll 1
+        for (int i = 0; i < 15; ++i) (void)rng_float(rng);
+    }
 
     auto accept = [&](float4 cand, float cost, int idx) {
         cand.w = cost;
@@ -169,87 +188,89 @@ PM_DEV void propagate_tile(const PmPassArgs& a, int tbx, int tby) {
         if (cand.w + theta * da <= self.w + theta * db) { self = cand; win = idx; }
     };
 
-    /* candidates 1-8: the 3x3 neighbourhood of `old`, clamped to the edge
-     * (:330-342).  With the shared-window costs of k_nbcost (FAST), only
-     * neighbours the clamp moves (pixels on the image border) are evaluated
-     * here; the others are read. */
-    const bool shared = a.nbcost != nullptr;
-#pragma unroll 1
-    for (int b = 0; b < 2; ++b) {
-        float4 s[4]; bool act[4]; float c[4];
-#pragma unroll
-        for (int i = 0; i < 4; ++i) {
-            int n = b * 4 + i;                 /* 0..7 over the 8 neighbours in raster order */
-            int nn = n < 4 ? n : n + 1;        /* skip the centre */
-            int px = nn % 3 - 1, py = nn / 3 - 1;
-            s[i] = a.old[(size_t)clampi(yc + py, 0, H - 1) * W + clampi(xc + px, 0, W - 1)];
-            const bool edge = xc + px < 0 || xc + px >= W || yc + py < 0 || yc + py >= H;
-            act[i] = !shared || edge;
-            c[i] = act[i] ? 0.0f : a.nbcost[(size_t)n * W * H + o];
-        }
-        bool any = act[0] || act[1] || act[2] || act[3];
-        if (!shared || __any_sync(0xffffffffu, any)) {
-            float ce[4];
-            eval_costs<4, EXACT>(a.k, a.v1, a.v2, xc, yc, s, act, ce);
-#pragma unroll
-            for (int i = 0; i < 4; ++i)
-                if (act[i]) c[i] = ce[i];
-        }
-#pragma unroll
-        for (int i = 0; i < 4; ++i) accept(s[i], c[i], 1 + b * 4 + i);
-    }
-    /* candidates 9-16: the smoothed plane (:345-352), six random neighbours
-     * (:355-361), a fresh random plane (:364-368).  FAST evaluates the eight
-     * in one window sweep (1 % faster per pass than two sweeps of four,
-     * measured); EXACT in two, which keeps it at two blocks per SM. */
-    constexpr int NB = EXACT ? 4 : PM_FAST_SWEEP;
-#pragma unroll
-    for (int b0 = 0; b0 < 8; b0 += NB) {
-        float4 s[NB]; bool act[NB]; float c[NB];
-#pragma unroll
-        for (int j = 0; j < NB; ++j) {
-            const int i = b0 + j;
-            act[j] = true;
-            if (i == 0) {
-                const float4 sc = f4(1.0f - (-smooth.x / smooth.z), 0.0f - (-smooth.y / smooth.z),
-                                     0.0f - ((smooth.x * cx + smooth.y * cy) / smooth.z + smooth.w), 0.0f - 0.0f);
-                s[j] = lr ? sc : viewprop(sc);
-            } else if (i < 7) {
-                const int ox = (int)(rng_float(rng) * 7.0f + 0.5f);
-                const int oy = (int)(rng_float(rng) * 7.0f + 0.5f);
-                s[j] = a.old[(size_t)clampi(yc + oy, 0, H - 1) * W + clampi(xc + ox, 0, W - 1)];
-            } else {
-                s[j] = state_init(rng, cx, cy, lr, 2.0f, dmax);
-            }
-        }
-        eval_costs<NB, EXACT>(a.k, a.v1, a.v2, xc, yc, s, act, c);
-#pragma unroll
-        for (int j = 0; j < NB; ++j) accept(s[j], c[j], 9 + b0 + j);
-    }
-    /* 17-20: candidates from the other view (:372-379) */
     int nview_total = 0;
-    if (a.viewin) {
-        short4 l = a.viewin[o];
-        short li[4] = {l.x, l.y, l.z, l.w};
-        int nview = (li[0] < 0) ? 0 : (li[1] < 0) ? 1 : (li[2] < 0) ? 2 : (li[3] < 0) ? 3 : 4;
-        if (!inside) nview = 0;
-        nview_total = nview;
-        if (__any_sync(0xffffffffu, nview > 0)) {
+    if (STAGE != 2) {
+        /* candidates 1-8: the 3x3 neighbourhood of `old`, clamped to the edge
+         * (:330-342).  With the shared-window costs of k_nbcost (FAST), only
+         * neighbours the clamp moves (pixels on the image border) are evaluated
+         * here; the others are read. */
+        const bool shared = a.nbcost != nullptr;
+#pragma unroll 1
+        for (int b = 0; b < 2; ++b) {
             float4 s[4]; bool act[4]; float c[4];
 #pragma unroll
             for (int i = 0; i < 4; ++i) {
-                act[i] = i < nview;
-                s[i] = act[i] ? viewprop(a.viewsrc[(size_t)yc * W + li[i]]) : f4s(0.0f);
+                int n = b * 4 + i;                 /* 0..7 over the 8 neighbours in raster order */
+                int nn = n < 4 ? n : n + 1;        /* skip the centre */
+                int px = nn % 3 - 1, py = nn / 3 - 1;
+                s[i] = a.old[(size_t)clampi(yc + py, 0, H - 1) * W + clampi(xc + px, 0, W - 1)];
+                const bool edge = xc + px < 0 || xc + px >= W || yc + py < 0 || yc + py >= H;
+                act[i] = !shared || edge;
+                c[i] = act[i] ? 0.0f : a.nbcost[(size_t)n * W * H + o];
             }
-            eval_costs<4, EXACT>(a.k, a.v1, a.v2, xc, yc, s, act, c);
+            bool any = act[0] || act[1] || act[2] || act[3];
+            if (!shared || __any_sync(0xffffffffu, any)) {
+                float ce[4];
+                eval_costs<4, EXACT>(a.k, a.v1, a.v2, xc, yc, s, act, ce);
 #pragma unroll
-            for (int i = 0; i < 4; ++i)
-                if (act[i]) accept(s[i], c[i], 17 + i);
+                for (int i = 0; i < 4; ++i)
+                    if (act[i]) c[i] = ce[i];
+            }
+#pragma unroll
+            for (int i = 0; i < 4; ++i) accept(s[i], c[i], 1 + b * 4 + i);
+        }
+        /* candidates 9-16: the smoothed plane (:345-352), six random neighbours
+         * (:355-361), a fresh random plane (:364-368).  FAST evaluates the eight
+         * in one window sweep (1 % faster per pass than two sweeps of four,
+         * measured); EXACT in two, which keeps it at two blocks per SM. */
+        constexpr int NB = EXACT ? 4 : PM_FAST_SWEEP;
+#pragma unroll
+        for (int b0 = 0; b0 < 8; b0 += NB) {
+            float4 s[NB]; bool act[NB]; float c[NB];
+#pragma unroll
+            for (int j = 0; j < NB; ++j) {
+                const int i = b0 + j;
+                act[j] = true;
+                if (i == 0) {
+                    const float4 sc = f4(1.0f - (-smooth.x / smooth.z), 0.0f - (-smooth.y / smooth.z),
+                                         0.0f - ((smooth.x * cx + smooth.y * cy) / smooth.z + smooth.w), 0.0f - 0.0f);
+                    s[j] = lr ? sc : viewprop(sc);
+                } else if (i < 7) {
+                    const int ox = (int)(rng_float(rng) * 7.0f + 0.5f);
+                    const int oy = (int)(rng_float(rng) * 7.0f + 0.5f);
+                    s[j] = a.old[(size_t)clampi(yc + oy, 0, H - 1) * W + clampi(xc + ox, 0, W - 1)];
+                } else {
+                    s[j] = state_init(rng, cx, cy, lr, 2.0f, dmax);
+                }
+            }
+            eval_costs<NB, EXACT>(a.k, a.v1, a.v2, xc, yc, s, act, c);
+#pragma unroll
+            for (int j = 0; j < NB; ++j) accept(s[j], c[j], 9 + b0 + j);
+        }
+        /* 17-20: candidates from the other view (:372-379) */
+        if (a.viewin) {
+            short4 l = a.viewin[o];
+            short li[4] = {l.x, l.y, l.z, l.w};
+            int nview = (li[0] < 0) ? 0 : (li[1] < 0) ? 1 : (li[2] < 0) ? 2 : (li[3] < 0) ? 3 : 4;
+            if (!inside) nview = 0;
+            nview_total = nview;
+            if (__any_sync(0xffffffffu, nview > 0)) {
+                float4 s[4]; bool act[4]; float c[4];
+#pragma unroll
+                for (int i = 0; i < 4; ++i) {
+                    act[i] = i < nview;
+                    s[i] = act[i] ? viewprop(a.viewsrc[(size_t)yc * W + li[i]]) : f4s(0.0f);
+                }
+                eval_costs<4, EXACT>(a.k, a.v1, a.v2, xc, yc, s, act, c);
+#pragma unroll
+                for (int i = 0; i < 4; ++i)
+                    if (act[i]) accept(s[i], c[i], 17 + i);
+            }
         }
     }
     /* 21-22: random refinements of the current best (:383-389) */
 #pragma unroll 1
-    for (int i = 0; i < 2; ++i) {
+    for (int i = 0; i < (STAGE == 1 ? 0 : 2); ++i) {
         float4 s[1] = {state_refine(rng, self, cx, cy, dmax, lr)};
         bool act[1] = {true};
         float c[1];
@@ -258,9 +279,9 @@ PM_DEV void propagate_tile(const PmPassArgs& a, int tbx, int tby) {
     }
     if (inside) {
         a.out[o] = self;
-        if (a.winners) a.winners[o] = (uint8_t)win;
+        if (a.winners && win >= 0) a.winners[o] = (uint8_t)win;
     }
-    if (a.counters) {
+    if (STAGE != 2 && a.counters) {
         /* evaluations = 18 + view candidates; taps = in-image window taps */
         unsigned long long ev = 0, taps = 0;
         if (inside) {
@@ -282,9 +303,12 @@ PM_DEV void propagate_tile(const PmPassArgs& a, int tbx, int tby) {
     }
 }
 
-template <bool EXACT>
-__global__ void __launch_bounds__(256, EXACT ? 1 : PM_PROP_MINB) k_propagate(PmPassArgs a) {
-    propagate_tile<EXACT>(a, blockIdx.x, blockIdx.y);
+/* Registers: the candidate stages at two blocks per SM (FAST) or one
+ * (EXACT, 128 registers, still two blocks); the refinement stage at four. */
+template <bool EXACT, int STAGE>
+__global__ void __launch_bounds__(256, STAGE == 2 ? PM_REFINE_MINB : (EXACT ? 1 : PM_PROP_MINB))
+k_propagate(PmPassArgs a) {
+    propagate_tile<EXACT, STAGE>(a, blockIdx.x, blockIdx.y);
 }
 
 /* ---------------------------------------- shared neighbour windows -- */
@@ -1093,11 +1117,12 @@ __global__ void __launch_bounds__(32 * NB_WARPS, PM_NB_MINB) kb_nbcost(const __g
     }
 }
 
-template <bool EXACT>
-__global__ void __launch_bounds__(256, 2) kb_propagate(const __grid_constant__ PmBatch<PmPassArgs> b) {
+template <bool EXACT, int STAGE>
+__global__ void __launch_bounds__(256, STAGE == 2 ? PM_REFINE_MINB : 2)
+kb_propagate(const __grid_constant__ PmBatch<PmPassArgs> b) {
     for (int item = blockIdx.x; item < b.first[b.n]; item += gridDim.x) {
         const int p = batch_pair(b, item), t = item - b.first[p];
-        propagate_tile<EXACT>(b.a[p], t % b.tx[p], t / b.tx[p]);
+        propagate_tile<EXACT, STAGE>(b.a[p], t % b.tx[p], t / b.tx[p]);
     }
 }
 
@@ -1205,8 +1230,16 @@ cudaError_t pm_launch_propagate(const PmPassArgs& a, bool exact, cudaStream_t st
         else k_nbcost<false><<<nbgrid, dim3(32, NB_WARPS), smem, st>>>(b);
         PM_LAUNCH_CHECK();
     }
-    if (exact) k_propagate<true><<<grid, dim3(32, 8), 0, st>>>(b);
-    else k_propagate<false><<<grid, dim3(32, 8), 0, st>>>(b);
+#if PM_PROP_SPLIT
+    if (exact) k_propagate<true, 1><<<grid, dim3(32, 8), 0, st>>>(b);
+    else k_propagate<false, 1><<<grid, dim3(32, 8), 0, st>>>(b);
+    PM_LAUNCH_CHECK();
+    if (exact) k_propagate<true, 2><<<grid, dim3(32, 8), 0, st>>>(b);
+    else k_propagate<false, 2><<<grid, dim3(32, 8), 0, st>>>(b);
+#else
+    if (exact) k_propagate<true, 0><<<grid, dim3(32, 8), 0, st>>>(b);
+    else k_propagate<false, 0><<<grid, dim3(32, 8), 0, st>>>(b);
+#endif
     PM_LAUNCH_CHECK();
     return cudaSuccess;
 }
@@ -1370,8 +1403,26 @@ cudaError_t pm_batch_nbcost(const PmBatch<PmPassArgs>& b, bool exact, const PmBa
     PM_BATCH_LAUNCH(kb_nbcost<false>, dim3(32, NB_WARPS), smem);
 }
 cudaError_t pm_batch_propagate(const PmBatch<PmPassArgs>& b, bool exact, const PmBatchKnobs& kn, cudaStream_t st) {
-    if (exact) PM_BATCH_LAUNCH(kb_propagate<true>, dim3(32, 8), 0);
-    PM_BATCH_LAUNCH(kb_propagate<false>, dim3(32, 8), 0);
+#if PM_PROP_SPLIT
+    {
+        const int items_ = b.first[b.n];
+        if (items_ <= 0) return cudaSuccess;
+        if (exact) {
+            kb_propagate<true, 1><<<batch_grid(kb_propagate<true, 1>, 256, 0, items_, kn.grid_mult), dim3(32, 8), 0, st>>>(b);
+            PM_LAUNCH_CHECK();
+            kb_propagate<true, 2><<<batch_grid(kb_propagate<true, 2>, 256, 0, items_, kn.grid_mult), dim3(32, 8), 0, st>>>(b);
+        } else {
+            kb_propagate<false, 1><<<batch_grid(kb_propagate<false, 1>, 256, 0, items_, kn.grid_mult), dim3(32, 8), 0, st>>>(b);
+            PM_LAUNCH_CHECK();
+            kb_propagate<false, 2><<<batch_grid(kb_propagate<false, 2>, 256, 0, items_, kn.grid_mult), dim3(32, 8), 0, st>>>(b);
+        }
+        PM_LAUNCH_CHECK();
+        return cudaSuccess;
+    }
+#else
+    if (exact) PM_BATCH_LAUNCH((kb_propagate<true, 0>), dim3(32, 8), 0);
+    PM_BATCH_LAUNCH((kb_propagate<false, 0>), dim3(32, 8), 0);
+#endif
 }
 cudaError_t pm_batch_view_list(const PmBatch<PmViewListArgs>& b, int maxW, const PmBatchKnobs& kn, cudaStream_t st) {
     PM_BATCH_LAUNCH(kb_view_list, dim3(32), sizeof(int) * (size_t)maxW);
