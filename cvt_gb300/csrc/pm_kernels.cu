@@ -34,6 +34,14 @@
 #ifndef PM_REFINE_MINB
 #define PM_REFINE_MINB 4
 #endif
+/* The other view's candidates as a launch of their own (at PM_VIEW_MINB
+ * blocks per SM) between the two. */
+#ifndef PM_VIEW_SPLIT
+#define PM_VIEW_SPLIT 1
+#endif
+#ifndef PM_VIEW_MINB
+#define PM_VIEW_MINB 3
+#endif
 #ifndef PM_FAST_SWEEP
 #define PM_FAST_SWEEP 8
 #endif
@@ -147,13 +155,14 @@ __global__ void __launch_bounds__(256) k_cost_field(PmPassArgs a, const float4* 
  * the 111 it took under the plain 256-thread bound); FAST needs the
  * two-block cap (it takes 153 registers and one block per SM otherwise: pass
  * 39.2 against 31.6 ms), where it also stops spilling. */
-/* STAGE 0: the whole candidate schedule.  STAGE 1: candidates 1-20, the
- * best so far written to out (and its index to winners).  STAGE 2: the two
- * refinements of that best (read back from out), from the random stream
- * after the 15 draws stage 1 made (12 for the random neighbours' offsets,
- * 3 for the random plane).  Stages 1 then 2 give the bits of stage 0; the
- * split lets the single-candidate refinement sweeps run at the occupancy
- * their few registers allow. */
+/* STAGE 0: the whole candidate schedule.  STAGE 1: candidates 1-16 (and
+ * 17-20 unless PM_VIEW_SPLIT), the best so far written to out (its index to
+ * winners).  STAGE 3: the other view's candidates 17-20 against that best.
+ * STAGE 2: the two refinements of the best (read back from out), from the
+ * random stream after the 15 draws stage 1 made (12 for the random
+ * neighbours' offsets, 3 for the random plane).  Stages 1, (3,) 2 in order
+ * give the bits of stage 0; the split lets each sweep run at the occupancy
+ * its registers allow. */
 template <bool EXACT, int STAGE>
 PM_DEV void propagate_tile(const PmPassArgs& a, int tbx, int tby) {
     const int W = a.k.W, H = a.k.H;
@@ -172,8 +181,8 @@ PM_DEV void propagate_tile(const PmPassArgs& a, int tbx, int tby) {
     float nf = fmaxf(pm_sqrt(sm.x * sm.x + sm.y * sm.y) + 0.001f, 1.0f);
     float smx = sm.x / nf, smy = sm.y / nf;
     const float4 smooth = f4(smx, smy, pm_sqrt(1.0f - smx * smx - smy * smy), sm.z * dmax);
-    float4 self = STAGE == 2 ? a.out[o] : a.old[o];
-    int win = STAGE == 2 ? -1 : 0;
+    float4 self = STAGE >= 2 ? a.out[o] : a.old[o];    /* stages 2, 3: the best so far */
+    int win = STAGE >= 2 ? -1 : 0;
     PmRng rng;
     seed_rng(rng, a, xc, yc, false);
     if (STAGE == 2) {
@@ -189,7 +198,7 @@ PM_DEV void propagate_tile(const PmPassArgs& a, int tbx, int tby) {
     };
 
     int nview_total = 0;
-    if (STAGE != 2) {
+    if (STAGE != 2 && STAGE != 3) {
         /* candidates 1-8: the 3x3 neighbourhood of `old`, clamped to the edge
          * (:330-342).  With the shared-window costs of k_nbcost (FAST), only
          * neighbours the clamp moves (pixels on the image border) are evaluated
@@ -247,6 +256,8 @@ PM_DEV void propagate_tile(const PmPassArgs& a, int tbx, int tby) {
 #pragma unroll
             for (int j = 0; j < NB; ++j) accept(s[j], c[j], 9 + b0 + j);
         }
+    }
+    if (STAGE == 0 || STAGE == 3 || (STAGE == 1 && !PM_VIEW_SPLIT)) {
         /* 17-20: candidates from the other view (:372-379) */
         if (a.viewin) {
             short4 l = a.viewin[o];
@@ -270,7 +281,7 @@ PM_DEV void propagate_tile(const PmPassArgs& a, int tbx, int tby) {
     }
     /* 21-22: random refinements of the current best (:383-389) */
 #pragma unroll 1
-    for (int i = 0; i < (STAGE == 1 ? 0 : 2); ++i) {
+    for (int i = 0; i < ((STAGE == 0 || STAGE == 2) ? 2 : 0); ++i) {
         float4 s[1] = {state_refine(rng, self, cx, cy, dmax, lr)};
         bool act[1] = {true};
         float c[1];
@@ -288,7 +299,7 @@ PM_DEV void propagate_tile(const PmPassArgs& a, int tbx, int tby) {
             const int P = a.k.P;
             const int nx = min(xc + P, W - 1) - max(xc - P, 0) + 1;
             const int ny = min(yc + P, H - 1) - max(yc - P, 0) + 1;
-            ev = 18ull + (unsigned long long)nview_total;
+            ev = (STAGE == 3 ? 0ull : 18ull) + (unsigned long long)nview_total;
             taps = ev * (unsigned long long)(nx * ny);
         }
 #pragma unroll
@@ -306,7 +317,7 @@ PM_DEV void propagate_tile(const PmPassArgs& a, int tbx, int tby) {
 /* Registers: the candidate stages at two blocks per SM (FAST) or one
  * (EXACT, 128 registers, still two blocks); the refinement stage at four. */
 template <bool EXACT, int STAGE>
-__global__ void __launch_bounds__(256, STAGE == 2 ? PM_REFINE_MINB : (EXACT ? 1 : PM_PROP_MINB))
+__global__ void __launch_bounds__(256, STAGE == 2 ? PM_REFINE_MINB : STAGE == 3 ? PM_VIEW_MINB : (EXACT ? 1 : PM_PROP_MINB))
 k_propagate(PmPassArgs a) {
     propagate_tile<EXACT, STAGE>(a, blockIdx.x, blockIdx.y);
 }
@@ -1118,7 +1129,7 @@ __global__ void __launch_bounds__(32 * NB_WARPS, PM_NB_MINB) kb_nbcost(const __g
 }
 
 template <bool EXACT, int STAGE>
-__global__ void __launch_bounds__(256, STAGE == 2 ? PM_REFINE_MINB : 2)
+__global__ void __launch_bounds__(256, STAGE == 2 ? PM_REFINE_MINB : STAGE == 3 ? PM_VIEW_MINB : 2)
 kb_propagate(const __grid_constant__ PmBatch<PmPassArgs> b) {
     for (int item = blockIdx.x; item < b.first[b.n]; item += gridDim.x) {
         const int p = batch_pair(b, item), t = item - b.first[p];
@@ -1234,6 +1245,13 @@ cudaError_t pm_launch_propagate(const PmPassArgs& a, bool exact, cudaStream_t st
     if (exact) k_propagate<true, 1><<<grid, dim3(32, 8), 0, st>>>(b);
     else k_propagate<false, 1><<<grid, dim3(32, 8), 0, st>>>(b);
     PM_LAUNCH_CHECK();
+#if PM_VIEW_SPLIT
+    if (b.viewin) {
+        if (exact) k_propagate<true, 3><<<grid, dim3(32, 8), 0, st>>>(b);
+        else k_propagate<false, 3><<<grid, dim3(32, 8), 0, st>>>(b);
+        PM_LAUNCH_CHECK();
+    }
+#endif
     if (exact) k_propagate<true, 2><<<grid, dim3(32, 8), 0, st>>>(b);
     else k_propagate<false, 2><<<grid, dim3(32, 8), 0, st>>>(b);
 #else
@@ -1410,10 +1428,22 @@ cudaError_t pm_batch_propagate(const PmBatch<PmPassArgs>& b, bool exact, const P
         if (exact) {
             kb_propagate<true, 1><<<batch_grid(kb_propagate<true, 1>, 256, 0, items_, kn.grid_mult), dim3(32, 8), 0, st>>>(b);
             PM_LAUNCH_CHECK();
+#if PM_VIEW_SPLIT
+            if (b.a[0].viewin) {
+                kb_propagate<true, 3><<<batch_grid(kb_propagate<true, 3>, 256, 0, items_, kn.grid_mult), dim3(32, 8), 0, st>>>(b);
+                PM_LAUNCH_CHECK();
+            }
+#endif
             kb_propagate<true, 2><<<batch_grid(kb_propagate<true, 2>, 256, 0, items_, kn.grid_mult), dim3(32, 8), 0, st>>>(b);
         } else {
             kb_propagate<false, 1><<<batch_grid(kb_propagate<false, 1>, 256, 0, items_, kn.grid_mult), dim3(32, 8), 0, st>>>(b);
             PM_LAUNCH_CHECK();
+#if PM_VIEW_SPLIT
+            if (b.a[0].viewin) {
+                kb_propagate<false, 3><<<batch_grid(kb_propagate<false, 3>, 256, 0, items_, kn.grid_mult), dim3(32, 8), 0, st>>>(b);
+                PM_LAUNCH_CHECK();
+            }
+#endif
             kb_propagate<false, 2><<<batch_grid(kb_propagate<false, 2>, 256, 0, items_, kn.grid_mult), dim3(32, 8), 0, st>>>(b);
         }
         PM_LAUNCH_CHECK();
