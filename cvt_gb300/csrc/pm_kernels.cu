@@ -511,7 +511,8 @@ __device__ __forceinline__ void nbcost_lane(const PmPassArgs& a, int mx, int my)
  * in lockstep; per row:
  *   A. the image-1 row Yq over the block's columns mx0 - P - 1 ..
  *      mx0 + 32 + P (colour and gradient) is staged into shared memory by
- *      cp.async;
+ *      cp.async (double-buffered: row Yq + 1 is copied while the taps of
+ *      row Yq run, so a row costs two block barriers);
  *   B. warp w forms the weights of its user row at that image row for
  *      every offset rx (one weight per lane and offset) into a table
  *      T[w][rx][lane];
@@ -531,11 +532,10 @@ PM_DEV void cp_async16(void* smem, const void* gmem) {
     const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
     asm volatile("cp.async.ca.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem) : "memory");
 }
-PM_DEV void cp_async_wait_all() { asm volatile("cp.async.commit_group;\ncp.async.wait_group 0;\n" ::: "memory"); }
 
 /* dynamic shared memory of nbcost_block for window radius P */
 __host__ __device__ constexpr size_t nb_block_smem(int P) {
-    return (size_t)2 * (32 + 2 * (P + 1)) * 16 + (size_t)NB_WARPS * (2 * P + 5) * 32 * 4;
+    return (size_t)4 * (32 + 2 * (P + 1)) * 16 + (size_t)NB_WARPS * (2 * P + 5) * 32 * 4;
 }
 
 template <bool EXACT>
@@ -544,9 +544,10 @@ PM_DEV void nbcost_block(const PmPassArgs& a, int mx0, int my0) {
     const int W = a.k.W, H = a.k.H, P = a.k.P;
     const int NQ = 32 + 2 * (P + 1);                 /* staged columns mx0 - P - 1 .. mx0 + 32 + P */
     const int NR = 2 * P + 5;                        /* table columns: offsets rx = -P-3 .. P+1 */
-    float4* s_col = nb_smem;
-    float4* s_grad = nb_smem + NQ;
-    float* T = reinterpret_cast<float*>(nb_smem + 2 * NQ);
+    /* two staged rows (colour then gradient, NQ float4 each): the copy of
+     * the next row overlaps the taps of the current one */
+    float4* const rows = nb_smem;
+    float* T = reinterpret_cast<float*>(nb_smem + 4 * NQ);
     const int lane = threadIdx.x, w = threadIdx.y, tid = w * 32 + lane;
     const int U = my0 + w - 1;                       /* this warp's user row */
     const float4 uc = __ldg(&a.v1.col[(size_t)clampi(U, 0, H - 1) * W + mx0 + lane - 1]);
@@ -571,28 +572,38 @@ PM_DEV void nbcost_block(const PmPassArgs& a, int mx0, int my0) {
     float r1[8], r2[8], ws[8];
 #pragma unroll
     for (int k = 0; k < 8; ++k) { r1[k] = 0.0f; r2[k] = 0.0f; ws[k] = 0.0f; }
-    const int steps = NB_ROWS + 2 * P + 2;
-    for (int t = 0; t < steps; ++t) {
-        const int Yq = my0 - P - 1 + t;
-        if (Yq < 0 || Yq >= H) continue;             /* block-uniform */
-        /* A: the image-1 row */
+    /* the image rows the block's windows reach: Yq = t0 .. t1 */
+    const int t0 = max(my0 - P - 1, 0), t1 = min(my0 + NB_ROWS + P, H - 1);
+    auto stage = [&](int Yq, int buf) {                 /* A: an image-1 row, by cp.async */
         const size_t rb = (size_t)Yq * W + (mx0 - P - 1);
+        float4* dst = rows + buf * 2 * NQ;
         for (int i = tid; i < 2 * NQ; i += NB_WARPS * 32)
-            cp_async16(&nb_smem[i], i < NQ ? (const void*)(a.v1.col + rb + i) : (const void*)(a.v1.grad + rb + i - NQ));
-        cp_async_wait_all();
-        __syncthreads();
-        /* B: this user row's weights at image row Yq */
+            cp_async16(&dst[i], i < NQ ? (const void*)(a.v1.col + rb + i) : (const void*)(a.v1.grad + rb + i - NQ));
+        asm volatile("cp.async.commit_group;\n" ::: "memory");
+    };
+    auto weights = [&](int Yq, int buf) {               /* B: this user row's weights at image row Yq */
+        const float4* s_col = rows + buf * 2 * NQ;
         const int dy = Yq - U;
-        if (abs(dy) <= P) {                          /* warp-uniform */
+        if (abs(dy) <= P) {                             /* warp-uniform */
             const float* prow = c_prof + (dy + PM_PMAX) * PM_PROF_N + PM_PMAX;
             for (int rxi = 0; rxi < 2 * P + 3; ++rxi) {
-                const int dx = rxi - P;                  /* tap offset from the user: rx + 1 */
+                const int dx = rxi - P;                     /* tap offset from the user: rx + 1 */
                 T[(w * NR + rxi + 2) * 32 + lane] = abs(dx) <= P ? tap_weight(uc, s_col[lane + rxi], prow[dx]) : 0.0f;
             }
         } else {
             for (int rxi = 0; rxi < 2 * P + 3; ++rxi) T[(w * NR + rxi + 2) * 32 + lane] = 0.0f;
         }
-        __syncthreads();
+    };
+    stage(t0, 0);
+    asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+    __syncthreads();
+    weights(t0, 0);
+    __syncthreads();
+    for (int Yq = t0; Yq <= t1; ++Yq) {
+        const int buf = (Yq - t0) & 1;
+        if (Yq < t1) stage(Yq + 1, buf ^ 1);           /* its buffer was last read before the previous barrier */
+        const float4* s_col = rows + buf * 2 * NQ;
+        const float4* s_grad = s_col + NQ;
         /* C: the plane rows' window row Yq */
         const int ry = Yq - my;
         if (prow && ry >= -P - 1 && ry <= P + 1) {
@@ -633,7 +644,12 @@ PM_DEV void nbcost_block(const PmPassArgs& a, int mx0, int my0) {
                 }
             }
         }
-        __syncthreads();
+        if (Yq < t1) {
+            asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+            __syncthreads();                            /* the taps of Yq are done with T; row Yq + 1 is staged */
+            weights(Yq + 1, buf ^ 1);
+            __syncthreads();
+        }
     }
     if (!own) return;
 #pragma unroll
