@@ -259,12 +259,24 @@ PM_DEV float2 fsub2(float2 a, float2 b) {
  * against 30.7 ms. */
 typedef size_t pm_idx;
 
-PM_DEV void fast_tap_terms(const PmCostConsts& k, const PmView& v2, pm_idx j, float a, float4 a1, float4 g1,
+/* One row of the other view's record planes.  A window row is one image row
+ * for every candidate, so the row's four plane pointers are formed once per
+ * row and a tap addresses each plane with its signed column alone. */
+struct PmRecRow {
+    const float4 *A, *B, *C;
+    const float2* D;
+};
+PM_DEV PmRecRow rec_row(const PmView& v, int rp, int y) {
+    const pm_idx o = (pm_idx)y * (pm_idx)rp;
+    return {v.recA + o, v.recB + o, v.recC + o, v.recD + o};
+}
+
+PM_DEV void fast_tap_terms(const PmCostConsts& k, const PmRecRow& row, int xi, float a, float4 a1, float4 g1,
                            float& cc, float& gc) {
-    const float4 A = __ldg(&v2.recA[j]);
-    const float4 B = __ldg(&v2.recB[j]);
-    const float4 Cc = __ldg(&v2.recC[j]);
-    const float2 D = __ldg(&v2.recD[j]);
+    const float4 A = __ldg(row.A + xi);
+    const float4 B = __ldg(row.B + xi);
+    const float4 Cc = __ldg(row.C + xi);
+    const float2 D = __ldg(row.D + xi);
     const float2 aa = make_float2(a, a);
     const float2 v01 = ffma2(aa, make_float2(B.x, B.y), make_float2(A.x, A.y));     /* c0, c1 */
     const float2 v23 = ffma2(aa, make_float2(B.z, B.w), make_float2(A.z, A.w));     /* c2, g0 */
@@ -299,8 +311,17 @@ template <int K, bool EXACT>
 PM_DEV void eval_costs(const PmCostConsts& k, const PmView& v1, const PmView& v2, int x, int y,
                        const float4 (&s)[K], const bool (&act)[K], float (&cost)[K]) {
     float sx[K], sy[K], sz[K];
-    long long S0[K], S1[K], XC[K];
+    /* FAST: X is the candidate's Q31.32 position at the current tap, S0 its
+     * step along a row and D the step from a row's end to the next row's
+     * start (S1 - n * S0 for rows of n taps).  Integer adds are exact, so X
+     * at every tap equals XC + (qy - H/2) * S1 + (qx - W/2) * S0 formed
+     * directly, with two fewer 64-bit values per candidate held over the
+     * sweep. */
+    long long S0[K], D[K], X[K];
     bool live[K];
+    const int P = k.P;
+    const int dxlo = max(-P, -x), dxhi = min(P, k.W - 1 - x);
+    const int qy0 = max(y - P, 0), qy1 = min(y + P, k.H - 1);
 #pragma unroll
     for (int c = 0; c < K; ++c) {
         live[c] = act[c] && finite3(s[c]);
@@ -309,28 +330,23 @@ PM_DEV void eval_costs(const PmCostConsts& k, const PmView& v1, const PmView& v2
             sy[c] = live[c] ? s[c].y : 0.0f;
             sz[c] = live[c] ? s[c].z : -1.0e30f;    /* never inside [0, W) */
         } else {
-            pm_fix_plane(live[c], s[c].x, s[c].y, s[c].z, k.W / 2, k.H / 2, &S0[c], &S1[c], &XC[c]);
+            long long S1, XC;
+            pm_fix_plane(live[c], s[c].x, s[c].y, s[c].z, k.W / 2, k.H / 2, &S0[c], &S1, &XC);
+            X[c] = XC + (long long)(qy0 - k.H / 2) * S1 + (long long)(x + dxlo - k.W / 2) * S0[c];
+            D[c] = S1 - (long long)(dxhi - dxlo + 1) * S0[c];
         }
     }
     float ws[K], r1[K], r2[K];
 #pragma unroll
     for (int c = 0; c < K; ++c) { ws[c] = 0.0f; r1[c] = 0.0f; r2[c] = 0.0f; }
     const float4 vc = __ldg(&v1.col[(size_t)y * k.W + x]);
-    const int P = k.P;
-    const int dxlo = max(-P, -x), dxhi = min(P, k.W - 1 - x);
-    for (int dy = -P; dy <= P; ++dy) {
-        const int qy = y + dy;
-        if (qy < 0 || qy >= k.H) continue;
+    for (int qy = qy0; qy <= qy1; ++qy) {
+        const int dy = qy - y;
         const float qyf = (float)qy;
         const float4* c1row = v1.col + (size_t)qy * k.W;
         const float4* g1row = v1.grad + (size_t)qy * k.W;
         const float* prow = c_prof + (dy + PM_PMAX) * PM_PROF_N + PM_PMAX;
-        long long X[K];
-        if (!EXACT) {
-#pragma unroll
-            for (int c = 0; c < K; ++c)
-                X[c] = XC[c] + (long long)(qy - k.H / 2) * S1[c] + (long long)(x + dxlo - k.W / 2) * S0[c];
-        }
+        const PmRecRow rrow = rec_row(v2, k.rp, qy);
         for (int dx = dxlo; dx <= dxhi; ++dx) {
             const int qx = x + dx;
             const float qxf = (float)qx;
@@ -366,13 +382,17 @@ PM_DEV void eval_costs(const PmCostConsts& k, const PmView& v1, const PmView& v2
                     const int xi = (int)(Xt >> 32);
                     if ((unsigned)xi >= (unsigned)k.W) continue;
                     float cc, gc;
-                    fast_tap_terms(k, v2, (pm_idx)qy * (pm_idx)k.rp + (pm_idx)xi, pm_fix_frac(Xt), a1, g1, cc, gc);
+                    fast_tap_terms(k, rrow, xi, pm_fix_frac(Xt), a1, g1, cc, gc);
                     const float2 r = ffma2(make_float2(w1, w1), make_float2(cc, gc), make_float2(r1[c], r2[c]));
                     r1[c] = r.x;                   /* fmaf(w1, cc, r1), fmaf(w1, gc, r2) */
                     r2[c] = r.y;
                     ws[c] = ws[c] + w1;
                 }
             }
+        }
+        if (!EXACT) {
+#pragma unroll
+            for (int c = 0; c < K; ++c) X[c] += D[c];
         }
     }
 #pragma unroll

@@ -351,7 +351,7 @@ k_propagate(PmPassArgs a) {
  * the tap gets the same values.  Returns false where x' is outside the other
  * view (the tap is skipped, as eval_costs skips it). */
 template <bool EXACT>
-__device__ __forceinline__ bool nb_tap_terms(const PmCostConsts& k, const PmView& v2, int qx, int qy, pm_idx jrow,
+__device__ __forceinline__ bool nb_tap_terms(const PmCostConsts& k, const PmView& v2, int qx, int qy, const PmRecRow& rrow,
                                              float sx, float sy, float sz, long long Xt, float4 a1, float4 g1,
                                              float& cc, float& gc) {
     if (EXACT) {
@@ -378,7 +378,7 @@ __device__ __forceinline__ bool nb_tap_terms(const PmCostConsts& k, const PmView
     } else {
         const int xi = (int)(Xt >> 32);
         if ((unsigned)xi >= (unsigned)k.W) return false;
-        fast_tap_terms(k, v2, jrow + (pm_idx)xi, pm_fix_frac(Xt), a1, g1, cc, gc);
+        fast_tap_terms(k, rrow, xi, pm_fix_frac(Xt), a1, g1, cc, gc);
         return true;
     }
 }
@@ -462,7 +462,7 @@ __device__ __forceinline__ void nbcost_lane(const PmPassArgs& a, int mx, int my)
         if (!rmask) continue;
         const float4* c1row = a.v1.col + (size_t)qy * W;
         const float4* g1row = a.v1.grad + (size_t)qy * W;
-        const pm_idx jrow = (pm_idx)qy * (pm_idx)a.k.rp;
+        const PmRecRow rrow = rec_row(a.v2, a.k.rp, qy);
         long long X = XA + (long long)(qy - H / 2) * S1 + (long long)(qx0 - W / 2) * S0;
         for (int qx = qx0; qx <= qx1; ++qx) {
             const long long Xt = X;
@@ -479,7 +479,7 @@ __device__ __forceinline__ void nbcost_lane(const PmPassArgs& a, int mx, int my)
             const float4 a1 = __ldg(&c1row[qx]);
             const float4 g1 = __ldg(&g1row[qx]);
             float cc, gc;
-            if (!nb_tap_terms<EXACT>(a.k, a.v2, qx, qy, jrow, sx, sy, sz, Xt, a1, g1, cc, gc)) continue;
+            if (!nb_tap_terms<EXACT>(a.k, a.v2, qx, qy, rrow, sx, sy, sz, Xt, a1, g1, cc, gc)) continue;
 #pragma unroll
             for (int k = 0; k < 8; ++k) {
                 if (!((mask >> k) & 1u)) continue;
@@ -615,7 +615,7 @@ PM_DEV void nbcost_block(const PmPassArgs& a, int mx0, int my0) {
             }
             rmask &= uok;
             if (rmask && own) {
-                const pm_idx jrow = (pm_idx)Yq * (pm_idx)a.k.rp;
+                const PmRecRow rrow = rec_row(a.v2, a.k.rp, Yq);
                 long long X = XA + (long long)(Yq - H / 2) * S1 + (long long)(mx - P - 1 - W / 2) * S0;
                 for (int rx = -P - 1; rx <= P + 1; ++rx) {
                     const int rxi = rx + P + 1;
@@ -632,7 +632,7 @@ PM_DEV void nbcost_block(const PmPassArgs& a, int mx0, int my0) {
                     const float4 a1 = s_col[lane + rxi];
                     const float4 g1 = s_grad[lane + rxi];
                     float cc, gc;
-                    if (!nb_tap_terms<EXACT>(a.k, a.v2, mx + rx, Yq, jrow, sx, sy, sz, Xt, a1, g1, cc, gc)) continue;
+                    if (!nb_tap_terms<EXACT>(a.k, a.v2, mx + rx, Yq, rrow, sx, sy, sz, Xt, a1, g1, cc, gc)) continue;
 #pragma unroll
                     for (int k = 0; k < 8; ++k) {
                         if (!((mask >> k) & 1u)) continue;
@@ -981,7 +981,9 @@ k_pd_step(float4* __restrict__ uout, float4* __restrict__ pout, const float4* __
  * tile is exact.  Image borders keep the reference's semantics: u is read
  * clamped to the edge, the dual and the weight are zero outside. */
 #define PDB_TX 32
+#ifndef PDB_TY
 #define PDB_TY 16        /* the plain path's tile height; the batch tuner may choose 8 */
+#endif
 #define PDB_K 4
 
 /* (k % w, k / w) without an integer division: the fraction of (k + 0.5) / w
