@@ -21,6 +21,7 @@ EXPORTS = (
     "cvtpm_depthmap_host", "cvtpm_depthmap_resumable", "cvtpm_depthmap_inpaint", "cvtpm_cost_eval", "cvtpm_cost_adjoint", "cvtpm_polish_planes", "cvtpm_depthmap_batched", "cvtpm_set_batch_knobs", "cvtpm_set_memory_budget",
     "cvtpm_set_batch_lanes", "cvtpm_get_batch_info",
     "cvtpm_set_timing", "cvtpm_reset_stats", "cvtpm_get_stats", "cvtpm_tool_fp32_peak",
+    "cvtpm_tool_pd_time",
     "cvtpm_cost_eval_noalloc",
     "cvtpm_iformat_bpp", "cvtpm_image_to_rgbaf", "cvtpm_depthmap_image", "cvtpm_raw_read", "cvtpm_raw_write",
     "cvtpm_ppm_read", "cvtpm_pfm_write", "cvtpm_png_read", "cvtpm_png_write", "cvtpm_float_to_srgb_u8", "cvtpm_stereo_rectify", "cvtpm_warp_apply",
@@ -143,6 +144,7 @@ def lib() -> ctypes.CDLL:
     L.cvtpm_reset_stats.argtypes = [vp]
     L.cvtpm_get_stats.argtypes = [vp, ctypes.POINTER(CvtpmStats)]
     L.cvtpm_tool_fp32_peak.argtypes = [i, vp, ctypes.POINTER(ctypes.c_float)]
+    L.cvtpm_tool_pd_time.argtypes = [vp, i, vp, ctypes.POINTER(ctypes.c_float)]
     L.cvtpm_cost_eval_noalloc.argtypes = [P, vp, vp, i, i, sz, vp, vp, vp]
     IP = ctypes.POINTER(CvtpmImage)
     L.cvtpm_iformat_bpp.argtypes = [i]

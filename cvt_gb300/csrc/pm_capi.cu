@@ -47,6 +47,12 @@ struct cvtpm_ctx {
     float4* smooth[2];
     float4 *tmp, *tmp2, *pdT;
     float4* pdP[2];
+    /* the right view's smoother runs on `side`, beside the next left pass,
+     * with scratch of its own */
+    float4 *tmpR, *tmp2R, *pdTR;
+    float4* pdPR[2];
+    cudaStream_t side = nullptr;
+    cudaEvent_t side_fork = nullptr, side_join = nullptr;
     short4* list[2];
     uint8_t* win[2];
     uint8_t* valid;
@@ -226,9 +232,21 @@ cvtpm_status ensure_buffers(cvtpm_ctx* ctx, int W, int H) {
     add((void**)&ctx->tmp, n * 16);
     add((void**)&ctx->tmp2, n * 16);
     add((void**)&ctx->pdT, n * 16);
+    add((void**)&ctx->tmpR, n * 16);
+    add((void**)&ctx->tmp2R, n * 16);
+    add((void**)&ctx->pdTR, n * 16);
+    add((void**)&ctx->pdPR[0], n * 32);
+    add((void**)&ctx->pdPR[1], n * 32);
     add((void**)&ctx->valid, n);
     add((void**)&ctx->occ, n * 4);
     const size_t need = align_up(off, 256);
+    if (!ctx->side) {
+        if (ctx->no_alloc) return fail(ctx, CVTPM_ERR_ALLOC, "side stream not created before capture");
+        cudaError_t e = cudaStreamCreateWithFlags(&ctx->side, cudaStreamNonBlocking);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->side_fork, cudaEventDisableTiming);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->side_join, cudaEventDisableTiming);
+        if (e != cudaSuccess) return cuda_fail(ctx, e, "side stream");
+    }
     if (need > ctx->pool_bytes) {
         if (ctx->no_alloc) return fail(ctx, CVTPM_ERR_ALLOC, "scratch not sized before capture");
         if (ctx->pool) { cudaFree(ctx->pool); ctx->pool = nullptr; ctx->pool_bytes = 0; }
@@ -348,13 +366,16 @@ cvtpm_status prep_views(cvtpm_ctx* ctx, const cvtpm_params& p, const float* img0
  * kernel (identical arithmetic); iters == 0 keeps the reference's single
  * extra step from a copy of the input. */
 cvtpm_status pd_apply(cvtpm_ctx* ctx, float4* output, const float4* input, const float* wgt, float lambda, int iters,
-                      int W, int H, cudaStream_t st, const float* mask = nullptr) {
+                      int W, int H, cudaStream_t st, const float* mask = nullptr, int scratch = 0) {
     const size_t n = (size_t)W * H;
+    float4* const pdT = scratch ? ctx->pdTR : ctx->pdT;
+    float4* const pdP0 = scratch ? ctx->pdPR[0] : ctx->pdP[0];
+    float4* const pdP1 = scratch ? ctx->pdPR[1] : ctx->pdP[1];
     PhaseTimer tm(ctx, st, ctx->ev_pd);
     if (iters == 0) {
-        CK(cudaMemcpyAsync(ctx->pdT, input, n * 16, cudaMemcpyDeviceToDevice, st), "pd copy");
-        CK(cudaMemsetAsync(ctx->pdP[0], 0, n * 32, st), "pd clear");
-        LK(pm_launch_pd_step(output, ctx->pdP[1], ctx->pdT, ctx->pdP[0], input, wgt, mask, lambda, W, H, st), "pd step");
+        CK(cudaMemcpyAsync(pdT, input, n * 16, cudaMemcpyDeviceToDevice, st), "pd copy");
+        CK(cudaMemsetAsync(pdP0, 0, n * 32, st), "pd clear");
+        LK(pm_launch_pd_step(output, pdP1, pdT, pdP0, input, wgt, mask, lambda, W, H, st), "pd step");
         ++ctx->stats.pd_launches;
         ++ctx->stats.pd_steps;
         tm.stop();
@@ -362,8 +383,8 @@ cvtpm_status pd_apply(cvtpm_ctx* ctx, float4* output, const float4* input, const
     }
     const int total = iters + (iters & 1);
     const int K = pm_pd_block_steps();
-    float4* U[2] = {output, ctx->pdT};
-    float4* Pp[2] = {ctx->pdP[0], ctx->pdP[1]};
+    float4* U[2] = {output, pdT};
+    float4* Pp[2] = {pdP0, pdP1};
     int l = 0;
     for (int done = 0; done < total; done += K, ++l) {
         const int steps = total - done < K ? total - done : K;
@@ -488,6 +509,7 @@ cvtpm_status run_depthmap(cvtpm_ctx* ctx, const cvtpm_params& p, float* dmap, si
         LK(pm_launch_view_list(ctx->S[0][1 - sw], W, H, ctx->list[0], st), "view list");
         aR.old = ctx->S[1][sw]; aR.out = ctx->S[1][1 - sw]; aR.smooth = ctx->smooth[1];
         aR.viewin = ctx->list[0]; aR.viewsrc = ctx->S[0][1 - sw]; aR.winners = ctx->win[1];
+        if (iter > first) CK(cudaStreamWaitEvent(st, ctx->side_join, 0), "join");   /* smooth[1] */
         {
             NvtxRange r("propagate right");
             PhaseTimer tm(ctx, st, ctx->ev_prop);
@@ -497,16 +519,29 @@ cvtpm_status run_depthmap(cvtpm_ctx* ctx, const cvtpm_params& p, float* dmap, si
         ctx->stats.propagate_launches += 2;
         LK(pm_launch_view_list(ctx->S[1][1 - sw], W, H, ctx->list[1], st), "view list");
         const float lambda = theta * p.thetascale + 5.0f;
-        for (int v = 0; v < 2; ++v) {                              /* :228-261 */
+        /* :228-261.  The right view's consistency, fill and smoother need only
+         * this iteration's planes and write only smooth[1] and scratch of
+         * their own, so they run on the side stream while the left view's
+         * smoother and the next left pass run here: the side work fills the
+         * SMs the tails of those launches leave idle.  The next right pass
+         * waits for it (side_join). */
+        CK(cudaEventRecord(ctx->side_fork, st), "fork");
+        CK(cudaStreamWaitEvent(ctx->side, ctx->side_fork, 0), "fork");
+        for (int v = 1; v >= 0; --v) {
             NvtxRange r(v == 0 ? "consistency, fill, PD left" : "consistency, fill, PD right");
+            cudaStream_t sv = v == 0 ? st : ctx->side;
+            float4* const t1 = v == 0 ? ctx->tmp : ctx->tmpR;
+            float4* const t2 = v == 0 ? ctx->tmp2 : ctx->tmp2R;
             LK(pm_launch_consistency(ctx->S[v][1 - sw], ctx->S[1 - v][1 - sw], W, H, p.maxdispdiff, p.maxanglediff,
-                                     v == 0 ? 1 : 0, ctx->tmp, nullptr, st), "consistency");
-            LK(pm_launch_fill_state(ctx->tmp, W, H, dmax, v == 0 ? 1 : 0, ctx->tmp2, st), "fill");
-            if ((s = pd_apply(ctx, ctx->smooth[v], ctx->tmp2, ctx->wgt[v], lambda, p.pd_iterations, W, H, st)) != CVTPM_OK)
+                                     v == 0 ? 1 : 0, t1, nullptr, sv), "consistency");
+            LK(pm_launch_fill_state(t1, W, H, dmax, v == 0 ? 1 : 0, t2, sv), "fill");
+            if ((s = pd_apply(ctx, ctx->smooth[v], t2, ctx->wgt[v], lambda, p.pd_iterations, W, H, sv, nullptr, v)) != CVTPM_OK)
                 return s;
         }
+        CK(cudaEventRecord(ctx->side_join, ctx->side), "join");
         if (iter >= 5) theta = smoothstep01(((float)iter - 5.0f) / ((float)N - 5.0f)) * 1.0f;
     }
+    if (last > first) CK(cudaStreamWaitEvent(st, ctx->side_join, 0), "join");
     if (save) {
         const int sw = last & 1;
         for (int v = 0; v < 2; ++v) {
@@ -726,6 +761,9 @@ cvtpm_status cvtpm_destroy(cvtpm_ctx* ctx) {
         if (l.s) cudaStreamDestroy(l.s);
         if (l.done) cudaEventDestroy(l.done);
     }
+    if (ctx->side) cudaStreamDestroy(ctx->side);
+    if (ctx->side_fork) cudaEventDestroy(ctx->side_fork);
+    if (ctx->side_join) cudaEventDestroy(ctx->side_join);
     if (ctx->bstream) cudaStreamDestroy(ctx->bstream);
     if (ctx->bfork) cudaEventDestroy(ctx->bfork);
     if (ctx->bjoin) cudaEventDestroy(ctx->bjoin);
@@ -1737,6 +1775,39 @@ cvtpm_status cvtpm_tool_fp32_peak(int device, void* stream, float* tflops) {
     if (s != CVTPM_OK) return s;
     const double flops = 2.0 * 8.0 * (double)iters * blocks * 256.0;
     *tflops = (float)(flops / (best * 1e-3) / 1e12);
+    return CVTPM_OK;
+}
+
+cvtpm_status cvtpm_tool_pd_time(cvtpm_ctx* ctx, int steps, void* stream, float* us_per_step) {
+    if (!ctx || !us_per_step || steps < 2 || (steps & 1)) return CVTPM_ERR_INVALID_ARGUMENT;
+    if (!ctx->pool || ctx->capW <= 0 || ctx->capH <= 0)
+        return fail(ctx, CVTPM_ERR_INVALID_ARGUMENT, "no depthMap has sized this context yet");
+    if (cudaSetDevice(ctx->device) != cudaSuccess) return CVTPM_ERR_CUDA;
+    cudaStream_t st = (cudaStream_t)stream;
+    const int W = ctx->capW, H = ctx->capH;
+    const bool timing = ctx->timing;
+    ctx->timing = false;
+    cudaEvent_t a = nullptr, b = nullptr;
+    cudaEventCreate(&a);
+    cudaEventCreate(&b);
+    float best = 1e30f;
+    cvtpm_status s = CVTPM_OK;
+    for (int rep = 0; rep < 3 && s == CVTPM_OK; ++rep) {
+        /* the left view's smoother input of the last call, smoothed into
+         * scratch that the next call rewrites before reading */
+        cudaEventRecord(a, st);
+        s = pd_apply(ctx, ctx->tmpR, ctx->tmp2, ctx->wgt[0], 5.0f, steps, W, H, st, nullptr, 1);
+        cudaEventRecord(b, st);
+        if (s == CVTPM_OK && cudaEventSynchronize(b) != cudaSuccess) s = CVTPM_ERR_CUDA;
+        float ms = 0.0f;
+        cudaEventElapsedTime(&ms, a, b);
+        if (rep > 0 && ms < best) best = ms;    /* the first run warms up */
+    }
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    ctx->timing = timing;
+    if (s != CVTPM_OK) return s;
+    *us_per_step = best * 1e3f / (float)steps;
     return CVTPM_OK;
 }
 
