@@ -918,43 +918,16 @@ PM_DEV float div_pos(float x, float d) { return x == 0.0f ? x : x / d; }
 /* The dual at q from u(q), u(q+x), u(q+y), the old dual and w(q) (:49-68).
  * INPAINT: PDHuberWeightedInpaint.cl projects every channel on its own
  * (:67) instead of (x, y) jointly and z apart. */
-#ifndef PM_PD_PACKED
-#define PM_PD_PACKED 0
-#endif
-/* float4 arithmetic on packed pairs: each half is the scalar IEEE operation */
-PM_DEV float2 fmul2(float2 a, float2 b) {
-    unsigned long long d;
-    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(pk2(a)), "l"(pk2(b)));
-    return upk2(d);
-}
-PM_DEV float2 lo2(float4 v) { return make_float2(v.x, v.y); }
-PM_DEV float2 hi2(float4 v) { return make_float2(v.z, v.w); }
-PM_DEV float4 cat2(float2 a, float2 b) { return f4(a.x, a.y, b.x, b.y); }
-PM_DEV float4 add4p(float4 a, float4 b) { return cat2(fadd2(lo2(a), lo2(b)), fadd2(hi2(a), hi2(b))); }
-PM_DEV float4 sub4p(float4 a, float4 b) { return cat2(fsub2(lo2(a), lo2(b)), fsub2(hi2(a), hi2(b))); }
-PM_DEV float4 mul4p(float4 a, float4 b) { return cat2(fmul2(lo2(a), lo2(b)), fmul2(hi2(a), hi2(b))); }
-
 template <bool INPAINT>
 PM_DEV void pd_dual(float w, float den, float4 uq, float4 ux, float4 uy, float4 plo, float4 phi,
                     float4& lo, float4& hi) {
     const float SIGMA = 1.0f / pm_sqrt(8.0f);
-#if PM_PD_PACKED
-    const float4 ww = f4s(w), ss = f4s(SIGMA);
-    const float4 dx = mul4p(ww, sub4p(uq, ux));
-    const float4 dy = mul4p(ww, sub4p(uq, uy));
-    const float4 nl = add4p(plo, mul4p(ss, dx)), nh = add4p(phi, mul4p(ss, dy));
-#else
     const float4 dx = w * (uq - ux);
     const float4 dy = w * (uq - uy);
     const float4 nl = plo + SIGMA * dx, nh = phi + SIGMA * dy;
-#endif
     const float4 l = f4(div_pos(nl.x, den), div_pos(nl.y, den), div_pos(nl.z, den), div_pos(nl.w, den));
     const float4 h = f4(div_pos(nh.x, den), div_pos(nh.y, den), div_pos(nh.z, den), div_pos(nh.w, den));
-#if PM_PD_PACKED
-    const float4 pt = add4p(mul4p(l, l), mul4p(h, h));
-#else
     const float4 pt = l * l + h * h;
-#endif
     float sx, sy, sz, sw;
     if (INPAINT) {
         sx = fmaxf(1.0f, pm_sqrt(pt.x));
@@ -975,18 +948,11 @@ PM_DEV void pd_dual(float w, float den, float4 uq, float4 ux, float4 uy, float4 
 PM_DEV float4 pd_primal(float4 uc, float4 img, float wc, float4 lo_c, float4 lo_l, float4 hi_c, float4 hi_u,
                         float lambda, float den_u) {
     const float TAU = 1.0f / pm_sqrt(8.0f), THETA = 0.5f;
-#if PM_PD_PACKED
-    const float4 div = sub4p(add4p(sub4p(lo_c, lo_l), hi_c), hi_u);
-    const float4 num = add4p(uc, mul4p(f4s(TAU), sub4p(mul4p(f4s(lambda), img), mul4p(f4s(wc), div))));
-    float4 un = f4(num.x / den_u, num.y / den_u, num.z / den_u, 0.0f);   /* .w is overwritten below */
-    un = add4p(un, mul4p(f4s(THETA), sub4p(un, uc)));
-#else
     const float4 div = lo_c - lo_l + hi_c - hi_u;
     const float4 lam = f4s(lambda);
     const float4 num = uc + TAU * (lam * img - wc * div);
     float4 un = f4(num.x / den_u, num.y / den_u, num.z / den_u, 0.0f);   /* .w is overwritten below */
     un = un + THETA * (un - uc);
-#endif
     un.w = 1.0f;
     return un;
 }
