@@ -452,6 +452,7 @@ def batch_record(npairs: int, iters: int) -> dict:
                         "knobs": {"grid_mult": info["grid_mult"], "pd_rows": info["pd_rows"],
                                   "pd_halo": info["pd_halo"]},
                         "tuning_ms": info["tune_ms"], "tuning": info["candidates"],
+                        "mode_proxy_ms": info["mode_ms"],
                         "shared_windows": info["shared_windows"]},
             "speedup": t_plain / t_bat, "bit_identical_to_plain": same,
             "timing": "CUDA events on the launching stream, one run each (inputs in HBM)",

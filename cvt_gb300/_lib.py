@@ -72,7 +72,7 @@ class CvtpmBatchInfo(ctypes.Structure):
                 ("pd_rows", ctypes.c_int), ("pd_halo", ctypes.c_int),
                 ("cand_grid_mult", ctypes.c_int * BATCH_MAX_CAND), ("cand_pd_rows", ctypes.c_int * BATCH_MAX_CAND),
                 ("cand_pd_halo", ctypes.c_int * BATCH_MAX_CAND), ("launches", ctypes.c_longlong),
-                ("tune_ms", ctypes.c_float)]
+                ("tune_ms", ctypes.c_float), ("mode_ms", ctypes.c_float * 2)]
 
     def as_dict(self) -> dict:
         n = self.ncand
@@ -85,7 +85,8 @@ class CvtpmBatchInfo(ctypes.Structure):
         return {"lanes": self.lanes, "shared_windows": self.shared_windows, "tuned": self.tuned,
                 "candidates": cands, "graph_nodes": self.graph_nodes, "replays": self.replays,
                 "phased": self.phased, "grid_mult": self.grid_mult, "pd_rows": self.pd_rows,
-                "pd_halo": self.pd_halo, "launches": self.launches, "tune_ms": self.tune_ms}
+                "pd_halo": self.pd_halo, "launches": self.launches, "tune_ms": self.tune_ms,
+                "mode_ms": {"phase_batched": self.mode_ms[0], "one_lane": self.mode_ms[1]}}
 
 
 class CvtpmStats(ctypes.Structure):

@@ -73,7 +73,8 @@ struct cvtpm_ctx {
     /* phase-batched mode: one scratch context per pair of the batch, the
      * tuned launch knobs per batch shape and the knobs of the current graph */
     std::vector<cvtpm_ctx*> bpairs;
-    std::vector<std::pair<std::vector<unsigned char>, PmBatchKnobs>> tuned_knobs;
+    struct TunedBatch { std::vector<unsigned char> key; PmBatchKnobs kn; bool phased; float mode_ms[2]; };
+    std::vector<TunedBatch> tuned_knobs;
     PmBatchKnobs knobs{1, 16, 4};     /* pinned by cvtpm_set_batch_knobs */
     bool pinned_knobs = false;
     cudaStream_t bstream = nullptr;
@@ -1611,9 +1612,76 @@ cvtpm_status capture_phased(PhaseState& S, cudaGraphExec_t* exec, size_t* nodes)
     return CVTPM_OK;
 }
 
+/* The batch mode: the phase-batched schedule (knobs S.kn) against one lane
+ * of per-pair launch sequences (run_depthmap, whose smoothers overlap on its
+ * side stream), each timed once on the tuner's subset (the first pairs, up
+ * to 4 Mpx) for one iteration, after the lane's scratch is sized for the
+ * subset.  ms[0]: phase-batched, ms[1]: one lane. */
+cvtpm_status tune_mode(PhaseState& full, float ms[2]) {
+    PhaseState S = full;
+    long long px = 0;
+    int maxW = 1, maxH = 1;
+    S.n = 0;
+    while (S.n < full.n && (S.n == 0 || px < 4000000)) {
+        px += (long long)full.pairs[S.n].width * full.pairs[S.n].height;
+        maxW = std::max(maxW, full.pairs[S.n].width);
+        maxH = std::max(maxH, full.pairs[S.n].height);
+        ++S.n;
+    }
+    cvtpm_ctx* ctx = S.ctx;
+    cvtpm_ctx* lane = ctx->lanes[0].c;
+    cvtpm_status s = cvtpm_set_memory_budget(lane, ctx->nb_budget);
+    if (s == CVTPM_OK) s = ensure_buffers(lane, maxW, maxH);
+    if (s == CVTPM_OK) s = ensure_nbcost(lane, maxW, maxH);
+    if (s != CVTPM_OK) return fail(ctx, s, lane->err);
+    EventPair ev;
+    CK(cudaEventCreate(&ev.a), "tune event");
+    CK(cudaEventCreate(&ev.b), "tune event");
+    for (int mode = 0; mode < 2; ++mode) {
+        if (cudaEventRecord(ev.a, S.st) != cudaSuccess) return cuda_fail(ctx, cudaGetLastError(), "tune record");
+        if (mode == 0) {
+            if ((s = phase_schedule(S, 1)) != CVTPM_OK) return s;
+        } else {
+            for (int i = 0; i < S.n; ++i) {
+                const cvtpm_pair& q = S.pairs[i];
+                cvtpm_params pq = S.p;
+                pq.iterations = 1;
+                pq.depthmax = q.depthmax;
+                lane->prm = pq;
+                lane->timing = false;
+                if ((s = run_depthmap(lane, pq, q.dmap, q.dmap_pitch, q.left, q.right, q.width, q.height, q.pitch,
+                                      nullptr, 0, nullptr, S.st)) != CVTPM_OK)
+                    return fail(ctx, s, lane->err);
+            }
+        }
+        float t = 0.0f;
+        if (cudaEventRecord(ev.b, S.st) != cudaSuccess || cudaEventSynchronize(ev.b) != cudaSuccess ||
+            cudaEventElapsedTime(&t, ev.a, ev.b) != cudaSuccess)
+            return cuda_fail(ctx, cudaGetLastError(), "tune timing");
+        ms[mode] = t;
+    }
+    return CVTPM_OK;
+}
+
 }  // namespace
 
 extern "C" {
+
+/* The graph of k lanes of per-pair launch sequences, captured and launched. */
+static cvtpm_status batch_lanes(cvtpm_ctx* ctx, const cvtpm_pair* pairs, int npairs, int k,
+                                const std::vector<unsigned char>& key, cudaStream_t st) {
+    cvtpm_status s;
+    ctx->binfo.phased = 0;
+    size_t nodes = 0;
+    if ((s = capture_batch(ctx, pairs, npairs, k, ctx->prm.iterations, &ctx->bexec, &nodes)) != CVTPM_OK) return s;
+    ctx->bkey = key;
+    ctx->binfo.lanes = k;
+    ctx->binfo.shared_windows = ctx->prm.arith == CVTPM_ARITH_FAST && ctx->nb_budget > 0 ? 1 : 0;
+    ctx->binfo.graph_nodes = (long long)nodes;
+    ctx->binfo.replays = 0;
+    ctx->binfo.launches = 0;
+    return launch_batch(ctx, ctx->bexec, st);
+}
 
 static cvtpm_status depthmap_batched(cvtpm_ctx* ctx, const cvtpm_pair* pairs, int npairs, void* stream) {
     if (!ctx) return CVTPM_ERR_INVALID_ARGUMENT;
@@ -1661,19 +1729,31 @@ static cvtpm_status depthmap_batched(cvtpm_ctx* ctx, const cvtpm_pair* pairs, in
         if ((s = phase_prepare(S)) != CVTPM_OK) return s;
         CK(cudaStreamSynchronize(ctx->bstream), "batch prepare");
         ctx->binfo.tuned = 0;
-        bool cached = false;
-        if (ctx->pinned_knobs) { S.kn = ctx->knobs; cached = true; }
+        bool cached = false, phased = true;
+        if (ctx->pinned_knobs) { S.kn = ctx->knobs; cached = true; ctx->binfo.mode_ms[0] = ctx->binfo.mode_ms[1] = 0.0f; }
         for (auto& tk : ctx->tuned_knobs)
-            if (!cached && tk.first == tkey) { S.kn = tk.second; cached = true; }
+            if (!cached && tk.key == tkey) {
+                S.kn = tk.kn;
+                phased = tk.phased;
+                ctx->binfo.mode_ms[0] = tk.mode_ms[0];
+                ctx->binfo.mode_ms[1] = tk.mode_ms[1];
+                cached = true;
+            }
         if (!cached) {
             const auto c0 = std::chrono::steady_clock::now();
             PmBatchKnobs best{1, 16, 4};
             if ((s = tune_phased(S, &best)) != CVTPM_OK) return s;
-            ctx->binfo.tune_ms = std::chrono::duration<float, std::milli>(std::chrono::steady_clock::now() - c0).count();
-            ctx->tuned_knobs.push_back({tkey, best});
             S.kn = best;
+            float ms[2] = {0.0f, 0.0f};
+            if ((s = tune_mode(S, ms)) != CVTPM_OK) return s;
+            phased = ms[0] <= ms[1];
+            ctx->binfo.tune_ms = std::chrono::duration<float, std::milli>(std::chrono::steady_clock::now() - c0).count();
+            ctx->tuned_knobs.push_back({tkey, best, phased, {ms[0], ms[1]}});
+            ctx->binfo.mode_ms[0] = ms[0];
+            ctx->binfo.mode_ms[1] = ms[1];
             ctx->binfo.tuned = 1;
         }
+        if (!phased) return batch_lanes(ctx, pairs, npairs, 1, key, st);
         size_t nodes = 0;
         if ((s = capture_phased(S, &ctx->bexec, &nodes)) != CVTPM_OK) return s;
         ctx->bkey = key;
@@ -1690,9 +1770,9 @@ static cvtpm_status depthmap_batched(cvtpm_ctx* ctx, const cvtpm_pair* pairs, in
         ctx->binfo.replays = 0;
         return launch_batch(ctx, ctx->bexec, st);
     }
-    ctx->binfo.phased = 0;
     int k = ctx->batch_lanes > 0 ? ctx->batch_lanes : 0;
     ctx->binfo.tuned = 0;
+    ctx->binfo.mode_ms[0] = ctx->binfo.mode_ms[1] = 0.0f;
     if (k <= 0) {
         if (!ctx->tkey.empty() && tkey == ctx->tkey) {   /* same shapes: keep the tuned choice */
             k = ctx->tuned_lanes;
@@ -1703,15 +1783,7 @@ static cvtpm_status depthmap_batched(cvtpm_ctx* ctx, const cvtpm_pair* pairs, in
         }
         ctx->binfo.tuned = 1;
     }
-    size_t nodes = 0;
-    if ((s = capture_batch(ctx, pairs, npairs, k, ctx->prm.iterations, &ctx->bexec, &nodes)) != CVTPM_OK) return s;
-    ctx->bkey = key;
-    ctx->binfo.lanes = k;
-    ctx->binfo.shared_windows = ctx->prm.arith == CVTPM_ARITH_FAST && ctx->nb_budget > 0 ? 1 : 0;
-    ctx->binfo.graph_nodes = (long long)nodes;
-    ctx->binfo.replays = 0;
-    ctx->binfo.launches = 0;
-    return launch_batch(ctx, ctx->bexec, st);
+    return batch_lanes(ctx, pairs, npairs, k, key, st);
 }
 
 /* the lane plans are sized by npairs: a failed host allocation becomes a

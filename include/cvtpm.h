@@ -350,10 +350,14 @@ typedef struct cvtpm_batch_info {
     int cand_pd_halo[CVTPM_BATCH_MAX_CAND];
     long long launches;        /* kernel launches in the phase-batched graph */
     float tune_ms;             /* host time the last tuning took */
+    float mode_ms[2];          /* the mode proxies of the last tuning (ms; 0: not run): the tuning subset for one
+                                  iteration, [0] phase-batched with the chosen knobs, [1] one lane */
 } cvtpm_batch_info;
 
-/* The lane count of cvtpm_depthmap_batched: 0 (default) for the
- * phase-batched launches, k >= 1 for k lanes of per-pair launch sequences. */
+/* The lane count of cvtpm_depthmap_batched: 0 (default) lets the autotuner
+ * choose between the phase-batched launches and one lane of per-pair launch
+ * sequences (the faster of the two on its proxy, mode_ms); k >= 1 fixes k
+ * lanes of per-pair launch sequences. */
 cvtpm_status cvtpm_set_batch_lanes(cvtpm_ctx* ctx, int lanes);
 /* Pin the phase-batched launch knobs instead of tuning them: grid_mult 0
  * (a block per work item), 1 or 2 (persistent grid of that many times the

@@ -53,15 +53,42 @@ def test_batched_matches_plain_per_pair(cuda, preset):
             assert not bit_diff(g.cpu().numpy(), w).any(), f"pair {i}, call {attempt}"
     info = bat.batch_info()
     assert info["tuned"] == 1 and info["replays"] == 1
-    assert info["phased"] == 1 and info["lanes"] == 0
+    # the tuner timed both modes and kept the faster
+    modes = info["mode_ms"]
+    assert modes["phase_batched"] > 0 and modes["one_lane"] > 0
+    phased = modes["phase_batched"] <= modes["one_lane"]
+    assert (info["phased"], info["lanes"]) == ((1, 0) if phased else (0, 1))
     assert info["grid_mult"] in (0, 1, 2) and info["pd_rows"] in (8, 16) and info["pd_halo"] in (2, 4)
     assert len(info["candidates"]) == 11 and all(c["proxy_ms"] > 0 for c in info["candidates"])
     assert info["shared_windows"] == 1
-    # one launch per phase for all pairs: about one plain call's launches, not one call's per pair
-    plain.reset_stats()
-    plain.depthMap(torch.empty(0, device="cuda"), pairs[0][0], pairs[0][1], p.patchsize, pairs[0][2], p.iterations, 4)
+    if phased:
+        # one launch per phase for all pairs: about one plain call's launches, not one call's per pair
+        plain.reset_stats()
+        plain.depthMap(torch.empty(0, device="cuda"), pairs[0][0], pairs[0][1], p.patchsize, pairs[0][2], p.iterations, 4)
+        torch.cuda.synchronize()
+        assert 0 < info["launches"] <= 2 * plain.stats()["launches"] < len(pairs) * plain.stats()["launches"]
+
+
+def test_phased_tuned_knobs_match_plain(cuda):
+    """The phase-batched graph with the knobs the tuner chose, pinned on a
+    second context so that the phase-batched mode runs whichever mode the
+    tuner's proxy preferred."""
+    from cvt_gb300.stereo import PMHuberStereo
+    p = default_params(PRESET_BASELINE, patchsize=5, iterations=2, pd_iterations=6)
+    pairs = _pairs(SIZES[:4], seed0=600)
+    want = _plain(PMHuberStereo(0, p), pairs, p)
+    bat = PMHuberStereo(0, p)
+    got = bat.depthMapBatched(pairs)
+    info = bat.batch_info()
+    kn = (info["grid_mult"], info["pd_rows"], info["pd_halo"])
+    bat2 = PMHuberStereo(0, p)
+    bat2.set_batch_knobs(*kn)
+    got2 = bat2.depthMapBatched(pairs)
     torch.cuda.synchronize()
-    assert 0 < info["launches"] <= 2 * plain.stats()["launches"] < len(pairs) * plain.stats()["launches"]
+    assert bat2.batch_info()["phased"] == 1
+    for i, (g, g2, w) in enumerate(zip(got, got2, want)):
+        assert not bit_diff(g.cpu().numpy(), w).any(), f"pair {i}"
+        assert not bit_diff(g2.cpu().numpy(), w).any(), f"pair {i} (phase-batched, tuned knobs)"
 
 
 @pytest.mark.parametrize("knobs", [(0, 16, 4), (1, 8, 2), (2, 8, 4), (1, 16, 2)])
@@ -116,7 +143,12 @@ def test_batched_fixed_lanes_and_changed_batch(cuda):
         bat.set_batch_lanes(lanes)
         got = bat.depthMapBatched(pairs2)
         torch.cuda.synchronize()
-        assert bat.batch_info()["phased"] == (1 if lanes == 0 else 0)
+        info = bat.batch_info()
+        if lanes:
+            assert info["phased"] == 0 and info["lanes"] == lanes
+        else:                                       # the tuner's faster mode
+            m = info["mode_ms"]
+            assert info["phased"] == (1 if m["phase_batched"] <= m["one_lane"] else 0)
         for g, w in zip(got, want[::-1]):
             assert not bit_diff(g.cpu().numpy(), w).any()
 
