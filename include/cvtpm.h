@@ -144,7 +144,14 @@ cvtpm_status cvtpm_synchronize(cvtpm_ctx* ctx, void* stream);
 /* PMHuberStereo::depthMap (PMHuberStereo.h:40, PMHuberStereo.cpp:64-291).
  * patchsize, depthmax, iterations, viewsamples and dscale override the
  * context's parameters for this call, as the reference's arguments do.
- * normalmap may be NULL (reference default).  trace may be NULL. */
+ * normalmap may be NULL (reference default).  trace may be NULL.
+ * Stream order: the call's work is ordered after earlier work on `stream`
+ * and everything it writes is complete, in `stream`'s order, when later
+ * work on `stream` runs.  Inside, the right view's smoother runs on a
+ * second stream of the context, forked from `stream` by an event and joined
+ * back before the call's last launch, so the call also works under stream
+ * capture.  Calls on one context from different streams must be ordered by
+ * the caller. */
 cvtpm_status cvtpm_depthmap(cvtpm_ctx* ctx,
                             float* dmap, size_t dmap_pitch,
                             const float* left, const float* right,
