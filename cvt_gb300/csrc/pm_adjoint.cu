@@ -111,7 +111,7 @@ __global__ void __launch_bounds__(256) k_cost_adjoint(PmAdjArgs a) {
             const float4 a1 = __ldg(&a.v1.col[q]);
             const float4 g1 = __ldg(&a.v1.grad[q]);
             const float d = (fabsf(vc.x - a1.x) + fabsf(vc.y - a1.y)) + fabsf(vc.z - a1.z);
-            const float w1 = pm_exp(-d * prow[dx]);
+            const float w1 = pm_wexp(-d * prow[dx]);
             TapVals t;
             load_tap(a.v2, (size_t)qy * a.k.rp + xi, pm_fix_frac(Xt), t);
             const float cc = (fminf(fabsf(a1.x - t.v[0]), a.k.cmax) + fminf(fabsf(a1.y - t.v[1]), a.k.cmax)) +
@@ -152,7 +152,7 @@ __global__ void __launch_bounds__(256) k_cost_adjoint(PmAdjArgs a) {
                 const float4 g1 = __ldg(&a.v1.grad[q]);
                 const float dcx = vc.x - a1.x, dcy = vc.y - a1.y, dcz = vc.z - a1.z;
                 const float prof = prow[dx];
-                const float w1 = pm_exp(-((fabsf(dcx) + fabsf(dcy)) + fabsf(dcz)) * prof);
+                const float w1 = pm_wexp(-((fabsf(dcx) + fabsf(dcy)) + fabsf(dcz)) * prof);
                 const float af = pm_fix_frac(Xt);
                 TapVals t;
                 load_tap(a.v2, (size_t)qy * a.k.rp + xi, af, t);

@@ -298,7 +298,7 @@ PM_DEV void fast_tap_terms(const PmCostConsts& k, const PmRecRow& row, int xi, f
  * value prof): the FAST and EXACT paths and k_nbcost share it. */
 PM_DEV float tap_weight(float4 vc, float4 a1, float prof) {
     const float d = (fabsf(vc.x - a1.x) + fabsf(vc.y - a1.y)) + fabsf(vc.z - a1.z);
-    return pm_exp(-d * prof);
+    return pm_wexp(-d * prof);
 }
 
 #ifdef PM_KERNELS_TU

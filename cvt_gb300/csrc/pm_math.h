@@ -13,6 +13,11 @@
  *              then the degree-7 Taylor polynomial of e^r (|r| <= ln2/2,
  *              truncation error < 2.6e-9), scaled by 2^k in two exact steps so
  *              that subnormal results are rounded once.
+ *   pm_wexp    the ASW weight's exponential (native_exp, :199), evaluated once
+ *              per tap and pixel: the same reduction and polynomial on x
+ *              clamped to [-87.3, 88.7], scaled by adding k to the exponent
+ *              bits (the clamp keeps the result normal).  So the weight has a
+ *              floor of e^-87.3 (1.2e-38) and a NaN argument gives the floor.
  *   pm_log     x = m 2^e with m in [sqrt(1/2), sqrt(2)); log m = 2 atanh(s),
  *              s = (m-1)/(m+1), by its odd power series to s^13.
  *   pm_pow     exp(y log x) for x >= 0.
@@ -170,6 +175,28 @@ PM_HD float pm_exp(float x) {
     int kb = k - ka;
     float res = (p * pm_pow2i(ka)) * pm_pow2i(kb);
     return (x != x) ? x : res;
+}
+
+PM_HD float pm_wexp(float x) {
+    const float L2E = 1.44269504088896341f;
+    const float LN2_HI = 0.693145751953125f;      /* 16 significant bits */
+    const float LN2_LO = 1.4286068202862268e-06f; /* ln2 - LN2_HI */
+    const float SHIFT = 12582912.0f;              /* 1.5 * 2^23 */
+    const float xc = fminf(fmaxf(x, -87.3f), 88.7f);
+    const float big = fmaf(xc, L2E, SHIFT);       /* SHIFT + k, k = round(xc / ln2) */
+    const float kf = big - SHIFT;
+    float r = fmaf(-kf, LN2_HI, xc);
+    r = fmaf(-kf, LN2_LO, r);
+    float p = 1.98412698e-04f;                    /* 1/7! */
+    p = fmaf(p, r, 1.38888889e-03f);              /* 1/6! */
+    p = fmaf(p, r, 8.33333333e-03f);              /* 1/5! */
+    p = fmaf(p, r, 4.16666667e-02f);              /* 1/4! */
+    p = fmaf(p, r, 1.66666667e-01f);              /* 1/3! */
+    p = fmaf(p, r, 0.5f);
+    p = fmaf(p, r, 1.0f);
+    p = fmaf(p, r, 1.0f);
+    /* k in [-126, 128] and p in [0.70, 1.42]: 2^k p stays normal */
+    return pm_i2f(pm_f2i(p) + ((pm_f2i(big) - 0x4B400000) << 23));
 }
 
 PM_HD float pm_log(float x) {

@@ -34,12 +34,13 @@ def lib():
         L.orc_max_threads.restype = c_int
         L.orc_gradxy.argtypes = [f32p, c_int, c_int, f32p]
         L.orc_edge_weight.argtypes = [f32p, c_int, c_int, f32p]
-        for n in ("orc_exp", "orc_acospi"):
+        for n in ("orc_exp", "orc_wexp", "orc_acospi"):
             getattr(L, n).argtypes = [c_float]
             getattr(L, n).restype = c_float
         L.orc_pow.argtypes = [c_float, c_float]
         L.orc_pow.restype = c_float
         L.orc_exp_array.argtypes = [f32p, f32p, ctypes.c_long]
+        L.orc_wexp_array.argtypes = [f32p, f32p, ctypes.c_long]
         L.orc_acospi_array.argtypes = [f32p, f32p, ctypes.c_long]
         L.orc_pow_array.argtypes = [f32p, c_float, f32p, ctypes.c_long]
         L.orc_mwc_mulmod_serial.argtypes = [ctypes.c_uint64, ctypes.c_uint64]

@@ -294,7 +294,7 @@ static float cost_eval(const CostCfg& k, const View& v1, const View& v2, int cx,
                 const F4 a1 = v1.col[(size_t)(int)py * W + (int)px];
                 const F4 g1 = v1.grad[(size_t)(int)py * W + (int)px];
                 float d = (fabsf(vc.x - a1.x) + fabsf(vc.y - a1.y)) + fabsf(vc.z - a1.z);
-                float w1 = pm_exp(-d * k.prof[(size_t)(dy + P) * n + (dx + P)]);
+                float w1 = pm_wexp(-d * k.prof[(size_t)(dy + P) * n + (dx + P)]);
                 float xp = s.x * px + s.y * py + s.z;
                 if (!(xp >= 0.0f && xp < Wf)) continue;
                 wsum += w1;
@@ -337,7 +337,7 @@ static float cost_eval(const CostCfg& k, const View& v1, const View& v2, int cx,
             const F4 a1 = v1.col[(size_t)qy * W + qx];
             const F4 g1 = v1.grad[(size_t)qy * W + qx];
             float d = (fabsf(vc.x - a1.x) + fabsf(vc.y - a1.y)) + fabsf(vc.z - a1.z);
-            float w1 = pm_exp(-d * k.prof[(size_t)(dy + P) * n + (dx + P)]);
+            float w1 = pm_wexp(-d * k.prof[(size_t)(dy + P) * n + (dx + P)]);
             const long long X = XC + (long long)(qy - H / 2) * S1 + (long long)(qx - W / 2) * S0;
             const int xi = (int)(X >> 32);
             if ((unsigned)xi >= (unsigned)W) continue;
@@ -1031,9 +1031,11 @@ void orc_gradxy(const float* img, int W, int H, float* out) { gradxy((const F4*)
 void orc_edge_weight(const float* img, int W, int H, float* out) { edge_weight((const F4*)img, W, H, out); }
 
 float orc_exp(float x) { return pm_exp(x); }
+float orc_wexp(float x) { return pm_wexp(x); }
 float orc_pow(float x, float y) { return pm_pow(x, y); }
 float orc_acospi(float x) { return pm_acospi(x); }
 void orc_exp_array(const float* x, float* y, long n) { for (long i = 0; i < n; ++i) y[i] = pm_exp(x[i]); }
+void orc_wexp_array(const float* x, float* y, long n) { for (long i = 0; i < n; ++i) y[i] = pm_wexp(x[i]); }
 void orc_pow_array(const float* x, float e, float* y, long n) { for (long i = 0; i < n; ++i) y[i] = pm_pow(x[i], e); }
 void orc_acospi_array(const float* x, float* y, long n) { for (long i = 0; i < n; ++i) y[i] = pm_acospi(x[i]); }
 

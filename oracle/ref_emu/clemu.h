@@ -6,7 +6,7 @@
  * fixtures that pin the oracle.
  *
  * What it fixes where OpenCL leaves a choice:
- *  - native_exp/exp -> pm_exp, pow -> pm_pow, acospi -> pm_acospi
+ *  - native_exp -> pm_wexp, exp -> pm_exp, pow -> pm_pow, acospi -> pm_acospi
  *    (cvt_gb300/csrc/pm_math.h); native_sqrt/sqrt -> IEEE sqrt,
  *    native_rsqrt -> 1/sqrt; dot/length/smoothstep evaluated left to right
  *    without contraction (the build uses -ffp-contract=off);
@@ -226,7 +226,7 @@ inline float sqrt(float v) { return std::sqrt(v); }
 inline float4 sqrt(const float4& v) { return float4(std::sqrt(v.x), std::sqrt(v.y), std::sqrt(v.z), std::sqrt(v.w)); }
 inline float native_sqrt(float v) { return std::sqrt(v); }
 inline float native_rsqrt(float v) { return 1.0f / std::sqrt(v); }
-inline float native_exp(float v) { return pm_exp(v); }
+inline float native_exp(float v) { return pm_wexp(v); }
 inline float exp(float v) { return pm_exp(v); }
 inline float pow(float a, float b) { return pm_pow(a, b); }
 inline float acospi(float v) { return pm_acospi(v); }

@@ -49,3 +49,24 @@ def test_pow_and_acospi(oracle):
     want = np.arccos(c.astype(np.float64)) / np.pi
     assert np.abs(a - want).max() < 3e-7
     assert np.isnan(oracle.lib().orc_acospi(1.0000001))
+
+
+def test_weight_exp(oracle):
+    """pm_wexp, the ASW weight's exponential (the reference's native_exp,
+    pmhstereo.cl:199): within 2 ulp of exp on its range, a floor of
+    e^-87.3 below it (and for NaN), and the same floats as pm_exp wherever
+    both round k the same way."""
+    rng = np.random.default_rng(3)
+    x = np.concatenate([rng.uniform(-87.3, 88.7, 300000), rng.uniform(-30, 0, 300000),
+                        np.array([0.0, -0.0, -1.0, 1.0, -87.3, 88.7])]).astype(np.float32)
+    y = np.empty_like(x)
+    oracle.lib().orc_wexp_array(x, y, x.size)
+    assert ulp_err(y, np.exp(x.astype(np.float64))).max() <= 2.0
+    assert oracle.lib().orc_wexp(0.0) == 1.0
+    e = np.empty_like(x)
+    oracle.lib().orc_exp_array(x, e, x.size)
+    assert (y != e).mean() < 1e-3
+    f = oracle.lib().orc_wexp
+    floor = f(-87.3)
+    assert 1.17e-38 < floor < 1.3e-38
+    assert f(-100.0) == floor and f(-1e30) == floor and f(float("nan")) == floor
