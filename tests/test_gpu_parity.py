@@ -140,6 +140,35 @@ def test_depthmap_odd_sizes(stereo, oracle, W, H, P):
     assert_bitexact(dm, want, "dmap")
 
 
+@pytest.mark.parametrize("W,H,P", [(2100, 19, 7), (21, 900, 5)], ids=["wide", "tall"])
+def test_depthmap_wide_and_tall(stereo, oracle, W, H, P):
+    """Strip-shaped pairs: one row of smoother tiles and a single column of
+    propagation blocks, with both views' smoothers on their two streams."""
+    sc = scenes.make_scene(W, H, 2, 9.0, seed=W + 7 * H)
+    p = default_params(PRESET_BASELINE, patchsize=P, depthmax=9.0, iterations=2, pd_iterations=6)
+    dm, nm, tr, want, ex = run_both(stereo, oracle, sc, p)
+    assert_bitexact(tr["winners"], ex["winners"], "winners")
+    assert_bitexact(tr["states"], ex["states"], "states")
+    assert_bitexact(dm, want, "dmap")
+    assert_bitexact(nm, ex["normalmap"], "normalmap")
+
+
+def test_pd_tool_time(stereo):
+    """cvtpm_tool_pd_time: refused before a depthMap has sized the context,
+    a positive time per step afterwards."""
+    from cvt_gb300 import _lib
+    import ctypes
+    from cvt_gb300.stereo import PMHuberStereo
+    fresh = PMHuberStereo(0, default_params(PRESET_BASELINE))
+    us = ctypes.c_float(0.0)
+    assert _lib.lib().cvtpm_tool_pd_time(fresh._h, 8, None, ctypes.byref(us)) != 0
+    sc = scenes.make_scene(64, 40, 2, 8.0, seed=5)
+    fresh.depthMap(None, to_dev(sc.left), to_dev(sc.right), 5, 8.0, 1, 4)
+    assert _lib.lib().cvtpm_tool_pd_time(fresh._h, 7, None, ctypes.byref(us)) != 0      # odd step count
+    assert _lib.lib().cvtpm_tool_pd_time(fresh._h, 8, None, ctypes.byref(us)) == 0
+    assert us.value > 0.0
+
+
 def test_pitched_input_and_host_entry(stereo, oracle):
     sc = scenes.make_scene(50, 30, 3, 10.0, seed=4)
     p = default_params(PRESET_BASELINE, patchsize=5, depthmax=10.0, iterations=2, pd_iterations=4)
