@@ -363,8 +363,8 @@ typedef struct cvtpm_batch_info {
 
 /* The lane count of cvtpm_depthmap_batched: 0 (default) lets the autotuner
  * choose between the phase-batched launches and one lane of per-pair launch
- * sequences (the faster of the two on its proxy, mode_ms); k >= 1 fixes k
- * lanes of per-pair launch sequences. */
+ * sequences (mode_ms: the phase-batched schedule is taken when its proxy is
+ * at least 3 % faster); k >= 1 fixes k lanes of per-pair launch sequences. */
 cvtpm_status cvtpm_set_batch_lanes(cvtpm_ctx* ctx, int lanes);
 /* Pin the phase-batched launch knobs instead of tuning them: grid_mult 0
  * (a block per work item), 1 or 2 (persistent grid of that many times the

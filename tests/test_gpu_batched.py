@@ -56,7 +56,7 @@ def test_batched_matches_plain_per_pair(cuda, preset):
     # the tuner timed both modes and kept the faster
     modes = info["mode_ms"]
     assert modes["phase_batched"] > 0 and modes["one_lane"] > 0
-    phased = modes["phase_batched"] <= modes["one_lane"]
+    phased = bool(np.float32(modes["phase_batched"]) < np.float32(0.97) * np.float32(modes["one_lane"]))
     assert (info["phased"], info["lanes"]) == ((1, 0) if phased else (0, 1))
     assert info["grid_mult"] in (0, 1, 2) and info["pd_rows"] in (8, 16) and info["pd_halo"] in (2, 4)
     assert len(info["candidates"]) == 11 and all(c["proxy_ms"] > 0 for c in info["candidates"])
@@ -148,7 +148,8 @@ def test_batched_fixed_lanes_and_changed_batch(cuda):
             assert info["phased"] == 0 and info["lanes"] == lanes
         else:                                       # the tuner's faster mode
             m = info["mode_ms"]
-            assert info["phased"] == (1 if m["phase_batched"] <= m["one_lane"] else 0)
+            faster = np.float32(m["phase_batched"]) < np.float32(0.97) * np.float32(m["one_lane"])
+            assert info["phased"] == (1 if faster else 0)
         for g, w in zip(got, want[::-1]):
             assert not bit_diff(g.cpu().numpy(), w).any()
 
