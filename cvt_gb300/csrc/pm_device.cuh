@@ -246,6 +246,12 @@ PM_DEV float2 fsub2(float2 a, float2 b) {
     asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(pk2(a)), "l"(pk2(b)));
     return upk2(d);
 }
+PM_DEV float2 fmul2(float2 a, float2 b) {
+    unsigned long long d;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(pk2(a)), "l"(pk2(b)));
+    return upk2(d);
+}
+PM_DEV float2 f2s(float v) { return make_float2(v, v); }
 
 /* The matching terms of one tap in the FAST arithmetic: colour and gradient
  * truncated-L1 distances between image 1 at the tap (a1, g1) and the other
@@ -301,12 +307,57 @@ PM_DEV float tap_weight(float4 vc, float4 a1, float prof) {
     return pm_wexp(-d * prof);
 }
 
+/* tap_weight of two taps (colours a, b; profile values pa, pb) on packed
+ * pairs: each half of every packed operation is the scalar operation
+ * tap_weight and pm_wexp perform on that tap, so wa and wb are their floats.
+ * -d * prof is formed as -(d * prof) (the same float: RN is symmetric), and
+ * fmaf(-kf, c, r) as a fused kf * (-c) + r (the same exact product). */
+PM_DEV void tap_weight2(float4 vc, float4 a, float4 b, float pa, float pb, float& wa, float& wb) {
+    const float2 ex = fsub2(f2s(vc.x), make_float2(a.x, b.x));
+    const float2 ey = fsub2(f2s(vc.y), make_float2(a.y, b.y));
+    const float2 ez = fsub2(f2s(vc.z), make_float2(a.z, b.z));
+    const float da = (fabsf(ex.x) + fabsf(ey.x)) + fabsf(ez.x);
+    const float db = (fabsf(ex.y) + fabsf(ey.y)) + fabsf(ez.y);
+    const float2 y = fmul2(make_float2(da, db), make_float2(pa, pb));
+    const float2 xc = make_float2(fminf(fmaxf(-y.x, -87.3f), 88.7f), fminf(fmaxf(-y.y, -87.3f), 88.7f));
+    const float2 big = ffma2(xc, f2s(1.44269504088896341f), f2s(12582912.0f));
+    const float2 kf = fsub2(big, f2s(12582912.0f));
+    float2 r = ffma2(kf, f2s(-0.693145751953125f), xc);
+    r = ffma2(kf, f2s(-1.4286068202862268e-06f), r);
+    float2 p = f2s(1.98412698e-04f);
+    p = ffma2(p, r, f2s(1.38888889e-03f));
+    p = ffma2(p, r, f2s(8.33333333e-03f));
+    p = ffma2(p, r, f2s(4.16666667e-02f));
+    p = ffma2(p, r, f2s(1.66666667e-01f));
+    p = ffma2(p, r, f2s(0.5f));
+    p = ffma2(p, r, f2s(1.0f));
+    p = ffma2(p, r, f2s(1.0f));
+    wa = __int_as_float(__float_as_int(p.x) + ((__float_as_int(big.x) - 0x4B400000) << 23));
+    wb = __int_as_float(__float_as_int(p.y) + ((__float_as_int(big.y) - 0x4B400000) << 23));
+}
+
 #ifdef PM_KERNELS_TU
 /* Aggregated ASW cost (patch_eval_color_grad_weighted, pmhstereo.cl:170-228)
  * of K candidate planes at pixel (x, y), sharing the image-1 reads and the
  * bilateral weight of every tap.  Each candidate's sum is accumulated in the
  * reference's tap order, so its value equals a separate evaluation.
  * Candidates with act[k] == false contribute nothing and return 1e5. */
+/* FAST sweeps of at most PM_PAIR_TAPS_MAXK candidates form their weights two
+ * taps at a time (tap_weight2).  Measured per depthMap of the 1242x375 bench
+ * pair, same bits: 517.6 -> 509.8 ms with every FAST sweep of 1-4 (the
+ * neighbour kernel's weight phase alone: 513.6; sweeps of 3-4 or 2-4 only:
+ * within 0.5 ms of 1-4).  The EXACT sweeps keep one tap per step: paired,
+ * its stage-1 sweeps of 4 took 148 registers and one block per SM (596 ->
+ * 681 ms). */
+#ifndef PM_PAIR_TAPS_MAXK
+#define PM_PAIR_TAPS_MAXK 4
+#endif
+#ifndef PM_PAIR_TAPS_MINK
+#define PM_PAIR_TAPS_MINK 1
+#endif
+#ifndef PM_PAIR_TAPS_EXACT
+#define PM_PAIR_TAPS_EXACT 0
+#endif
 template <int K, bool EXACT>
 PM_DEV void eval_costs(const PmCostConsts& k, const PmView& v1, const PmView& v2, int x, int y,
                        const float4 (&s)[K], const bool (&act)[K], float (&cost)[K]) {
@@ -347,17 +398,12 @@ PM_DEV void eval_costs(const PmCostConsts& k, const PmView& v1, const PmView& v2
         const float4* g1row = v1.grad + (size_t)qy * k.W;
         const float* prow = c_prof + (dy + PM_PMAX) * PM_PROF_N + PM_PMAX;
         const PmRecRow rrow = rec_row(v2, k.rp, qy);
-        for (int dx = dxlo; dx <= dxhi; ++dx) {
-            const int qx = x + dx;
-            const float qxf = (float)qx;
-            const float4 a1 = __ldg(&c1row[qx]);
-            const float4 g1 = __ldg(&g1row[qx]);
-            const float w1 = tap_weight(vc, a1, prow[dx]);
-#pragma unroll
-            for (int c = 0; c < K; ++c) {
+        /* candidate c's terms at tap column qx, folded into its sums */
+        auto one = [&](int c, int qx, float4 a1, float4 g1, float w1) {
                 if (EXACT) {
+                    const float qxf = (float)qx;
                     const float xp = sx[c] * qxf + sy[c] * qyf + sz[c];
-                    if (!(xp >= 0.0f && xp < k.Wf)) continue;
+                    if (!(xp >= 0.0f && xp < k.Wf)) return;
                     ws[c] += w1;
                     const float u = xp + 0.5f;
                     const float t = u - 0.5f;
@@ -380,7 +426,7 @@ PM_DEV void eval_costs(const PmCostConsts& k, const PmView& v1, const PmView& v2
                     const long long Xt = X[c];
                     X[c] += S0[c];
                     const int xi = (int)(Xt >> 32);
-                    if ((unsigned)xi >= (unsigned)k.W) continue;
+                    if ((unsigned)xi >= (unsigned)k.W) return;
                     float cc, gc;
                     fast_tap_terms(k, rrow, xi, pm_fix_frac(Xt), a1, g1, cc, gc);
                     const float2 r = ffma2(make_float2(w1, w1), make_float2(cc, gc), make_float2(r1[c], r2[c]));
@@ -388,7 +434,31 @@ PM_DEV void eval_costs(const PmCostConsts& k, const PmView& v1, const PmView& v2
                     r2[c] = r.y;
                     ws[c] = ws[c] + w1;
                 }
+        };
+        int dx = dxlo;
+        if (K >= PM_PAIR_TAPS_MINK && K <= PM_PAIR_TAPS_MAXK && (!EXACT || PM_PAIR_TAPS_EXACT)) {
+            /* two taps per step: their weights on packed pairs; each
+             * candidate still takes tap dx before tap dx + 1 */
+            for (; dx < dxhi; dx += 2) {
+                const int qx = x + dx;
+                const float4 a1 = __ldg(&c1row[qx]), a1b = __ldg(&c1row[qx + 1]);
+                const float4 g1 = __ldg(&g1row[qx]), g1b = __ldg(&g1row[qx + 1]);
+                float w1, w1b;
+                tap_weight2(vc, a1, a1b, prow[dx], prow[dx + 1], w1, w1b);
+#pragma unroll
+                for (int c = 0; c < K; ++c) {
+                    one(c, qx, a1, g1, w1);
+                    one(c, qx + 1, a1b, g1b, w1b);
+                }
             }
+        }
+        for (; dx <= dxhi; ++dx) {
+            const int qx = x + dx;
+            const float4 a1 = __ldg(&c1row[qx]);
+            const float4 g1 = __ldg(&g1row[qx]);
+            const float w1 = tap_weight(vc, a1, prow[dx]);
+#pragma unroll
+            for (int c = 0; c < K; ++c) one(c, qx, a1, g1, w1);
         }
         if (!EXACT) {
 #pragma unroll

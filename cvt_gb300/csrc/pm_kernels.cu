@@ -611,7 +611,14 @@ PM_DEV void nbcost_block(const PmPassArgs& a, int mx0, int my0) {
         const int dy = Yq - U;
         if (abs(dy) <= P) {                             /* warp-uniform */
             const float* prow = c_prof + (dy + PM_PMAX) * PM_PROF_N + PM_PMAX;
-            for (int rxi = 0; rxi < 2 * P + 3; ++rxi) {
+            int rxi = 0;
+            for (; rxi < 2 * P; rxi += 2) {                 /* two offsets at a time, on packed pairs */
+                float wa, wb;
+                tap_weight2(uc, s_col[lane + rxi], s_col[lane + rxi + 1], prow[rxi - P], prow[rxi + 1 - P], wa, wb);
+                T[(w * NR + rxi + 2) * 32 + lane] = wa;
+                T[(w * NR + rxi + 3) * 32 + lane] = wb;
+            }
+            for (; rxi < 2 * P + 3; ++rxi) {
                 const int dx = rxi - P;                     /* tap offset from the user: rx + 1 */
                 T[(w * NR + rxi + 2) * 32 + lane] = abs(dx) <= P ? tap_weight(uc, s_col[lane + rxi], prow[dx]) : 0.0f;
             }
