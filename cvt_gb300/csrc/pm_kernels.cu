@@ -17,6 +17,8 @@
 #define PM_KERNELS_TU 1
 #include "pm_kernels.cuh"
 
+#include <type_traits>
+
 /* Blocks of 256 threads per SM the FAST propagation and the neighbour
  * costs are compiled for. */
 #ifndef PM_PROP_MINB
@@ -38,9 +40,6 @@
  * blocks per SM) between the two. */
 #ifndef PM_VIEW_SPLIT
 #define PM_VIEW_SPLIT 1
-#endif
-#ifndef PM_VIEW_DISPATCH
-#define PM_VIEW_DISPATCH 1
 #endif
 #ifndef PM_VIEW_MINB
 #define PM_VIEW_MINB 3
@@ -268,8 +267,8 @@ PM_DEV void propagate_tile(const PmPassArgs& a, int tbx, int tby) {
             int nview = (li[0] < 0) ? 0 : (li[1] < 0) ? 1 : (li[2] < 0) ? 2 : (li[3] < 0) ? 3 : 4;
             if (!inside) nview = 0;
             nview_total = nview;
-#if PM_VIEW_DISPATCH
-            /* one window sweep of as many candidates as the warp's fullest list holds */
+            /* one window sweep of as many candidates as the warp's fullest list
+             * holds (against always 4: 552.0 -> 551.1 ms per depthMap) */
             const int nmax = __reduce_max_sync(0xffffffffu, (unsigned)nview);
             auto sweep = [&](auto m) {
                 constexpr int M = decltype(m)::value;
@@ -288,20 +287,6 @@ PM_DEV void propagate_tile(const PmPassArgs& a, int tbx, int tby) {
             else if (nmax == 2) sweep(std::integral_constant<int, 2>());
             else if (nmax == 3) sweep(std::integral_constant<int, 3>());
             else if (nmax == 4) sweep(std::integral_constant<int, 4>());
-#else
-            if (__any_sync(0xffffffffu, nview > 0)) {
-                float4 s[4]; bool act[4]; float c[4];
-#pragma unroll
-                for (int i = 0; i < 4; ++i) {
-                    act[i] = i < nview;
-                    s[i] = act[i] ? viewprop(a.viewsrc[(size_t)yc * W + li[i]]) : f4s(0.0f);
-                }
-                eval_costs<4, EXACT>(a.k, a.v1, a.v2, xc, yc, s, act, c);
-#pragma unroll
-                for (int i = 0; i < 4; ++i)
-                    if (act[i]) accept(s[i], c[i], 17 + i);
-            }
-#endif
         }
     }
     /* 21-22: random refinements of the current best (:383-389) */
