@@ -634,6 +634,8 @@ PM_DEV void nbcost_block(const PmPassArgs& a, int mx0, int my0) {
             if (rmask && own) {
                 const PmRecRow rrow = rec_row(a.v2, a.k.rp, Yq);
                 long long X = XA + (long long)(Yq - H / 2) * S1 + (long long)(mx - P - 1 - W / 2) * S0;
+                /* two taps per iteration: 509.3 -> 507.5 ms per depthMap (4: 508.3) */
+#pragma unroll 2
                 for (int rx = -P - 1; rx <= P + 1; ++rx) {
                     const int rxi = rx + P + 1;
                     const long long Xt = X;
