@@ -57,6 +57,9 @@ def test_null_arguments_rejected(L):
     assert L.cvtpm_destroy(None) != 0
     assert L.cvtpm_set_params(None, None) != 0
     assert L.cvtpm_depthmap(None, None, 0, None, None, 1, 1, 16, 17, 64.0, 1, 4, -1.0, None, 0, None, None) != 0
+    us = ctypes.c_float(0.0)
+    assert L.cvtpm_tool_pd_time(None, 8, None, ctypes.byref(us)) == 1      # CVTPM_ERR_INVALID_ARGUMENT
+    assert L.cvtpm_tool_fp32_peak(0, None, None) == 1
 
 
 def test_params_struct_layout():
