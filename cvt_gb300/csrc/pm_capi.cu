@@ -1746,10 +1746,10 @@ static cvtpm_status depthmap_batched(cvtpm_ctx* ctx, const cvtpm_pair* pairs, in
             S.kn = best;
             float ms[2] = {0.0f, 0.0f};
             if ((s = tune_mode(S, ms)) != CVTPM_OK) return s;
-            /* one lane is the plain call sequence in a graph, so it never loses to
-             * a loop of plain calls; the phase-batched schedule has to beat it
-             * clearly on the proxy (on full batches it measured 1-2 % behind
-             * where the proxy had it 1 % ahead) */
+            /* one lane is the plain call sequence in a graph (it measured level
+             * with a loop of plain calls); the phase-batched schedule has to
+             * beat it clearly on the proxy (on a full batch it measured 1 %
+             * behind where the proxy had it 1 % ahead) */
             phased = ms[0] < 0.97f * ms[1];
             ctx->binfo.tune_ms = std::chrono::duration<float, std::milli>(std::chrono::steady_clock::now() - c0).count();
             ctx->tuned_knobs.push_back({tkey, best, phased, {ms[0], ms[1]}});
