@@ -29,6 +29,9 @@ def R():
     i, f, vp = ctypes.c_int, ctypes.c_float, ctypes.c_void_p
     L.ref_cost_field.argtypes = [f32, f32, i, i, f32, i, f32]
     L.ref_depthmap.argtypes = [f32, f32, i, i, i, f, i, f, f32, vp, vp]
+    L.ref_depthmap_inpaint.argtypes = [f32, f32, i, i, i, f, i, f32, vp]
+    L.ref_pdrof.argtypes = [f32, f32, f32, i, i, f, i]
+    L.ref_weight.argtypes = [f32, i, i, f32]
     return L
 
 
@@ -76,3 +79,40 @@ def test_depthmap_live(oracle, R, seed):
     assert_bits(ex["states"], s2, "states " + what)
     assert_bits(dmap, d, "dmap " + what)
     assert_bits(ex["normalmap"], nm, "normalmap " + what)
+
+
+@pytest.mark.parametrize("seed", [601, 602])
+def test_depthmap_inpaint_live(oracle, R, seed):
+    rng = np.random.default_rng(seed)
+    W, H = int(rng.integers(24, 48)), int(rng.integers(14, 30))
+    P = int(rng.choice([3, 5, 7]))
+    dmax = float(rng.choice([6.0, 9.0, 12.0]))
+    iters = int(rng.integers(2, 7))
+    sc = scenes.make_scene(W, H, 3, dmax, seed=seed)
+    d = np.empty((H, W), np.float32)
+    s2 = np.empty((2, H, W, 4), np.float32)
+    rc = R.ref_depthmap_inpaint(sc.left, sc.right, W, H, P, dmax, iters, d, s2.ctypes.data)
+    assert rc == 0, rc
+    p = default_params(PRESET_REFERENCE, patchsize=P, depthmax=dmax, iterations=iters)
+    dmap, ex = oracle.depthmap_inpaint(p, sc.left, sc.right, trace=True)
+    what = f"{W}x{H} P={P} dmax={dmax} iterations={iters}"
+    assert_bits(ex["states"], s2, "states " + what)
+    assert_bits(dmap, d, "dmap " + what)
+
+
+@pytest.mark.parametrize("seed,steps,lam", [(701, 9, 5.0), (702, 30, 12.5)])
+def test_pdrof_live(oracle, R, seed, steps, lam):
+    rng = np.random.default_rng(seed)
+    W, H = int(rng.integers(16, 50)), int(rng.integers(10, 40))
+    img = scenes.make_scene(W, H, 2, 8.0, seed=seed).left
+    w = np.empty((H, W), np.float32)
+    R.ref_weight(img, W, H, w)
+    fin = np.zeros((H, W, 4), np.float32)
+    fin[..., :3] = rng.normal(0, 0.3, (H, W, 3))
+    fin[..., 3] = 1.0
+    u0 = np.zeros((H, W, 4), np.float32)
+    u0[..., :3] = rng.normal(0, 0.3, (H, W, 3))
+    want = u0.copy()
+    R.ref_pdrof(want, fin, w, W, H, lam, steps)
+    got = oracle.pd_apply(u0.copy(), fin, w, lam, steps)
+    assert_bits(got, want, f"PDROF {W}x{H} {steps} steps")
